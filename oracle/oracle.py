@@ -1,0 +1,121 @@
+"""Test infrastructure only: ctypes binding of oracle/liboracle.so (the C
+restatement in gliomauq_oracle.c). Used by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg as the checker and the timed CPU port."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-C", HERE, "lib"], check=True, stdout=subprocess.DEVNULL)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        dp = C.POINTER(C.c_double)
+        fp = C.POINTER(C.c_float)
+        L.orc_rd_step_f64.argtypes = [C.c_int, dp, dp, dp, dp, C.c_double, C.c_double, C.c_double,
+                                      C.c_double, C.c_double, C.c_int]
+        L.orc_rd_step_f32ref.argtypes = [C.c_int, fp, fp, fp, fp, C.c_float, C.c_float, C.c_float,
+                                         C.c_double, C.c_double, C.c_int]
+        L.orc_rd_solve_f64.argtypes = [C.c_int, dp, dp, dp, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_double, C.c_long, C.c_int]
+        L.orc_rd_solve_f32ref.argtypes = [C.c_int, fp, fp, fp, C.c_float, C.c_float, C.c_float,
+                                          C.c_double, C.c_double, C.c_long, C.c_int]
+        L.orc_blockgrid_create.restype = C.c_void_p
+        L.orc_blockgrid_create.argtypes = [C.c_int, fp, fp, fp]
+        L.orc_blockgrid_steps.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_double,
+                                          C.c_double, C.c_long, C.c_int]
+        L.orc_blockgrid_get_phi.argtypes = [C.c_void_p, fp]
+        L.orc_blockgrid_destroy.argtypes = [C.c_void_p]
+        L.orc_loglik.argtypes = [C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, C.c_long,
+                                 C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.orc_num_steps.restype = C.c_long
+        L.orc_num_steps.argtypes = [C.c_double, C.c_double]
+        _lib = L
+    return _lib
+
+
+class LikParams(C.Structure):
+    _fields_ = [("pet_sigma2", C.c_double), ("pet_scale", C.c_double), ("t1_uc", C.c_double),
+                ("t2_uc", C.c_double), ("slope", C.c_double)]
+
+
+class LikResult(C.Structure):
+    _fields_ = [("l_pet", C.c_double), ("l_t1", C.c_double), ("l_t2", C.c_double),
+                ("total", C.c_double), ("n_pet", C.c_long)]
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def rd_solve(pw, pg, phi0, Dw, Dg, rho, dt, nsteps, prec="f64", nthreads=0):
+    """nsteps reference steps on a uniform periodic grid; returns the final field."""
+    n = pw.shape[0]
+    h = 1.0 / n
+    if prec == "f64":
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (pw, pg)]
+        phi = np.array(phi0, dtype=np.float64, order="C", copy=True)
+        lib().orc_rd_solve_f64(n, _p(a[0], C.c_double), _p(a[1], C.c_double),
+                               _p(phi, C.c_double), Dw, Dg, rho, dt, h, nsteps, nthreads)
+    elif prec == "f32ref":
+        a = [np.ascontiguousarray(x, dtype=np.float32) for x in (pw, pg)]
+        phi = np.array(phi0, dtype=np.float32, order="C", copy=True)
+        lib().orc_rd_solve_f32ref(n, _p(a[0], C.c_float), _p(a[1], C.c_float),
+                                  _p(phi, C.c_float), np.float32(Dw), np.float32(Dg),
+                                  np.float32(rho), dt, h, nsteps, nthreads)
+    else:
+        raise ValueError(prec)
+    return phi
+
+
+class BlockGrid:
+    """The block-lab restatement of the reference's CPU step (timed baseline)."""
+
+    def __init__(self, pw, pg, phi):
+        self.n = pw.shape[0]
+        a = [np.ascontiguousarray(x, dtype=np.float32) for x in (pw, pg, phi)]
+        self._h = lib().orc_blockgrid_create(self.n, *[_p(x, C.c_float) for x in a])
+        if not self._h:
+            raise ValueError("n must be a multiple of 16")
+
+    def steps(self, Dw, Dg, rho, dt, nsteps, nthreads=0):
+        lib().orc_blockgrid_steps(self._h, np.float32(Dw), np.float32(Dg), np.float32(rho), dt,
+                                  1.0 / self.n, nsteps, nthreads)
+
+    def phi(self):
+        out = np.empty((self.n,) * 3, dtype=np.float32)
+        lib().orc_blockgrid_get_phi(self._h, _p(out, C.c_float))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_blockgrid_destroy(self._h)
+            self._h = None
+
+
+def loglik(model, pet, t1, t2, points, params, step_pet=3, step_ti=2, selective=True):
+    """HGG_Likelihood restated; returns dict of l_pet, l_t1, l_t2, total, n_pet."""
+    nz, ny, nx = model.shape
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (model, pet, t1, t2)]
+    pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).T)  # column-major D2D
+    npts = pts.shape[1] if pts.size else 0
+    lp = LikParams(*params)
+    res = LikResult()
+    lib().orc_loglik(nx, ny, nz, *[_p(a, C.c_double) for a in arrs],
+                     _p(pts, C.c_double) if npts else None, npts, C.byref(lp), step_pet, step_ti,
+                     1 if selective else 0, C.byref(res))
+    return dict(l_pet=res.l_pet, l_t1=res.l_t1, l_t2=res.l_t2, total=res.total, n_pet=res.n_pet)

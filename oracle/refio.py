@@ -1,0 +1,106 @@
+"""Test infrastructure only: file formats of oracle/ref_harness.cpp and a
+runner for the reference binaries compiled into oracle/_ref/."""
+from __future__ import annotations
+
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+def write_input(path, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, adaptive=0, nsteps=-1,
+                dumpfreq=1e30):
+    with open(path, "wb") as f:
+        f.write(b"GBGREF01")
+        f.write(struct.pack("<4i", n, bpd, adaptive, nsteps))
+        f.write(struct.pack("<5d", Dw_file, rho, tend, L, dumpfreq))
+        for a in (pw, pg, phi):
+            np.ascontiguousarray(a, dtype="<f8").tofile(f)
+
+
+def read_solve_output(path):
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"GBGOUT01"
+    n, real_bytes, steps, regrids = struct.unpack_from("<4i", raw, 8)
+    dt, dw, dg, rho = struct.unpack_from("<4d", raw, 24)
+    off = 56
+    N = n ** 3
+    u = np.frombuffer(raw, "<f8", N, off).reshape(n, n, n).copy()
+    off += 8 * N
+    (nb,) = struct.unpack_from("<i", raw, off)
+    off += 4
+    blocks = []
+    for _ in range(nb):
+        bid, lvl, ix, iy, iz = struct.unpack_from("<5i", raw, off)
+        off += 20
+        d = np.frombuffer(raw, "<f8", 3 * 4096, off).reshape(3, 16, 16, 16).copy()
+        off += 8 * 3 * 4096
+        blocks.append(dict(id=bid, level=lvl, index=(ix, iy, iz), phi=d[0], p_w=d[1], p_g=d[2]))
+    return dict(n=n, real_bytes=real_bytes, steps=steps, regrids=regrids, dt=dt, Dw=dw, Dg=dg,
+                rho=rho, phi=u, blocks=blocks)
+
+
+def read_ghosts(path):
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"GBGGHO01"
+    off = 8
+    (nb,) = struct.unpack_from("<i", raw, off)
+    off += 4
+    out = []
+    for _ in range(nb):
+        bid, lvl, ix, iy, iz, ng = struct.unpack_from("<6i", raw, off)
+        off += 24
+        regions = np.frombuffer(raw, "<i4", 54, off).reshape(27, 2).copy()
+        off += 4 * 54
+        ghosts = []
+        for _g in range(ng):
+            (cnt,) = struct.unpack_from("<i", raw, off)
+            off += 4
+            items = []
+            for _k in range(cnt):
+                sb, si = struct.unpack_from("<2i", raw, off)
+                w = struct.unpack_from("<3d", raw, off + 8)
+                off += 32
+                items.append((sb, si, w[0], w[1], w[2]))
+            ghosts.append(items)
+        out.append(dict(id=bid, level=lvl, index=(ix, iy, iz), regions=regions, ghosts=ghosts))
+    return out
+
+
+def read_fwt(path):
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"GBGFWT01"
+    (nb,) = struct.unpack_from("<i", raw, 8)
+    off = 12
+    out = []
+    for _ in range(nb):
+        bid, lvl, ix, iy, iz = struct.unpack_from("<5i", raw, off)
+        (d,) = struct.unpack_from("<d", raw, off + 20)
+        off += 28
+        out.append(dict(id=bid, level=lvl, index=(ix, iy, iz), detail=d))
+    return out
+
+
+def run_harness(cmd, variant, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, adaptive=0,
+                nsteps=-1, dumpfreq=1e30, timeout=3600):
+    exe = os.path.join(REF_DIR, f"ref_harness_{variant}")
+    if not os.path.exists(exe):
+        raise FileNotFoundError(exe)
+    with tempfile.TemporaryDirectory() as td:
+        inp = os.path.join(td, "in.bin")
+        outp = os.path.join(td, "out.bin")
+        write_input(inp, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, adaptive, nsteps, dumpfreq)
+        subprocess.run([exe, cmd, inp, outp], check=True, timeout=timeout,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+        if cmd == "solve":
+            return read_solve_output(outp)
+        if cmd == "ghosts":
+            return read_ghosts(outp)
+        if cmd == "fwt":
+            return read_fwt(outp)
+    raise ValueError(cmd)

@@ -1,0 +1,2 @@
+#pragma once
+#include "_vtk_shim.h"
