@@ -1,0 +1,242 @@
+"""ctypes binding of libgbglioma.so (include/gbglioma.h).
+
+The library is the product; this module only marshals numpy arrays across
+its C ABI. There is no CPU fallback: if the shared library is missing or no
+GPU is present, calls raise GbgError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libgbglioma.so")
+
+GBG_OK = 0
+STATUS_NAMES = {0: "OK", -1: "ERR_ARG", -2: "ERR_CUDA", -3: "ERR_TIMEOUT", -4: "ERR_NONFINITE",
+                -5: "ERR_STATE", -6: "ERR_NOMEM", -7: "ERR_UNSUPPORTED"}
+PREC_F64, PREC_F32REF, PREC_F32 = 0, 1, 2
+PREC_BY_NAME = {"f64": PREC_F64, "f32ref": PREC_F32REF, "f32": PREC_F32}
+
+# every symbol the C header declares
+EXPORTS = [
+    "gbg_create", "gbg_destroy", "gbg_last_error", "gbg_version", "gbg_set_anatomy",
+    "gbg_set_phi", "gbg_get_phi", "gbg_rd_step", "gbg_run", "gbg_set_observations",
+    "gbg_loglik", "gbg_batch_solve", "gbg_batch_solve_device", "gbg_launch_count",
+    "gbg_stream", "gbg_sync", "gbg_last_population_ms",
+]
+
+
+class GbgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("n", C.c_int), ("precision", C.c_int), ("device", C.c_int),
+                ("max_samples", C.c_int)]
+
+
+class LikParams(C.Structure):
+    _fields_ = [("pet_sigma2", C.c_double), ("pet_scale", C.c_double), ("t1_uc", C.c_double),
+                ("t2_uc", C.c_double), ("slope", C.c_double), ("step_pet", C.c_int),
+                ("step_ti", C.c_int), ("selective", C.c_int)]
+
+
+class LikResult(C.Structure):
+    _fields_ = [("l_pet", C.c_double), ("l_t1", C.c_double), ("l_t2", C.c_double),
+                ("total", C.c_double), ("n_pet", C.c_long)]
+
+    def as_dict(self):
+        return dict(l_pet=self.l_pet, l_t1=self.l_t1, l_t2=self.l_t2, total=self.total,
+                    n_pet=self.n_pet)
+
+
+class Sample(C.Structure):
+    _fields_ = [("Dw", C.c_double), ("rho", C.c_double), ("x0", C.c_double), ("y0", C.c_double),
+                ("z0", C.c_double), ("tend", C.c_double)]
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("L", C.c_double), ("ic_peak", C.c_double), ("ic_sigma", C.c_double),
+                ("with_loglik", C.c_int)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libgbglioma.so and declare its signatures (raises if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise GbgError(-7, f"{path} not built: run gliomauq_gb300.build.build()")
+    L = C.CDLL(path)
+    vp, dp, fp = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_float)
+    lp = C.POINTER(C.c_long)
+    sig = {
+        "gbg_create": [C.POINTER(Config), C.POINTER(vp)],
+        "gbg_destroy": [vp],
+        "gbg_version": [C.POINTER(C.c_int), C.POINTER(C.c_int)],
+        "gbg_set_anatomy": [vp, dp, dp],
+        "gbg_set_phi": [vp, dp],
+        "gbg_get_phi": [vp, dp],
+        "gbg_rd_step": [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_long],
+        "gbg_run": [vp, C.c_double, C.c_double, C.c_double, C.c_double, lp, dp],
+        "gbg_set_observations": [vp, dp, dp, dp, dp, C.c_long, C.POINTER(LikParams)],
+        "gbg_loglik": [vp, C.POINTER(LikResult)],
+        "gbg_batch_solve": [vp, C.POINTER(Sample), C.c_int, C.POINTER(BatchOpts),
+                            C.POINTER(LikResult), lp, fp],
+        "gbg_batch_solve_device": [vp, C.c_void_p, C.c_int, C.POINTER(BatchOpts), C.c_void_p],
+        "gbg_launch_count": [vp, C.POINTER(C.c_longlong)],
+        "gbg_stream": [vp, C.POINTER(vp)],
+        "gbg_sync": [vp],
+        "gbg_last_population_ms": [vp, C.POINTER(C.c_float)],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.gbg_last_error.argtypes = []
+    L.gbg_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != GBG_OK:
+        msg = load().gbg_last_error().decode(errors="replace")
+        raise GbgError(rc, msg)
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def as_f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Handle:
+    """One libgbglioma handle (one CUDA stream, one n^3 grid)."""
+
+    def __init__(self, n: int, precision="f64", device: int = 0, max_samples: int = 0):
+        self.lib = load()
+        self.n = n
+        self.N = n ** 3
+        self.precision = PREC_BY_NAME[precision] if isinstance(precision, str) else precision
+        cfg = Config(n, self.precision, device, max_samples)
+        h = C.c_void_p()
+        check(self.lib.gbg_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.gbg_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _field(self, a):
+        a = as_f64(a)
+        if a.size != self.N:
+            raise ValueError(f"field must have {self.N} cells")
+        return a
+
+    def set_anatomy(self, p_w, p_g):
+        a, b = self._field(p_w), self._field(p_g)
+        check(self.lib.gbg_set_anatomy(self._h, dptr(a), dptr(b)))
+
+    def set_phi(self, phi):
+        a = self._field(phi)
+        check(self.lib.gbg_set_phi(self._h, dptr(a)))
+
+    def get_phi(self) -> np.ndarray:
+        out = np.empty((self.n,) * 3, dtype=np.float64)
+        check(self.lib.gbg_get_phi(self._h, dptr(out)))
+        return out
+
+    def rd_step(self, Dw, Dg, rho, dt, nsteps=1):
+        check(self.lib.gbg_rd_step(self._h, Dw, Dg, rho, dt, nsteps))
+
+    def run(self, Dw_file, rho, tend, L):
+        ns = C.c_long()
+        dt = C.c_double()
+        check(self.lib.gbg_run(self._h, Dw_file, rho, tend, L, C.byref(ns), C.byref(dt)))
+        return ns.value, dt.value
+
+    def set_observations(self, pet, t1, t2, points, params, step_pet=3, step_ti=2,
+                         selective=True):
+        pet, t1, t2 = self._field(pet), self._field(t1), self._field(t2)
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).T) if selective else None
+        npts = pts.shape[1] if pts is not None and pts.size else 0
+        lp = LikParams(*params, step_pet, step_ti, 1 if selective else 0)
+        check(self.lib.gbg_set_observations(self._h, dptr(pet), dptr(t1), dptr(t2),
+                                            dptr(pts) if npts else None, npts, C.byref(lp)))
+
+    def loglik(self) -> dict:
+        r = LikResult()
+        check(self.lib.gbg_loglik(self._h, C.byref(r)))
+        return r.as_dict()
+
+    def batch_solve(self, samples, L, ic_peak=0.1, ic_sigma=1.0, with_loglik=True,
+                    want_phi=False):
+        S = len(samples)
+        arr = (Sample * S)(*[Sample(*s) for s in samples])
+        opts = BatchOpts(L, ic_peak, ic_sigma, 1 if with_loglik else 0)
+        lik = (LikResult * S)()
+        steps = np.zeros(S, dtype=np.int64)
+        phi = np.empty((S, self.n, self.n, self.n), dtype=np.float32) if want_phi else None
+        check(self.lib.gbg_batch_solve(self._h, arr, S, C.byref(opts),
+                                       lik if with_loglik else None,
+                                       steps.ctypes.data_as(C.POINTER(C.c_long)),
+                                       fptr(phi) if want_phi else None))
+        out = dict(nsteps=steps)
+        if with_loglik:
+            out["loglik"] = [lik[i].as_dict() for i in range(S)]
+        if want_phi:
+            out["phi"] = phi
+        return out
+
+    def batch_solve_device(self, samples_dev_ptr: int, S: int, L, lik_dev_ptr: int | None,
+                           ic_peak=0.1, ic_sigma=1.0):
+        opts = BatchOpts(L, ic_peak, ic_sigma, 1 if lik_dev_ptr else 0)
+        check(self.lib.gbg_batch_solve_device(self._h, C.c_void_p(samples_dev_ptr), S,
+                                              C.byref(opts),
+                                              C.c_void_p(lik_dev_ptr) if lik_dev_ptr else None))
+
+    def launch_count(self) -> int:
+        c = C.c_longlong()
+        check(self.lib.gbg_launch_count(self._h, C.byref(c)))
+        return c.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(self.lib.gbg_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def sync(self):
+        check(self.lib.gbg_sync(self._h))
+
+    def last_population_ms(self) -> float:
+        ms = C.c_float()
+        check(self.lib.gbg_last_population_ms(self._h, C.byref(ms)))
+        return ms.value

@@ -1,0 +1,461 @@
+// The C ABI of libgbglioma (include/gbglioma.h): handle lifetime, state
+// upload/download, and the entry points that replace the reference's block
+// processing of the RD step, its time loop and its likelihood.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gbg_internal.cuh"
+
+namespace gbg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+// Glioma_HG_UQ::run, source/Glioma/Glioma_HG_UQ.cpp:519-539. In the float
+// build Dw, Dg and rho are Real = float: Dw is read as float, Dw/(L*L) is a
+// double division rounded back to float, Dg = 0.1*Dw likewise.
+void reference_dt(int n, double Dw_file, double L, bool f32, double *dt, double *Dw, double *Dg,
+                  double *rho) {
+    double dw, dg;
+    if (f32) {
+        const float dwf = (float)((double)(float)Dw_file / (L * L));
+        const float dgf = (float)(0.1 * (double)dwf);
+        dw = dwf;
+        dg = dgf;
+        *rho = (double)(float)*rho;
+    } else {
+        dw = Dw_file / (L * L);
+        dg = 0.1 * dw;
+    }
+    const double h = 1. / n;
+    const double mx = dw >= dg ? dw : dg;
+    *dt = 0.99 * h * h / (2. * 3 * mx);
+    *Dw = dw;
+    *Dg = dg;
+}
+
+long reference_num_steps(double dt, double tend) {
+    double t = 0.0;
+    long k = 0;
+    while (t <= tend && k < 100000000L) {
+        t += dt;
+        ++k;
+    }
+    return k;
+}
+
+}  // namespace gbg
+
+using gbg::Handle;
+using gbg::set_error;
+
+namespace {
+
+int check_handle(gbg_handle *hh) {
+    if (!hh) {
+        set_error("null handle");
+        return GBG_ERR_ARG;
+    }
+    return GBG_OK;
+}
+
+size_t storage_bytes(int prec) { return prec == GBG_PREC_F64 ? sizeof(double) : sizeof(float); }
+
+bool all_finite(const double *a, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(a[i])) return false;
+    return true;
+}
+
+void free_handle(Handle &h) {
+    void *ptrs[] = {h.pw, h.pg, h.phi[0], h.phi[1], h.b0, h.dfx, h.dfy, h.dfz, h.cx, h.cy, h.cz,
+                    h.msk, h.bphi[0], h.bphi[1], h.bwork, h.dev_status, h.barrier,
+                    h.obs.pet_idx, h.obs.pet_val, h.obs.ti_idx, h.obs.t1_val, h.obs.t2_val,
+                    h.lik_partials, h.lik_out};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (cudaEvent_t e : h.ev_pop)
+        if (e) cudaEventDestroy(e);
+    if (h.stream) cudaStreamDestroy(h.stream);
+}
+
+int ensure_lik_out(Handle &h, int S) {
+    if (h.lik_out_cap >= S) return GBG_OK;
+    if (h.lik_out) cudaFree(h.lik_out);
+    h.lik_out = nullptr;
+    h.lik_out_cap = 0;
+    GBG_CUDA_TRY(cudaMalloc(&h.lik_out, sizeof(gbg_lik_result) * (size_t)S));
+    h.lik_out_cap = S;
+    return GBG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gbg_last_error(void) { return gbg::g_last_error.c_str(); }
+
+int gbg_version(int *major, int *minor) {
+    if (major) *major = GBG_VERSION_MAJOR;
+    if (minor) *minor = GBG_VERSION_MINOR;
+    return GBG_OK;
+}
+
+int gbg_create(const gbg_config *cfg, gbg_handle **out) {
+    if (!cfg || !out) {
+        set_error("null argument");
+        return GBG_ERR_ARG;
+    }
+    *out = nullptr;
+    if (cfg->n < 4 || cfg->n > 1024 || cfg->precision < GBG_PREC_F64 ||
+        cfg->precision > GBG_PREC_F32 || cfg->max_samples < 0) {
+        set_error("bad configuration");
+        return GBG_ERR_ARG;
+    }
+    int ndev = 0;
+    GBG_CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (cfg->device < 0 || cfg->device >= ndev) {
+        set_error("device ordinal out of range");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(cfg->device));
+    gbg_handle *hh = new gbg_handle();
+    Handle &h = hh->h;
+    h.n = cfg->n;
+    h.N = (size_t)cfg->n * cfg->n * cfg->n;
+    h.prec = cfg->precision;
+    h.device = cfg->device;
+    h.max_samples = cfg->max_samples;
+    auto fail = [&](int rc) {
+        free_handle(h);
+        delete hh;
+        return rc;
+    };
+#define TRY_ALLOC(ptr, bytes)                                                  \
+    do {                                                                       \
+        cudaError_t e = cudaMalloc((void **)&(ptr), (bytes));                  \
+        if (e != cudaSuccess) {                                                \
+            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));    \
+            return fail(e == cudaErrorMemoryAllocation ? GBG_ERR_NOMEM : GBG_ERR_CUDA); \
+        }                                                                      \
+    } while (0)
+    if (cudaDeviceGetAttribute(&h.num_sms, cudaDevAttrMultiProcessorCount, h.device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&h.ev_pop[0]) != cudaSuccess || cudaEventCreate(&h.ev_pop[1]) != cudaSuccess) {
+        set_error("stream creation failed");
+        return fail(GBG_ERR_CUDA);
+    }
+    const size_t sb = storage_bytes(h.prec);
+    TRY_ALLOC(h.pw, h.N * sizeof(double));
+    TRY_ALLOC(h.pg, h.N * sizeof(double));
+    TRY_ALLOC(h.phi[0], h.N * sb);
+    TRY_ALLOC(h.phi[1], h.N * sb);
+    if (h.prec == GBG_PREC_F32) {
+        TRY_ALLOC(h.cx, h.N * sizeof(float));
+        TRY_ALLOC(h.cy, h.N * sizeof(float));
+        TRY_ALLOC(h.cz, h.N * sizeof(float));
+        TRY_ALLOC(h.msk, h.N * sizeof(float));
+        if (h.max_samples > 0) {
+            TRY_ALLOC(h.bphi[0], h.N * (size_t)h.max_samples * sizeof(float));
+            TRY_ALLOC(h.bphi[1], h.N * (size_t)h.max_samples * sizeof(float));
+        }
+    } else {
+        TRY_ALLOC(h.b0, h.N * sb);
+        TRY_ALLOC(h.dfx, h.N * sizeof(double));
+        TRY_ALLOC(h.dfy, h.N * sizeof(double));
+        TRY_ALLOC(h.dfz, h.N * sizeof(double));
+    }
+    h.bwork_bytes = gbg::bwork_total(h);
+    TRY_ALLOC(h.bwork, h.bwork_bytes);
+    TRY_ALLOC(h.dev_status, sizeof(int));
+    TRY_ALLOC(h.barrier, 2 * sizeof(unsigned));
+#undef TRY_ALLOC
+    if (cudaMemset(h.dev_status, 0, sizeof(int)) != cudaSuccess ||
+        cudaMemset(h.barrier, 0, 2 * sizeof(unsigned)) != cudaSuccess) {
+        set_error("memset failed");
+        return fail(GBG_ERR_CUDA);
+    }
+    *out = hh;
+    return GBG_OK;
+}
+
+int gbg_destroy(gbg_handle *hh) {
+    if (!hh) return GBG_OK;
+    cudaSetDevice(hh->h.device);
+    if (hh->h.stream) cudaStreamSynchronize(hh->h.stream);
+    free_handle(hh->h);
+    delete hh;
+    return GBG_OK;
+}
+
+int gbg_set_anatomy(gbg_handle *hh, const double *p_w, const double *p_g) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!p_w || !p_g) {
+        set_error("null field");
+        return GBG_ERR_ARG;
+    }
+    if (!all_finite(p_w, h.N) || !all_finite(p_g, h.N)) {
+        set_error("anatomy has NaN or Inf");
+        return GBG_ERR_NONFINITE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    GBG_CUDA_TRY(cudaMemcpyAsync(h.pw, p_w, h.N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    GBG_CUDA_TRY(cudaMemcpyAsync(h.pg, p_g, h.N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    h.anatomy_set = true;
+    h.tables_valid = false;
+    h.fast_valid = false;
+    return GBG_OK;
+}
+
+int gbg_set_phi(gbg_handle *hh, const double *phi) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!phi) {
+        set_error("null field");
+        return GBG_ERR_ARG;
+    }
+    if (!all_finite(phi, h.N)) {
+        set_error("phi has NaN or Inf");
+        return GBG_ERR_NONFINITE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    h.cur = 0;
+    if (h.prec == GBG_PREC_F64) {
+        GBG_CUDA_TRY(cudaMemcpyAsync(h.phi[0], phi, h.N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    } else {
+        std::vector<float> tmp(h.N);
+        for (size_t i = 0; i < h.N; ++i) tmp[i] = (float)phi[i];
+        GBG_CUDA_TRY(cudaMemcpyAsync(h.phi[0], tmp.data(), h.N * sizeof(float), cudaMemcpyHostToDevice, h.stream));
+        GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    }
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    h.phi_set = true;
+    return GBG_OK;
+}
+
+int gbg_get_phi(gbg_handle *hh, double *phi) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!phi) {
+        set_error("null field");
+        return GBG_ERR_ARG;
+    }
+    if (!h.phi_set) {
+        set_error("phi not set");
+        return GBG_ERR_STATE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    if (h.prec == GBG_PREC_F64) {
+        GBG_CUDA_TRY(cudaMemcpyAsync(phi, h.phi[h.cur], h.N * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+        GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    } else {
+        std::vector<float> tmp(h.N);
+        GBG_CUDA_TRY(cudaMemcpyAsync(tmp.data(), h.phi[h.cur], h.N * sizeof(float), cudaMemcpyDeviceToHost, h.stream));
+        GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        for (size_t i = 0; i < h.N; ++i) phi[i] = (double)tmp[i];
+    }
+    return GBG_OK;
+}
+
+int gbg_rd_step(gbg_handle *hh, double Dw, double Dg, double rho, double dt, long nsteps) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!h.anatomy_set || !h.phi_set) {
+        set_error("set anatomy and phi before stepping");
+        return GBG_ERR_STATE;
+    }
+    if (nsteps < 0 || !std::isfinite(Dw) || !std::isfinite(Dg) || !std::isfinite(rho) ||
+        !std::isfinite(dt) || !(Dw > 0) || !(Dg >= 0) || !(dt > 0)) {
+        set_error("bad step parameters");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    if (h.prec == GBG_PREC_F32) {
+        int rc = gbg::fast_build_tables(h, (double)(float)(Dg / Dw));
+        if (rc) return rc;
+        return gbg::fast_steps_single(h, Dw, rho, dt, nsteps);
+    }
+    return gbg::exact_steps(h, Dw, Dg, rho, dt, nsteps);
+}
+
+int gbg_run(gbg_handle *hh, double Dw_file, double rho, double tend, double L, long *nsteps_out,
+            double *dt_out) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!std::isfinite(Dw_file) || !std::isfinite(rho) || !std::isfinite(tend) || !(L > 0) ||
+        !(Dw_file > 0)) {
+        set_error("bad run parameters");
+        return GBG_ERR_ARG;
+    }
+    double dt, Dw, Dg, r = rho;
+    // the fast path keeps the double-precision timeline of the FP64 reference
+    gbg::reference_dt(h.n, Dw_file, L, h.prec == GBG_PREC_F32REF, &dt, &Dw, &Dg, &r);
+    const long ns = gbg::reference_num_steps(dt, tend);
+    if (nsteps_out) *nsteps_out = ns;
+    if (dt_out) *dt_out = dt;
+    int rc = gbg_rd_step(hh, Dw, Dg, r, dt, ns);
+    if (rc) return rc;
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    return GBG_OK;
+}
+
+int gbg_set_observations(gbg_handle *hh, const double *pet, const double *t1, const double *t2,
+                         const double *points, long npoints, const gbg_lik_params *p) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!pet || !t1 || !t2 || !p || (p->selective && (npoints < 0 || (npoints > 0 && !points)))) {
+        set_error("null observation argument");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    return gbg::lik_set_observations(h, pet, t1, t2, points, npoints, *p);
+}
+
+int gbg_loglik(gbg_handle *hh, gbg_lik_result *out) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!out) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    if (!h.phi_set) {
+        set_error("phi not set");
+        return GBG_ERR_STATE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    if (int rc = ensure_lik_out(h, 1)) return rc;
+    int rc;
+    if (h.prec == GBG_PREC_F64)
+        rc = gbg::lik_evaluate(h, nullptr, (const double *)h.phi[h.cur], 1, (gbg_lik_result *)h.lik_out);
+    else
+        rc = gbg::lik_evaluate(h, (const float *)h.phi[h.cur], nullptr, 1, (gbg_lik_result *)h.lik_out);
+    if (rc) return rc;
+    GBG_CUDA_TRY(cudaMemcpyAsync(out, h.lik_out, sizeof(gbg_lik_result), cudaMemcpyDeviceToHost, h.stream));
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    return GBG_OK;
+}
+
+static int validate_batch(Handle &h, int S, const gbg_batch_opts *o) {
+    if (!o || S <= 0 || S > h.max_samples || !(o->L > 0) || !(o->ic_sigma > 0) ||
+        !std::isfinite(o->ic_peak)) {
+        set_error("bad batch arguments");
+        return GBG_ERR_ARG;
+    }
+    if (!h.anatomy_set) {
+        set_error("anatomy not set");
+        return GBG_ERR_STATE;
+    }
+    if (o->with_loglik && !h.obs.valid) {
+        set_error("observations not set");
+        return GBG_ERR_STATE;
+    }
+    return GBG_OK;
+}
+
+int gbg_batch_solve_device(gbg_handle *hh, const gbg_sample *samples_device, int S,
+                           const gbg_batch_opts *o, gbg_lik_result *loglik_device) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (int rc = validate_batch(h, S, o)) return rc;
+    if (!samples_device) {
+        set_error("null samples");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    return gbg::batch_solve_device(h, samples_device, S, *o, loglik_device, nullptr);
+}
+
+int gbg_batch_solve(gbg_handle *hh, const gbg_sample *samples, int S, const gbg_batch_opts *o,
+                    gbg_lik_result *loglik, long *nsteps_out, float *phi_out) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (int rc = validate_batch(h, S, o)) return rc;
+    if (!samples) {
+        set_error("null samples");
+        return GBG_ERR_ARG;
+    }
+    for (int s = 0; s < S; ++s) {
+        const gbg_sample &q = samples[s];
+        if (!std::isfinite(q.Dw) || !(q.Dw > 0) || !std::isfinite(q.rho) || !std::isfinite(q.x0) ||
+            !std::isfinite(q.y0) || !std::isfinite(q.z0) || !std::isfinite(q.tend)) {
+            set_error("non-finite or non-positive sample parameter");
+            return GBG_ERR_NONFINITE;
+        }
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    gbg_sample *d_samples = gbg::batch_samples(h);
+    GBG_CUDA_TRY(cudaMemcpyAsync(d_samples, samples, sizeof(gbg_sample) * S, cudaMemcpyHostToDevice, h.stream));
+    gbg_lik_result *d_lik = nullptr;
+    if (o->with_loglik) {
+        if (int rc = ensure_lik_out(h, S)) return rc;
+        d_lik = (gbg_lik_result *)h.lik_out;
+    }
+    std::vector<long> steps(S);
+    int rc = gbg::batch_solve_device(h, d_samples, S, *o, d_lik, steps.data());
+    if (rc) return rc;
+    rc = gbg::check_device_status(h);
+    if (rc) return rc;
+    if (nsteps_out)
+        for (int s = 0; s < S; ++s) nsteps_out[s] = steps[s];
+    if (loglik && d_lik)
+        GBG_CUDA_TRY(cudaMemcpyAsync(loglik, d_lik, sizeof(gbg_lik_result) * S, cudaMemcpyDeviceToHost, h.stream));
+    if (phi_out) {
+        for (int s = 0; s < S; ++s) {
+            const float *src = h.bphi[steps[s] & 1] + (size_t)s * h.N;
+            GBG_CUDA_TRY(cudaMemcpyAsync(phi_out + (size_t)s * h.N, src, h.N * sizeof(float),
+                                         cudaMemcpyDeviceToHost, h.stream));
+        }
+    }
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    return GBG_OK;
+}
+
+int gbg_launch_count(gbg_handle *hh, long long *count) {
+    if (int rc = check_handle(hh)) return rc;
+    if (!count) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    *count = hh->h.launches;
+    return GBG_OK;
+}
+
+int gbg_stream(gbg_handle *hh, void **stream) {
+    if (int rc = check_handle(hh)) return rc;
+    if (!stream) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    *stream = (void *)hh->h.stream;
+    return GBG_OK;
+}
+
+int gbg_last_population_ms(gbg_handle *hh, float *ms) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!ms) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    if (!h.ev_pop_recorded) {
+        set_error("no population kernel launched yet");
+        return GBG_ERR_STATE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    GBG_CUDA_TRY(cudaEventSynchronize(h.ev_pop[1]));
+    GBG_CUDA_TRY(cudaEventElapsedTime(ms, h.ev_pop[0], h.ev_pop[1]));
+    return GBG_OK;
+}
+
+int gbg_sync(gbg_handle *hh) {
+    if (int rc = check_handle(hh)) return rc;
+    GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
+    GBG_CUDA_TRY(cudaStreamSynchronize(hh->h.stream));
+    return GBG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,149 @@
+// Internal declarations shared by the libgbglioma translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/gbglioma.h"
+
+namespace gbg {
+
+// Thread-local last error message (gbg_last_error).
+void set_error(const std::string &msg);
+
+#define GBG_CUDA_TRY(expr)                                                            \
+    do {                                                                              \
+        cudaError_t _e = (expr);                                                      \
+        if (_e != cudaSuccess) {                                                      \
+            ::gbg::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));     \
+            return _e == cudaErrorMemoryAllocation ? GBG_ERR_NOMEM : GBG_ERR_CUDA;    \
+        }                                                                             \
+    } while (0)
+
+// Device-side error codes written to the handle's status word.
+enum DeviceStatus : int { DEV_OK = 0, DEV_BARRIER_TIMEOUT = 1 };
+
+// Compact observation lists for the likelihood (see likelihood.cu).
+struct ObsDevice {
+    int n_pet = 0;           // PET voxels kept (stride and PET > 0)
+    int *pet_idx = nullptr;  // cell indices
+    double *pet_val = nullptr;
+    int n_ti = 0;            // T1/T2 evaluation points
+    int *ti_idx = nullptr;
+    double *t1_val = nullptr;
+    double *t2_val = nullptr;
+    double pet_sigma2 = 0, pet_scale = 0, t1_uc = 0, t2_uc = 0, slope = 0;
+    bool valid = false;
+};
+
+struct Handle {
+    int n = 0;
+    size_t N = 0;
+    int prec = GBG_PREC_F64;
+    int device = 0;
+    int max_samples = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    long long launches = 0;
+
+    // anatomy, kept in double so any mode can rebuild its tables
+    double *pw = nullptr, *pg = nullptr;
+    bool anatomy_set = false;
+
+    // single-solve state: phi ping-pong in the storage type
+    void *phi[2] = {nullptr, nullptr};
+    int cur = 0;
+    bool phi_set = false;
+
+    // exact modes: brain sum b0 (storage type) and face diffusivities (double)
+    void *b0 = nullptr;
+    double *dfx = nullptr, *dfy = nullptr, *dfz = nullptr;
+    double tab_Dw = -1, tab_Dg = -1;  // (Dw, Dg) the tables were built for
+    bool tables_valid = false;
+
+    // fast mode: unit-diffusivity face coefficients and tissue mask (float SoA)
+    float *cx = nullptr, *cy = nullptr, *cz = nullptr, *msk = nullptr;
+    double fast_ratio = -1;  // Dg/Dw the fast coefficients were built for
+    bool fast_valid = false;
+
+    // batched population buffers
+    float *bphi[2] = {nullptr, nullptr};  // max_samples * N each
+    void *bwork = nullptr;                // per-sample schedule records
+    size_t bwork_bytes = 0;
+    int *dev_status = nullptr;            // device status word
+    unsigned *barrier = nullptr;          // grid barrier {count, generation}
+
+    // events bracketing the latest population-kernel launch
+    cudaEvent_t ev_pop[2] = {nullptr, nullptr};
+    bool ev_pop_recorded = false;
+
+    // likelihood
+    ObsDevice obs;
+    double *lik_partials = nullptr;  // scratch for the two-pass reduction
+    size_t lik_partials_cap = 0;
+    void *lik_out = nullptr;         // device gbg_lik_result scratch
+    int lik_out_cap = 0;
+};
+
+// ---- rd_exact.cu ----
+int exact_build_tables(Handle &h, double Dw, double Dg);
+int exact_steps(Handle &h, double Dw, double Dg, double rho, double dt, long nsteps);
+
+// ---- rd_fast.cu ----
+// Per-sample schedule record of the batched solver (stored sorted by nsteps,
+// longest first, for the population kernel; unsorted for everything else).
+struct SampleRec {
+    float a, b;   // dt*Dw/h^2 and dt*rho
+    int nsteps;   // reference step count
+    int order;    // sample index
+    double dt;
+};
+// Layout of Handle::bwork, each region 256-byte aligned, cap = max(1, max_samples):
+// unsorted records | sorted records | rank_of ints | staged gbg_sample inputs.
+inline size_t bwork_align(size_t b) { return (b + 255) & ~(size_t)255; }
+inline int bwork_cap(const Handle &h) { return h.max_samples > 1 ? h.max_samples : 1; }
+inline size_t bwork_off_sorted(const Handle &h) { return bwork_align(bwork_cap(h) * sizeof(SampleRec)); }
+inline size_t bwork_off_rank(const Handle &h) { return 2 * bwork_off_sorted(h); }
+inline size_t bwork_off_samples(const Handle &h) {
+    return bwork_off_rank(h) + bwork_align(bwork_cap(h) * sizeof(int));
+}
+inline size_t bwork_total(const Handle &h) {
+    return bwork_off_samples(h) + bwork_align(bwork_cap(h) * sizeof(gbg_sample));
+}
+inline SampleRec *batch_unsorted(Handle &h) { return reinterpret_cast<SampleRec *>(h.bwork); }
+inline SampleRec *batch_sorted(Handle &h) {
+    return reinterpret_cast<SampleRec *>((char *)h.bwork + bwork_off_sorted(h));
+}
+inline int *batch_rank_of(Handle &h) { return reinterpret_cast<int *>((char *)h.bwork + bwork_off_rank(h)); }
+inline gbg_sample *batch_samples(Handle &h) {
+    return reinterpret_cast<gbg_sample *>((char *)h.bwork + bwork_off_samples(h));
+}
+int fast_build_tables(Handle &h, double ratio);
+int fast_steps_single(Handle &h, double Dw, double rho, double dt, long nsteps);
+// reads and clears the device status word (synchronises the stream)
+int check_device_status(Handle &h);
+int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
+                       const gbg_batch_opts &o, gbg_lik_result *loglik_device, long *nsteps_host);
+
+// ---- likelihood.cu ----
+int lik_set_observations(Handle &h, const double *pet, const double *t1, const double *t2,
+                         const double *points, long npoints, const gbg_lik_params &p);
+// phi_f32 or phi_f64 (one non-null): S fields of N cells at stride N.
+int lik_evaluate(Handle &h, const float *phi_f32, const double *phi_f64, int S,
+                 gbg_lik_result *out_device);
+// population: sample s's final field is in buf[recs[s].nsteps & 1] + s*N.
+int lik_evaluate_population(Handle &h, const float *buf0, const float *buf1,
+                            const SampleRec *recs_unsorted, int S, gbg_lik_result *out_device);
+
+// dt and unit-cube Dw/Dg as Glioma_HG_UQ::run computes them (float modes round
+// Dw and Dg to float at each assignment).
+void reference_dt(int n, double Dw_file, double L, bool f32, double *dt, double *Dw, double *Dg,
+                  double *rho_in_out);
+long reference_num_steps(double dt, double tend);
+
+}  // namespace gbg
+
+struct gbg_handle {
+    gbg::Handle h;
+};

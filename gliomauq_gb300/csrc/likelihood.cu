@@ -1,0 +1,251 @@
+// Imaging log-likelihood of HGG_Likelihood (source/Likelihood/source/HGG_Likelihood.cpp),
+// as a gather-and-reduce over compact observation lists:
+//   PET term  (:40-75)   over voxels with ix,iy,iz = 0 mod stepPet and PET > 0:
+//             -0.5 N log(2 pi sigma^2) - 0.5/sigma^2 * sum (u - scale*PET)^2
+//   T1/T2     (:77-128)  over the Sphere.dat points with coordinates = 0 mod
+//             stepTi (or every voxel): sum of log Bernoulli(alpha(u)) with
+//             alpha = 0.5 + 0.5 sgn(u - uc) (1 - exp(-(u - uc)^2 / slope))
+//             (:136-160)
+// The lists are built once per observation set on the host. Per sample, each
+// CTA reduces a chunk of both lists with warp shuffles into three double
+// partial sums (scratch), and a second pass adds a sample's partials in a
+// fixed order, so results are deterministic. Accumulation is double (the
+// reference's is long double).
+//
+// Compiled with -fmad=false: (u - scale*PET)^2 and the exponent round as the
+// reference's plain double expressions do.
+#include <vector>
+
+#include "gbg_internal.cuh"
+
+namespace gbg {
+namespace {
+
+constexpr int kLikThreads = 256;
+constexpr int kLikPerThread = 8;
+constexpr int kLikChunk = kLikThreads * kLikPerThread;
+
+__device__ __forceinline__ int sgn_d(double d) {  // HGG_Likelihood::sgn, eps = 0
+    if (d < -0.0) return -1;
+    return d > 0.0;
+}
+
+__device__ __forceinline__ double log_bernoulli(double u, double y, double uc, double is2) {
+    const double diff = u - uc;
+    const double alpha = 0.5 + 0.5 * sgn_d(diff) * (1. - exp(-diff * diff * is2));
+    return (y == 1) ? log(alpha) : log(1. - alpha);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct LikArgs {
+    int n_pet, n_ti, chunks;
+    const int *pet_idx;
+    const double *pet_val;
+    const int *ti_idx;
+    const double *t1_val, *t2_val;
+    double pet_scale, t1_uc, t2_uc, is2;
+    size_t stride;
+    double *partials;  // [S][chunks][3]
+};
+
+// phi of sample s: F32 buffers chosen per sample by its step parity, or one
+// double / float field array at stride.
+struct PhiSource {
+    const float *f0, *f1;       // population buffers (f1 may equal f0)
+    const double *d;            // double fields (exact FP64 mode)
+    const SampleRec *recs;      // if non-null, buffer = recs[s].nsteps & 1
+    __device__ __forceinline__ double at(int s, size_t stride, int c) const {
+        if (d) return d[(size_t)s * stride + c];
+        const float *b = (recs && (recs[s].nsteps & 1)) ? f1 : f0;
+        return (double)b[(size_t)s * stride + c];
+    }
+};
+
+__global__ void __launch_bounds__(kLikThreads) k_lik_partial(LikArgs a, PhiSource src) {
+    const int s = blockIdx.y;
+    const int chunk = blockIdx.x;
+    double sp = 0.0, s1 = 0.0, s2 = 0.0;
+    const int base = chunk * kLikChunk;
+    for (int k = 0; k < kLikPerThread; ++k) {
+        const int i = base + k * kLikThreads + threadIdx.x;
+        if (i < a.n_pet) {
+            const double u = src.at(s, a.stride, a.pet_idx[i]);
+            const double pv = a.pet_val[i];
+            const double r = u - a.pet_scale * pv;
+            sp += r * r;
+        }
+        if (i < a.n_ti) {
+            const double u = src.at(s, a.stride, a.ti_idx[i]);
+            s1 += log_bernoulli(u, a.t1_val[i], a.t1_uc, a.is2);
+            s2 += log_bernoulli(u, a.t2_val[i], a.t2_uc, a.is2);
+        }
+    }
+    sp = warp_sum(sp);
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    __shared__ double red[3][kLikThreads / 32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        red[0][w] = sp;
+        red[1][w] = s1;
+        red[2][w] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int j = 0; j < kLikThreads / 32; ++j) t += red[threadIdx.x][j];
+        a.partials[((size_t)s * a.chunks + chunk) * 3 + threadIdx.x] = t;
+    }
+}
+
+__global__ void k_lik_final(const double *__restrict__ partials, int chunks, int S, int n_pet,
+                            double pet_sigma2, gbg_lik_result *__restrict__ out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    double sp = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int c = 0; c < chunks; ++c) {
+        const double *p = partials + ((size_t)s * chunks + c) * 3;
+        sp += p[0];
+        s1 += p[1];
+        s2 += p[2];
+    }
+    // :70-74
+    const double p1 = -0.5 * n_pet * log(2. * 3.14159265358979323846 * pet_sigma2);
+    const double p2 = -0.5 * (1. / pet_sigma2) * sp;
+    gbg_lik_result r;
+    r.l_pet = p1 + p2;
+    r.l_t1 = s1;
+    r.l_t2 = s2;
+    r.total = r.l_pet + r.l_t1 + r.l_t2;
+    r.n_pet = n_pet;
+    out[s] = r;
+}
+
+template <typename T>
+int upload(T **dst, const std::vector<T> &v) {
+    if (*dst) {
+        cudaFree(*dst);
+        *dst = nullptr;
+    }
+    if (v.empty()) return GBG_OK;
+    GBG_CUDA_TRY(cudaMalloc((void **)dst, v.size() * sizeof(T)));
+    GBG_CUDA_TRY(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return GBG_OK;
+}
+
+int run_lik(Handle &h, const PhiSource &src, int S, gbg_lik_result *out_device) {
+    if (!h.obs.valid) {
+        set_error("observations not set");
+        return GBG_ERR_STATE;
+    }
+    const int items = h.obs.n_pet > h.obs.n_ti ? h.obs.n_pet : h.obs.n_ti;
+    const int chunks = items > 0 ? (items + kLikChunk - 1) / kLikChunk : 1;
+    const size_t need = (size_t)S * chunks * 3;
+    if (need > h.lik_partials_cap) {
+        if (h.lik_partials) cudaFree(h.lik_partials);
+        h.lik_partials = nullptr;
+        h.lik_partials_cap = 0;
+        GBG_CUDA_TRY(cudaMalloc((void **)&h.lik_partials, need * sizeof(double)));
+        h.lik_partials_cap = need;
+    }
+    LikArgs a;
+    a.n_pet = h.obs.n_pet;
+    a.n_ti = h.obs.n_ti;
+    a.chunks = chunks;
+    a.pet_idx = h.obs.pet_idx;
+    a.pet_val = h.obs.pet_val;
+    a.ti_idx = h.obs.ti_idx;
+    a.t1_val = h.obs.t1_val;
+    a.t2_val = h.obs.t2_val;
+    a.pet_scale = h.obs.pet_scale;
+    a.t1_uc = h.obs.t1_uc;
+    a.t2_uc = h.obs.t2_uc;
+    a.is2 = 1. / h.obs.slope;
+    a.stride = h.N;
+    a.partials = h.lik_partials;
+    k_lik_partial<<<dim3(chunks, S), kLikThreads, 0, h.stream>>>(a, src);
+    k_lik_final<<<(S + 127) / 128, 128, 0, h.stream>>>(h.lik_partials, chunks, S, h.obs.n_pet,
+                                                       h.obs.pet_sigma2, out_device);
+    h.launches += 2;
+    GBG_CUDA_TRY(cudaGetLastError());
+    return GBG_OK;
+}
+
+}  // namespace
+
+int lik_set_observations(Handle &h, const double *pet, const double *t1, const double *t2,
+                         const double *points, long npoints, const gbg_lik_params &p) {
+    const int n = h.n;
+    if (p.step_pet <= 0 || p.step_ti <= 0 || !(p.pet_sigma2 > 0) || !(p.slope > 0)) {
+        set_error("likelihood parameters out of range");
+        return GBG_ERR_ARG;
+    }
+    std::vector<int> pet_idx, ti_idx;
+    std::vector<double> pet_val, v1, v2;
+    for (int iz = 0; iz < n; iz++)
+        for (int iy = 0; iy < n; iy++)
+            for (int ix = 0; ix < n; ix++)
+                if ((ix % p.step_pet == 0) && (iy % p.step_pet == 0) && (iz % p.step_pet == 0)) {
+                    const size_t g = (size_t)ix + (size_t)n * ((size_t)iy + (size_t)n * iz);
+                    if (pet[g] > 0.) {
+                        pet_idx.push_back((int)g);
+                        pet_val.push_back(pet[g]);
+                    }
+                }
+    if (p.selective) {
+        for (long i = 0; i < npoints; i++) {
+            // Points(i,0..2) read as int as the reference does (:113-115)
+            const int ix = (int)points[i], iy = (int)points[i + npoints], iz = (int)points[i + 2 * npoints];
+            if (ix < 0 || iy < 0 || iz < 0 || ix >= n || iy >= n || iz >= n) {
+                set_error("point outside the grid");
+                return GBG_ERR_ARG;
+            }
+            if ((ix % p.step_ti == 0) && (iy % p.step_ti == 0) && (iz % p.step_ti == 0)) {
+                const size_t g = (size_t)ix + (size_t)n * ((size_t)iy + (size_t)n * iz);
+                ti_idx.push_back((int)g);
+                v1.push_back(t1[g]);
+                v2.push_back(t2[g]);
+            }
+        }
+    } else {
+        for (size_t g = 0; g < h.N; ++g) {
+            ti_idx.push_back((int)g);
+            v1.push_back(t1[g]);
+            v2.push_back(t2[g]);
+        }
+    }
+    ObsDevice &o = h.obs;
+    o.valid = false;
+    int rc;
+    if ((rc = upload(&o.pet_idx, pet_idx)) || (rc = upload(&o.pet_val, pet_val)) ||
+        (rc = upload(&o.ti_idx, ti_idx)) || (rc = upload(&o.t1_val, v1)) || (rc = upload(&o.t2_val, v2)))
+        return rc;
+    o.n_pet = (int)pet_idx.size();
+    o.n_ti = (int)ti_idx.size();
+    o.pet_sigma2 = p.pet_sigma2;
+    o.pet_scale = p.pet_scale;
+    o.t1_uc = p.t1_uc;
+    o.t2_uc = p.t2_uc;
+    o.slope = p.slope;
+    o.valid = true;
+    return GBG_OK;
+}
+
+int lik_evaluate(Handle &h, const float *phi_f32, const double *phi_f64, int S,
+                 gbg_lik_result *out_device) {
+    PhiSource src{phi_f32, phi_f32, phi_f64, nullptr};
+    return run_lik(h, src, S, out_device);
+}
+
+int lik_evaluate_population(Handle &h, const float *buf0, const float *buf1,
+                            const SampleRec *recs_unsorted, int S, gbg_lik_result *out_device) {
+    PhiSource src{buf0, buf1, nullptr, recs_unsorted};
+    return run_lik(h, src, S, out_device);
+}
+
+}  // namespace gbg

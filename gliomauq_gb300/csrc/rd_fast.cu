@@ -1,0 +1,449 @@
+// Fast FP32 path and the batched population solver.
+//
+// Arithmetic (float storage, float math, FMA allowed):
+//   k_c   = (p_w + r p_g) / (p_w + p_g)          unit diffusivity, r = Dg/Dw
+//   c_f   = 2 k_c k_n / (k_c + k_n)              face coefficient (harmonic mean),
+//                                                 precomputed per face in double
+//   phi' = phi + a * sum_f c_f (phi_f - phi) + b * phi (1 - phi)
+//          with a = dt * Dw / h^2 and b = dt * rho, clamped to [0, 1]
+//   cells that are not tissue, or that touch a non-tissue face neighbour,
+//   are set to 0 (mask = 0)
+// This is the reference's Case2 operator (source/Glioma/Glioma_ReactionDiffusionOperator.h:174-216)
+// written with Dw factored out of the face diffusivities, the flux sum written
+// as sum c_f (phi_f - phi), and its boundary behaviour stated as a mask: in
+// the reference a tissue cell with a face neighbour of zero tissue fraction
+// gets df = 0/0 = NaN, hence phi = max(0, NaN) = 0 every step, and a
+// non-tissue cell stays at 0.
+//
+// Data layout in HBM: one n^3 float field per sample, x fastest, samples
+// contiguous (sample s at s*n^3); coefficient fields cx, cy, cz (face to the
+// +x/+y/+z neighbour) and the mask as four n^3 float arrays shared by every
+// sample.
+//
+// Thread mapping: a warp segment of n/4 lanes covers one x-row, each lane
+// four consecutive cells (float4); x-neighbours across lanes come by shuffle
+// within the segment, which also wraps the periodic x boundary. A 256-thread
+// CTA covers 256/(n/4) rows in y and marches TZ planes in z, keeping the
+// z-1, z, z+1 planes of its cells in registers.
+//
+// The density buffers are rewritten inside one launch (they alternate between
+// input and output every round), so they are read with __ldcg (L2, coherent)
+// and never through the read-only path; the anatomy tables use __ldg.
+//
+// Population schedule: a persistent cooperative kernel advances every active
+// sample by one step per round, rounds separated by a bounded grid barrier.
+// Samples are ordered by step count, longest first, so the active samples of
+// round k are a prefix of that order.
+#include <vector>
+
+#include "gbg_internal.cuh"
+
+namespace gbg {
+
+namespace {
+
+__device__ __forceinline__ int wrapm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+__device__ __forceinline__ int wrapp(int i, int n) { return i == n - 1 ? 0 : i + 1; }
+
+__global__ void k_fast_tables(int n, const double *__restrict__ pw, const double *__restrict__ pg,
+                              double ratio, float *__restrict__ cx, float *__restrict__ cy,
+                              float *__restrict__ cz, float *__restrict__ msk) {
+    const size_t N = (size_t)n * n * n;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
+         c += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        const size_t nn = n;
+        const size_t nb[7] = {c,
+                              c - x + wrapp(x, n),
+                              c + ((size_t)wrapp(y, n) - y) * nn,
+                              c + ((size_t)wrapp(z, n) - z) * nn * nn,
+                              c - x + wrapm(x, n),
+                              c + ((size_t)wrapm(y, n) - y) * nn,
+                              c + ((size_t)wrapm(z, n) - z) * nn * nn};
+        double k[4];
+        bool all = true;
+        for (int i = 0; i < 7; ++i) {
+            const double b = pw[nb[i]] + pg[nb[i]];
+            all = all && (b > 0.0);
+            if (i < 4) k[i] = b > 0.0 ? (pw[nb[i]] + ratio * pg[nb[i]]) / b : 0.0;
+        }
+        float *dst[3] = {cx, cy, cz};
+        for (int f = 0; f < 3; ++f) {
+            const double s = k[0] + k[f + 1];
+            dst[f][c] = (k[0] > 0.0 && k[f + 1] > 0.0 && s > 0.0) ? (float)(2.0 * k[0] * k[f + 1] / s) : 0.0f;
+        }
+        msk[c] = all ? 1.0f : 0.0f;
+    }
+}
+
+// Reference time loop per sample (Glioma_HG_UQ.cpp:532-552): Dw /= L^2;
+// Dg = 0.1 Dw; dt = 0.99 h^2 / (6 max(Dw, Dg)); steps while t <= tend.
+// f32 rounds Dw and Dg to float as the default build does. Explicit _rn
+// intrinsics keep every operation rounded on its own.
+__global__ void k_schedule(const gbg_sample *__restrict__ smp, int S, int n, double L, int f32,
+                           SampleRec *__restrict__ unsorted) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const double h = __ddiv_rn(1.0, (double)n);
+    double Dw, Dg, rho;
+    if (f32) {
+        const float dwf = (float)__ddiv_rn((double)(float)smp[s].Dw, __dmul_rn(L, L));
+        const float dgf = (float)__dmul_rn(0.1, (double)dwf);
+        Dw = dwf;
+        Dg = dgf;
+        rho = (double)(float)smp[s].rho;
+    } else {
+        Dw = __ddiv_rn(smp[s].Dw, __dmul_rn(L, L));
+        Dg = __dmul_rn(0.1, Dw);
+        rho = smp[s].rho;
+    }
+    const double mx = Dw >= Dg ? Dw : Dg;
+    const double dt = __ddiv_rn(__dmul_rn(__dmul_rn(0.99, h), h), __dmul_rn(__dmul_rn(2., 3.), mx));
+    int k = 0;
+    double t = 0.0;
+    const double tend = smp[s].tend;
+    // bounded: at most 10^8 steps per sample
+    while (t <= tend && k < 100000000) {
+        t = __dadd_rn(t, dt);
+        ++k;
+    }
+    const double ih2 = __ddiv_rn(1., __dmul_rn(h, h));
+    SampleRec r;
+    r.a = (float)(dt * Dw * ih2);
+    r.b = (float)(dt * rho);
+    r.nsteps = k;
+    r.order = s;
+    r.dt = dt;
+    unsorted[s] = r;
+}
+
+// Stable rank by nsteps descending; S is small (<= a few thousand).
+__global__ void k_sort_schedule(const SampleRec *__restrict__ unsorted, int S,
+                                SampleRec *__restrict__ sorted, int *__restrict__ rank_of) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int ks = unsorted[s].nsteps;
+    int r = 0;
+    for (int j = 0; j < S; ++j) {
+        const int kj = unsorted[j].nsteps;
+        r += (kj > ks) || (kj == ks && j < s);
+    }
+    sorted[r] = unsorted[s];
+    rank_of[s] = r;
+}
+
+__global__ void k_gaussian_ic(int n, const gbg_sample *__restrict__ smp, int S, double peak,
+                              double sigma, const float *__restrict__ msk_tissue,
+                              const double *__restrict__ pw, const double *__restrict__ pg,
+                              float *__restrict__ phi) {
+    const size_t N = (size_t)n * n * n;
+    const size_t total = N * S;
+    const double two_s2 = __dmul_rn(__dmul_rn(2.0, sigma), sigma);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = i / N, c = i % N;
+        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        float v = 0.0f;
+        if (pw[c] + pg[c] > 0.0) {
+            // d2 and the exponent rounded operation by operation (no FMA), as
+            // peak * exp(-d2 / (2 sigma^2)) evaluates in plain double arithmetic
+            const double dx = x - smp[s].x0, dy = y - smp[s].y0, dz = z - smp[s].z0;
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            v = (float)__dmul_rn(peak, exp(__ddiv_rn(-d2, two_s2)));
+        }
+        phi[i] = v;
+    }
+}
+
+// Bounded grid barrier for the cooperative persistent kernel. Returns false
+// (and records DEV_BARRIER_TIMEOUT) if the other CTAs do not arrive within
+// the spin limit; the caller then leaves the kernel.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *status, unsigned nblocks) {
+    __syncthreads();
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u);
+        int good = 1;
+        if (arrived == nblocks - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == gen) {
+                __nanosleep(64);
+                if (++spins > (1ll << 25)) {  // ~ a few seconds
+                    atomicExch(status, (int)DEV_BARRIER_TIMEOUT);
+                    good = 0;
+                    break;
+                }
+                if ((spins & 1023) == 0 && *(volatile int *)status != DEV_OK) {
+                    good = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int LR>  // lanes per x-row = n/4
+__device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
+                                           const float *__restrict__ in, float *__restrict__ out,
+                                           const float *__restrict__ cx, const float *__restrict__ cy,
+                                           const float *__restrict__ cz, const float *__restrict__ msk,
+                                           float a, float b) {
+    const int lane = threadIdx.x & 31;
+    const int li = lane % LR;
+    const int y = ty0 + (int)(threadIdx.x / LR);
+    const int x0 = 4 * li;
+    const int ym = wrapm(y, n), yp = wrapp(y, n);
+    const size_t nn = n, plane = nn * nn;
+    auto at = [&](int yy, int zz) -> size_t { return (size_t)x0 + nn * (size_t)yy + plane * (size_t)zz; };
+    const int zs = wrapm(tz0, n);
+    float4 Pp = __ldcg(reinterpret_cast<const float4 *>(in + at(y, zs)));
+    float4 Pc = __ldcg(reinterpret_cast<const float4 *>(in + at(y, tz0)));
+    float4 CZp = __ldg(reinterpret_cast<const float4 *>(cz + at(y, zs)));
+    for (int dz = 0; dz < TZ; ++dz) {
+        const int z = tz0 + dz;
+        const int zn = wrapp(z, n);
+        const float4 Pn = __ldcg(reinterpret_cast<const float4 *>(in + at(y, zn)));
+        const float4 PS = __ldcg(reinterpret_cast<const float4 *>(in + at(ym, z)));
+        const float4 PN = __ldcg(reinterpret_cast<const float4 *>(in + at(yp, z)));
+        const float4 CX = __ldg(reinterpret_cast<const float4 *>(cx + at(y, z)));
+        const float4 CY = __ldg(reinterpret_cast<const float4 *>(cy + at(y, z)));
+        const float4 CYm = __ldg(reinterpret_cast<const float4 *>(cy + at(ym, z)));
+        const float4 CZ = __ldg(reinterpret_cast<const float4 *>(cz + at(y, z)));
+        const float4 M = __ldg(reinterpret_cast<const float4 *>(msk + at(y, z)));
+        const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
+        const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
+        const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
+        const float p[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
+        const float cxa[5] = {cxl, CX.x, CX.y, CX.z, CX.w};
+        const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
+        const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
+        const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
+        const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
+        const float m4[4] = {M.x, M.y, M.z, M.w};
+        float o[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float f0 = p[i + 1];
+            float lap = cxa[i] * (p[i] - f0);
+            lap = fmaf(cxa[i + 1], p[i + 2] - f0, lap);
+            lap = fmaf(cym4[i], ps[i] - f0, lap);
+            lap = fmaf(cy4[i], pn[i] - f0, lap);
+            lap = fmaf(czp4[i], pp[i] - f0, lap);
+            lap = fmaf(cz4[i], pq[i] - f0, lap);
+            float v = fmaf(a, lap, f0);
+            v = fmaf(b * f0, 1.0f - f0, v);
+            v = fminf(fmaxf(v, 0.0f), 1.0f);
+            o[i] = m4[i] != 0.0f ? v : 0.0f;
+        }
+        *reinterpret_cast<float4 *>(out + at(y, z)) = make_float4(o[0], o[1], o[2], o[3]);
+        Pp = Pc;
+        Pc = Pn;
+        CZp = CZ;
+    }
+}
+
+struct PopArgs {
+    int n, S, TZ, tiles_y, tiles;  // tiles per sample = tiles_y * (n / TZ)
+    size_t stride;                 // cells per sample field
+    float *buf0, *buf1;
+    const float *cx, *cy, *cz, *msk;
+    const SampleRec *rec;          // sorted by nsteps descending
+    unsigned *barrier;
+    int *status;
+};
+
+template <int LR>
+__global__ void __launch_bounds__(256) k_population(PopArgs p) {
+    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
+    int active = p.S;
+    const int rows = 256 / LR;
+    for (int k = 0; k < maxsteps; ++k) {
+        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
+        const float *in = (k & 1) ? p.buf1 : p.buf0;
+        float *out = (k & 1) ? p.buf0 : p.buf1;
+        const long items = (long)active * p.tiles;
+        for (long it = blockIdx.x; it < items; it += gridDim.x) {
+            const int r = (int)(it / p.tiles), t = (int)(it % p.tiles);
+            const int ty = t % p.tiles_y, tz = t / p.tiles_y;
+            const size_t off = (size_t)p.rec[r].order * p.stride;
+            march_tile<LR>(p.n, p.TZ, ty * rows, tz * p.TZ, in + off, out + off, p.cx, p.cy, p.cz,
+                           p.msk, p.rec[r].a, p.rec[r].b);
+        }
+        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
+    }
+}
+
+int grid_for(const Handle &h, size_t work) {
+    const size_t blocks = (work + 255) / 256;
+    const size_t cap = (size_t)h.num_sms * 8;
+    return (int)(blocks < cap ? blocks : cap);
+}
+
+// Lanes per row for the supported fast-path sizes.
+int lanes_per_row(int n) {
+    if (n == 32 || n == 64 || n == 128) return n / 4;
+    return 0;
+}
+
+template <int LR>
+int launch_population_t(Handle &h, PopArgs &a) {
+    static int cached_blocks_per_sm = -1;
+    if (cached_blocks_per_sm < 0) {
+        int bps = 0;
+        GBG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_population<LR>, 256, 0));
+        cached_blocks_per_sm = bps;
+    }
+    if (cached_blocks_per_sm <= 0) {
+        set_error("population kernel cannot be resident");
+        return GBG_ERR_CUDA;
+    }
+    const long maxitems = (long)a.S * a.tiles;
+    long grid = (long)cached_blocks_per_sm * h.num_sms;
+    if (grid > maxitems) grid = maxitems;
+    if (grid < 1) grid = 1;
+    GBG_CUDA_TRY(cudaMemsetAsync(a.barrier, 0, sizeof(unsigned), h.stream));
+    void *args[] = {&a};
+    GBG_CUDA_TRY(cudaEventRecord(h.ev_pop[0], h.stream));
+    GBG_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_population<LR>, dim3((unsigned)grid),
+                                             dim3(256), args, 0, h.stream));
+    GBG_CUDA_TRY(cudaEventRecord(h.ev_pop[1], h.stream));
+    h.ev_pop_recorded = true;
+    h.launches++;
+    return GBG_OK;
+}
+
+int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_sorted, int S) {
+    const int LR = lanes_per_row(h.n);
+    if (!LR) {
+        set_error("fast path supports n = 32, 64 or 128");
+        return GBG_ERR_UNSUPPORTED;
+    }
+    PopArgs a;
+    a.n = h.n;
+    a.S = S;
+    a.TZ = h.n >= 64 ? 16 : 8;
+    const int rows = 256 / LR;
+    a.tiles_y = h.n / rows;
+    a.tiles = a.tiles_y * (h.n / a.TZ);
+    a.stride = h.N;
+    a.buf0 = buf0;
+    a.buf1 = buf1;
+    a.cx = h.cx;
+    a.cy = h.cy;
+    a.cz = h.cz;
+    a.msk = h.msk;
+    a.rec = rec_sorted;
+    a.barrier = h.barrier;
+    a.status = h.dev_status;
+    switch (LR) {
+        case 8: return launch_population_t<8>(h, a);
+        case 16: return launch_population_t<16>(h, a);
+        case 32: return launch_population_t<32>(h, a);
+    }
+    return GBG_ERR_UNSUPPORTED;
+}
+
+}  // namespace
+
+int check_device_status(Handle &h) {
+    int st = 0;
+    GBG_CUDA_TRY(cudaMemcpyAsync(&st, h.dev_status, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    if (st != DEV_OK) {
+        const int zero = 0;
+        cudaMemcpy(h.dev_status, &zero, sizeof(int), cudaMemcpyHostToDevice);
+        set_error("device-side grid barrier timed out");
+        return GBG_ERR_TIMEOUT;
+    }
+    return GBG_OK;
+}
+
+int fast_build_tables(Handle &h, double ratio) {
+    if (h.fast_valid && h.fast_ratio == ratio) return GBG_OK;
+    k_fast_tables<<<grid_for(h, h.N), 256, 0, h.stream>>>(h.n, h.pw, h.pg, ratio, h.cx, h.cy,
+                                                           h.cz, h.msk);
+    h.launches++;
+    GBG_CUDA_TRY(cudaGetLastError());
+    h.fast_ratio = ratio;
+    h.fast_valid = true;
+    return GBG_OK;
+}
+
+// Single solve on the fast path: a one-sample population.
+int fast_steps_single(Handle &h, double Dw, double rho, double dt, long nsteps) {
+    if (nsteps <= 0) return GBG_OK;
+    if (nsteps > 100000000L) {
+        set_error("nsteps too large");
+        return GBG_ERR_ARG;
+    }
+    const double hh = 1.0 / h.n;
+    SampleRec r;
+    r.a = (float)(dt * Dw * (1. / (hh * hh)));
+    r.b = (float)(dt * rho);
+    r.nsteps = (int)nsteps;
+    r.order = 0;
+    r.dt = dt;
+    SampleRec *d_rec = reinterpret_cast<SampleRec *>(h.bwork);
+    GBG_CUDA_TRY(cudaMemcpyAsync(d_rec, &r, sizeof(r), cudaMemcpyHostToDevice, h.stream));
+    int rc = launch_population(h, (float *)h.phi[h.cur], (float *)h.phi[h.cur ^ 1], d_rec, 1);
+    if (rc) return rc;
+    rc = check_device_status(h);
+    if (rc) return rc;
+    h.cur ^= (int)(nsteps & 1);
+    return GBG_OK;
+}
+
+int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
+                       const gbg_batch_opts &o, gbg_lik_result *loglik_device, long *nsteps_host) {
+    if (S <= 0 || S > h.max_samples) {
+        set_error("S out of range (1..max_samples)");
+        return GBG_ERR_ARG;
+    }
+    const bool f32ref = h.prec == GBG_PREC_F32REF;
+    SampleRec *unsorted = batch_unsorted(h);
+    SampleRec *sorted = batch_sorted(h);
+    int *rank_of = batch_rank_of(h);
+    k_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(samples_device, S, h.n, o.L, f32ref ? 1 : 0,
+                                                      unsorted);
+    k_sort_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(unsorted, S, sorted, rank_of);
+    k_gaussian_ic<<<grid_for(h, h.N * S), 256, 0, h.stream>>>(h.n, samples_device, S, o.ic_peak,
+                                                               o.ic_sigma, h.msk, h.pw, h.pg,
+                                                               h.bphi[0]);
+    h.launches += 3;
+    GBG_CUDA_TRY(cudaGetLastError());
+    if (f32ref) {
+        set_error("the batched solver runs on the fast path (GBG_PREC_F32) only");
+        return GBG_ERR_UNSUPPORTED;
+    }
+    int rc = fast_build_tables(h, (double)0.1f);
+    if (rc) return rc;
+    rc = launch_population(h, h.bphi[0], h.bphi[1], sorted, S);
+    if (rc) return rc;
+    if (o.with_loglik && loglik_device) {
+        // final field of sample s sits in buffer (nsteps_s & 1); the likelihood
+        // kernel resolves that per sample through the unsorted records.
+        rc = lik_evaluate_population(h, h.bphi[0], h.bphi[1], unsorted, S, loglik_device);
+        if (rc) return rc;
+    }
+    if (nsteps_host) {
+        std::vector<SampleRec> tmp(S);
+        GBG_CUDA_TRY(cudaMemcpyAsync(tmp.data(), unsorted, sizeof(SampleRec) * S,
+                                     cudaMemcpyDeviceToHost, h.stream));
+        GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        for (int s = 0; s < S; ++s) nsteps_host[s] = tmp[s].nsteps;
+    }
+    return GBG_OK;
+}
+
+}  // namespace gbg

@@ -1,0 +1,171 @@
+/* gbglioma -- GB300-native Fisher-Kolmogorov tumour-growth step and imaging
+ * log-likelihood for GliomaUQ, behind a plain C ABI.
+ *
+ * Conventions
+ *  - Every function returns int status: GBG_OK (0) or a negative GBG_ERR_*.
+ *    gbg_last_error() gives a one-line message for the calling thread's last
+ *    failure.
+ *  - Fields are cubic grids of n^3 cells, x fastest: cell (x, y, z) is at
+ *    x + n*(y + n*z) -- the order of Matrix::D3D (source/Glioma/Matrix.h:593-602).
+ *    The domain is the unit cube, periodic in x, y and z
+ *    (source/MRAGcore/MRAGrid.inl:37-39), cell size h = 1/n.
+ *  - Host pointers unless a name ends in _device. The caller owns host arrays;
+ *    the library owns its device memory.
+ *  - A handle owns one CUDA stream. A handle is not thread-safe; different
+ *    handles may be used from different threads at once.
+ *  - There is no CPU fallback: without a usable GPU, gbg_create fails.
+ */
+#ifndef GBGLIOMA_H
+#define GBGLIOMA_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBG_VERSION_MAJOR 0
+#define GBG_VERSION_MINOR 1
+
+enum gbg_status {
+    GBG_OK = 0,
+    GBG_ERR_ARG = -1,         /* bad argument (null pointer, size, range) */
+    GBG_ERR_CUDA = -2,        /* a CUDA runtime call failed */
+    GBG_ERR_TIMEOUT = -3,     /* a bounded device-side wait ran out */
+    GBG_ERR_NONFINITE = -4,   /* NaN/Inf in an input that must be finite */
+    GBG_ERR_STATE = -5,       /* call out of order (e.g. step before anatomy) */
+    GBG_ERR_NOMEM = -6,       /* device allocation failed */
+    GBG_ERR_UNSUPPORTED = -7  /* configuration not supported by this build */
+};
+
+/* Arithmetic of the step.
+ *  GBG_PREC_F64    : the reference built with -D_MRAG_REAL_=double: double
+ *                    storage and arithmetic, every operation rounded as the
+ *                    reference's source writes it (bit-identical results).
+ *  GBG_PREC_F32REF : the reference's default build (Real=float,
+ *                    source/MRAGcore/MRAGCommon.h:43-48): float storage and
+ *                    Dw/Dg/rho, double per-cell temporaries, dphidt rounded to
+ *                    float (bit-identical results).
+ *  GBG_PREC_F32    : fast path: float storage and float arithmetic with the
+ *                    face diffusivities precomputed; its error against the
+ *                    FP64 result is measured and stated, not zero. */
+enum gbg_precision { GBG_PREC_F64 = 0, GBG_PREC_F32REF = 1, GBG_PREC_F32 = 2 };
+
+typedef struct gbg_handle gbg_handle;
+
+typedef struct {
+    int n;           /* cells per side (n >= 4) */
+    int precision;   /* enum gbg_precision */
+    int device;      /* CUDA device ordinal */
+    int max_samples; /* capacity of the batched population (0: no batch buffers) */
+} gbg_config;
+
+/* ---- lifetime ------------------------------------------------------------ */
+int gbg_create(const gbg_config *cfg, gbg_handle **out);
+int gbg_destroy(gbg_handle *h);
+const char *gbg_last_error(void);
+int gbg_version(int *major, int *minor);
+
+/* ---- anatomy and state ----------------------------------------------------
+ * gbg_set_anatomy replaces the p_w/p_g fields of every cell (the block fields
+ * of CCell_extended, source/Glioma/Glioma_Types.h:27-28) and invalidates the
+ * precomputed face diffusivities. Values must be finite. */
+int gbg_set_anatomy(gbg_handle *h, const double *p_w, const double *p_g);
+/* density field phi (CCell_extended::phi), n^3 doubles, converted to the
+ * storage type (rounded to float in the float modes). */
+int gbg_set_phi(gbg_handle *h, const double *phi);
+int gbg_get_phi(gbg_handle *h, double *phi);
+
+/* ---- the step ---------------------------------------------------------------
+ * nsteps fused steps of Glioma_ReactionDiffusionOperator<3> (Case2 branch,
+ * source/Glioma/Glioma_ReactionDiffusionOperator.h:148-218) followed by
+ * UpdateTumor<3> (:254-261), on the uniform periodic grid. Replaces one call of
+ * Glioma_HG_UQ::_reactionDiffusionStep (source/Glioma/Glioma_HG_UQ.cpp:266-277),
+ * i.e. BlockProcessing::pipeline_process(rhs) + BlockProcessing::process(update)
+ * per step. Dw, Dg are the operator's arguments (already divided by L^2), rho
+ * in 1/day, dt in days. In the float modes Dw, Dg and rho are rounded to float
+ * as the reference's Real-typed operator members are. */
+int gbg_rd_step(gbg_handle *h, double Dw, double Dg, double rho, double dt, long nsteps);
+
+/* The whole time loop of Glioma_HG_UQ::run for a uniform grid
+ * (source/Glioma/Glioma_HG_UQ.cpp:519-552): Dw_file in cm^2/day and rho in 1/day
+ * as read from HGG_InputParameters.txt, tend in days, L the brain length in cm
+ * (Glioma_HG_UQ.cpp:104). Computes Dw = Dw_file/L^2, Dg = 0.1*Dw,
+ * dt = 0.99*h^2/(6*max(Dw,Dg)) with the reference's rounding, then steps while
+ * t <= tend. Writes the step count and dt if the pointers are non-null. */
+int gbg_run(gbg_handle *h, double Dw_file, double rho, double tend, double L, long *nsteps_out,
+            double *dt_out);
+
+/* ---- imaging log-likelihood (source/Likelihood/source/HGG_Likelihood.cpp) --
+ * Observations: PET, T1, T2 fields (n^3 doubles each, PET_data.dat,
+ * T1_data.dat, T2_data.dat) and the Sphere.dat point set, npoints x 3 voxel
+ * indices stored column-major as Matrix::D2D stores them (all x, then all y,
+ * then all z). selective!=0 evaluates the T1/T2 terms on those points
+ * (HGG_Likelihood.cpp:105-124), otherwise on every voxel (:97-104). */
+typedef struct {
+    double pet_sigma2, pet_scale, t1_uc, t2_uc, slope; /* LikelihoodInput.txt order */
+    int step_pet, step_ti, selective;                  /* -stepPet, -stepTi, -selectivePoints */
+} gbg_lik_params;
+
+typedef struct {
+    double l_pet, l_t1, l_t2; /* the three partial log-likelihoods */
+    double total;             /* log L = l_pet + l_t1 + l_t2; Likelihood.txt holds -total */
+    long n_pet;               /* PET voxels used */
+} gbg_lik_result;
+
+int gbg_set_observations(gbg_handle *h, const double *pet, const double *t1, const double *t2,
+                         const double *points, long npoints, const gbg_lik_params *p);
+/* log-likelihood of the handle's current phi (HGG_Likelihood::run, :173-189),
+ * accumulated in double. */
+int gbg_loglik(gbg_handle *h, gbg_lik_result *out);
+
+/* ---- batched population ----------------------------------------------------
+ * S independent forward solves sharing the handle's anatomy, each from a
+ * Gaussian initial density phi0 = peak*exp(-|x-x0|^2/(2 sigma^2)) (voxel
+ * units) on tissue cells, each with its own parameters and step count (the
+ * reference's time loop per sample), followed by each sample's
+ * log-likelihood against the handle's observations. The unit of work of the
+ * external sampler's one `brain` + `likelihood` process pair per sample. */
+typedef struct {
+    double Dw;   /* cm^2/day, as in HGG_InputParameters.txt */
+    double rho;  /* 1/day */
+    double x0, y0, z0; /* seed, voxel units (cell centre of voxel i is i) */
+    double tend; /* days */
+} gbg_sample;
+
+typedef struct {
+    double L;          /* brain length in cm (n*0.1 for 1 mm voxels) */
+    double ic_peak;    /* initial peak density */
+    double ic_sigma;   /* initial width in voxels */
+    int with_loglik;   /* evaluate the likelihood per sample */
+} gbg_batch_opts;
+
+/* Host entry: copies the S samples in, solves, copies loglik (S results, may
+ * be null when with_loglik==0) and per-sample step counts (may be null) out.
+ * phi_out, if non-null, receives S*n^3 floats of final densities. Float
+ * modes only (GBG_PREC_F32 or GBG_PREC_F32REF). */
+int gbg_batch_solve(gbg_handle *h, const gbg_sample *samples, int S, const gbg_batch_opts *o,
+                    gbg_lik_result *loglik, long *nsteps_out, float *phi_out);
+/* Device-resident entry: samples_device (S gbg_sample) and loglik_device (S
+ * gbg_lik_result, or null) are device pointers; runs on the handle's stream
+ * and returns without synchronising. */
+int gbg_batch_solve_device(gbg_handle *h, const gbg_sample *samples_device, int S,
+                           const gbg_batch_opts *o, gbg_lik_result *loglik_device);
+
+/* ---- introspection ---------------------------------------------------------- */
+/* number of kernels this handle has launched since creation */
+int gbg_launch_count(gbg_handle *h, long long *count);
+/* the handle's CUDA stream (a cudaStream_t) */
+int gbg_stream(gbg_handle *h, void **stream);
+/* synchronise the handle's stream */
+int gbg_sync(gbg_handle *h);
+/* device time in milliseconds of the handle's most recent population-kernel
+ * launch (the persistent step kernel of gbg_batch_solve* and of the fast
+ * single solve), measured with CUDA events around that launch on the handle's
+ * stream; waits for it to finish. */
+int gbg_last_population_ms(gbg_handle *h, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,131 @@
+"""Generates the golden fixtures in this folder from the reference itself.
+
+Runs the GliomaUQ sources compiled in place by oracle/Makefile (oracle/_ref/:
+the MRAG grid + TBB pipeline + Glioma operators through oracle/ref_harness.cpp,
+and the reference's own `likelihood` program) on seeded synthetic inputs, and
+stores inputs and outputs as small .npz/.json files. Inputs are rounded to
+float32 values so that they are exact in both the FP32 and the FP64 build and
+independent of the platform that regenerates them.
+
+Usage (needs /root/reference and `make -C oracle ref`):
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from gliomauq_gb300 import matrix_io, synthetic as S  # noqa: E402
+from oracle import refio  # noqa: E402
+
+LIK_PARAMS = (0.0025, 1.0, 0.7, 0.25, 0.09)  # sigma2_PET, PETscale, T1uc, T2uc, slope
+
+
+def f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
+def inputs(n, seed, seed_xyz):
+    an = S.make_anatomy(n, seed=seed)
+    pw, pg = f32(an.p_w), f32(an.p_g)
+    an32 = S.Anatomy(n=n, p_w=pw, p_g=pg, psi=an.psi)
+    phi0 = f32(S.gaussian_ic(an32, *seed_xyz))
+    return pw, pg, phi0
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def rd_fixtures():
+    # 32^3 (2^3 blocks): snapshots after 1, 10 and 60 steps, FP64 and FP32 builds
+    n, bpd = 32, 2
+    pw, pg, phi0 = inputs(n, 3, (14.6, 16.3, 15.2))
+    Dw, rho, L = 0.13 / 100, 0.025, n * 0.1
+    out = dict(p_w=pw.astype(np.float32), p_g=pg.astype(np.float32),
+               phi0=phi0.astype(np.float32), Dw_file=Dw, rho=rho, L=L)
+    for variant in ("f64", "f32"):
+        for k in (1, 10, 60):
+            r = refio.run_harness("solve", variant, n, bpd, pw, pg, phi0, Dw, rho, 0.0, L, nsteps=k)
+            out[f"phi_{variant}_{k}"] = r["phi"] if variant == "f64" else r["phi"].astype(np.float32)
+            out[f"dt_{variant}"] = r["dt"]
+            out[f"Dw_{variant}"] = r["Dw"]
+            out[f"Dg_{variant}"] = r["Dg"]
+    np.savez_compressed(os.path.join(HERE, "rd32.npz"), **out)
+
+    # config 1: 64^3 (4^3 blocks), Dw = 0.13 mm^2/day, rho = 0.025/day, T = 300 days
+    n, bpd = 64, 4
+    pw, pg, phi0 = inputs(n, 1, (30.2, 33.7, 31.1))
+    np.savez_compressed(os.path.join(HERE, "anatomy64.npz"), p_w=pw.astype(np.float32),
+                        p_g=pg.astype(np.float32), phi0=phi0.astype(np.float32))
+    meta = dict(n=n, Dw_file=0.13 / 100, rho=0.025, tend=300.0, L=n * 0.1)
+    for variant in ("f64", "f32"):
+        r = refio.run_harness("solve", variant, n, bpd, pw, pg, phi0, meta["Dw_file"], meta["rho"],
+                              meta["tend"], meta["L"])
+        u = r["phi"]
+        meta[variant] = dict(steps=r["steps"], dt=r["dt"], sha256=sha(u), sum=float(u.sum()),
+                             l2=float(np.linalg.norm(u)), max=float(u.max()))
+        if variant == "f64":
+            # a sparse sample of the field for readable failures
+            rng = np.random.default_rng(0)
+            idx = rng.choice(u.size, 256, replace=False)
+            meta["sample_idx"] = idx.tolist()
+            meta["sample_f64"] = u.ravel()[idx].tolist()
+    with open(os.path.join(HERE, "c1_64.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
+def lik_fixture():
+    """The reference `likelihood` program on a 32^3 model and seeded observations."""
+    d = np.load(os.path.join(HERE, "rd32.npz"))
+    model = d["phi_f64_60"]
+    n = model.shape[0]
+    an = S.Anatomy(n=n, p_w=d["p_w"].astype(np.float64), p_g=d["p_g"].astype(np.float64),
+                   psi=None)
+    # truth: the model itself a few steps later is not needed; use a shifted copy
+    truth = np.roll(model, 1, axis=2)
+    obs = S.make_observations(truth, an, seed=11, centre_xyz=(15.0, 16.0, 15.0), radius_vox=9.0)
+    pet, t1, t2 = f32(obs.pet), obs.t1, obs.t2
+    res = {}
+    exe = os.path.join(refio.REF_DIR, "likelihood")
+    for mode in ("sel", "all"):
+        with tempfile.TemporaryDirectory() as td:
+            matrix_io.write_d3d(os.path.join(td, "HGG_data.dat"), model)
+            matrix_io.write_d3d(os.path.join(td, "PET_data.dat"), pet)
+            matrix_io.write_d3d(os.path.join(td, "T1_data.dat"), t1)
+            matrix_io.write_d3d(os.path.join(td, "T2_data.dat"), t2)
+            matrix_io.write_d2d(os.path.join(td, "Sphere.dat"), obs.points.T)
+            with open(os.path.join(td, "LikelihoodInput.txt"), "w") as f:
+                f.write("\n".join(repr(x) for x in LIK_PARAMS) + "\n")
+            args = [exe, "-selectivePoints", "1" if mode == "sel" else "0", "-stepPet", "2",
+                    "-stepTi", "1"]
+            p = subprocess.run(args, cwd=td, capture_output=True, text=True, check=True)
+            m = re.search(r"L_Pet=([-\d.]+), L_T1=([-\d.]+), L_T2 = ([-\d.]+)", p.stdout)
+            npet = int(re.search(r"Points=(\d+)", p.stdout).group(1))
+            txt = float(open(os.path.join(td, "Likelihood.txt")).read().split()[0])
+            res[mode] = dict(l_pet=float(m.group(1)), l_t1=float(m.group(2)),
+                             l_t2=float(m.group(3)), minus_loglik=txt, n_pet=npet)
+    np.savez_compressed(os.path.join(HERE, "lik32.npz"), model=model, pet=pet.astype(np.float32),
+                        t1=t1.astype(np.uint8), t2=t2.astype(np.uint8),
+                        points=obs.points.astype(np.int16))
+    res.update(params=LIK_PARAMS, step_pet=2, step_ti=1)
+    with open(os.path.join(HERE, "lik32.json"), "w") as f:
+        json.dump(res, f, indent=1)
+
+
+if __name__ == "__main__":
+    rd_fixtures()
+    lik_fixture()
+    for f in sorted(os.listdir(HERE)):
+        print(f, os.path.getsize(os.path.join(HERE, f)))

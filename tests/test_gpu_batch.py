@@ -1,0 +1,101 @@
+"""GPU: the batched population solver (persistent cooperative kernel) through
+the C ABI: per-sample results equal the single-solve fast path bitwise, step
+counts follow the reference's time loop, densities stay within the stated
+error of the FP64 oracle, and the per-sample likelihood matches the oracle."""
+import numpy as np
+import pytest
+
+from gliomauq_gb300 import _lib, synthetic as S
+from helpers import golden_npz, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+F32_REL_L2_TOL = 1e-5
+LIK = (0.0025, 1.0, 0.7, 0.25, 0.09)
+
+
+def _setup(n=32, seed=4):
+    an = S.make_anatomy(n, seed=seed)
+    samples = [S.SampleParams(Dw=0.0013, rho=0.025, x0=15.2, y0=16.1, z0=15.7, T=60.0),
+               S.SampleParams(Dw=0.0025, rho=0.2, x0=14.0, y0=15.0, z0=16.0, T=25.0),
+               S.SampleParams(Dw=0.0002, rho=0.01, x0=16.4, y0=16.6, z0=14.9, T=130.0)]
+    return an, samples
+
+
+def test_batch_equals_single_solve_bitwise(gbg):
+    an, samples = _setup()
+    n = an.n
+    with _lib.Handle(n, "f32", max_samples=len(samples)) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        ic = h.batch_solve([s.as_tuple()[:5] + (-1.0,) for s in samples], an.L,
+                           with_loglik=False, want_phi=True)
+        assert np.all(ic["nsteps"] == 0)
+        res = h.batch_solve([s.as_tuple() for s in samples], an.L, with_loglik=False,
+                            want_phi=True)
+    for i, s in enumerate(samples):
+        dt, dw, dg = S.reference_dt(n, s.Dw, an.L)
+        assert res["nsteps"][i] == S.num_steps(dt, s.T)
+        with _lib.Handle(n, "f32") as h1:
+            h1.set_anatomy(an.p_w, an.p_g)
+            h1.set_phi(ic["phi"][i].astype(np.float64))
+            h1.rd_step(dw, dg, s.rho, dt, int(res["nsteps"][i]))
+            single = h1.get_phi()
+        assert np.array_equal(single, res["phi"][i].astype(np.float64)), i
+
+
+def test_batch_initial_condition(gbg):
+    an, samples = _setup()
+    with _lib.Handle(an.n, "f32", max_samples=3) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        ic = h.batch_solve([s.as_tuple()[:5] + (-1.0,) for s in samples], an.L,
+                           with_loglik=False, want_phi=True)
+    for i, s in enumerate(samples):
+        exp = S.gaussian_ic(an, s.x0, s.y0, s.z0).astype(np.float32)
+        d = np.abs(ic["phi"][i] - exp)
+        assert d.max() <= np.spacing(np.float32(0.1)), d.max()
+
+
+def test_batch_vs_fp64_oracle_and_loglik(gbg, oracle_lib):
+    an, samples = _setup()
+    n = an.n
+    truth = S.gaussian_ic(an, 15.0, 16.0, 15.0) * 5
+    obs = S.make_observations(np.clip(truth, 0, 1), an, seed=3, centre_xyz=(15, 16, 15),
+                              radius_vox=9.0)
+    with _lib.Handle(n, "f32", max_samples=3) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2)
+        res = h.batch_solve([s.as_tuple() for s in samples], an.L, with_loglik=True,
+                            want_phi=True)
+    for i, s in enumerate(samples):
+        dt, dw, dg = S.reference_dt(n, s.Dw, an.L)
+        phi0 = S.gaussian_ic(an, s.x0, s.y0, s.z0).astype(np.float32).astype(np.float64)
+        ref = oracle_lib.rd_solve(an.p_w, an.p_g, phi0, dw, dg, s.rho, dt, int(res["nsteps"][i]))
+        err = rel_l2(res["phi"][i], ref)
+        print(f"sample {i}: steps {res['nsteps'][i]} rel L2 vs FP64 = {err:.3e}")
+        assert err <= F32_REL_L2_TOL
+        model = res["phi"][i].astype(np.float64)
+        o = oracle_lib.loglik(model, obs.pet, obs.t1, obs.t2, obs.points, LIK, 3, 2, True)
+        g = res["loglik"][i]
+        assert g["n_pet"] == o["n_pet"]
+        for k in ("l_pet", "l_t1", "l_t2", "total"):
+            assert abs(g[k] - o[k]) <= 1e-11 * max(1.0, abs(o[k]))
+
+
+def test_batch_argument_errors(gbg):
+    an, samples = _setup()
+    with _lib.Handle(an.n, "f32", max_samples=2) as h:
+        with pytest.raises(_lib.GbgError) as e:
+            h.batch_solve([s.as_tuple() for s in samples[:2]], an.L, with_loglik=False)
+        assert e.value.status == -5  # anatomy not set
+        h.set_anatomy(an.p_w, an.p_g)
+        with pytest.raises(_lib.GbgError) as e:
+            h.batch_solve([s.as_tuple() for s in samples], an.L, with_loglik=False)  # S > max
+        assert e.value.status == -1
+        bad = list(samples[0].as_tuple())
+        bad[0] = float("nan")
+        with pytest.raises(_lib.GbgError) as e:
+            h.batch_solve([tuple(bad)], an.L, with_loglik=False)
+        assert e.value.status == -4
+        with pytest.raises(_lib.GbgError) as e:
+            h.batch_solve([samples[0].as_tuple()], an.L, with_loglik=True)  # no observations
+        assert e.value.status == -5

@@ -1,0 +1,135 @@
+"""CPU: the oracle restatement against the reference's own outputs (golden
+fixtures made by tests/golden/make_golden.py from oracle/_ref) and host logic."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from gliomauq_gb300 import matrix_io, synthetic as S
+from helpers import boundary_layer, golden_json, golden_npz
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("k", [1, 10, 60])
+def test_oracle_f64_matches_reference_bitwise(oracle_lib, k):
+    d = golden_npz("rd32.npz")
+    pw, pg, phi0 = (d[x].astype(np.float64) for x in ("p_w", "p_g", "phi0"))
+    out = oracle_lib.rd_solve(pw, pg, phi0, float(d["Dw_f64"]), float(d["Dg_f64"]),
+                              float(d["rho"]), float(d["dt_f64"]), k, prec="f64")
+    assert np.array_equal(out, d[f"phi_f64_{k}"])
+
+
+@pytest.mark.parametrize("k", [1, 10, 60])
+def test_oracle_f32ref_matches_reference_bitwise(oracle_lib, k):
+    d = golden_npz("rd32.npz")
+    pw, pg, phi0 = (d[x] for x in ("p_w", "p_g", "phi0"))
+    out = oracle_lib.rd_solve(pw, pg, phi0, float(d["Dw_f32"]), float(d["Dg_f32"]),
+                              float(d["rho"]), float(d["dt_f32"]), k, prec="f32ref")
+    assert np.array_equal(out, d[f"phi_f32_{k}"])
+
+
+@pytest.mark.parametrize("variant", ["f64", "f32"])
+def test_oracle_config1_full_solve(oracle_lib, variant):
+    meta = golden_json("c1_64.json")
+    a = golden_npz("anatomy64.npz")
+    f32 = variant == "f32"
+    dt, dw, dg = S.reference_dt(meta["n"], meta["Dw_file"], meta["L"], f32=f32)
+    assert dt == meta[variant]["dt"]
+    ns = S.num_steps(dt, meta["tend"])
+    assert ns == meta[variant]["steps"] == 237
+    out = oracle_lib.rd_solve(a["p_w"], a["p_g"], a["phi0"], dw, dg, meta["rho"], dt, ns,
+                              prec="f32ref" if f32 else "f64")
+    assert _sha(out.astype(np.float64)) == meta[variant]["sha256"]
+
+
+def test_blocklab_port_matches_reference(oracle_lib):
+    d = golden_npz("rd32.npz")
+    g = oracle_lib.BlockGrid(d["p_w"], d["p_g"], d["phi0"])
+    g.steps(float(d["Dw_f32"]), float(d["Dg_f32"]), float(d["rho"]), float(d["dt_f32"]), 10)
+    assert np.array_equal(g.phi(), d["phi_f32_10"])
+
+
+def test_boundary_layer_is_pinned_in_reference_output():
+    d = golden_npz("rd32.npz")
+    brain = (d["p_w"].astype(np.float64) + d["p_g"]) > 0
+    layer = boundary_layer(brain)
+    assert layer.sum() > 0
+    for k in (1, 10, 60):
+        u = d[f"phi_f64_{k}"]
+        assert np.all(u[layer] == 0.0)
+        assert np.all(u[~brain] == 0.0)
+        assert not np.isnan(u).any()
+
+
+@pytest.mark.parametrize("mode", ["sel", "all"])
+def test_oracle_likelihood_matches_reference_program(oracle_lib, mode):
+    d = golden_npz("lik32.npz")
+    ref = golden_json("lik32.json")
+    r = oracle_lib.loglik(d["model"], d["pet"], d["t1"], d["t2"], d["points"],
+                          ref["params"], step_pet=ref["step_pet"], step_ti=ref["step_ti"],
+                          selective=(mode == "sel"))
+    exp = ref[mode]
+    # the reference prints %Lf: six decimals
+    assert r["n_pet"] == exp["n_pet"]
+    assert abs(r["l_pet"] - exp["l_pet"]) <= 1e-6
+    assert abs(r["l_t1"] - exp["l_t1"]) <= 1e-6
+    assert abs(r["l_t2"] - exp["l_t2"]) <= 1e-6
+    assert abs(-r["total"] - exp["minus_loglik"]) <= 1e-6
+
+
+def test_num_steps_matches_oracle(oracle_lib):
+    for dt, tend in [(1.2692307692307696, 300.0), (0.66, 100.0), (8.25, 500.0), (1.0, 3.0),
+                     (0.1, 0.0), (1.0, -1.0)]:
+        assert S.num_steps(dt, tend) == oracle_lib.lib().orc_num_steps(dt, tend)
+
+
+def test_matrix_io_roundtrip_and_errors(tmp_path):
+    a = np.random.default_rng(0).random((3, 4, 5))
+    p = tmp_path / "a.dat"
+    matrix_io.write_d3d(str(p), a)
+    assert np.array_equal(matrix_io.read_d3d(str(p)), a)
+    b = np.arange(12.0).reshape(3, 4)
+    q = tmp_path / "b.dat"
+    matrix_io.write_d2d(str(q), b)
+    assert np.array_equal(matrix_io.read_d2d(str(q)), b)
+    raw = bytearray(open(p, "rb").read())
+    raw[0] = 0
+    (tmp_path / "bad.dat").write_bytes(bytes(raw))
+    with pytest.raises(matrix_io.MatrixFormatError):
+        matrix_io.read_d3d(str(tmp_path / "bad.dat"))
+    (tmp_path / "short.dat").write_bytes(open(p, "rb").read()[:40])
+    with pytest.raises(matrix_io.MatrixFormatError):
+        matrix_io.read_d3d(str(tmp_path / "short.dat"))
+    with pytest.raises(matrix_io.MatrixFormatError):
+        matrix_io.read_d2d(str(p))  # a 3-D file read as 2-D
+
+
+def test_reference_sphere_file_format_reads():
+    """The reference's own Sphere.dat (D2D<double> 80160 x 3) parses, when present."""
+    path = "/root/reference/source/Likelihood/makefile/Sphere.dat"
+    if not os.path.exists(path):
+        pytest.skip("reference tree not present")
+    m = matrix_io.read_d2d(path)
+    assert m.shape == (3, 80160)
+    assert m[0].min() >= 0 and m.max() < 128
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle",
+                                                    "_ref", "ref_harness_f64")),
+                    reason="reference binaries not built here")
+def test_oracle_live_vs_reference_random_case(oracle_lib):
+    from oracle import refio
+    rng = np.random.default_rng(123)
+    n = 32
+    an = S.make_anatomy(n, seed=77)
+    pw = an.p_w.astype(np.float32).astype(np.float64)
+    pg = an.p_g.astype(np.float32).astype(np.float64)
+    phi0 = (rng.random((n, n, n)) * (pw + pg > 0)).astype(np.float32).astype(np.float64)
+    Dw, rho = 0.002, 0.15
+    r = refio.run_harness("solve", "f64", n, 2, pw, pg, phi0, Dw, rho, 0.0, n * 0.1, nsteps=5)
+    out = oracle_lib.rd_solve(pw, pg, phi0, r["Dw"], r["Dg"], r["rho"], r["dt"], 5, prec="f64")
+    assert np.array_equal(out, r["phi"])
