@@ -44,6 +44,11 @@ LIK = (0.0025, 1.0, 0.7, 0.25, 0.09)
 METRIC = "forward solves/s at 128^3 (batched population of 512, with log-likelihood)"
 
 
+def set_population(samples):
+    global S
+    S = samples
+
+
 def rank_info():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
             int(os.environ.get("WORLD_SIZE", "1")))
@@ -184,9 +189,12 @@ def main():
     ap.add_argument("--impl", default="gbglioma", choices=["gbglioma", "reference"])
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--samples", type=int, default=S,
+                    help="population size (profiling runs use a smaller one)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    set_population(args.samples)
 
     import torch
     import torch.distributed as dist
