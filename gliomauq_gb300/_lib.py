@@ -25,7 +25,7 @@ EXPORTS = [
     "gbg_create", "gbg_destroy", "gbg_last_error", "gbg_version", "gbg_set_anatomy",
     "gbg_set_phi", "gbg_get_phi", "gbg_rd_step", "gbg_run", "gbg_set_observations",
     "gbg_loglik", "gbg_batch_solve", "gbg_batch_solve_device", "gbg_launch_count",
-    "gbg_stream", "gbg_sync", "gbg_last_population_ms",
+    "gbg_stream", "gbg_sync", "gbg_last_population_ms", "gbg_loglik_noalloc",
 ]
 
 
@@ -96,6 +96,8 @@ def load(path: str = LIB_PATH):
         "gbg_stream": [vp, C.POINTER(vp)],
         "gbg_sync": [vp],
         "gbg_last_population_ms": [vp, C.POINTER(C.c_float)],
+        "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
+                               C.POINTER(LikParams), vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -14,6 +14,7 @@
 //
 // Compiled with -fmad=false: (u - scale*PET)^2 and the exponent round as the
 // reference's plain double expressions do.
+#include <mutex>
 #include <vector>
 
 #include "gbg_internal.cuh"
@@ -249,3 +250,90 @@ int lik_evaluate_population(Handle &h, const float *buf0, const float *buf1,
 }
 
 }  // namespace gbg
+
+// ---- gbg_loglik_noalloc: the same reduction with library-owned scratch ------
+// Callers that cannot allocate device memory (graph capture in progress, an
+// external allocator owning the device, a fixed real-time budget) get this
+// variant: its partial sums live in a fixed file-scope device array instead of
+// a handle's buffer, so the entry point allocates nothing. The array is shared
+// by every call; each call overwrites every partial it later reads, so nothing
+// needs clearing, but overlapping calls race.
+namespace {
+
+constexpr long kNoAllocMaxChunks = 4096;
+static_assert(GBG_NOALLOC_MAX_ENTRIES == kNoAllocMaxChunks * gbg::kLikChunk,
+              "header limit and scratch size disagree");
+
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxChunks * 3];
+
+// Device address of g_noalloc_partials per device ordinal, looked up once per
+// device with that device current (a host-side name of a __device__ array is
+// not a device address).
+constexpr int kMaxDevices = 64;
+double *g_noalloc_ptr[kMaxDevices] = {};
+std::mutex g_noalloc_mu;
+
+int noalloc_scratch(double **out) {
+    int dev = -1;
+    GBG_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        gbg::set_error("device ordinal beyond the no-alloc scratch table");
+        return GBG_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        GBG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_partials));
+        g_noalloc_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return GBG_OK;
+}
+
+}  // namespace
+
+extern "C" int gbg_loglik_noalloc(const float *phi_device, int n, const int *pet_idx,
+                                  const double *pet_val, long n_pet, const int *ti_idx,
+                                  const double *t1_val, const double *t2_val, long n_ti,
+                                  const gbg_lik_params *p, gbg_lik_result *out_device,
+                                  void *stream) {
+    using namespace gbg;
+    if (!phi_device || !p || !out_device || n < 1 || n_pet < 0 || n_ti < 0 ||
+        (n_pet > 0 && (!pet_idx || !pet_val)) || (n_ti > 0 && (!ti_idx || !t1_val || !t2_val))) {
+        set_error("gbg_loglik_noalloc: bad argument");
+        return GBG_ERR_ARG;
+    }
+    if (n_pet > GBG_NOALLOC_MAX_ENTRIES || n_ti > GBG_NOALLOC_MAX_ENTRIES) {
+        set_error("gbg_loglik_noalloc: list longer than GBG_NOALLOC_MAX_ENTRIES");
+        return GBG_ERR_ARG;
+    }
+    if (!(p->pet_sigma2 > 0) || !(p->slope > 0)) {
+        set_error("gbg_loglik_noalloc: likelihood parameters out of range");
+        return GBG_ERR_ARG;
+    }
+    double *scratch = nullptr;
+    if (int rc = noalloc_scratch(&scratch)) return rc;
+    const long items = n_pet > n_ti ? n_pet : n_ti;
+    const int chunks = items > 0 ? (int)((items + kLikChunk - 1) / kLikChunk) : 1;
+    LikArgs a;
+    a.n_pet = (int)n_pet;
+    a.n_ti = (int)n_ti;
+    a.chunks = chunks;
+    a.pet_idx = pet_idx;
+    a.pet_val = pet_val;
+    a.ti_idx = ti_idx;
+    a.t1_val = t1_val;
+    a.t2_val = t2_val;
+    a.pet_scale = p->pet_scale;
+    a.t1_uc = p->t1_uc;
+    a.t2_uc = p->t2_uc;
+    a.is2 = 1. / p->slope;
+    a.stride = (size_t)n * n * n;
+    a.partials = scratch;
+    PhiSource src{phi_device, phi_device, nullptr, nullptr};
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    k_lik_partial<<<dim3(chunks, 1), kLikThreads, 0, st>>>(a, src);
+    k_lik_final<<<1, 128, 0, st>>>(scratch, chunks, 1, (int)n_pet, p->pet_sigma2, out_device);
+    GBG_CUDA_TRY(cudaGetLastError());
+    return GBG_OK;
+}

@@ -165,6 +165,40 @@ int gbg_sync(gbg_handle *h);
  * stream; waits for it to finish. */
 int gbg_last_population_ms(gbg_handle *h, float *ms);
 
+/* ---- log-likelihood without any allocation -----------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory -- code running while a CUDA graph is being
+ * captured, a host framework whose device memory is owned by its own
+ * allocator, or a real-time loop with a fixed memory budget. It evaluates the
+ * same log-likelihood as gbg_loglik for one density field, without a handle,
+ * and calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * The caller passes everything in device memory: the field phi_device (n^3
+ * floats, x fastest) and the compact observation lists that
+ * gbg_set_observations builds internally --
+ *   pet_idx/pet_val  : cell index and PET value of every voxel with
+ *                      ix,iy,iz = 0 mod stepPet and PET > 0 (n_pet entries)
+ *   ti_idx/t1_val/t2_val : cell index and T1/T2 value of every evaluation
+ *                      point (n_ti entries)
+ * -- the scalar parameters in p (its step/selective fields are not used: the
+ * lists already encode them), and out_device, one gbg_lik_result.
+ * stream is a cudaStream_t (null: the legacy default stream); the call only
+ * enqueues work and does not synchronise.
+ *
+ * Its scratch is a fixed device array inside the library (3 doubles per chunk
+ * of 2048 list entries, at most GBG_NOALLOC_MAX_ENTRIES entries, 96 KiB),
+ * which every GPU that loads the library keeps until the process exits. The
+ * first call on a device looks that array's address up with that device
+ * current, so make the first call before any stream capture. Every call
+ * shares the array: calls whose kernels may overlap on the GPU (different
+ * streams, or different host threads) race and must be serialised by the
+ * caller. Lists longer than the maximum are rejected with GBG_ERR_ARG. */
+#define GBG_NOALLOC_MAX_ENTRIES (4096L * 2048L)
+int gbg_loglik_noalloc(const float *phi_device, int n, const int *pet_idx, const double *pet_val,
+                       long n_pet, const int *ti_idx, const double *t1_val, const double *t2_val,
+                       long n_ti, const gbg_lik_params *p, gbg_lik_result *out_device,
+                       void *stream);
+
 #ifdef __cplusplus
 }
 #endif
