@@ -210,6 +210,10 @@ def main():
     per_solve, steps_list = mean_cell_steps(an, prior)
     h = _lib.Handle(N, "f32", device=local_rank, max_samples=S)
     h.set_anatomy(an.p_w, an.p_g)
+    tune_cache = os.path.join(ROOT, "gliomauq_gb300", "_build", "tune.json")
+    os.makedirs(os.path.dirname(tune_cache), exist_ok=True)
+    variant = h.autotune(probe_samples=min(S, 64), cache_path=tune_cache)
+    shape = h.population_variants()[variant]
     obs = observations(h, an, truth)
     h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2,
                        selective=True)
@@ -286,10 +290,14 @@ def main():
                                    "+ per-sample log-likelihood",
                        "n": N, "samples_per_gpu": S, "mean_steps_per_solve": per_solve / N ** 3,
                        "cell_steps_per_step": cell_steps, "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (population state 8.6 GB per GPU)"},
+                       "l2": "inputs larger than L2 (population state 8.6 GB per GPU)",
+                       "population_kernel_shape": {"rows_per_tile": shape[0],
+                                                   "samples_per_cta": shape[1],
+                                                   "threads": shape[2],
+                                                   "chosen_by": "gbg_autotune"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
-                         "kernel": "k_population", "kernel_ms": kern_ms,
+                         "kernel": "k_population2", "kernel_ms": kern_ms,
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "peak_source": f"{peak_kind} hbm_gbs"},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 48 * S,

@@ -26,6 +26,8 @@ EXPORTS = [
     "gbg_set_phi", "gbg_get_phi", "gbg_rd_step", "gbg_run", "gbg_set_observations",
     "gbg_loglik", "gbg_batch_solve", "gbg_batch_solve_device", "gbg_launch_count",
     "gbg_stream", "gbg_sync", "gbg_last_population_ms", "gbg_loglik_noalloc",
+    "gbg_population_variants", "gbg_set_population_variant", "gbg_population_variant_shape",
+    "gbg_autotune",
 ]
 
 
@@ -96,6 +98,11 @@ def load(path: str = LIB_PATH):
         "gbg_stream": [vp, C.POINTER(vp)],
         "gbg_sync": [vp],
         "gbg_last_population_ms": [vp, C.POINTER(C.c_float)],
+        "gbg_population_variants": [vp, C.POINTER(C.c_int)],
+        "gbg_set_population_variant": [vp, C.c_int],
+        "gbg_population_variant_shape": [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int)],
+        "gbg_autotune": [vp, C.c_int, C.c_char_p, C.POINTER(C.c_int)],
         "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
                                C.POINTER(LikParams), vp, vp],
     }
@@ -237,6 +244,27 @@ class Handle:
 
     def sync(self):
         check(self.lib.gbg_sync(self._h))
+
+    def population_variants(self) -> list[tuple[int, int, int]]:
+        """(rows per tile, samples per CTA, threads) of every population-kernel shape."""
+        c = C.c_int()
+        check(self.lib.gbg_population_variants(self._h, C.byref(c)))
+        out = []
+        for i in range(c.value):
+            r, g, t = C.c_int(), C.c_int(), C.c_int()
+            check(self.lib.gbg_population_variant_shape(self._h, i, C.byref(r), C.byref(g),
+                                                        C.byref(t)))
+            out.append((r.value, g.value, t.value))
+        return out
+
+    def set_population_variant(self, index: int):
+        check(self.lib.gbg_set_population_variant(self._h, index))
+
+    def autotune(self, probe_samples: int = 32, cache_path: str | None = None) -> int:
+        c = C.c_int()
+        check(self.lib.gbg_autotune(self._h, probe_samples,
+                                    cache_path.encode() if cache_path else None, C.byref(c)))
+        return c.value
 
     def last_population_ms(self) -> float:
         ms = C.c_float()

@@ -2,7 +2,12 @@
 // upload/download, and the entry points that replace the reference's block
 // processing of the RD step, its time loop and its likelihood.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
 #include <vector>
 
 #include "gbg_internal.cuh"
@@ -448,6 +453,154 @@ int gbg_last_population_ms(gbg_handle *hh, float *ms) {
     GBG_CUDA_TRY(cudaSetDevice(h.device));
     GBG_CUDA_TRY(cudaEventSynchronize(h.ev_pop[1]));
     GBG_CUDA_TRY(cudaEventElapsedTime(ms, h.ev_pop[0], h.ev_pop[1]));
+    return GBG_OK;
+}
+
+int gbg_population_variants(gbg_handle *hh, int *count) {
+    if (int rc = check_handle(hh)) return rc;
+    if (!count) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    *count = gbg::population_variant_count(hh->h.n);
+    return GBG_OK;
+}
+
+int gbg_set_population_variant(gbg_handle *hh, int index) {
+    if (int rc = check_handle(hh)) return rc;
+    if (index < 0 || index >= gbg::population_variant_count(hh->h.n)) {
+        set_error("variant index out of range");
+        return GBG_ERR_ARG;
+    }
+    hh->h.pop_variant = index;
+    return GBG_OK;
+}
+
+int gbg_population_variant_shape(gbg_handle *hh, int index, int *rows, int *samples_per_cta,
+                                 int *threads) {
+    if (int rc = check_handle(hh)) return rc;
+    if (!rows || !samples_per_cta || !threads) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    if (gbg::population_variant_shape(hh->h.n, index, rows, samples_per_cta, threads) != GBG_OK) {
+        set_error("variant index out of range");
+        return GBG_ERR_ARG;
+    }
+    return GBG_OK;
+}
+
+namespace {
+
+// The tuning cache is a flat JSON object {"key": index, ...}.
+std::map<std::string, int> read_tune_cache(const char *path) {
+    std::map<std::string, int> m;
+    std::ifstream f(path);
+    if (!f) return m;
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string t = ss.str();
+    size_t i = 0;
+    while ((i = t.find('"', i)) != std::string::npos) {
+        const size_t j = t.find('"', i + 1);
+        if (j == std::string::npos) break;
+        const std::string key = t.substr(i + 1, j - i - 1);
+        const size_t c = t.find(':', j);
+        if (c == std::string::npos) break;
+        m[key] = std::atoi(t.c_str() + c + 1);
+        i = t.find_first_of(",}", c);
+        if (i == std::string::npos) break;
+    }
+    return m;
+}
+
+void write_tune_cache(const char *path, const std::map<std::string, int> &m) {
+    FILE *f = std::fopen(path, "w");
+    if (!f) return;
+    std::fprintf(f, "{");
+    bool first = true;
+    for (const auto &kv : m) {
+        std::fprintf(f, "%s\n \"%s\": %d", first ? "" : ",", kv.first.c_str(), kv.second);
+        first = false;
+    }
+    std::fprintf(f, "\n}\n");
+    std::fclose(f);
+}
+
+}  // namespace
+
+int gbg_autotune(gbg_handle *hh, int probe_samples, const char *cache_path, int *chosen) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!chosen || probe_samples < 1 || probe_samples > h.max_samples) {
+        set_error("bad autotune arguments (1 <= probe_samples <= max_samples)");
+        return GBG_ERR_ARG;
+    }
+    if (h.prec != GBG_PREC_F32) {
+        set_error("autotune applies to GBG_PREC_F32");
+        return GBG_ERR_UNSUPPORTED;
+    }
+    if (!h.anatomy_set) {
+        set_error("anatomy not set");
+        return GBG_ERR_STATE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    cudaDeviceProp prop;
+    GBG_CUDA_TRY(cudaGetDeviceProperties(&prop, h.device));
+    int bucket = 1;
+    while (bucket < h.max_samples) bucket <<= 1;
+    char key[512];
+    std::snprintf(key, sizeof(key), "%s|n=%d|S<=%d|f32", prop.name, h.n, bucket);
+    std::map<std::string, int> cache;
+    const int nv = gbg::population_variant_count(h.n);
+    if (cache_path) {
+        cache = read_tune_cache(cache_path);
+        auto it = cache.find(key);
+        if (it != cache.end() && it->second >= 0 && it->second < nv) {
+            h.pop_variant = it->second;
+            *chosen = it->second;
+            return GBG_OK;
+        }
+    }
+    // probe: samples near the centre, about 24 steps each
+    std::vector<gbg_sample> probe(probe_samples);
+    const double L = h.n * 0.1, c = 0.5 * (h.n - 1);
+    for (int i = 0; i < probe_samples; ++i) {
+        const double Dw = 0.0013;
+        double dt, Dwu, Dgu, r = 0.05;
+        gbg::reference_dt(h.n, Dw, L, false, &dt, &Dwu, &Dgu, &r);
+        probe[i] = gbg_sample{Dw, 0.05, c + (i % 3) - 1.0, c, c + (i % 5) - 2.0, 23.5 * dt};
+    }
+    gbg_batch_opts o{L, 0.1, 1.0, 0};
+    int best = 0;
+    float best_ms = 1e30f;
+    const int saved = h.pop_variant;
+    for (int v = 0; v < nv; ++v) {
+        h.pop_variant = v;
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {
+            int rc = gbg_batch_solve(hh, probe.data(), probe_samples, &o, nullptr, nullptr, nullptr);
+            if (rc) {
+                h.pop_variant = saved;
+                return rc;
+            }
+            rc = gbg_last_population_ms(hh, &ms);
+            if (rc) {
+                h.pop_variant = saved;
+                return rc;
+            }
+        }
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = v;
+        }
+    }
+    h.pop_variant = best;
+    *chosen = best;
+    if (cache_path) {
+        cache[key] = best;
+        write_tune_cache(cache_path, cache);
+    }
     return GBG_OK;
 }
 

@@ -74,6 +74,9 @@ struct Handle {
     int *dev_status = nullptr;            // device status word
     unsigned *barrier = nullptr;          // grid barrier {count, generation}
 
+    // population-kernel shape (index into the candidates for this n; 0 = default)
+    int pop_variant = 0;
+
     // events bracketing the latest population-kernel launch
     cudaEvent_t ev_pop[2] = {nullptr, nullptr};
     bool ev_pop_recorded = false;
@@ -121,6 +124,8 @@ inline gbg_sample *batch_samples(Handle &h) {
 }
 int fast_build_tables(Handle &h, double ratio);
 int fast_steps_single(Handle &h, double Dw, double rho, double dt, long nsteps);
+int population_variant_count(int n);
+int population_variant_shape(int n, int vi, int *ry, int *g, int *threads);
 // reads and clears the device status word (synchronises the stream)
 int check_device_status(Handle &h);
 int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,

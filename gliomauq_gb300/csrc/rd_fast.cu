@@ -149,7 +149,10 @@ __global__ void k_gaussian_ic(int n, const gbg_sample *__restrict__ smp, int S, 
             // peak * exp(-d2 / (2 sigma^2)) evaluates in plain double arithmetic
             const double dx = x - smp[s].x0, dy = y - smp[s].y0, dz = z - smp[s].z0;
             const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-            v = (float)__dmul_rn(peak, exp(__ddiv_rn(-d2, two_s2)));
+            const double e = __ddiv_rn(-d2, two_s2);
+            // below -745 exp underflows to 0; below -110 peak*exp(e) <= 1e-47
+            // rounds to float 0 for any peak <= 1e+0: skip the FP64 exp there
+            if (e > -110.0 || peak > 1.0) v = (float)__dmul_rn(peak, exp(e));
         }
         phi[i] = v;
     }
@@ -193,6 +196,28 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *status, unsigne
     return ok != 0;
 }
 
+struct PopArgs {
+    int n, S, TZ, tiles_y, tiles;  // tiles per sample = tiles_y * (n / TZ)
+    size_t stride;                 // cells per sample field
+    float *buf0, *buf1;
+    const float *cx, *cy, *cz, *msk;
+    const SampleRec *rec;          // sorted by nsteps descending
+    unsigned *barrier;
+    int *status;
+};
+
+__device__ __forceinline__ void cp_async16(float *smem_dst, const float *gmem_src) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Population kernel, register variant: a thread marches TZ planes keeping
+// the z-1, z, z+1 planes of its four cells in registers; the y-neighbour
+// rows and the anatomy come through L2 (density, __ldcg) and L1 (anatomy,
+// __ldg).
 template <int LR>  // lanes per x-row = n/4
 __device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
                                            const float *__restrict__ in, float *__restrict__ out,
@@ -253,18 +278,8 @@ __device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
     }
 }
 
-struct PopArgs {
-    int n, S, TZ, tiles_y, tiles;  // tiles per sample = tiles_y * (n / TZ)
-    size_t stride;                 // cells per sample field
-    float *buf0, *buf1;
-    const float *cx, *cy, *cz, *msk;
-    const SampleRec *rec;          // sorted by nsteps descending
-    unsigned *barrier;
-    int *status;
-};
-
-template <int LR>
-__global__ void __launch_bounds__(256) k_population(PopArgs p) {
+template <int LR, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_population1(PopArgs p) {
     const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
     int active = p.S;
     const int rows = 256 / LR;
@@ -284,6 +299,152 @@ __global__ void __launch_bounds__(256) k_population(PopArgs p) {
     }
 }
 
+
+// Population kernel.
+//   LR lanes per x-row (n = 4 LR), RY rows per sample slot, G sample slots per
+//   CTA (CTA = LR*RY*G threads). An item is one (y-tile, z-chunk of TZ planes)
+//   of up to G samples: the G slots run the same tile of G different samples.
+//   Everything the stencil reads is staged in shared memory by cp.async.cg two
+//   planes ahead of the plane being computed, in rings of 4 planes:
+//     density, per slot: rows y0-1 .. y0+RY (periodic), RY+2 rows
+//     anatomy, shared by the slots: cy rows y0-1 .. y0+RY-1, then cx, cz and
+//     the mask rows y0 .. y0+RY-1 (4 RY + 1 rows)
+//   cp.async.cg reads L2, which is coherent with the previous round's stores;
+//   the z-1 and z planes of a thread's own row are carried in registers.
+template <int LR, int RY, int G>
+__global__ void __launch_bounds__(LR *RY *G, (LR * RY * G >= 1024) ? 1 : 1024 / (LR * RY * G))
+    k_population3(PopArgs p) {
+    constexpr int n = 4 * LR;
+    constexpr int SLOT_T = LR * RY;       // threads per slot
+    constexpr int NT = SLOT_T * G;
+    constexpr int PROWS = RY + 2;
+    constexpr int PPLANE = PROWS * n;     // floats per staged density plane
+    constexpr int AROWS = 4 * RY + 1;
+    constexpr int APLANE = AROWS * n;     // floats per staged anatomy plane
+    constexpr int plane_sz = n * n;       // cell indices within a field fit in int (n <= 128)
+    extern __shared__ __align__(16) float smem[];
+    float *aring = smem;                                // [4][AROWS][n]
+    const int g = threadIdx.x / SLOT_T;
+    const int t = threadIdx.x % SLOT_T;
+    const int r = t / LR;
+    const int li = t % LR;
+    const int x0 = 4 * li;
+    float *pring = smem + 4 * APLANE + g * 4 * PPLANE;  // this slot's [4][PROWS][n]
+    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
+    int active = p.S;
+    for (int k = 0; k < maxsteps; ++k) {
+        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
+        const float *in = (k & 1) ? p.buf1 : p.buf0;
+        float *out = (k & 1) ? p.buf0 : p.buf1;
+        const int groups = (active + G - 1) / G;
+        const long items = (long)groups * p.tiles;
+        for (long it = blockIdx.x; it < items; it += gridDim.x) {
+            const int grp = (int)(it / p.tiles), tile = (int)(it % p.tiles);
+            const int y0 = (tile % p.tiles_y) * RY, z0 = (tile / p.tiles_y) * p.TZ;
+            const int rank = grp * G + g;
+            const bool valid = rank < active;
+            float a = 0.f, b = 0.f;
+            size_t off = 0;
+            if (valid) {
+                a = p.rec[rank].a;
+                b = p.rec[rank].b;
+                off = (size_t)p.rec[rank].order * p.stride;
+            }
+            const float *src = in + off;
+            auto stage = [&](int zz, int q) {
+                const int zw = (zz + n) % n;
+                float *ad = aring + q * APLANE;
+                for (int c = threadIdx.x; c < AROWS * LR; c += NT) {
+                    const int ar = c / LR, col = 4 * (c % LR);
+                    const float *base;
+                    int yy;
+                    if (ar < RY + 1) { base = p.cy; yy = y0 - 1 + ar; }
+                    else if (ar < 2 * RY + 1) { base = p.cx; yy = y0 + ar - (RY + 1); }
+                    else if (ar < 3 * RY + 1) { base = p.cz; yy = y0 + ar - (2 * RY + 1); }
+                    else { base = p.msk; yy = y0 + ar - (3 * RY + 1); }
+                    yy = (yy + n) % n;
+                    cp_async16(ad + ar * n + col, base + (yy * n + col + plane_sz * zw));
+                }
+                if (valid) {
+                    float *pd = pring + q * PPLANE;
+                    for (int c = t; c < PROWS * LR; c += SLOT_T) {
+                        const int row = c / LR, col = 4 * (c % LR);
+                        const int yw = (y0 - 1 + row + n) % n;
+                        cp_async16(pd + row * n + col, src + (yw * n + col + plane_sz * zw));
+                    }
+                }
+                cp_async_commit();
+            };
+            stage(z0 - 1, 0);
+            stage(z0, 1);
+            stage(z0 + 1, 2);
+            const int y = y0 + r;
+            float4 Pp, Pc, CZp;
+            for (int dz = 0; dz < p.TZ; ++dz) {
+                const int z = z0 + dz;
+                if (dz + 2 <= p.TZ) stage(z + 2, (dz + 3) & 3);
+                else cp_async_commit();
+                cp_async_wait<1>();
+                __syncthreads();
+                const float *A0 = aring + ((dz + 1) & 3) * APLANE;
+                if (dz == 0) {
+                    const float *Am = aring + (dz & 3) * APLANE;
+                    CZp = *reinterpret_cast<const float4 *>(Am + (2 * RY + 1 + r) * n + x0);
+                }
+                if (valid) {
+                    const float *Lp = pring + ((dz + 2) & 3) * PPLANE;   // z+1
+                    const float *L0 = pring + ((dz + 1) & 3) * PPLANE;   // z
+                    if (dz == 0) {
+                        Pp = *reinterpret_cast<const float4 *>(pring + (dz & 3) * PPLANE + (r + 1) * n + x0);
+                        Pc = *reinterpret_cast<const float4 *>(L0 + (r + 1) * n + x0);
+                    }
+                    const float4 Pn = *reinterpret_cast<const float4 *>(Lp + (r + 1) * n + x0);
+                    const float4 PS = *reinterpret_cast<const float4 *>(L0 + r * n + x0);
+                    const float4 PN = *reinterpret_cast<const float4 *>(L0 + (r + 2) * n + x0);
+                    const float4 CYm = *reinterpret_cast<const float4 *>(A0 + r * n + x0);
+                    const float4 CY = *reinterpret_cast<const float4 *>(A0 + (r + 1) * n + x0);
+                    const float4 CX = *reinterpret_cast<const float4 *>(A0 + (RY + 1 + r) * n + x0);
+                    const float4 CZ = *reinterpret_cast<const float4 *>(A0 + (2 * RY + 1 + r) * n + x0);
+                    const float4 M = *reinterpret_cast<const float4 *>(A0 + (3 * RY + 1 + r) * n + x0);
+                    const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
+                    const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
+                    const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
+                    const float pv[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
+                    const float cxa[5] = {cxl, CX.x, CX.y, CX.z, CX.w};
+                    const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
+                    const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
+                    const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
+                    const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
+                    const float m4[4] = {M.x, M.y, M.z, M.w};
+                    float o[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float f0 = pv[i + 1];
+                        float lap = cxa[i] * (pv[i] - f0);
+                        lap = fmaf(cxa[i + 1], pv[i + 2] - f0, lap);
+                        lap = fmaf(cym4[i], ps[i] - f0, lap);
+                        lap = fmaf(cy4[i], pn[i] - f0, lap);
+                        lap = fmaf(czp4[i], pp[i] - f0, lap);
+                        lap = fmaf(cz4[i], pq[i] - f0, lap);
+                        float v = fmaf(a, lap, f0);
+                        v = fmaf(b * f0, 1.0f - f0, v);
+                        v = fminf(fmaxf(v, 0.0f), 1.0f);
+                        o[i] = m4[i] != 0.0f ? v : 0.0f;
+                    }
+                    const int ci = x0 + n * y + plane_sz * z;
+                    __stcg(reinterpret_cast<float4 *>(out + off + ci), make_float4(o[0], o[1], o[2], o[3]));
+                    Pp = Pc;
+                    Pc = Pn;
+                    CZp = CZ;
+                }
+                __syncthreads();  // ring slot dz&3 is refilled next iteration
+            }
+            cp_async_wait<0>();
+        }
+        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
+    }
+}
+
 int grid_for(const Handle &h, size_t work) {
     const size_t blocks = (work + 255) / 256;
     const size_t cap = (size_t)h.num_sms * 8;
@@ -296,27 +457,91 @@ int lanes_per_row(int n) {
     return 0;
 }
 
-template <int LR>
-int launch_population_t(Handle &h, PopArgs &a) {
-    static int cached_blocks_per_sm = -1;
-    if (cached_blocks_per_sm < 0) {
-        int bps = 0;
-        GBG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_population<LR>, 256, 0));
-        cached_blocks_per_sm = bps;
+struct PopVariant {
+    const void *fn;
+    int ry, g, threads, tz;
+    size_t smem;
+};
+
+template <int LR, int MINB = 1>
+PopVariant make_register_variant(int tz) {
+    PopVariant v;
+    v.fn = (const void *)k_population1<LR, MINB>;
+    v.ry = 256 / LR;
+    v.g = 1;
+    v.threads = 256;
+    v.tz = tz;
+    v.smem = 0;
+    return v;
+}
+
+template <int LR, int RY, int G>
+PopVariant make_variant(int tz) {
+    PopVariant v;
+    v.fn = (const void *)k_population3<LR, RY, G>;
+    v.ry = RY;
+    v.g = G;
+    v.threads = LR * RY * G;
+    v.tz = tz;
+    const int n = 4 * LR;
+    v.smem = (size_t)(4 * (4 * RY + 1) * n + G * 4 * (RY + 2) * n) * sizeof(float);
+    return v;
+}
+
+// Candidate shapes per grid size; index 0 is the default.
+int variants_for(int n, PopVariant *out) {
+    int k = 0;
+    switch (n) {
+        case 128:
+            out[k++] = make_register_variant<32>(16);
+            out[k++] = make_register_variant<32>(32);
+            out[k++] = make_register_variant<32, 4>(16);
+            out[k++] = make_register_variant<32, 5>(16);
+            out[k++] = make_register_variant<32, 6>(16);
+            out[k++] = make_register_variant<32, 6>(32);
+            out[k++] = make_variant<32, 8, 2>(32);
+            out[k++] = make_variant<32, 8, 1>(32);
+            out[k++] = make_variant<32, 8, 2>(16);
+            out[k++] = make_variant<32, 4, 4>(32);
+            out[k++] = make_variant<32, 8, 1>(64);
+            out[k++] = make_variant<32, 4, 2>(32);
+            out[k++] = make_variant<32, 16, 1>(32);
+            break;
+        case 64:
+            out[k++] = make_register_variant<16>(16);
+            out[k++] = make_register_variant<16, 6>(16);
+            out[k++] = make_variant<16, 16, 2>(16);
+            out[k++] = make_variant<16, 16, 1>(16);
+            out[k++] = make_variant<16, 8, 2>(16);
+            out[k++] = make_variant<16, 8, 4>(32);
+            break;
+        case 32:
+            out[k++] = make_register_variant<8>(8);
+            out[k++] = make_variant<8, 32, 1>(8);
+            out[k++] = make_variant<8, 32, 2>(8);
+            out[k++] = make_variant<8, 16, 2>(16);
+            break;
     }
-    if (cached_blocks_per_sm <= 0) {
+    return k;
+}
+
+int launch_population_v(Handle &h, PopArgs &a, const PopVariant &v) {
+    GBG_CUDA_TRY(cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem));
+    int bps = 0;
+    GBG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, v.fn, v.threads, v.smem));
+    if (bps <= 0) {
         set_error("population kernel cannot be resident");
         return GBG_ERR_CUDA;
     }
-    const long maxitems = (long)a.S * a.tiles;
-    long grid = (long)cached_blocks_per_sm * h.num_sms;
+    const long maxitems = (long)((a.S + v.g - 1) / v.g) * a.tiles;
+    long grid = (long)bps * h.num_sms;
     if (grid > maxitems) grid = maxitems;
     if (grid < 1) grid = 1;
     GBG_CUDA_TRY(cudaMemsetAsync(a.barrier, 0, sizeof(unsigned), h.stream));
     void *args[] = {&a};
     GBG_CUDA_TRY(cudaEventRecord(h.ev_pop[0], h.stream));
-    GBG_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_population<LR>, dim3((unsigned)grid),
-                                             dim3(256), args, 0, h.stream));
+    GBG_CUDA_TRY(cudaLaunchCooperativeKernel(v.fn, dim3((unsigned)grid), dim3(v.threads), args, v.smem,
+                                             h.stream));
     GBG_CUDA_TRY(cudaEventRecord(h.ev_pop[1], h.stream));
     h.ev_pop_recorded = true;
     h.launches++;
@@ -329,12 +554,16 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
         set_error("fast path supports n = 32, 64 or 128");
         return GBG_ERR_UNSUPPORTED;
     }
+    PopVariant vs[16];
+    const int nv = variants_for(h.n, vs);
+    int vi = h.pop_variant;
+    if (vi < 0 || vi >= nv) vi = 0;
+    const PopVariant &v = vs[vi];
     PopArgs a;
     a.n = h.n;
     a.S = S;
-    a.TZ = h.n >= 64 ? 16 : 8;
-    const int rows = 256 / LR;
-    a.tiles_y = h.n / rows;
+    a.TZ = v.tz;
+    a.tiles_y = h.n / v.ry;
     a.tiles = a.tiles_y * (h.n / a.TZ);
     a.stride = h.N;
     a.buf0 = buf0;
@@ -346,15 +575,25 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
     a.rec = rec_sorted;
     a.barrier = h.barrier;
     a.status = h.dev_status;
-    switch (LR) {
-        case 8: return launch_population_t<8>(h, a);
-        case 16: return launch_population_t<16>(h, a);
-        case 32: return launch_population_t<32>(h, a);
-    }
-    return GBG_ERR_UNSUPPORTED;
+    return launch_population_v(h, a, v);
 }
 
 }  // namespace
+
+int population_variant_count(int n) {
+    PopVariant vs[16];
+    return variants_for(n, vs);
+}
+
+int population_variant_shape(int n, int vi, int *ry, int *g, int *threads) {
+    PopVariant vs[16];
+    const int nv = variants_for(n, vs);
+    if (vi < 0 || vi >= nv) return GBG_ERR_ARG;
+    *ry = vs[vi].ry;
+    *g = vs[vi].g;
+    *threads = vs[vi].threads;
+    return GBG_OK;
+}
 
 int check_device_status(Handle &h) {
     int st = 0;

@@ -165,6 +165,22 @@ int gbg_sync(gbg_handle *h);
  * stream; waits for it to finish. */
 int gbg_last_population_ms(gbg_handle *h, float *ms);
 
+/* ---- population-kernel shape and autotuner --------------------------------
+ * No counterpart in the reference (its TBB pipeline has a compile-time
+ * thread hint). The fast population kernel has several tile shapes per grid
+ * size (rows per tile x samples per CTA). gbg_population_variants reports
+ * how many; gbg_set_population_variant picks one by index (0 = default).
+ * gbg_autotune times every shape on a probe population of probe_samples
+ * samples (<= max_samples) over the handle's anatomy and keeps the fastest;
+ * with cache_path non-null it first looks the choice up in that JSON file,
+ * keyed by GPU name, n, population-size bucket and precision, and records
+ * new choices there. Writes the chosen index to *chosen. GBG_PREC_F32 only. */
+int gbg_population_variants(gbg_handle *h, int *count);
+int gbg_set_population_variant(gbg_handle *h, int index);
+int gbg_population_variant_shape(gbg_handle *h, int index, int *rows, int *samples_per_cta,
+                                 int *threads);
+int gbg_autotune(gbg_handle *h, int probe_samples, const char *cache_path, int *chosen);
+
 /* ---- log-likelihood without any allocation -----------------------------------
  * No counterpart in the reference: an addition for callers that cannot
  * allocate device memory -- code running while a CUDA graph is being

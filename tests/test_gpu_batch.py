@@ -99,3 +99,39 @@ def test_batch_argument_errors(gbg):
         with pytest.raises(_lib.GbgError) as e:
             h.batch_solve([samples[0].as_tuple()], an.L, with_loglik=True)  # no observations
         assert e.value.status == -5
+
+
+def test_every_population_shape_gives_identical_results(gbg):
+    """The per-cell arithmetic does not depend on the tile shape: all
+    population-kernel variants agree bitwise."""
+    an, samples = _setup(n=64, seed=6)
+    sm = [S.SampleParams(Dw=0.0013, rho=0.03, x0=30.2, y0=33.1, z0=31.5, T=40.0),
+          S.SampleParams(Dw=0.0021, rho=0.1, x0=28.0, y0=31.0, z0=33.0, T=25.0),
+          S.SampleParams(Dw=0.0009, rho=0.05, x0=33.4, y0=30.6, z0=29.9, T=60.0)]
+    with _lib.Handle(64, "f32", max_samples=3) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        shapes = h.population_variants()
+        assert len(shapes) >= 2
+        outs = []
+        for i in range(len(shapes)):
+            h.set_population_variant(i)
+            outs.append(h.batch_solve([s.as_tuple() for s in sm], an.L, with_loglik=False,
+                                      want_phi=True)["phi"])
+    for i, o in enumerate(outs[1:], 1):
+        assert np.array_equal(o, outs[0]), shapes[i]
+
+
+def test_autotune_picks_and_caches(gbg, tmp_path):
+    an, samples = _setup()
+    cache = str(tmp_path / "tune.json")
+    with _lib.Handle(an.n, "f32", max_samples=8) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        c1 = h.autotune(probe_samples=8, cache_path=cache)
+        assert 0 <= c1 < len(h.population_variants())
+        h.set_population_variant(0)
+        c2 = h.autotune(probe_samples=8, cache_path=cache)  # served from the cache
+        assert c2 == c1
+    import json
+    with open(cache) as f:
+        d = json.load(f)
+    assert list(d.values()) == [c1]

@@ -133,3 +133,20 @@ def test_oracle_live_vs_reference_random_case(oracle_lib):
     r = refio.run_harness("solve", "f64", n, 2, pw, pg, phi0, Dw, rho, 0.0, n * 0.1, nsteps=5)
     out = oracle_lib.rd_solve(pw, pg, phi0, r["Dw"], r["Dg"], r["rho"], r["dt"], 5, prec="f64")
     assert np.array_equal(out, r["phi"])
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/source"), reason="reference tree not present")
+def test_dropin_backend_compiles_against_reference_types():
+    """include/gbglioma_blockprocessing.hpp instantiated at the reference's own
+    call-site types (Grid, BlockCollection, BoundaryInfo, Glioma operators, the
+    TBB pipeline as CPU back-end): a compile-only check."""
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    ref = "/root/reference/source"
+    r = subprocess.run(["g++", "-fsyntax-only", "-std=gnu++11", "-fpermissive", "-w",
+                        "-I" + os.path.join(root, "oracle", "shim"),
+                        "-I" + os.path.join(root, "oracle", "shim", "vtk"), "-I" + ref,
+                        "-I" + os.path.join(ref, "Glioma"), "-I" + os.path.join(root, "include"),
+                        os.path.join(root, "tests", "cpp", "dropin_reference_compile.cpp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
