@@ -27,7 +27,8 @@ EXPORTS = [
     "gbg_loglik", "gbg_batch_solve", "gbg_batch_solve_device", "gbg_launch_count",
     "gbg_stream", "gbg_sync", "gbg_last_population_ms", "gbg_loglik_noalloc",
     "gbg_population_variants", "gbg_set_population_variant", "gbg_population_variant_shape",
-    "gbg_autotune",
+    "gbg_autotune", "gbg_amr_create", "gbg_amr_set_grid", "gbg_amr_set_ghosts", "gbg_amr_step",
+    "gbg_amr_get_phi", "gbg_amr_fwt_detail",
 ]
 
 
@@ -60,6 +61,10 @@ class LikResult(C.Structure):
 class Sample(C.Structure):
     _fields_ = [("Dw", C.c_double), ("rho", C.c_double), ("x0", C.c_double), ("y0", C.c_double),
                 ("z0", C.c_double), ("tend", C.c_double)]
+
+
+class AmrConfig(C.Structure):
+    _fields_ = [("max_blocks", C.c_int), ("precision", C.c_int), ("device", C.c_int)]
 
 
 class BatchOpts(C.Structure):
@@ -103,6 +108,12 @@ def load(path: str = LIB_PATH):
         "gbg_population_variant_shape": [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)],
         "gbg_autotune": [vp, C.c_int, C.c_char_p, C.POINTER(C.c_int)],
+        "gbg_amr_create": [C.POINTER(AmrConfig), C.POINTER(vp)],
+        "gbg_amr_set_grid": [vp, C.c_int, vp, dp, dp, dp],
+        "gbg_amr_set_ghosts": [vp, vp, vp, vp, dp, C.c_long],
+        "gbg_amr_step": [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_long],
+        "gbg_amr_get_phi": [vp, dp],
+        "gbg_amr_fwt_detail": [vp, dp],
         "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
                                C.POINTER(LikParams), vp, vp],
     }
@@ -270,3 +281,59 @@ class Handle:
         ms = C.c_float()
         check(self.lib.gbg_last_population_ms(self._h, C.byref(ms)))
         return ms.value
+
+
+class AmrHandle:
+    """A libgbglioma handle on MRAG's multiresolution grid of 16^3 blocks."""
+
+    GHOSTS_PER_BLOCK = 1736
+
+    def __init__(self, max_blocks: int, precision="f64", device: int = 0):
+        self.lib = load()
+        prec = PREC_BY_NAME[precision] if isinstance(precision, str) else precision
+        cfg = AmrConfig(max_blocks, prec, device)
+        h = C.c_void_p()
+        check(self.lib.gbg_amr_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.nb = 0
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.gbg_destroy(self._h)
+            self._h = C.c_void_p()
+
+    __del__ = Handle.__del__
+    __enter__ = Handle.__enter__
+    __exit__ = Handle.__exit__
+
+    def set_grid(self, blocks, p_w, p_g, phi):
+        """blocks: (nb, 4) ints (level, ix, iy, iz); fields: nb*4096 values per field."""
+        b = np.ascontiguousarray(blocks, dtype=np.int32)
+        nb = b.shape[0]
+        f = [as_f64(x).reshape(-1) for x in (p_w, p_g, phi)]
+        if any(x.size != nb * 4096 for x in f):
+            raise ValueError("fields must have nb*4096 cells")
+        check(self.lib.gbg_amr_set_grid(self._h, nb, b.ctypes.data, dptr(f[0]), dptr(f[1]),
+                                        dptr(f[2])))
+        self.nb = nb
+
+    def set_ghosts(self, start, src_block, src_cell, w):
+        st = np.ascontiguousarray(start, dtype=np.int64)
+        sb = np.ascontiguousarray(src_block, dtype=np.int32)
+        sc = np.ascontiguousarray(src_cell, dtype=np.int32)
+        ww = as_f64(w)
+        check(self.lib.gbg_amr_set_ghosts(self._h, st.ctypes.data, sb.ctypes.data, sc.ctypes.data,
+                                          dptr(ww), int(ww.size)))
+
+    def step(self, Dw, Dg, rho, dt, nsteps=1):
+        check(self.lib.gbg_amr_step(self._h, Dw, Dg, rho, dt, nsteps))
+
+    def get_phi(self) -> np.ndarray:
+        out = np.empty((self.nb, 16, 16, 16), dtype=np.float64)
+        check(self.lib.gbg_amr_get_phi(self._h, dptr(out)))
+        return out
+
+    def fwt_detail(self) -> np.ndarray:
+        out = np.empty(self.nb, dtype=np.float64)
+        check(self.lib.gbg_amr_fwt_detail(self._h, dptr(out)))
+        return out

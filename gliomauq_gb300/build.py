@@ -18,8 +18,8 @@ LIB = os.path.join(PKG, "libgbglioma.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr"]
-NOFMA = {"rd_exact.cu", "likelihood.cu"}
-SOURCES = ["abi.cu", "rd_exact.cu", "rd_fast.cu", "likelihood.cu"]
+NOFMA = {"rd_exact.cu", "likelihood.cu", "amr.cu"}
+SOURCES = ["abi.cu", "rd_exact.cu", "rd_fast.cu", "likelihood.cu", "amr.cu"]
 
 
 def nvcc() -> str:

@@ -83,6 +83,7 @@ void free_handle(Handle &h) {
         if (p) cudaFree(p);
     for (cudaEvent_t e : h.ev_pop)
         if (e) cudaEventDestroy(e);
+    if (h.is_amr) gbg::amr_free(h);
     if (h.stream) cudaStreamDestroy(h.stream);
 }
 
@@ -417,6 +418,124 @@ int gbg_batch_solve(gbg_handle *hh, const gbg_sample *samples, int S, const gbg_
     }
     GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
     return GBG_OK;
+}
+
+int gbg_amr_create(const gbg_amr_config *cfg, gbg_handle **out) {
+    if (!cfg || !out) {
+        set_error("null argument");
+        return GBG_ERR_ARG;
+    }
+    *out = nullptr;
+    if (cfg->max_blocks < 1 || (cfg->precision != GBG_PREC_F64 && cfg->precision != GBG_PREC_F32REF)) {
+        set_error("bad AMR configuration (max_blocks >= 1; GBG_PREC_F64 or GBG_PREC_F32REF)");
+        return GBG_ERR_ARG;
+    }
+    int ndev = 0;
+    GBG_CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (cfg->device < 0 || cfg->device >= ndev) {
+        set_error("device ordinal out of range");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(cfg->device));
+    gbg_handle *hh = new gbg_handle();
+    Handle &h = hh->h;
+    h.is_amr = true;
+    h.prec = cfg->precision;
+    h.device = cfg->device;
+    h.amr.max_blocks = cfg->max_blocks;
+    if (cudaDeviceGetAttribute(&h.num_sms, cudaDevAttrMultiProcessorCount, h.device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete hh;
+        set_error("stream creation failed");
+        return GBG_ERR_CUDA;
+    }
+    if (int rc = gbg::amr_alloc(h)) {
+        free_handle(h);
+        delete hh;
+        return rc;
+    }
+    *out = hh;
+    return GBG_OK;
+}
+
+static int check_amr(gbg_handle *hh) {
+    if (int rc = check_handle(hh)) return rc;
+    if (!hh->h.is_amr) {
+        set_error("not a handle made by gbg_amr_create");
+        return GBG_ERR_STATE;
+    }
+    return GBG_OK;
+}
+
+int gbg_amr_set_grid(gbg_handle *hh, int nb, const gbg_block *blocks, const double *p_w, const double *p_g,
+                     const double *phi) {
+    if (int rc = check_amr(hh)) return rc;
+    Handle &h = hh->h;
+    if (nb < 1 || nb > h.amr.max_blocks || !blocks || !p_w || !p_g || !phi) {
+        set_error("bad grid arguments");
+        return GBG_ERR_ARG;
+    }
+    for (int i = 0; i < nb; ++i) {
+        const gbg_block &b = blocks[i];
+        const int side = b.level >= 0 && b.level < 16 ? 1 << b.level : -1;
+        if (side < 0 || b.ix < 0 || b.iy < 0 || b.iz < 0 || b.ix >= side || b.iy >= side || b.iz >= side) {
+            set_error("block position outside its level");
+            return GBG_ERR_ARG;
+        }
+    }
+    const size_t n = (size_t)nb * 4096;
+    if (!all_finite(p_w, n) || !all_finite(p_g, n) || !all_finite(phi, n)) {
+        set_error("grid fields have NaN or Inf");
+        return GBG_ERR_NONFINITE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    return gbg::amr_set_grid(h, nb, blocks, p_w, p_g, phi);
+}
+
+int gbg_amr_set_ghosts(gbg_handle *hh, const long *start, const int *src_block, const int *src_cell,
+                       const double *w, long nentries) {
+    if (int rc = check_amr(hh)) return rc;
+    Handle &h = hh->h;
+    if (h.amr.nb < 1) {
+        set_error("set the grid before its ghost tables");
+        return GBG_ERR_STATE;
+    }
+    if (!start || nentries < 0 || (nentries > 0 && (!src_block || !src_cell || !w))) {
+        set_error("bad ghost-table arguments");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    return gbg::amr_set_ghosts(h, start, src_block, src_cell, w, nentries);
+}
+
+int gbg_amr_step(gbg_handle *hh, double Dw, double Dg, double rho, double dt, long nsteps) {
+    if (int rc = check_amr(hh)) return rc;
+    if (nsteps < 0 || !std::isfinite(Dw) || !std::isfinite(Dg) || !std::isfinite(rho) || !std::isfinite(dt)) {
+        set_error("bad step parameters");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
+    return gbg::amr_steps(hh->h, Dw, Dg, rho, dt, nsteps);
+}
+
+int gbg_amr_get_phi(gbg_handle *hh, double *phi) {
+    if (int rc = check_amr(hh)) return rc;
+    if (!phi || hh->h.amr.nb < 1) {
+        set_error("bad arguments or no grid");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
+    return gbg::amr_get_phi(hh->h, phi);
+}
+
+int gbg_amr_fwt_detail(gbg_handle *hh, double *detail) {
+    if (int rc = check_amr(hh)) return rc;
+    if (!detail) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
+    return gbg::amr_fwt_detail(hh->h, detail);
 }
 
 int gbg_launch_count(gbg_handle *hh, long long *count) {

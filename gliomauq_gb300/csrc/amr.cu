@@ -1,0 +1,409 @@
+// Multiresolution block grid on the GPU: the RD step and the wavelet detail
+// measure on MRAG's 16^3 blocks at mixed levels, with ghosts built from
+// MRAG's ghost instruction tables.
+//
+// Layout in HBM: every field is block-major, 4096 cells per block, x fastest
+// inside a block (the order of Block<...,16,16,16>::data). Ghost values of a
+// block are stored in the order BlockLab::load visits them
+// (source/MRAGcore/MRAGBlockLab.h:256-295): the 26 neighbour regions by code
+// (x fastest, the centre skipped), each region z-y-x, for the stencil [-1, 2)
+// per axis -- 1736 ghost cells per block.
+//
+// A ghost is sum_k value(src_k) * w_k in Real, starting from 0, terms in
+// table order (BlockLab.h:286-291); w_k is the Real product of its three
+// weights as BlockLab forms it (:289). The step is the Case2 operator and the
+// Euler update of the uniform exact kernels, with the cell's face neighbours
+// taken from the block or from its ghosts, h from the block's level, and the
+// face diffusivities precomputed per cell and face from the same values
+// (static between regrids). The FWT detail is BlockFWT::_fwt
+// (source/MRAGcore/MRAGBlockFWT.h:219-298) with Interp2ndOrder filters on
+// phi: for each of the 8^3 coarse points and each of the 7 detail subbands,
+// the filter sum in the loop order of _filter, and the block's report is the
+// largest magnitude (FWTReport::getOverAll_DetailMaxMag, :184-190).
+//
+// Compiled with -fmad=false: every operation rounds on its own.
+#include <vector>
+
+#include "gbg_internal.cuh"
+
+namespace gbg {
+namespace {
+
+constexpr int BS = 16;
+constexpr int BC = BS * BS * BS;  // cells per block
+constexpr int NG = 1736;          // ghost cells per block, stencil [-1, 2)
+
+// start of each of the 27 regions in the ghost list (region 13 is the block)
+__host__ __device__ inline int region_start(int code) {
+    int start = 0;
+    for (int c = 0; c < code; ++c) {
+        if (c == 13) continue;
+        const int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = (c / 9) % 3 - 1;
+        const int n0 = d0 == 0 ? BS : 1, n1 = d1 == 0 ? BS : 1, n2 = d2 == 0 ? BS : 1;
+        start += n0 * n1 * n2;
+    }
+    return start;
+}
+
+struct RegionTable {
+    int start[27];
+};
+
+// ghost slot of lab coordinate (x, y, z), each in [-1, 16], not all inside
+__device__ __forceinline__ int ghost_slot(const RegionTable &rt, int x, int y, int z) {
+    const int d0 = x < 0 ? -1 : (x >= BS ? 1 : 0);
+    const int d1 = y < 0 ? -1 : (y >= BS ? 1 : 0);
+    const int d2 = z < 0 ? -1 : (z >= BS ? 1 : 0);
+    const int code = (d0 + 1) + 3 * (d1 + 1) + 9 * (d2 + 1);
+    const int n0 = d0 == 0 ? BS : 1, n1 = d1 == 0 ? BS : 1;
+    const int lx = d0 == 0 ? x : 0, ly = d1 == 0 ? y : 0, lz = d2 == 0 ? z : 0;
+    return rt.start[code] + lx + n0 * (ly + n1 * lz);
+}
+
+template <typename Real>
+__global__ void k_ghost_eval(int nb, const long *__restrict__ start, const int *__restrict__ src_block,
+                             const int *__restrict__ src_cell, const double *__restrict__ w,
+                             const Real *__restrict__ field, Real *__restrict__ ghost) {
+    const long total = (long)nb * NG;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        Real acc = (Real)0;
+        for (long k = start[i]; k < start[i + 1]; ++k) {
+            const Real v = field[(size_t)src_block[k] * BC + src_cell[k]];
+            acc = acc + v * (Real)w[k];
+        }
+        ghost[i] = acc;
+    }
+}
+
+// value of `field` at lab coordinate (x, y, z) of block b
+template <typename Real>
+__device__ __forceinline__ Real lab_at(const RegionTable &rt, const Real *field, const Real *ghost, int b,
+                                       int x, int y, int z) {
+    if (x >= 0 && x < BS && y >= 0 && y < BS && z >= 0 && z < BS)
+        return field[(size_t)b * BC + x + BS * (y + BS * z)];
+    return ghost[(size_t)b * NG + ghost_slot(rt, x, y, z)];
+}
+
+// per cell: brain sum b0 and the six face diffusivities df[0..5] (W E S N B F)
+template <typename Real>
+__global__ void k_amr_tables(int nb, RegionTable rt, const Real *__restrict__ pw, const Real *__restrict__ pg,
+                             const Real *__restrict__ gpw, const Real *__restrict__ gpg, Real Dw, Real Dg,
+                             Real *__restrict__ b0, double *__restrict__ df) {
+    const long total = (long)nb * BC;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / BC), c = (int)(i % BC);
+        const int x = c % BS, y = (c / BS) % BS, z = c / (BS * BS);
+        const int nx[7] = {x, x - 1, x + 1, x, x, x, x};
+        const int ny[7] = {y, y, y, y - 1, y + 1, y, y};
+        const int nz[7] = {z, z, z, z, z, z - 1, z + 1};
+        double inv[7];
+        for (int k = 0; k < 7; ++k) {
+            const Real a = lab_at(rt, pw, gpw, b, nx[k], ny[k], nz[k]);
+            const Real g = lab_at(rt, pg, gpg, b, nx[k], ny[k], nz[k]);
+            const Real brain = a + g;
+            const Real kk = (a * Dw + g * Dg) / brain;
+            inv[k] = 1.0 / (double)kk;
+            if (k == 0) b0[i] = brain;
+        }
+        for (int f = 0; f < 6; ++f) df[(size_t)i * 6 + f] = 2.0 * (1.0 / (inv[0] + inv[f + 1]));
+    }
+}
+
+__device__ __forceinline__ double reaction(double rho, double p) { return rho * p * (1. - p); }
+__device__ __forceinline__ double reaction(float rho, float p) {
+    const float rp = rho * p;
+    return (double)rp * (1. - (double)p);
+}
+
+template <typename Real>
+__global__ void k_amr_step(int nb, RegionTable rt, const int *__restrict__ level, const Real *__restrict__ phi,
+                           const Real *__restrict__ gphi, const Real *__restrict__ b0,
+                           const double *__restrict__ df, Real *__restrict__ out, Real rho, double dt) {
+    const long total = (long)nb * BC;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / BC), c = (int)(i % BC);
+        const int x = c % BS, y = (c / BS) % BS, z = c / (BS * BS);
+        // h = info.h[0] is Real: 1 / (2^level * 16), a power of two
+        const Real hR = (Real)1 / (Real)((1 << level[b]) * BS);
+        const double h = (double)hR;
+        const double ih2 = 1. / (h * h);
+        const Real p0 = phi[i];
+        const Real pW = lab_at(rt, phi, gphi, b, x - 1, y, z), pE = lab_at(rt, phi, gphi, b, x + 1, y, z);
+        const Real pS = lab_at(rt, phi, gphi, b, x, y - 1, z), pN = lab_at(rt, phi, gphi, b, x, y + 1, z);
+        const Real pB = lab_at(rt, phi, gphi, b, x, y, z - 1), pF = lab_at(rt, phi, gphi, b, x, y, z + 1);
+        double d0 = 0.0, d1 = 0.0, d2 = 0.0, d3 = 0.0, d4 = 0.0, d5 = 0.0;
+        const Real tissue = b0[i] + p0;
+        if (tissue > 0.) {
+            const double *t = df + (size_t)i * 6;
+            d0 = t[0]; d1 = t[1]; d2 = t[2]; d3 = t[3]; d4 = t[4]; d5 = t[5];
+        }
+        if (d0 == 0 && pW > 0.) d1 *= 2.0;
+        if (d1 == 0 && pE > 0.) d0 *= 2.0;
+        if (d2 == 0 && pS > 0.) d3 *= 2.0;
+        if (d3 == 0 && pN > 0.) d2 *= 2.0;
+        if (d4 == 0 && pB > 0.) d5 *= 2.0;
+        if (d5 == 0 && pF > 0.) d4 *= 2.0;
+        const double fin = ih2 * (d0 * (double)pW + d1 * (double)pE + d2 * (double)pS + d3 * (double)pN +
+                                  d4 * (double)pB + d5 * (double)pF);
+        const double fout = -((d0 + d1 + d2 + d3 + d4 + d5) * (double)p0 * ih2);
+        const double react = reaction(rho, p0);
+        const Real dphidt = (Real)(fout + fin + react);
+        Real v = (Real)((double)p0 + dt * (double)dphidt);
+        v = ((Real)0 < v) ? v : (Real)0;
+        v = (v < (Real)1) ? v : (Real)1;
+        out[i] = v;
+    }
+}
+
+// One CTA per block, one thread per coarse point (8^3 = 512): the seven
+// detail subbands, then a max-reduction of their magnitudes.
+template <typename Real>
+__global__ void __launch_bounds__(512) k_amr_fwt(int nb, RegionTable rt, const Real *__restrict__ phi,
+                                                 const Real *__restrict__ gphi, double *__restrict__ detail) {
+    const int b = blockIdx.x;
+    const int t = threadIdx.x;
+    const int dx = t % 8, dy = (t / 8) % 8, dz = t / 64;
+    // Interp2ndOrder: Ha = {1} on [0,1), Ga = {-0.5, 1, -0.5} on [-2,1)
+    const Real ga[3] = {(Real)-0.5, (Real)1., (Real)-0.5};
+    double mx = 0.0;
+    for (int sb = 1; sb < 8; ++sb) {
+        const int wx = sb & 1, wy = (sb >> 1) & 1, wz = (sb >> 2) & 1;
+        const int s0 = wx ? -2 : 0, e0 = wx ? 1 : 1;
+        const int s1 = wy ? -2 : 0, e1 = wy ? 1 : 1;
+        const int s2 = wz ? -2 : 0, e2 = wz ? 1 : 1;
+        Real result = 0;
+        for (int iz = s2; iz < e2; iz++) {
+            const Real wZ = wz ? ga[iz + 2] : (Real)1;
+            for (int iy = s1; iy < e1; iy++) {
+                const Real wY = wy ? ga[iy + 2] : (Real)1;
+                const Real wZwY = wZ * wY;
+                for (int ix = s0; ix < e0; ix++) {
+                    const Real wX = wx ? ga[ix + 2] : (Real)1;
+                    const Real v = lab_at(rt, phi, gphi, b, 2 * dx - ix, 2 * dy - iy, 2 * dz - iz);
+                    result = result + v * (wZwY * wX);
+                }
+            }
+        }
+        const double a = fabs((double)result);
+        mx = a > mx ? a : mx;
+    }
+    __shared__ double red[512];
+    red[t] = mx;
+    __syncthreads();
+    for (int s = 256; s > 0; s >>= 1) {
+        if (t < s) red[t] = red[t] > red[t + s] ? red[t] : red[t + s];
+        __syncthreads();
+    }
+    if (t == 0) detail[b] = red[0];
+}
+
+RegionTable region_table() {
+    RegionTable rt;
+    for (int c = 0; c < 27; ++c) rt.start[c] = region_start(c);
+    return rt;
+}
+
+int grid_blocks(const Handle &h, long work) {
+    const long blocks = (work + 255) / 256;
+    const long cap = (long)h.num_sms * 8;
+    return (int)(blocks < cap ? blocks : cap);
+}
+
+}  // namespace
+
+int amr_region_start(int code) { return region_start(code); }
+
+int amr_alloc(Handle &h) {
+    const size_t sb = h.prec == GBG_PREC_F64 ? sizeof(double) : sizeof(float);
+    const size_t cells = (size_t)h.amr.max_blocks * BC;
+    const size_t ghosts = (size_t)h.amr.max_blocks * NG;
+    void **bufs[] = {&h.amr.phi[0], &h.amr.phi[1], &h.amr.pw, &h.amr.pg, &h.amr.b0};
+    for (void **b : bufs) GBG_CUDA_TRY(cudaMalloc(b, cells * sb));
+    void **gb[] = {&h.amr.gphi, &h.amr.gpw, &h.amr.gpg};
+    for (void **b : gb) GBG_CUDA_TRY(cudaMalloc(b, ghosts * sb));
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.df, cells * 6 * sizeof(double)));
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.level, (size_t)h.amr.max_blocks * sizeof(int)));
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.gstart, (ghosts + 1) * sizeof(long)));
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.detail, (size_t)h.amr.max_blocks * sizeof(double)));
+    return GBG_OK;
+}
+
+void amr_free(Handle &h) {
+    void *p[] = {h.amr.phi[0], h.amr.phi[1], h.amr.pw, h.amr.pg, h.amr.b0, h.amr.gphi, h.amr.gpw, h.amr.gpg,
+                 h.amr.df, h.amr.level, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell, h.amr.gw,
+                 h.amr.detail};
+    for (void *q : p)
+        if (q) cudaFree(q);
+}
+
+int amr_set_grid(Handle &h, int nb, const gbg_block *blocks, const double *pw, const double *pg,
+                 const double *phi) {
+    const size_t n = (size_t)nb * BC;
+    std::vector<int> lv(nb);
+    for (int i = 0; i < nb; ++i) lv[i] = blocks[i].level;
+    GBG_CUDA_TRY(cudaMemcpyAsync(h.amr.level, lv.data(), nb * sizeof(int), cudaMemcpyHostToDevice, h.stream));
+    const double *src[3] = {pw, pg, phi};
+    void *dst[3] = {h.amr.pw, h.amr.pg, h.amr.phi[0]};
+    if (h.prec == GBG_PREC_F64) {
+        for (int k = 0; k < 3; ++k)
+            GBG_CUDA_TRY(cudaMemcpyAsync(dst[k], src[k], n * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+        GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    } else {
+        std::vector<float> tmp(n);
+        for (int k = 0; k < 3; ++k) {
+            for (size_t i = 0; i < n; ++i) tmp[i] = (float)src[k][i];
+            GBG_CUDA_TRY(cudaMemcpy(dst[k], tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        }
+    }
+    h.amr.nb = nb;
+    h.amr.cur = 0;
+    h.amr.ghosts_valid = false;
+    h.amr.tables_valid = false;
+    return GBG_OK;
+}
+
+int amr_set_ghosts(Handle &h, const long *start, const int *src_block, const int *src_cell, const double *w,
+                   long nentries) {
+    const long ng = (long)h.amr.nb * NG;
+    for (long i = 0; i < ng; ++i)
+        if (start[i + 1] < start[i]) {
+            set_error("ghost table start offsets must not decrease");
+            return GBG_ERR_ARG;
+        }
+    if (start[0] != 0 || start[ng] != nentries) {
+        set_error("ghost table start offsets must span [0, nentries]");
+        return GBG_ERR_ARG;
+    }
+    for (long k = 0; k < nentries; ++k)
+        if (src_block[k] < 0 || src_block[k] >= h.amr.nb || src_cell[k] < 0 || src_cell[k] >= BC) {
+            set_error("ghost table entry points outside the grid");
+            return GBG_ERR_ARG;
+        }
+    if (h.amr.gsrc_block) cudaFree(h.amr.gsrc_block);
+    if (h.amr.gsrc_cell) cudaFree(h.amr.gsrc_cell);
+    if (h.amr.gw) cudaFree(h.amr.gw);
+    h.amr.gsrc_block = nullptr;
+    h.amr.gsrc_cell = nullptr;
+    h.amr.gw = nullptr;
+    const size_t ne = nentries > 0 ? (size_t)nentries : 1;
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.gsrc_block, ne * sizeof(int)));
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.gsrc_cell, ne * sizeof(int)));
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.gw, ne * sizeof(double)));
+    GBG_CUDA_TRY(cudaMemcpy(h.amr.gstart, start, (ng + 1) * sizeof(long), cudaMemcpyHostToDevice));
+    if (nentries > 0) {
+        GBG_CUDA_TRY(cudaMemcpy(h.amr.gsrc_block, src_block, nentries * sizeof(int), cudaMemcpyHostToDevice));
+        GBG_CUDA_TRY(cudaMemcpy(h.amr.gsrc_cell, src_cell, nentries * sizeof(int), cudaMemcpyHostToDevice));
+        GBG_CUDA_TRY(cudaMemcpy(h.amr.gw, w, nentries * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    // the anatomy's ghosts are static between regrids
+    const int g = grid_blocks(h, ng);
+    if (h.prec == GBG_PREC_F64) {
+        k_ghost_eval<double><<<g, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell,
+                                                      h.amr.gw, (const double *)h.amr.pw, (double *)h.amr.gpw);
+        k_ghost_eval<double><<<g, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell,
+                                                      h.amr.gw, (const double *)h.amr.pg, (double *)h.amr.gpg);
+    } else {
+        k_ghost_eval<float><<<g, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell,
+                                                     h.amr.gw, (const float *)h.amr.pw, (float *)h.amr.gpw);
+        k_ghost_eval<float><<<g, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell,
+                                                     h.amr.gw, (const float *)h.amr.pg, (float *)h.amr.gpg);
+    }
+    h.launches += 2;
+    GBG_CUDA_TRY(cudaGetLastError());
+    h.amr.ghosts_valid = true;
+    h.amr.tables_valid = false;
+    return GBG_OK;
+}
+
+int amr_steps(Handle &h, double Dw, double Dg, double rho, double dt, long nsteps) {
+    if (!h.amr.ghosts_valid) {
+        set_error("ghost tables not set");
+        return GBG_ERR_STATE;
+    }
+    const RegionTable rt = region_table();
+    const long cells = (long)h.amr.nb * BC, ng = (long)h.amr.nb * NG;
+    const int gc = grid_blocks(h, cells), gg = grid_blocks(h, ng);
+    const bool f64 = h.prec == GBG_PREC_F64;
+    if (!h.amr.tables_valid || h.amr.tab_Dw != Dw || h.amr.tab_Dg != Dg) {
+        if (f64)
+            k_amr_tables<double><<<gc, 256, 0, h.stream>>>(h.amr.nb, rt, (const double *)h.amr.pw,
+                                                           (const double *)h.amr.pg, (const double *)h.amr.gpw,
+                                                           (const double *)h.amr.gpg, Dw, Dg,
+                                                           (double *)h.amr.b0, h.amr.df);
+        else
+            k_amr_tables<float><<<gc, 256, 0, h.stream>>>(h.amr.nb, rt, (const float *)h.amr.pw,
+                                                          (const float *)h.amr.pg, (const float *)h.amr.gpw,
+                                                          (const float *)h.amr.gpg, (float)Dw, (float)Dg,
+                                                          (float *)h.amr.b0, h.amr.df);
+        h.launches++;
+        h.amr.tab_Dw = Dw;
+        h.amr.tab_Dg = Dg;
+        h.amr.tables_valid = true;
+    }
+    for (long s = 0; s < nsteps; ++s) {
+        void *in = h.amr.phi[h.amr.cur], *out = h.amr.phi[h.amr.cur ^ 1];
+        if (f64) {
+            k_ghost_eval<double><<<gg, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block,
+                                                           h.amr.gsrc_cell, h.amr.gw, (const double *)in,
+                                                           (double *)h.amr.gphi);
+            k_amr_step<double><<<gc, 256, 0, h.stream>>>(h.amr.nb, rt, h.amr.level, (const double *)in,
+                                                         (const double *)h.amr.gphi, (const double *)h.amr.b0,
+                                                         h.amr.df, (double *)out, rho, dt);
+        } else {
+            k_ghost_eval<float><<<gg, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block,
+                                                          h.amr.gsrc_cell, h.amr.gw, (const float *)in,
+                                                          (float *)h.amr.gphi);
+            k_amr_step<float><<<gc, 256, 0, h.stream>>>(h.amr.nb, rt, h.amr.level, (const float *)in,
+                                                        (const float *)h.amr.gphi, (const float *)h.amr.b0,
+                                                        h.amr.df, (float *)out, (float)rho, dt);
+        }
+        h.launches += 2;
+        h.amr.cur ^= 1;
+    }
+    GBG_CUDA_TRY(cudaGetLastError());
+    return GBG_OK;
+}
+
+int amr_get_phi(Handle &h, double *phi) {
+    const size_t n = (size_t)h.amr.nb * BC;
+    if (h.prec == GBG_PREC_F64) {
+        GBG_CUDA_TRY(cudaMemcpyAsync(phi, h.amr.phi[h.amr.cur], n * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+        GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    } else {
+        std::vector<float> tmp(n);
+        GBG_CUDA_TRY(cudaMemcpyAsync(tmp.data(), h.amr.phi[h.amr.cur], n * sizeof(float), cudaMemcpyDeviceToHost,
+                                     h.stream));
+        GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        for (size_t i = 0; i < n; ++i) phi[i] = tmp[i];
+    }
+    return GBG_OK;
+}
+
+int amr_fwt_detail(Handle &h, double *detail) {
+    if (!h.amr.ghosts_valid) {
+        set_error("ghost tables not set");
+        return GBG_ERR_STATE;
+    }
+    const RegionTable rt = region_table();
+    const long ng = (long)h.amr.nb * NG;
+    const int gg = grid_blocks(h, ng);
+    void *in = h.amr.phi[h.amr.cur];
+    if (h.prec == GBG_PREC_F64) {
+        k_ghost_eval<double><<<gg, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell,
+                                                       h.amr.gw, (const double *)in, (double *)h.amr.gphi);
+        k_amr_fwt<double><<<h.amr.nb, 512, 0, h.stream>>>(h.amr.nb, rt, (const double *)in,
+                                                          (const double *)h.amr.gphi, h.amr.detail);
+    } else {
+        k_ghost_eval<float><<<gg, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell,
+                                                      h.amr.gw, (const float *)in, (float *)h.amr.gphi);
+        k_amr_fwt<float><<<h.amr.nb, 512, 0, h.stream>>>(h.amr.nb, rt, (const float *)in,
+                                                         (const float *)h.amr.gphi, h.amr.detail);
+    }
+    h.launches += 2;
+    GBG_CUDA_TRY(cudaGetLastError());
+    GBG_CUDA_TRY(cudaMemcpyAsync(detail, h.amr.detail, h.amr.nb * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    return GBG_OK;
+}
+
+}  // namespace gbg

@@ -37,6 +37,22 @@ struct ObsDevice {
     bool valid = false;
 };
 
+// Multiresolution block grid state (amr.cu)
+struct AmrState {
+    int max_blocks = 0, nb = 0, cur = 0;
+    void *phi[2] = {nullptr, nullptr};
+    void *pw = nullptr, *pg = nullptr, *b0 = nullptr;
+    void *gphi = nullptr, *gpw = nullptr, *gpg = nullptr;  // ghost values
+    double *df = nullptr;      // six face diffusivities per cell
+    int *level = nullptr;      // per block
+    long *gstart = nullptr;    // ghost-table offsets, nb*1736+1
+    int *gsrc_block = nullptr, *gsrc_cell = nullptr;
+    double *gw = nullptr;
+    double *detail = nullptr;  // FWT maxima per block
+    bool ghosts_valid = false, tables_valid = false;
+    double tab_Dw = -1, tab_Dg = -1;
+};
+
 struct Handle {
     int n = 0;
     size_t N = 0;
@@ -80,6 +96,10 @@ struct Handle {
     // events bracketing the latest population-kernel launch
     cudaEvent_t ev_pop[2] = {nullptr, nullptr};
     bool ev_pop_recorded = false;
+
+    // multiresolution grid (handles made by gbg_amr_create)
+    bool is_amr = false;
+    AmrState amr;
 
     // likelihood
     ObsDevice obs;
@@ -130,6 +150,18 @@ int population_variant_shape(int n, int vi, int *ry, int *g, int *threads);
 int check_device_status(Handle &h);
 int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
                        const gbg_batch_opts &o, gbg_lik_result *loglik_device, long *nsteps_host);
+
+// ---- amr.cu ----
+int amr_region_start(int code);
+int amr_alloc(Handle &h);
+void amr_free(Handle &h);
+int amr_set_grid(Handle &h, int nb, const gbg_block *blocks, const double *pw, const double *pg,
+                 const double *phi);
+int amr_set_ghosts(Handle &h, const long *start, const int *src_block, const int *src_cell, const double *w,
+                   long nentries);
+int amr_steps(Handle &h, double Dw, double Dg, double rho, double dt, long nsteps);
+int amr_get_phi(Handle &h, double *phi);
+int amr_fwt_detail(Handle &h, double *detail);
 
 // ---- likelihood.cu ----
 int lik_set_observations(Handle &h, const double *pet, const double *t1, const double *t2,

@@ -152,6 +152,44 @@ int gbg_batch_solve(gbg_handle *h, const gbg_sample *samples, int S, const gbg_b
 int gbg_batch_solve_device(gbg_handle *h, const gbg_sample *samples_device, int S,
                            const gbg_batch_opts *o, gbg_lik_result *loglik_device);
 
+/* ---- multiresolution block grid ----------------------------------------------
+ * MRAG's grid of 16^3 blocks at mixed levels (source/MRAGcore/MRAGrid.h:44-186):
+ * block b at level l covers [index/2^l, (index+1)/2^l) of the unit cube with
+ * h = 1/(2^l * 16). Fields are block-major, 4096 cells per block, x fastest
+ * inside a block. Ghost cells come from MRAG's ghost instruction tables
+ * (BoundaryInfoBlock, source/MRAGcore/MRAGBoundaryBlockInfo.h:69-176) flattened:
+ * ghost g of block b (g in [0, 1736), the order BlockLab::load visits the 26
+ * neighbour regions for the stencil [-1, 2), source/MRAGcore/MRAGBlockLab.h:256-295)
+ * is sum_k value(src_block[k], src_cell[k]) * w[k] over
+ * k in [start[b*1736+g], start[b*1736+g+1]), evaluated in the handle's Real
+ * type in that order; w[k] is the Real product of the entry's three weights.
+ * src_block indexes the blocks in the order given to gbg_amr_set_grid. */
+typedef struct {
+    int level, ix, iy, iz;
+} gbg_block;
+
+typedef struct {
+    int max_blocks;  /* capacity */
+    int precision;   /* GBG_PREC_F64 or GBG_PREC_F32REF */
+    int device;
+} gbg_amr_config;
+
+int gbg_amr_create(const gbg_amr_config *cfg, gbg_handle **out);
+int gbg_amr_set_grid(gbg_handle *h, int nblocks, const gbg_block *blocks, const double *p_w,
+                     const double *p_g, const double *phi);
+int gbg_amr_set_ghosts(gbg_handle *h, const long *start, const int *src_block, const int *src_cell,
+                       const double *w, long nentries);
+/* nsteps steps of the RD operator + UpdateTumor on every block, exactly as
+ * BlockProcessing::pipeline_process(rhs) + process(update) do on the MRAG
+ * grid (source/Glioma/Glioma_HG_UQ.cpp:266-277). */
+int gbg_amr_step(gbg_handle *h, double Dw, double Dg, double rho, double dt, long nsteps);
+int gbg_amr_get_phi(gbg_handle *h, double *phi);
+/* per block: the largest interpolating-wavelet detail magnitude of phi,
+ * BlockFWT::multichannel_fwt + FWTReport::getOverAll_DetailMaxMag
+ * (source/MRAGcore/MRAGBlockFWT.h:184-190,219-298,447-468) -- the quantity
+ * Science::AutomaticRefinement/Compression compare with their tolerances. */
+int gbg_amr_fwt_detail(gbg_handle *h, double *detail);
+
 /* ---- introspection ---------------------------------------------------------- */
 /* number of kernels this handle has launched since creation */
 int gbg_launch_count(gbg_handle *h, long long *count);

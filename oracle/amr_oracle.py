@@ -1,0 +1,155 @@
+"""CPU oracle for the multiresolution block grid -- TEST INFRASTRUCTURE ONLY.
+
+NumPy restatement of what GliomaUQ does on MRAG's adaptive grid of 16^3
+blocks, vectorised over blocks and cells with every operation in the
+reference's Real type (IEEE single or double, one rounding per operation):
+
+  * ghost values: BlockLab::load (source/MRAGcore/MRAGBlockLab.h:254-295),
+    ghost = sum_k value_k * w_k from 0 in table order;
+  * the step: Glioma_ReactionDiffusionOperator<3> Case2 + UpdateTumor<3>
+    (source/Glioma/Glioma_ReactionDiffusionOperator.h:148-218, :254-261) on
+    each block's 18^3 lab with h = 1/(2^level * 16);
+  * the FWT detail maximum: BlockFWT::_filter/_fwt + FWTReport
+    (source/MRAGcore/MRAGBlockFWT.h:184-190, 219-298), Interp2ndOrder filters.
+
+Pinned against the reference's own outputs in tests/golden/amr64_*.npz.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+BS = 16
+NG = 1736
+
+
+def region_starts():
+    out, start = [], 0
+    for c in range(27):
+        d = (c % 3 - 1, (c // 3) % 3 - 1, (c // 9) % 3 - 1)
+        size = int(np.prod([BS if x == 0 else 1 for x in d]))
+        out.append(start if c != 13 else -1)
+        if c != 13:
+            start += size
+    return out
+
+
+def _lab_slots():
+    """(18,18,18) map from lab cell (z+1, y+1, x+1) to ghost slot (-1 inside)."""
+    rs = region_starts()
+    m = np.full((18, 18, 18), -1, dtype=np.int64)
+    for z in range(-1, 17):
+        for y in range(-1, 17):
+            for x in range(-1, 17):
+                if 0 <= x < BS and 0 <= y < BS and 0 <= z < BS:
+                    continue
+                d = [(-1 if v < 0 else (1 if v >= BS else 0)) for v in (x, y, z)]
+                code = (d[0] + 1) + 3 * (d[1] + 1) + 9 * (d[2] + 1)
+                n0 = BS if d[0] == 0 else 1
+                n1 = BS if d[1] == 0 else 1
+                lx = x if d[0] == 0 else 0
+                ly = y if d[1] == 0 else 0
+                lz = z if d[2] == 0 else 0
+                m[z + 1, y + 1, x + 1] = rs[code] + lx + n0 * (ly + n1 * lz)
+    return m
+
+
+LAB_SLOTS = _lab_slots()
+
+
+def ghost_values(field, start, src_block, src_cell, w, real):
+    """field: (nb, 4096) in `real`; returns (nb*1736,) ghost values."""
+    f = np.asarray(field, dtype=real).reshape(-1)
+    start = np.asarray(start, dtype=np.int64)
+    counts = np.diff(start)
+    acc = np.zeros(counts.size, dtype=real)
+    src = np.asarray(src_block, dtype=np.int64) * 4096 + np.asarray(src_cell, dtype=np.int64)
+    ww = np.asarray(w, dtype=real)
+    for k in range(int(counts.max()) if counts.size else 0):
+        sel = np.nonzero(counts > k)[0]
+        e = start[sel] + k
+        acc[sel] = acc[sel] + f[src[e]] * ww[e]
+    return acc
+
+
+def labs(field, ghosts, real):
+    """(nb, 18, 18, 18) labs, index [b, z+1, y+1, x+1]."""
+    f = np.asarray(field, dtype=real).reshape(-1, BS, BS, BS)
+    g = np.asarray(ghosts, dtype=real).reshape(f.shape[0], NG)
+    out = np.empty((f.shape[0], 18, 18, 18), dtype=real)
+    inside = LAB_SLOTS < 0
+    out[:, 1:17, 1:17, 1:17] = f
+    idx = np.nonzero(~inside)
+    out[:, idx[0], idx[1], idx[2]] = g[:, LAB_SLOTS[idx]]
+    return out
+
+
+def step(levels, pw, pg, phi, ghost_tables, Dw, Dg, rho, dt, real):
+    """One step on every block; returns the new phi (nb, 16, 16, 16) in `real`."""
+    st, sb, sc, w = ghost_tables
+    real = np.dtype(real).type
+    Lw = labs(pw, ghost_values(pw, st, sb, sc, w, real), real)
+    Lg = labs(pg, ghost_values(pg, st, sb, sc, w, real), real)
+    Lp = labs(phi, ghost_values(phi, st, sb, sc, w, real), real)
+    Dw, Dg, rho = real(Dw), real(Dg), real(rho)
+    c = (slice(None), slice(1, 17), slice(1, 17), slice(1, 17))
+    sh = {0: (0, 0, -1), 1: (0, 0, 1), 2: (0, -1, 0), 3: (0, 1, 0), 4: (-1, 0, 0), 5: (1, 0, 0)}
+
+    def at(L, f):
+        dz, dy, dx = sh[f]
+        return L[:, 1 + dz:17 + dz, 1 + dy:17 + dy, 1 + dx:17 + dx]
+
+    with np.errstate(all="ignore"):
+        brain0 = Lw[c] + Lg[c]
+        inv0 = 1.0 / ((Lw[c] * Dw + Lg[c] * Dg) / brain0).astype(np.float64)
+        tissue = brain0 + Lp[c]
+        df = []
+        for f in range(6):
+            bn = at(Lw, f) + at(Lg, f)
+            kn = (at(Lw, f) * Dw + at(Lg, f) * Dg) / bn
+            d = 2.0 * (1.0 / (inv0 + 1.0 / kn.astype(np.float64)))
+            df.append(np.where(tissue > 0, d, 0.0))
+        pn = [at(Lp, f).astype(np.float64) for f in range(6)]
+        pairs = [(0, 1, 0), (1, 0, 1), (2, 3, 2), (3, 2, 3), (4, 5, 4), (5, 4, 5)]
+        for zf, other, nb in pairs:
+            df[other] = np.where((df[zf] == 0) & (pn[nb] > 0), df[other] * 2.0, df[other])
+        h = np.array([real(1) / real((1 << int(l)) * BS) for l in levels], dtype=np.float64)
+        ih2 = (1.0 / (h * h))[:, None, None, None]
+        p0 = Lp[c]
+        fin = ih2 * (df[0] * pn[0] + df[1] * pn[1] + df[2] * pn[2] + df[3] * pn[3] + df[4] * pn[4]
+                     + df[5] * pn[5])
+        fout = -((df[0] + df[1] + df[2] + df[3] + df[4] + df[5]) * p0.astype(np.float64) * ih2)
+        react = (rho * p0).astype(np.float64) * (1.0 - p0.astype(np.float64))
+        dphidt = (fout + fin + react).astype(real)
+        v = (p0.astype(np.float64) + dt * dphidt.astype(np.float64)).astype(real)
+    v = np.where(real(0) < v, v, real(0))
+    v = np.where(v < real(1), v, real(1))
+    return v.astype(real)
+
+
+def fwt_detail(phi, ghost_tables, real):
+    """Per-block largest detail magnitude of the one-level interpolating
+    wavelet transform of phi (FWTReport::getOverAll_DetailMaxMag)."""
+    st, sb, sc, w = ghost_tables
+    real = np.dtype(real).type
+    L = labs(phi, ghost_values(phi, st, sb, sc, w, real), real)
+    ga = {-2: real(-0.5), -1: real(1.0), 0: real(-0.5)}
+    d = np.arange(8)
+    out = np.zeros(L.shape[0], dtype=np.float64)
+    for sbnd in range(1, 8):
+        wx, wy, wz = sbnd & 1, (sbnd >> 1) & 1, (sbnd >> 2) & 1
+        rx = [-2, -1, 0] if wx else [0]
+        ry = [-2, -1, 0] if wy else [0]
+        rz = [-2, -1, 0] if wz else [0]
+        res = np.zeros((L.shape[0], 8, 8, 8), dtype=real)
+        for iz in rz:
+            wZ = ga[iz] if wz else real(1)
+            for iy in ry:
+                wY = ga[iy] if wy else real(1)
+                wZwY = real(wZ * wY)
+                for ix in rx:
+                    wX = ga[ix] if wx else real(1)
+                    zz, yy, xx = 2 * d - iz + 1, 2 * d - iy + 1, 2 * d - ix + 1
+                    v = L[:, zz][:, :, yy][:, :, :, xx]
+                    res = res + v * real(wZwY * wX)
+        out = np.maximum(out, np.abs(res.astype(np.float64)).reshape(L.shape[0], -1).max(axis=1))
+    return out

@@ -22,6 +22,9 @@
 //                       regridded) grid: per block, per ghost cell, the
 //                       (source block, source cell, weight) triples
 //   fwt    <in> <out>   per-block detail maxima of BlockFWT on phi
+//   state  <in> <out> [k]  adaptive fixtures: blocks + ghost tables + FWT
+//                       maxima after the loop, blocks after k more steps,
+//                       blocks after one more regrid
 //   timing <in>         times steps only (no output), prints cell-steps/s
 #include "Glioma_Types.h"
 
@@ -132,8 +135,10 @@ struct Sim {
         BlockProcessing::process(vInfo, coll, updateTumor, gran);
     }
     void regrid() {
-        Science::AutomaticRefinement<0, 0>(*grid, blockfwt, refinement_tolerance, maxLevel, 1, &profiler);
-        Science::AutomaticCompression<0, 0>(*grid, blockfwt, compression_tolerance, -1, &profiler);
+        const int r = Science::AutomaticRefinement<0, 0>(*grid, blockfwt, refinement_tolerance, maxLevel, 1, &profiler);
+        const int c = Science::AutomaticCompression<0, 0>(*grid, blockfwt, compression_tolerance, -1, &profiler);
+        if (getenv("GBG_HARNESS_VERBOSE"))
+            fprintf(stderr, "regrid: refined %d collapsed %d -> %zu blocks\n", r, c, grid->getBlocksInfo().size());
     }
 };
 
@@ -145,7 +150,7 @@ struct RunInfo {
 };
 
 // Glioma_HG_UQ::run time loop (Glioma_HG_UQ.cpp:511-575); returns step count.
-static RunInfo runLoop(Sim &s, const Input &in, bool verbose, double *secs) {
+static RunInfo runLoop(Sim &s, const Input &in, bool verbose, double *secs, bool final_refine = true) {
     const int gran = (s.grid->getBlocksInfo().size() <= 8 ? 1 : 4);
     BoundaryInfo *boundaryInfo = &s.grid->getBoundaryInfo();
     Real Dw = (Real)in.Dw_file, rho = (Real)in.rho, Dg;
@@ -176,7 +181,7 @@ static RunInfo runLoop(Sim &s, const Input &in, bool verbose, double *secs) {
                 whenToWrite = whenToWrite + whenToWriteOffset;
             }
         }
-        if (in.adaptive) {
+        if (in.adaptive && final_refine) {
             Science::AutomaticRefinement<0, 0>(*s.grid, s.blockfwt, refinement_tolerance, maxLevel, 1,
                                                &s.profiler);
             ri.regrids++;
@@ -334,6 +339,85 @@ static int cmdFwt(const char *inp, const char *outp) {
     return 0;
 }
 
+static void writeGhostTables(FILE *f, Grid<W, B> &grid) {
+    BoundaryInfo &bi = grid.getBoundaryInfo();
+    std::vector<BlockInfo> vInfo = grid.getBlocksInfo();
+    int32_t nb = (int32_t)vInfo.size();
+    fwrite(&nb, 4, 1, f);
+    for (size_t i = 0; i < vInfo.size(); i++) {
+        const BlockInfo &info = vInfo[i];
+        BoundaryInfoBlock &bb = *bi.boundaryInfoOfBlock.find(info.blockID)->second;
+        bb.lock();
+        const vector<PointIndex> &pool = bb.getIndexPool();
+        const vector<vector<IndexWP> > &gh = bb.getGhosts();
+        int32_t hdr[2] = {info.blockID, (int32_t)gh.size()};
+        fwrite(hdr, 4, 2, f);
+        for (int c = 0; c < 27; c++) {
+            int32_t r[2] = {(int32_t)bb.boundary[c].start, (int32_t)bb.boundary[c].nGhosts};
+            fwrite(r, 4, 2, f);
+        }
+        for (size_t g = 0; g < gh.size(); g++) {
+            int32_t cnt = (int32_t)gh[g].size();
+            fwrite(&cnt, 4, 1, f);
+            for (size_t k = 0; k < gh[g].size(); k++) {
+                const IndexWP &w = gh[g][k];
+                // the weight product as BlockLab forms it, in Real (MRAGBlockLab.h:289)
+                const Real w0 = (Real)bb.weightsPool[w.weights_index[0]];
+                const Real w1 = (Real)bb.weightsPool[w.weights_index[1]];
+                const Real w2 = (Real)bb.weightsPool[w.weights_index[2]];
+                const Real wr = w0 * w1 * w2;
+                int32_t src[2] = {pool[w.point_index].blockID, pool[w.point_index].index};
+                double wd = (double)wr;
+                fwrite(src, 4, 2, f);
+                fwrite(&wd, 8, 1, f);
+            }
+        }
+        bb.release();
+    }
+}
+
+static void writeFwt(FILE *f, Grid<W, B> &grid) {
+    std::vector<BlockInfo> vInfo = grid.getBlocksInfo();
+    vector<FWTReport<1> > rep = BlockFWT<W, B, RD_Projector_Wavelets>::template multichannel_fwt<0, 0>(
+        vInfo, grid.getBlockCollection(), grid.getBoundaryInfo());
+    int32_t nb = (int32_t)vInfo.size();
+    fwrite(&nb, 4, 1, f);
+    for (size_t i = 0; i < vInfo.size(); i++) {
+        double d = rep[i].getOverAll_DetailMaxMag();
+        fwrite(&d, 8, 1, f);
+    }
+}
+
+// Adaptive state for the AMR fixtures: run the time loop (regridding at dump
+// times, without run()'s final refinement), then write S0 = blocks + ghost tables + FWT detail maxima; take
+// `extra` more steps without regridding and write S1 = blocks; then one
+// regrid (refinement then compression, as at a dump time) and write
+// S2 = blocks.
+static int cmdState(const char *inp, const char *outp, int extra) {
+    Input in = readInput(inp);
+    Sim s(in.bpd);
+    fillGrid(*s.grid, in);
+    RunInfo ri = runLoop(s, in, true, nullptr, false);
+    FILE *f = fopen(outp, "wb");
+    if (!f) die("cannot open output");
+    fwrite("GBGSTA01", 1, 8, f);
+    int32_t hdr[4] = {in.n, (int32_t)sizeof(Real), (int32_t)ri.steps, ri.regrids};
+    fwrite(hdr, 4, 4, f);
+    double dh[4] = {ri.dt, ri.Dw_unit, ri.Dg_unit, ri.rho};
+    fwrite(dh, 8, 4, f);
+    writeBlocks(f, *s.grid);
+    writeGhostTables(f, *s.grid);
+    writeFwt(f, *s.grid);
+    const int gran = (s.grid->getBlocksInfo().size() <= 8 ? 1 : 4);
+    for (int k = 0; k < extra; ++k)
+        s.step(&s.grid->getBoundaryInfo(), gran, (Real)ri.Dw_unit, (Real)ri.Dg_unit, (Real)ri.rho, ri.dt);
+    writeBlocks(f, *s.grid);
+    s.regrid();
+    writeBlocks(f, *s.grid);
+    fclose(f);
+    return 0;
+}
+
 static int cmdTiming(const char *inp, int nthreads) {
     Environment::setup(nthreads);
     Input in = readInput(inp);
@@ -357,6 +441,7 @@ int main(int argc, const char **argv) {
     if (cmd == "solve") return cmdSolve(argv[2], argv[3]);
     if (cmd == "ghosts") return cmdGhosts(argv[2], argv[3]);
     if (cmd == "fwt") return cmdFwt(argv[2], argv[3]);
+    if (cmd == "state") return cmdState(argv[2], argv[3], argc > 4 ? atoi(argv[4]) : 10);
     die("unknown command");
     return 2;
 }

@@ -104,3 +104,71 @@ def run_harness(cmd, variant, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, adapti
         if cmd == "fwt":
             return read_fwt(outp)
     raise ValueError(cmd)
+
+
+def _read_blocks(raw, off):
+    (nb,) = struct.unpack_from("<i", raw, off)
+    off += 4
+    blocks = []
+    for _ in range(nb):
+        bid, lvl, ix, iy, iz = struct.unpack_from("<5i", raw, off)
+        off += 20
+        d = np.frombuffer(raw, "<f8", 3 * 4096, off).reshape(3, 16, 16, 16).copy()
+        off += 8 * 3 * 4096
+        blocks.append(dict(id=bid, level=lvl, index=(ix, iy, iz), phi=d[0], p_w=d[1], p_g=d[2]))
+    return blocks, off
+
+
+def read_state(path):
+    """Output of `ref_harness state`: S0 blocks + ghost tables + FWT maxima,
+    S1 blocks (after k more steps), S2 blocks (after one more regrid)."""
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"GBGSTA01"
+    n, real_bytes, steps, regrids = struct.unpack_from("<4i", raw, 8)
+    dt, dw, dg, rho = struct.unpack_from("<4d", raw, 24)
+    off = 56
+    s0, off = _read_blocks(raw, off)
+    (nb,) = struct.unpack_from("<i", raw, off)
+    off += 4
+    ghosts = []
+    for _ in range(nb):
+        bid, ng = struct.unpack_from("<2i", raw, off)
+        off += 8
+        regions = np.frombuffer(raw, "<i4", 54, off).reshape(27, 2).copy()
+        off += 4 * 54
+        counts = np.empty(ng, dtype=np.int32)
+        src_b, src_c, w = [], [], []
+        for g in range(ng):
+            (cnt,) = struct.unpack_from("<i", raw, off)
+            off += 4
+            counts[g] = cnt
+            for _k in range(cnt):
+                sb, sc = struct.unpack_from("<2i", raw, off)
+                (ww,) = struct.unpack_from("<d", raw, off + 8)
+                off += 16
+                src_b.append(sb)
+                src_c.append(sc)
+                w.append(ww)
+        ghosts.append(dict(id=bid, regions=regions, counts=counts,
+                           src_block=np.array(src_b, dtype=np.int32),
+                           src_cell=np.array(src_c, dtype=np.int32), w=np.array(w)))
+    (nb2,) = struct.unpack_from("<i", raw, off)
+    off += 4
+    fwt = np.frombuffer(raw, "<f8", nb2, off).copy()
+    off += 8 * nb2
+    s1, off = _read_blocks(raw, off)
+    s2, off = _read_blocks(raw, off)
+    return dict(n=n, real_bytes=real_bytes, steps=steps, regrids=regrids, dt=dt, Dw=dw, Dg=dg,
+                rho=rho, s0=s0, ghosts=ghosts, fwt=fwt, s1=s1, s2=s2)
+
+
+def run_state(variant, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, dumpfreq, extra=10,
+              timeout=3600):
+    exe = os.path.join(REF_DIR, f"ref_harness_{variant}")
+    with tempfile.TemporaryDirectory() as td:
+        inp = os.path.join(td, "in.bin")
+        outp = os.path.join(td, "out.bin")
+        write_input(inp, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, 1, -1, dumpfreq)
+        subprocess.run([exe, "state", inp, outp, str(extra)], check=True, timeout=timeout,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+        return read_state(outp)

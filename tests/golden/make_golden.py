@@ -124,8 +124,60 @@ def lik_fixture():
         json.dump(res, f, indent=1)
 
 
+def region_starts():
+    """Start of each of the 27 neighbour regions in a block's ghost list for
+    the stencil [-1, 2) (region 13, the block itself, has none)."""
+    out, start = [], 0
+    for c in range(27):
+        d = (c % 3 - 1, (c // 3) % 3 - 1, (c // 9) % 3 - 1)
+        size = int(np.prod([16 if x == 0 else 1 for x in d]))
+        out.append((start if c != 13 else 0, size if c != 13 else 0))
+        if c != 13:
+            start += size
+    return out
+
+
+def amr_fixtures():
+    """Adaptive 64^3-effective grid (4^3 blocks at level 2, maximum level 2):
+    the reference time loop with a regrid every 25 days to T = 60, then its
+    blocks, ghost tables and FWT maxima, and the blocks after 10 more steps."""
+    a = np.load(os.path.join(HERE, "anatomy64.npz"))
+    pw, pg = a["p_w"].astype(np.float64), a["p_g"].astype(np.float64)
+    an = S.Anatomy(n=64, p_w=pw, p_g=pg, psi=None)
+    phi0 = f32(S.gaussian_ic(an, 20.3, 24.6, 22.1, peak=0.5, sigma=1.5))
+    for variant in ("f64", "f32"):
+        st = refio.run_state(f"{variant}_l2", 64, 4, pw, pg, phi0, 0.0013, 0.1, 60.0, 6.4, 25.0,
+                             extra=10)
+        blocks = st["s0"]
+        slot = {b["id"]: i for i, b in enumerate(blocks)}
+        rs = region_starts()
+        counts, sb, sc, w = [], [], [], []
+        for g in st["ghosts"]:
+            # region 13 is the block itself; MRAG leaves its record unset
+            got = [tuple(r) for i, r in enumerate(g["regions"]) if i != 13]
+            assert got == [r for i, r in enumerate(rs) if i != 13], "region layout differs"
+            counts.append(g["counts"])
+            sb.append(np.array([slot[x] for x in g["src_block"]], dtype=np.int32))
+            sc.append(g["src_cell"])
+            w.append(g["w"])
+        counts = np.concatenate(counts)
+        start = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        assert [b["id"] for b in st["s1"]] == [b["id"] for b in blocks]
+        np.savez_compressed(
+            os.path.join(HERE, f"amr64_{variant}.npz"),
+            blocks=np.array([[b["level"], *b["index"]] for b in blocks], dtype=np.int32),
+            p_w=np.stack([b["p_w"] for b in blocks]), p_g=np.stack([b["p_g"] for b in blocks]),
+            phi=np.stack([b["phi"] for b in blocks]), ghost_start=start,
+            ghost_src_block=np.concatenate(sb), ghost_src_cell=np.concatenate(sc).astype(np.int16),
+            ghost_w=np.concatenate(w).astype(np.float32), fwt=st["fwt"],
+            phi_after=np.stack([b["phi"] for b in st["s1"]]), steps_after=10,
+            dt=st["dt"], Dw=st["Dw"], Dg=st["Dg"], rho=st["rho"],
+            s2_levels=np.array([b["level"] for b in st["s2"]], dtype=np.int32))
+
+
 if __name__ == "__main__":
     rd_fixtures()
     lik_fixture()
+    amr_fixtures()
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
