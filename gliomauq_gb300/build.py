@@ -38,6 +38,32 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
+CLI = os.path.join(PKG, "cli")
+BIN = os.path.join(PKG, "bin")
+CLI_PROGRAMS = ["gbg_brain", "gbg_likelihood"]
+
+
+def build_cli() -> list[str]:
+    """The file-compatible brain/likelihood programs, linked to libgbglioma.so."""
+    os.makedirs(BIN, exist_ok=True)
+    cxx = shutil.which("g++") or "g++"
+    out = []
+
+    def one(name):
+        exe = os.path.join(BIN, name)
+        cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(os.path.dirname(PKG), "include"),
+               os.path.join(CLI, name + ".cpp"), "-o", exe, "-L" + PKG, "-lgbglioma",
+               "-Wl,-rpath,$ORIGIN/.."]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"{name} failed to build:\n{r.stderr}")
+        return exe
+
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        out = list(ex.map(one, CLI_PROGRAMS))
+    return out
+
+
 def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     """Compile every kernel source and link libgbglioma.so; returns its path."""
     os.makedirs(BUILD, exist_ok=True)
@@ -48,8 +74,9 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_cli()
     if verbose:
-        print(f"built {LIB}")
+        print(f"built {LIB} and {', '.join(CLI_PROGRAMS)}")
     return LIB
 
 

@@ -175,9 +175,93 @@ def amr_fixtures():
             s2_levels=np.array([b["level"] for b in st["s2"]], dtype=np.int32))
 
 
+def patient_files(d, pat):
+    """Write a synthetic patient the way the reference's `brain` reads it:
+    <d>/Anatmoy/Patient01/P01_{GM,WM,CSF,T1,T2}.dat; returns the work folder
+    <d>/run/work (the reference opens ../../Anatmoy/... from there)."""
+    folder = os.path.join(d, "Anatmoy", "Patient01")
+    os.makedirs(folder)
+    for k in ("GM", "WM", "CSF", "T1", "T2"):
+        matrix_io.write_d3d(os.path.join(folder, f"P01_{k}.dat"), pat[k].astype(np.float64))
+    work = os.path.join(d, "run", "work")
+    os.makedirs(work)
+    np.array(pat["ic"], dtype="<f4").tofile(os.path.join(work, "HGG_TumorIC.bin"))
+    with open(os.path.join(work, "HGG_InputParameters.txt"), "w") as f:
+        f.write("\n".join(repr(float(x)) for x in pat["params"]) + "\n")
+    return work
+
+
+def synthetic_patient():
+    """32^3 patient anatomy (float32-exact values): GM/WM from the seeded
+    anatomy, a CSF pocket, T1/T2 lesion masks around the tumour centre."""
+    an = S.make_anatomy(32, seed=5)
+    n = 32
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    r = np.sqrt((x - 20.0) ** 2 + (y - 14.0) ** 2 + (z - 16.0) ** 2)
+    csf = np.where((r < 3.5) & an.brain, 0.6, 0.0)
+    rt = np.sqrt((x - 15.0) ** 2 + (y - 17.0) ** 2 + (z - 15.0) ** 2)
+    t1 = (rt < 1.5).astype(np.float64)
+    t2 = (rt < 2.5).astype(np.float64)
+    return dict(GM=f32(an.p_g), WM=f32(an.p_w), CSF=f32(csf), T1=t1, T2=t2,
+                ic=[15.2 / 32, 17.1 / 32, 15.3 / 32], params=[0.0013, 0.2, 60.0])
+
+
+def cli_fixture():
+    """The reference's own `brain` (Glioma_HG_UQ.cpp built unmodified, FP32,
+    4^3 blocks) and `likelihood` on a synthetic patient: hashes and values
+    for gbg_brain / gbg_likelihood."""
+    pat = synthetic_patient()
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        work = patient_files(td, pat)
+        subprocess.run([os.path.join(refio.REF_DIR, "brain"), "-anatomy", "HGG_UQ", "-pID", "1",
+                        "-adaptive", "0", "-dumpfreq", "1000", "-vtk", "0", "-verbose", "0",
+                        "-nthreads", "1"], cwd=work, check=True, capture_output=True)
+        u = matrix_io.read_d3d(os.path.join(work, "HGG_data.dat"))
+        out["brain"] = dict(sha256=sha(u), sum=float(u.sum()), max=float(u.max()), n=u.shape[0])
+        # the initial state alone: tend < 0 takes no step
+        with open(os.path.join(work, "HGG_InputParameters.txt"), "w") as f:
+            f.write("0.0013\n0.2\n-1\n")
+        subprocess.run([os.path.join(refio.REF_DIR, "brain"), "-anatomy", "HGG_UQ", "-pID", "1",
+                        "-adaptive", "0", "-dumpfreq", "1000", "-vtk", "0", "-verbose", "0",
+                        "-nthreads", "1"], cwd=work, check=True, capture_output=True)
+        u0 = matrix_io.read_d3d(os.path.join(work, "HGG_data.dat"))
+        out["brain_ic"] = dict(sha256=sha(u0), sum=float(u0.sum()), max=float(u0.max()))
+        obs = cli_observations(u)
+        for k, v in obs.items():
+            if k == "Sphere":
+                matrix_io.write_d2d(os.path.join(work, "Sphere.dat"), v)
+            else:
+                matrix_io.write_d3d(os.path.join(work, f"{k}_data.dat"), v)
+        with open(os.path.join(work, "LikelihoodInput.txt"), "w") as f:
+            f.write("\n".join(repr(x) for x in LIK_PARAMS) + "\n")
+        p = subprocess.run([os.path.join(refio.REF_DIR, "likelihood")], cwd=work,
+                           capture_output=True, text=True, check=True)
+        out["likelihood"] = float(open(os.path.join(work, "Likelihood.txt")).read().split()[0])
+        out["likelihood_stdout"] = p.stdout.strip().splitlines()[-3:]
+    np.savez_compressed(os.path.join(HERE, "patient32.npz"),
+                        **{k: np.asarray(v, dtype=np.float32) for k, v in pat.items()
+                           if k in ("GM", "WM", "CSF", "T1", "T2")},
+                        ic=np.array(pat["ic"], dtype=np.float32), params=np.array(pat["params"]))
+    with open(os.path.join(HERE, "patient32.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+def cli_observations(u):
+    """Observations of a model field, deterministic from a seed (numpy only)."""
+    rng = np.random.default_rng(21)
+    t1 = (u > 0.7).astype(np.float64)
+    t2 = (u > 0.25).astype(np.float64)
+    pet = np.where(u > 0, np.maximum(0.0, u + rng.normal(0, 0.05, u.shape)), 0.0)
+    zz, yy, xx = np.nonzero(u > 1e-6)
+    pts = np.stack([xx, yy, zz], axis=0).astype(np.float64)  # D2D: row j = coordinate j
+    return dict(PET=pet, T1=t1, T2=t2, Sphere=pts)
+
+
 if __name__ == "__main__":
     rd_fixtures()
     lik_fixture()
     amr_fixtures()
+    cli_fixture()
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
