@@ -28,7 +28,7 @@ EXPORTS = [
     "gbg_stream", "gbg_sync", "gbg_last_population_ms", "gbg_loglik_noalloc",
     "gbg_population_variants", "gbg_set_population_variant", "gbg_population_variant_shape",
     "gbg_autotune", "gbg_amr_create", "gbg_amr_set_grid", "gbg_amr_set_ghosts", "gbg_amr_step",
-    "gbg_amr_get_phi", "gbg_amr_fwt_detail",
+    "gbg_amr_get_phi", "gbg_amr_fwt_detail", "gbg_adjoint_grad",
 ]
 
 
@@ -61,6 +61,11 @@ class LikResult(C.Structure):
 class Sample(C.Structure):
     _fields_ = [("Dw", C.c_double), ("rho", C.c_double), ("x0", C.c_double), ("y0", C.c_double),
                 ("z0", C.c_double), ("tend", C.c_double)]
+
+
+class AdjointOpts(C.Structure):
+    _fields_ = [("dt0", C.c_double), ("checkpoint_every", C.c_int), ("L", C.c_double),
+                ("ic_peak", C.c_double), ("ic_sigma", C.c_double), ("state_precision", C.c_int)]
 
 
 class AmrConfig(C.Structure):
@@ -108,6 +113,7 @@ def load(path: str = LIB_PATH):
         "gbg_population_variant_shape": [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)],
         "gbg_autotune": [vp, C.c_int, C.c_char_p, C.POINTER(C.c_int)],
+        "gbg_adjoint_grad": [vp, C.POINTER(Sample), C.c_int, C.POINTER(AdjointOpts), dp, dp],
         "gbg_amr_create": [C.POINTER(AmrConfig), C.POINTER(vp)],
         "gbg_amr_set_grid": [vp, C.c_int, vp, dp, dp, dp],
         "gbg_amr_set_ghosts": [vp, vp, vp, vp, dp, C.c_long],
@@ -242,6 +248,19 @@ class Handle:
         check(self.lib.gbg_batch_solve_device(self._h, C.c_void_p(samples_dev_ptr), S,
                                               C.byref(opts),
                                               C.c_void_p(lik_dev_ptr) if lik_dev_ptr else None))
+
+    def adjoint_grad(self, samples, dt0, L, ic_peak=0.1, ic_sigma=1.0, checkpoint_every=50,
+                     state="f32", want_grad=True):
+        """(loglik[S], grad[S, 6]) of the smooth-time-grid forward model;
+        grad columns: Dw, rho, x0, y0, z0, tend."""
+        S = len(samples)
+        arr = (Sample * S)(*[Sample(*s) for s in samples])
+        o = AdjointOpts(dt0, checkpoint_every, L, ic_peak, ic_sigma, PREC_BY_NAME[state])
+        ll = np.zeros(S)
+        g = np.zeros((S, 6))
+        check(self.lib.gbg_adjoint_grad(self._h, arr, S, C.byref(o), dptr(ll),
+                                        dptr(g) if want_grad else None))
+        return ll, (g if want_grad else None)
 
     def launch_count(self) -> int:
         c = C.c_longlong()

@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr"]
 NOFMA = {"rd_exact.cu", "likelihood.cu", "amr.cu"}
-SOURCES = ["abi.cu", "rd_exact.cu", "rd_fast.cu", "likelihood.cu", "amr.cu"]
+SOURCES = ["abi.cu", "rd_exact.cu", "rd_fast.cu", "likelihood.cu", "amr.cu", "adjoint.cu"]
 
 
 def nvcc() -> str:
@@ -51,7 +51,10 @@ def build_cli() -> list[str]:
 
     def one(name):
         exe = os.path.join(BIN, name)
-        cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(os.path.dirname(PKG), "include"),
+        # -ffp-contract=off: no fused multiply-add (GCC contracts by default on
+        # Arm), so the restated initial state rounds as the reference does
+        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off",
+               "-I" + os.path.join(os.path.dirname(PKG), "include"),
                os.path.join(CLI, name + ".cpp"), "-o", exe, "-L" + PKG, "-lgbglioma",
                "-Wl,-rpath,$ORIGIN/.."]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -420,6 +420,33 @@ int gbg_batch_solve(gbg_handle *hh, const gbg_sample *samples, int S, const gbg_
     return GBG_OK;
 }
 
+int gbg_adjoint_grad(gbg_handle *hh, const gbg_sample *samples, int S, const gbg_adjoint_opts *o,
+                     double *loglik, double *grad) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (h.is_amr) {
+        set_error("the adjoint runs on uniform-grid handles");
+        return GBG_ERR_STATE;
+    }
+    if (!samples || S < 1 || !o || !(o->dt0 > 0) || !(o->L > 0) || !(o->ic_sigma > 0) ||
+        o->checkpoint_every < 0 || (o->state_precision != GBG_PREC_F32 && o->state_precision != GBG_PREC_F64)) {
+        set_error("bad adjoint arguments");
+        return GBG_ERR_ARG;
+    }
+    for (int s = 0; s < S; ++s)
+        if (!std::isfinite(samples[s].Dw) || !std::isfinite(samples[s].rho) || !std::isfinite(samples[s].tend) ||
+            !(samples[s].tend > 0) || samples[s].tend / o->dt0 > 1e6) {
+            set_error("non-finite or out-of-range sample parameter");
+            return GBG_ERR_NONFINITE;
+        }
+    if (!h.anatomy_set || !h.obs.valid) {
+        set_error("set anatomy and observations first");
+        return GBG_ERR_STATE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    return gbg::adjoint_grad(h, samples, S, *o, loglik, grad);
+}
+
 int gbg_amr_create(const gbg_amr_config *cfg, gbg_handle **out) {
     if (!cfg || !out) {
         set_error("null argument");

@@ -1,0 +1,444 @@
+// Discrete adjoint of the tumour-growth solve for MALA gradients of the
+// imaging log-likelihood with respect to (Dw, rho, x0, y0, z0, T).
+//
+// Forward model (its own discretisation, smooth in the parameters): the
+// reference's time loop has dt = dt(Dw) and an integer step count, so its
+// output is piecewise constant in Dw and T. Here every sample of a call uses
+// one fixed step dt0, n = ceil(T/dt0) steps, the last of length
+// T - (n-1) dt0. Each step is the fast-path operator
+//   v   = phi + a_k sum_f c_f (phi_f - phi) + b_k phi (1 - phi)
+//   phi'= m * clamp(v, 0, 1)
+// with a_k = dt_k Dw / (L^2 h^2), b_k = dt_k rho, unit face coefficients c_f
+// (Case2 harmonic means with Dg = 0.1 Dw) and the tissue mask m, from the
+// Gaussian initial density peak * exp(-|x - x0|^2 / (2 sigma^2)) on tissue.
+//
+// Adjoint (L is symmetric, so L^T = L): with lambda = dlogL/dphi at step k+1,
+//   mu_c     = m_c [0 <= v_c < 1] lambda_c
+//   lambda_c'= mu_c (1 + b_k (1 - 2 phi_c)) + a_k sum_f c_f (mu_f - mu_c)
+//   dlogL/da_k = sum_c mu_c L(phi)_c,  dlogL/db_k = sum_c mu_c phi_c (1 - phi_c)
+// The clamp's derivative at v = 0 is taken from the right (cells at exactly 0
+// respond to growth of their neighbours), at v = 1 from the left is dropped.
+// The seed dlogL/dphi at the final state follows HGG_Likelihood's PET and
+// T1/T2 terms (source/Likelihood/source/HGG_Likelihood.cpp:40-153):
+//   PET: -(u - s PET) / sigma^2;  Ti: alpha'/alpha (y = 1) or -alpha'/(1 - alpha)
+//   with alpha' = |d| / slope * exp(-d^2 / slope), d = u - uc.
+// States are checkpointed every K steps and each segment is recomputed
+// before its backward sweep. Templated on the state type: float (the
+// production path) or double (used to check gradients against finite
+// differences).
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+#include <vector>
+
+#include "gbg_internal.cuh"
+
+namespace gbg {
+namespace {
+
+__device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+__device__ __forceinline__ int wp(int i, int n) { return i == n - 1 ? 0 : i + 1; }
+
+template <typename Real>
+__global__ void k_adj_tables(int n, const double *__restrict__ pw, const double *__restrict__ pg,
+                             Real *__restrict__ cx, Real *__restrict__ cy, Real *__restrict__ cz,
+                             Real *__restrict__ msk) {
+    const size_t N = (size_t)n * n * n;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        const size_t nn = n;
+        const size_t nb[7] = {c, c - x + wp(x, n), c + ((size_t)wp(y, n) - y) * nn,
+                              c + ((size_t)wp(z, n) - z) * nn * nn, c - x + wm(x, n),
+                              c + ((size_t)wm(y, n) - y) * nn, c + ((size_t)wm(z, n) - z) * nn * nn};
+        double k[4];
+        bool all = true;
+        for (int i = 0; i < 7; ++i) {
+            const double b = pw[nb[i]] + pg[nb[i]];
+            all = all && b > 0.0;
+            if (i < 4) k[i] = b > 0.0 ? (pw[nb[i]] + 0.1 * pg[nb[i]]) / b : 0.0;
+        }
+        Real *dst[3] = {cx, cy, cz};
+        for (int f = 0; f < 3; ++f) {
+            const double s = k[0] + k[f + 1];
+            dst[f][c] = (k[0] > 0.0 && k[f + 1] > 0.0 && s > 0.0) ? (Real)(2.0 * k[0] * k[f + 1] / s) : (Real)0;
+        }
+        msk[c] = all ? (Real)1 : (Real)0;
+    }
+}
+
+struct Tabs {
+    const void *cx, *cy, *cz, *msk;
+};
+
+// L(f)_c = sum_f c_f (f_nb - f_c)
+template <typename Real>
+__device__ __forceinline__ Real lap(const Real *f, const Real *cx, const Real *cy, const Real *cz, int n,
+                                    size_t c, int x, int y, int z) {
+    const size_t nn = n, pl = nn * nn;
+    const size_t cW = c - x + wm(x, n), cE = c - x + wp(x, n);
+    const size_t cS = c + ((size_t)wm(y, n) - y) * nn, cN = c + ((size_t)wp(y, n) - y) * nn;
+    const size_t cB = c + ((size_t)wm(z, n) - z) * pl, cF = c + ((size_t)wp(z, n) - z) * pl;
+    const Real f0 = f[c];
+    return cx[cW] * (f[cW] - f0) + cx[c] * (f[cE] - f0) + cy[cS] * (f[cS] - f0) + cy[c] * (f[cN] - f0) +
+           cz[cB] * (f[cB] - f0) + cz[c] * (f[cF] - f0);
+}
+
+template <typename Real>
+__global__ void k_adj_ic(int n, int S, const gbg_sample *__restrict__ smp, double peak, double sigma,
+                         const double *__restrict__ pw, const double *__restrict__ pg, Real *__restrict__ phi) {
+    const size_t N = (size_t)n * n * n;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N * S; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = i / N, c = i % N;
+        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        double v = 0.0;
+        if (pw[c] + pg[c] > 0.0) {
+            const double dx = x - smp[s].x0, dy = y - smp[s].y0, dz = z - smp[s].z0;
+            v = peak * exp(-(dx * dx + dy * dy + dz * dz) / (2.0 * sigma * sigma));
+        }
+        phi[i] = (Real)v;
+    }
+}
+
+// one forward step for every active sample (a[s] < 0 marks a finished sample)
+template <typename Real>
+__global__ void k_adj_fwd(int n, int S, const Real *__restrict__ in, Real *__restrict__ out, Tabs t,
+                          const double *__restrict__ a, const double *__restrict__ b) {
+    const size_t N = (size_t)n * n * n;
+    const Real *cx = (const Real *)t.cx, *cy = (const Real *)t.cy, *cz = (const Real *)t.cz,
+               *m = (const Real *)t.msk;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N * S; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = i / N, c = i % N;
+        const Real *f = in + s * N;
+        if (a[s] < 0) {
+            out[i] = f[c];
+            continue;
+        }
+        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        const Real p = f[c];
+        Real v = p + (Real)a[s] * lap(f, cx, cy, cz, n, c, x, y, z) + (Real)b[s] * p * ((Real)1 - p);
+        v = v < (Real)0 ? (Real)0 : (v > (Real)1 ? (Real)1 : v);
+        out[i] = m[c] != (Real)0 ? v : (Real)0;
+    }
+}
+
+template <typename Real>
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int j = 0; j < (int)(blockDim.x >> 5); ++j) t += red[j];
+    return t;
+}
+
+// mu = m [0 <= v < 1] lambda, and this step's parameter sensitivities.
+// grid: x over cells of one sample, y = sample
+template <typename Real>
+__global__ void k_adj_mu(int n, const Real *__restrict__ phi, const Real *__restrict__ lam, Real *__restrict__ mu,
+                         Tabs t, const double *__restrict__ a, const double *__restrict__ b,
+                         double *__restrict__ gA, double *__restrict__ gB) {
+    const size_t N = (size_t)n * n * n;
+    const int s = blockIdx.y;
+    const Real *cx = (const Real *)t.cx, *cy = (const Real *)t.cy, *cz = (const Real *)t.cz,
+               *m = (const Real *)t.msk;
+    const Real *f = phi + (size_t)s * N;
+    double sa = 0.0, sbb = 0.0;
+    const bool act = a[s] >= 0;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = (size_t)s * N + c;
+        if (!act) {
+            mu[i] = lam[i];
+            continue;
+        }
+        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        const Real p = f[c];
+        const Real L = lap(f, cx, cy, cz, n, c, x, y, z);
+        const Real v = p + (Real)a[s] * L + (Real)b[s] * p * ((Real)1 - p);
+        const Real g = (m[c] != (Real)0 && v >= (Real)0 && v < (Real)1) ? (Real)1 : (Real)0;
+        const Real u = g * lam[i];
+        mu[i] = u;
+        sa += (double)u * (double)L;
+        sbb += (double)u * (double)p * (1.0 - (double)p);
+    }
+    const double ta = block_sum<Real>(sa);
+    const double tb = block_sum<Real>(sbb);
+    if (threadIdx.x == 0 && act) {
+        atomicAdd(gA + s, ta);
+        atomicAdd(gB + s, tb);
+    }
+}
+
+template <typename Real>
+__global__ void k_adj_lam(int n, int S, const Real *__restrict__ phi, const Real *__restrict__ mu,
+                          Real *__restrict__ lam, Tabs t, const double *__restrict__ a, const double *__restrict__ b) {
+    const size_t N = (size_t)n * n * n;
+    const Real *cx = (const Real *)t.cx, *cy = (const Real *)t.cy, *cz = (const Real *)t.cz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N * S; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = i / N, c = i % N;
+        const Real *u = mu + s * N;
+        if (a[s] < 0) {
+            lam[i] = u[c];
+            continue;
+        }
+        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        const Real p = phi[i];
+        lam[i] = u[c] * ((Real)1 + (Real)b[s] * ((Real)1 - (Real)2 * p)) + (Real)a[s] * lap(u, cx, cy, cz, n, c, x, y, z);
+    }
+}
+
+// dlogL/du at the final state: PET list, then the T list (two launches keep
+// the order of additions fixed where a cell is in both lists)
+template <typename Real>
+__global__ void k_adj_seed_pet(int S, size_t N, int npet, const int *__restrict__ idx, const double *__restrict__ val,
+                               double scale, double sigma2, const Real *__restrict__ phi, Real *__restrict__ lam) {
+    const long total = (long)npet * S;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const size_t s = i / npet, c = idx[i % npet];
+        const double u = phi[s * N + c];
+        lam[s * N + c] = (Real)(-(u - scale * val[i % npet]) / sigma2);
+    }
+}
+
+template <typename Real>
+__global__ void k_adj_seed_ti(int S, size_t N, int nti, const int *__restrict__ idx, const double *__restrict__ y1,
+                              const double *__restrict__ y2, double uc1, double uc2, double slope,
+                              const Real *__restrict__ phi, Real *__restrict__ lam) {
+    const long total = (long)nti * S;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const size_t s = i / nti;
+        const int j = (int)(i % nti);
+        const size_t c = idx[j];
+        const double u = phi[s * N + c];
+        double g = 0.0;
+        for (int ti = 0; ti < 2; ++ti) {
+            const double d = u - (ti == 0 ? uc1 : uc2);
+            const double sg = d < 0 ? -1.0 : (d > 0 ? 1.0 : 0.0);
+            const double e = exp(-d * d / slope);
+            const double alpha = 0.5 + 0.5 * sg * (1. - e);
+            const double dal = fabs(d) / slope * e;
+            const double y = ti == 0 ? y1[j] : y2[j];
+            g += (y == 1) ? dal / alpha : -dal / (1. - alpha);
+        }
+        lam[s * N + c] = (Real)((double)lam[s * N + c] + g);
+    }
+}
+
+// dlogL/dx0 = sum_c lambda0_c * phi0_c * (x_c - x0) / sigma^2 (same for y0, z0)
+template <typename Real>
+__global__ void k_adj_ic_grad(int n, const gbg_sample *__restrict__ smp, double sigma, const Real *__restrict__ lam,
+                              const Real *__restrict__ phi0, double *__restrict__ gx) {
+    const size_t N = (size_t)n * n * n;
+    const int s = blockIdx.y;
+    double acc[3] = {0, 0, 0};
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = (size_t)s * N + c;
+        const double w = (double)lam[i] * (double)phi0[i] / (sigma * sigma);
+        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        acc[0] += w * (x - smp[s].x0);
+        acc[1] += w * (y - smp[s].y0);
+        acc[2] += w * (z - smp[s].z0);
+    }
+    for (int k = 0; k < 3; ++k) {
+        const double t = block_sum<Real>(acc[k]);
+        if (threadIdx.x == 0) atomicAdd(gx + 3 * s + k, t);
+    }
+}
+
+int grid_of(const Handle &h, size_t work) {
+    const size_t blocks = (work + 255) / 256;
+    const size_t cap = (size_t)h.num_sms * 16;
+    return (int)(blocks < cap ? blocks : cap);
+}
+
+template <typename Real>
+int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_opts &o, double *loglik,
+                double *grad) {
+    const int n = h.n;
+    const size_t N = h.N;
+    const double hh = 1.0 / n, ih2 = 1.0 / (hh * hh), L2 = o.L * o.L;
+    // per-sample step counts on the smooth time grid
+    std::vector<int> ns(S);
+    std::vector<double> dtl(S);
+    int nmax = 0;
+    for (int s = 0; s < S; ++s) {
+        const double T = samples[s].tend;
+        int k = (int)std::ceil(T / o.dt0);
+        if (k < 1) k = 1;
+        ns[s] = k;
+        dtl[s] = T - (k - 1) * o.dt0;
+        nmax = std::max(nmax, k);
+    }
+    const int K = o.checkpoint_every > 0 ? o.checkpoint_every : 50;
+    const int nck = nmax / K + 1;
+    // device buffers (freed at the end of the call)
+    std::vector<void *> owned;
+    auto alloc = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+        owned.push_back(p);
+        return p;
+    };
+    auto release = [&]() {
+        for (void *p : owned) cudaFree(p);
+    };
+    Real *tab = (Real *)alloc(4 * N * sizeof(Real));
+    Real *ck = (Real *)alloc((size_t)nck * S * N * sizeof(Real));
+    Real *seg = (Real *)alloc((size_t)K * S * N * sizeof(Real));
+    Real *lam = (Real *)alloc(S * N * sizeof(Real));
+    Real *mu = (Real *)alloc(S * N * sizeof(Real));
+    Real *fin = (Real *)alloc(S * N * sizeof(Real));
+    double *da = (double *)alloc((size_t)nmax * S * sizeof(double));
+    double *db = (double *)alloc((size_t)nmax * S * sizeof(double));
+    double *gA = (double *)alloc((size_t)nmax * S * sizeof(double));
+    double *gB = (double *)alloc((size_t)nmax * S * sizeof(double));
+    double *gX = (double *)alloc(3 * S * sizeof(double));
+    gbg_sample *dsm = (gbg_sample *)alloc(S * sizeof(gbg_sample));
+    gbg_lik_result *dlik = (gbg_lik_result *)alloc(S * sizeof(gbg_lik_result));
+    for (void *p : owned)
+        if (!p) {
+            release();
+            set_error("adjoint: device allocation failed");
+            return GBG_ERR_NOMEM;
+        }
+    if (owned.size() != 13) {
+        release();
+        set_error("adjoint: device allocation failed");
+        return GBG_ERR_NOMEM;
+    }
+    // per-step coefficients; a < 0 marks a finished sample
+    std::vector<double> ha((size_t)nmax * S), hb((size_t)nmax * S);
+    for (int k = 0; k < nmax; ++k)
+        for (int s = 0; s < S; ++s) {
+            const double dtk = k < ns[s] - 1 ? o.dt0 : (k == ns[s] - 1 ? dtl[s] : 0.0);
+            ha[(size_t)k * S + s] = k < ns[s] ? dtk * samples[s].Dw / L2 * ih2 : -1.0;
+            hb[(size_t)k * S + s] = k < ns[s] ? dtk * samples[s].rho : 0.0;
+        }
+    cudaStream_t st = h.stream;
+    int rc = GBG_OK;
+#define ADJ_TRY(expr)                                                        \
+    do {                                                                     \
+        cudaError_t _e = (expr);                                             \
+        if (_e != cudaSuccess) {                                             \
+            set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));   \
+            release();                                                       \
+            return GBG_ERR_CUDA;                                             \
+        }                                                                    \
+    } while (0)
+    ADJ_TRY(cudaMemcpyAsync(da, ha.data(), ha.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    ADJ_TRY(cudaMemcpyAsync(db, hb.data(), hb.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    ADJ_TRY(cudaMemcpyAsync(dsm, samples, S * sizeof(gbg_sample), cudaMemcpyHostToDevice, st));
+    ADJ_TRY(cudaMemsetAsync(gA, 0, (size_t)nmax * S * sizeof(double), st));
+    ADJ_TRY(cudaMemsetAsync(gB, 0, (size_t)nmax * S * sizeof(double), st));
+    ADJ_TRY(cudaMemsetAsync(gX, 0, 3 * S * sizeof(double), st));
+    Tabs t{tab, tab + N, tab + 2 * N, tab + 3 * N};
+    k_adj_tables<Real><<<grid_of(h, N), 256, 0, st>>>(n, h.pw, h.pg, tab, tab + N, tab + 2 * N, tab + 3 * N);
+    k_adj_ic<Real><<<grid_of(h, N * S), 256, 0, st>>>(n, S, dsm, o.ic_peak, o.ic_sigma, h.pw, h.pg, ck);
+    h.launches += 2;
+    // forward with checkpoints
+    const int gS = grid_of(h, N * S);
+    {
+        Real *cur = ck;
+        for (int k = 0; k < nmax; ++k) {
+            Real *nxt = ((k + 1) % K == 0) ? ck + (size_t)((k + 1) / K) * S * N
+                                           : ((k + 1) == nmax ? fin : seg + (size_t)((k + 1) % K) * S * N);
+            k_adj_fwd<Real><<<gS, 256, 0, st>>>(n, S, cur, nxt, t, da + (size_t)k * S, db + (size_t)k * S);
+            h.launches++;
+            cur = nxt;
+        }
+        if (nmax % K == 0) ADJ_TRY(cudaMemcpyAsync(fin, ck + (size_t)(nmax / K) * S * N, S * N * sizeof(Real),
+                                                   cudaMemcpyDeviceToDevice, st));
+    }
+    // log-likelihood and its gradient at the final state
+    {
+        rc = std::is_same<Real, float>::value
+                 ? lik_evaluate(h, (const float *)fin, nullptr, S, dlik)
+                 : lik_evaluate(h, nullptr, (const double *)fin, S, dlik);
+        if (rc) {
+            release();
+            return rc;
+        }
+        ADJ_TRY(cudaMemsetAsync(lam, 0, S * N * sizeof(Real), st));
+        const ObsDevice &ob = h.obs;
+        if (ob.n_pet > 0)
+            k_adj_seed_pet<Real><<<grid_of(h, (size_t)ob.n_pet * S), 256, 0, st>>>(
+                S, N, ob.n_pet, ob.pet_idx, ob.pet_val, ob.pet_scale, ob.pet_sigma2, fin, lam);
+        if (ob.n_ti > 0)
+            k_adj_seed_ti<Real><<<grid_of(h, (size_t)ob.n_ti * S), 256, 0, st>>>(
+                S, N, ob.n_ti, ob.ti_idx, ob.t1_val, ob.t2_val, ob.t1_uc, ob.t2_uc, ob.slope, fin, lam);
+        h.launches += 2;
+    }
+    if (!grad) {
+        std::vector<gbg_lik_result> hl(S);
+        ADJ_TRY(cudaMemcpyAsync(hl.data(), dlik, S * sizeof(gbg_lik_result), cudaMemcpyDeviceToHost, st));
+        ADJ_TRY(cudaStreamSynchronize(st));
+        release();
+        for (int s = 0; s < S; ++s)
+            if (loglik) loglik[s] = hl[s].total;
+        return GBG_OK;
+    }
+    // backward, segment by segment
+    const dim3 gC((unsigned)std::min<size_t>((N + 255) / 256, (size_t)h.num_sms * 4), (unsigned)S);
+    for (int sgm = (nmax - 1) / K; sgm >= 0; --sgm) {
+        const int k0 = sgm * K, k1 = std::min(nmax, k0 + K);
+        // recompute states k0+1 .. k1-1 into seg[1..]
+        ADJ_TRY(cudaMemcpyAsync(seg, ck + (size_t)sgm * S * N, S * N * sizeof(Real), cudaMemcpyDeviceToDevice, st));
+        for (int k = k0; k < k1 - 1; ++k) {
+            k_adj_fwd<Real><<<gS, 256, 0, st>>>(n, S, seg + (size_t)(k - k0) * S * N,
+                                                seg + (size_t)(k - k0 + 1) * S * N, t, da + (size_t)k * S,
+                                                db + (size_t)k * S);
+            h.launches++;
+        }
+        for (int k = k1 - 1; k >= k0; --k) {
+            const Real *phik = seg + (size_t)(k - k0) * S * N;
+            k_adj_mu<Real><<<gC, 256, 0, st>>>(n, phik, lam, mu, t, da + (size_t)k * S, db + (size_t)k * S,
+                                               gA + (size_t)k * S, gB + (size_t)k * S);
+            k_adj_lam<Real><<<gS, 256, 0, st>>>(n, S, phik, mu, lam, t, da + (size_t)k * S, db + (size_t)k * S);
+            h.launches += 2;
+        }
+    }
+    k_adj_ic_grad<Real><<<gC, 256, 0, st>>>(n, dsm, o.ic_sigma, lam, ck, gX);
+    h.launches++;
+    ADJ_TRY(cudaGetLastError());
+    std::vector<double> hA((size_t)nmax * S), hB((size_t)nmax * S), hX(3 * S);
+    std::vector<gbg_lik_result> hl(S);
+    ADJ_TRY(cudaMemcpyAsync(hA.data(), gA, hA.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ADJ_TRY(cudaMemcpyAsync(hB.data(), gB, hB.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ADJ_TRY(cudaMemcpyAsync(hX.data(), gX, hX.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ADJ_TRY(cudaMemcpyAsync(hl.data(), dlik, S * sizeof(gbg_lik_result), cudaMemcpyDeviceToHost, st));
+    ADJ_TRY(cudaStreamSynchronize(st));
+    release();
+#undef ADJ_TRY
+    for (int s = 0; s < S; ++s) {
+        double gDw = 0.0, gRho = 0.0;
+        for (int k = 0; k < ns[s]; ++k) {
+            const double dtk = k < ns[s] - 1 ? o.dt0 : dtl[s];
+            gDw += hA[(size_t)k * S + s] * dtk / L2 * ih2;
+            gRho += hB[(size_t)k * S + s] * dtk;
+        }
+        const int kl = ns[s] - 1;
+        const double gT = hA[(size_t)kl * S + s] * samples[s].Dw / L2 * ih2 + hB[(size_t)kl * S + s] * samples[s].rho;
+        double *g = grad + 6 * (size_t)s;
+        g[0] = gDw;
+        g[1] = gRho;
+        g[2] = hX[3 * s];
+        g[3] = hX[3 * s + 1];
+        g[4] = hX[3 * s + 2];
+        g[5] = gT;
+        if (loglik) loglik[s] = hl[s].total;
+    }
+    return GBG_OK;
+}
+
+}  // namespace
+
+int adjoint_grad(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_opts &o, double *loglik,
+                 double *grad) {
+    if (o.state_precision == GBG_PREC_F64) return run_adjoint<double>(h, samples, S, o, loglik, grad);
+    return run_adjoint<float>(h, samples, S, o, loglik, grad);
+}
+
+}  // namespace gbg

@@ -163,6 +163,10 @@ int amr_steps(Handle &h, double Dw, double Dg, double rho, double dt, long nstep
 int amr_get_phi(Handle &h, double *phi);
 int amr_fwt_detail(Handle &h, double *detail);
 
+// ---- adjoint.cu ----
+int adjoint_grad(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_opts &o, double *loglik,
+                 double *grad);
+
 // ---- likelihood.cu ----
 int lik_set_observations(Handle &h, const double *pet, const double *t1, const double *t2,
                          const double *points, long npoints, const gbg_lik_params &p);

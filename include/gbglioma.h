@@ -152,6 +152,31 @@ int gbg_batch_solve(gbg_handle *h, const gbg_sample *samples, int S, const gbg_b
 int gbg_batch_solve_device(gbg_handle *h, const gbg_sample *samples_device, int S,
                            const gbg_batch_opts *o, gbg_lik_result *loglik_device);
 
+/* ---- gradients for MALA: discrete adjoint ----------------------------------------
+ * No reference counterpart for the adjoint itself; the forward model it
+ * differentiates is the fast-path step with a smooth time grid: one fixed
+ * step dt0 for every sample of the call, n = ceil(tend/dt0) steps, the last
+ * one shortened to end exactly at tend (the reference's dt(Dw) and integer
+ * step count make its output piecewise constant in Dw and tend). Gradients
+ * are of the log-likelihood (gbg_set_observations) with respect to
+ * (Dw, rho, x0, y0, z0, tend), in the units of gbg_sample, written as
+ * grad[6*s + 0..5]; loglik[s] receives log L of the same forward model
+ * (either pointer may be null; with grad null no adjoint sweep runs).
+ * States are checkpointed every checkpoint_every steps (0: 50) and each
+ * segment is recomputed for its backward sweep; state_precision is
+ * GBG_PREC_F32 (float states) or GBG_PREC_F64 (double states). Works on
+ * any handle made by gbg_create; allocates its working set per call. */
+typedef struct {
+    double dt0;            /* step in days; e.g. 0.99 h^2 / (6 Dw_max / L^2) */
+    int checkpoint_every;
+    double L;              /* brain length in cm */
+    double ic_peak, ic_sigma;
+    int state_precision;   /* GBG_PREC_F32 or GBG_PREC_F64 */
+} gbg_adjoint_opts;
+
+int gbg_adjoint_grad(gbg_handle *h, const gbg_sample *samples, int S, const gbg_adjoint_opts *o,
+                     double *loglik, double *grad);
+
 /* ---- multiresolution block grid ----------------------------------------------
  * MRAG's grid of 16^3 blocks at mixed levels (source/MRAGcore/MRAGrid.h:44-186):
  * block b at level l covers [index/2^l, (index+1)/2^l) of the unit cube with

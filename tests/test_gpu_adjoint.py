@@ -1,0 +1,85 @@
+"""GPU: MALA gradients from the discrete adjoint (gbg_adjoint_grad) against
+central finite differences of the same forward model, h = 1e-4 relative to
+each parameter; and independence from the checkpoint interval."""
+import numpy as np
+import pytest
+
+from gliomauq_gb300 import _lib, synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+LIK = (0.0025, 1.0, 0.7, 0.25, 0.09)
+NAMES = ["Dw", "rho", "x0", "y0", "z0", "T"]
+
+
+def _problem(n=32):
+    an = S.make_anatomy(n, seed=4)
+    truth = np.clip(S.gaussian_ic(an, 15.0, 16.0, 15.0, peak=0.9, sigma=2.0), 0, 1)
+    obs = S.make_observations(truth, an, seed=3, centre_xyz=(15, 16, 15), radius_vox=9.0)
+    samples = [(0.0013, 0.05, 15.3, 16.2, 15.6, 41.3), (0.0021, 0.12, 14.6, 15.4, 16.3, 27.7)]
+    dt0 = S.reference_dt(n, 0.0025, an.L)[0]  # from the prior's largest Dw
+    return an, obs, samples, dt0
+
+
+def _fd(h, samples, dt0, L, state, rel=1e-4):
+    g = np.zeros((len(samples), 6))
+    for s, base in enumerate(samples):
+        for i in range(6):
+            step = rel * abs(base[i])
+            p, m = list(base), list(base)
+            p[i] += step
+            m[i] -= step
+            lp, _ = h.adjoint_grad([tuple(p)], dt0, L, state=state, want_grad=False)
+            lm, _ = h.adjoint_grad([tuple(m)], dt0, L, state=state, want_grad=False)
+            g[s, i] = (lp[0] - lm[0]) / (2 * step)
+    return g
+
+
+def _rel_err(ga, gf, samples):
+    # compare relative sensitivities theta_i * dlogL/dtheta_i so the units agree
+    th = np.abs(np.array(samples))
+    a, f = ga * th, gf * th
+    return np.linalg.norm(a - f, axis=1) / np.linalg.norm(f, axis=1), a, f
+
+
+@pytest.mark.parametrize("state,tol", [("f64", 1e-5), ("f32", 1e-3)])
+def test_adjoint_gradient_matches_central_differences(gbg, state, tol):
+    an, obs, samples, dt0 = _problem()
+    with _lib.Handle(an.n, "f32") as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=1, step_ti=1)
+        ll, ga = h.adjoint_grad(samples, dt0, an.L, state=state)
+        gf = _fd(h, samples, dt0, an.L, "f64")
+    err, a, f = _rel_err(ga, gf, samples)
+    for s in range(len(samples)):
+        print(f"{state} sample {s}: rel err {err[s]:.2e}")
+        for i in range(6):
+            print(f"   {NAMES[i]:4s} adjoint {a[s, i]: .6e}  fd {f[s, i]: .6e}")
+    assert np.all(np.isfinite(ll)) and np.all(err <= tol)
+
+
+def test_adjoint_is_independent_of_checkpoint_interval(gbg):
+    an, obs, samples, dt0 = _problem()
+    with _lib.Handle(an.n, "f32") as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=1, step_ti=1)
+        ref = h.adjoint_grad(samples, dt0, an.L, checkpoint_every=50)
+        for k in (1, 7, 13):
+            got = h.adjoint_grad(samples, dt0, an.L, checkpoint_every=k)
+            assert np.array_equal(got[0], ref[0])
+            assert np.allclose(got[1], ref[1], rtol=1e-12, atol=0)
+
+
+def test_adjoint_argument_errors(gbg):
+    an, obs, samples, dt0 = _problem()
+    with _lib.Handle(an.n, "f32") as h:
+        with pytest.raises(_lib.GbgError) as e:
+            h.adjoint_grad(samples, dt0, an.L)  # no anatomy / observations
+        assert e.value.status == -5
+        h.set_anatomy(an.p_w, an.p_g)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK)
+        with pytest.raises(_lib.GbgError):
+            h.adjoint_grad(samples, -1.0, an.L)
+        bad = [(np.nan,) + samples[0][1:]]
+        with pytest.raises(_lib.GbgError):
+            h.adjoint_grad(bad, dt0, an.L)

@@ -150,3 +150,34 @@ def test_dropin_backend_compiles_against_reference_types():
                         os.path.join(root, "tests", "cpp", "dropin_reference_compile.cpp")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle",
+                                                    "_ref", "brain")),
+                    reason="reference binaries not built here")
+def test_patient_initial_state_restatement_matches_reference_brain(tmp_path):
+    """gbg_brain's restatement of _ic_PatientCase (cli/patient_ic.hpp) against
+    the reference's own brain run with no time step (tend < 0)."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, os.path.join(root, "tests", "golden"))
+    import make_golden
+    from oracle import refio
+    exe = str(tmp_path / "ic_dump")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                    "-I" + os.path.join(root, "gliomauq_gb300", "cli"),
+                    os.path.join(root, "tests", "cpp", "patient_ic_dump.cpp"), "-o", exe], check=True)
+    d = golden_npz("patient32.npz")
+    pat = {k: d[k].astype(np.float64) for k in ("GM", "WM", "CSF", "T1", "T2")}
+    pat["ic"] = [float(v) for v in d["ic"]]
+    pat["params"] = [0.0013, 0.2, -1.0]
+    work = make_golden.patient_files(str(tmp_path / "p"), pat)
+    subprocess.run([os.path.join(refio.REF_DIR, "brain"), "-anatomy", "HGG_UQ", "-pID", "1",
+                    "-adaptive", "0", "-dumpfreq", "1000", "-vtk", "0", "-verbose", "0",
+                    "-nthreads", "1"], cwd=work, check=True, capture_output=True)
+    ref = matrix_io.read_d3d(os.path.join(work, "HGG_data.dat"))
+    out = str(tmp_path / "mine.dat")
+    subprocess.run([exe, str(tmp_path / "p" / "Anatmoy" / "Patient01" / "P01"),
+                    os.path.join(work, "HGG_TumorIC.bin"), out], check=True)
+    assert np.array_equal(matrix_io.read_d3d(out), ref)
