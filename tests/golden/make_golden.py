@@ -219,14 +219,6 @@ def cli_fixture():
                         "-nthreads", "1"], cwd=work, check=True, capture_output=True)
         u = matrix_io.read_d3d(os.path.join(work, "HGG_data.dat"))
         out["brain"] = dict(sha256=sha(u), sum=float(u.sum()), max=float(u.max()), n=u.shape[0])
-        # the initial state alone: tend < 0 takes no step
-        with open(os.path.join(work, "HGG_InputParameters.txt"), "w") as f:
-            f.write("0.0013\n0.2\n-1\n")
-        subprocess.run([os.path.join(refio.REF_DIR, "brain"), "-anatomy", "HGG_UQ", "-pID", "1",
-                        "-adaptive", "0", "-dumpfreq", "1000", "-vtk", "0", "-verbose", "0",
-                        "-nthreads", "1"], cwd=work, check=True, capture_output=True)
-        u0 = matrix_io.read_d3d(os.path.join(work, "HGG_data.dat"))
-        out["brain_ic"] = dict(sha256=sha(u0), sum=float(u0.sum()), max=float(u0.max()))
         obs = cli_observations(u)
         for k, v in obs.items():
             if k == "Sphere":
@@ -239,6 +231,14 @@ def cli_fixture():
                            capture_output=True, text=True, check=True)
         out["likelihood"] = float(open(os.path.join(work, "Likelihood.txt")).read().split()[0])
         out["likelihood_stdout"] = p.stdout.strip().splitlines()[-3:]
+        # the initial state alone: tend < 0 takes no step
+        with open(os.path.join(work, "HGG_InputParameters.txt"), "w") as f:
+            f.write("0.0013\n0.2\n-1\n")
+        subprocess.run([os.path.join(refio.REF_DIR, "brain"), "-anatomy", "HGG_UQ", "-pID", "1",
+                        "-adaptive", "0", "-dumpfreq", "1000", "-vtk", "0", "-verbose", "0",
+                        "-nthreads", "1"], cwd=work, check=True, capture_output=True)
+        u0 = matrix_io.read_d3d(os.path.join(work, "HGG_data.dat"))
+        out["brain_ic"] = dict(sha256=sha(u0), sum=float(u0.sum()), max=float(u0.max()))
     np.savez_compressed(os.path.join(HERE, "patient32.npz"),
                         **{k: np.asarray(v, dtype=np.float32) for k, v in pat.items()
                            if k in ("GM", "WM", "CSF", "T1", "T2")},
