@@ -158,6 +158,48 @@ def cpu_baseline(an, prior, seconds=12.0):
                        f"{per_solve / N ** 3:.1f} steps per solve")
 
 
+def mcmc_comparison(device, mala_steps=120, mala_burn=40, rwm_steps=2000, rwm_burn=500,
+                    n=64, chains=64):
+    """Posterior ESS/s of plain single-solve MCMC (one random-walk chain,
+    one forward solve per step) against batched MALA (64 chains, one batched
+    forward + adjoint call per generation), same posterior, at n^3."""
+    from gliomauq_gb300 import _lib, mcmc, synthetic as Syn
+    an = Syn.make_anatomy(n, seed=0)
+    truth = Syn.draw_prior(an, 1, seed=10_000)[0]
+    rng = np.random.default_rng(0)
+    h = _lib.Handle(n, "f32", device=device, max_samples=chains)
+    h.set_anatomy(an.p_w, an.p_g)
+    u = h.batch_solve([truth.as_tuple()], an.L, with_loglik=False, want_phi=True)["phi"][0]
+    obs = Syn.make_observations(u.astype(np.float64), an, seed=3,
+                                centre_xyz=(truth.x0, truth.y0, truth.z0),
+                                radius_vox=27.0 * n / 128)
+    h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2)
+    prior = mcmc.Prior.from_anatomy(an)
+    dt0 = Syn.reference_dt(n, prior.hi[0], an.L)[0]
+    th0 = np.array([truth.as_tuple()] * chains) + rng.normal(0, 1e-3, (chains, 6)) * prior.width
+    post = mcmc.Posterior(h, an.L, dt0, prior)
+    r = mcmc.mala(post, th0, mala_steps, 2e-3, rng, burn=mala_burn)
+    t_mala = r.seconds * (mala_steps - mala_burn) / mala_steps
+    e_mala = mcmc.ess(r.samples[mala_burn:])
+    post1 = mcmc.Posterior(h, an.L, dt0, prior)
+    r1 = mcmc.rwm(post1, th0[:1], rwm_steps, 1e-3, rng, burn=rwm_burn)
+    t_rwm = r1.seconds * (rwm_steps - rwm_burn) / rwm_steps
+    e_rwm = mcmc.ess(r1.samples[rwm_burn:])
+    h.close()
+    plain = float(e_rwm.min() / t_rwm)
+    mala = float(e_mala.min() / t_mala)
+    return {"grid": n, "posterior": "synthetic truth, PET/T1/T2 likelihood, smooth-time-grid model",
+            "plain": {"sampler": "RWM, 1 chain, 1 forward solve per step", "steps": rwm_steps - rwm_burn,
+                      "accept": float(r1.accept), "ess_min": float(e_rwm.min()),
+                      "seconds": t_rwm, "ess_per_s": plain},
+            "batched_adjoint": {"sampler": f"MALA, {chains} chains, batched forward+adjoint",
+                                "steps": mala_steps - mala_burn, "accept": float(r.accept),
+                                "ess_min": float(e_mala.min()), "seconds": t_mala,
+                                "ess_per_s": mala},
+            "ess_per_s_ratio": mala / plain if plain > 0 else None,
+            "surrogate": "not built"}
+
+
 def run_reference_arm(args):
     rank, _, world = rank_info()
     if rank != 0:
@@ -189,6 +231,8 @@ def main():
     ap.add_argument("--impl", default="gbglioma", choices=["gbglioma", "reference"])
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mcmc", action="store_true",
+                    help="skip the ESS/s comparison of plain and batched MALA sampling")
     ap.add_argument("--samples", type=int, default=S,
                     help="population size (profiling runs use a smaller one)")
     args = ap.parse_args()
@@ -307,6 +351,8 @@ def main():
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(an, prior)
+        if not args.no_mcmc:
+            line["mcmc"] = mcmc_comparison(local_rank)
         print(json.dumps(line))
     h.close()
     if world > 1:

@@ -12,7 +12,7 @@ LIK = (0.0025, 1.0, 0.7, 0.25, 0.09)
 
 def test_mala_and_rwm_generations(gbg):
     an = S.make_anatomy(32, seed=4)
-    truth = S.SampleParams(Dw=0.0013, rho=0.08, x0=15.2, y0=16.1, z0=15.7, T=60.0)
+    truth = S.SampleParams(Dw=0.0013, rho=0.08, x0=15.2, y0=16.1, z0=15.7, T=120.0)
     rng = np.random.default_rng(0)
     with _lib.Handle(32, "f32", max_samples=1) as h:
         h.set_anatomy(an.p_w, an.p_g)
