@@ -28,7 +28,8 @@ EXPORTS = [
     "gbg_stream", "gbg_sync", "gbg_last_population_ms", "gbg_loglik_noalloc",
     "gbg_population_variants", "gbg_set_population_variant", "gbg_population_variant_shape",
     "gbg_autotune", "gbg_amr_create", "gbg_amr_set_grid", "gbg_amr_set_ghosts", "gbg_amr_step",
-    "gbg_amr_get_phi", "gbg_amr_fwt_detail", "gbg_adjoint_grad",
+    "gbg_amr_get_phi", "gbg_amr_fwt_detail", "gbg_adjoint_grad", "gbg_amr_remap",
+    "gbg_amr_dump_uniform",
 ]
 
 
@@ -120,6 +121,8 @@ def load(path: str = LIB_PATH):
         "gbg_amr_step": [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_long],
         "gbg_amr_get_phi": [vp, dp],
         "gbg_amr_fwt_detail": [vp, dp],
+        "gbg_amr_remap": [vp, C.c_int, vp, vp, vp],
+        "gbg_amr_dump_uniform": [vp, C.c_int, C.c_int, dp],
         "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
                                C.POINTER(LikParams), vp, vp],
     }
@@ -355,4 +358,18 @@ class AmrHandle:
     def fwt_detail(self) -> np.ndarray:
         out = np.empty(self.nb, dtype=np.float64)
         check(self.lib.gbg_amr_fwt_detail(self._h, dptr(out)))
+        return out
+
+    def remap(self, new_blocks, kind, src):
+        """Split / collapse / copy into the grid `new_blocks` (see gbg_amr_remap)."""
+        b = np.ascontiguousarray(new_blocks, dtype=np.int32)
+        k = np.ascontiguousarray(kind, dtype=np.int32)
+        s = np.ascontiguousarray(src, dtype=np.int32).reshape(-1, 8)
+        check(self.lib.gbg_amr_remap(self._h, b.shape[0], b.ctypes.data, k.ctypes.data,
+                                     s.ctypes.data))
+        self.nb = b.shape[0]
+
+    def dump_uniform(self, gpd: int, reference_rules: bool = True) -> np.ndarray:
+        out = np.empty((gpd, gpd, gpd), dtype=np.float64)
+        check(self.lib.gbg_amr_dump_uniform(self._h, gpd, 1 if reference_rules else 0, dptr(out)))
         return out

@@ -565,6 +565,47 @@ int gbg_amr_fwt_detail(gbg_handle *hh, double *detail) {
     return gbg::amr_fwt_detail(hh->h, detail);
 }
 
+int gbg_amr_remap(gbg_handle *hh, int nbn, const gbg_block *blocks, const int *kind, const int *src) {
+    if (int rc = check_amr(hh)) return rc;
+    Handle &h = hh->h;
+    if (nbn < 1 || nbn > h.amr.max_blocks || !blocks || !kind || !src) {
+        set_error("bad remap arguments");
+        return GBG_ERR_ARG;
+    }
+    for (int i = 0; i < nbn; ++i) {
+        const int *s = src + 8 * (size_t)i;
+        const int nsrc = kind[i] == GBG_REMAP_COLLAPSE ? 8 : 1;
+        if (kind[i] < GBG_REMAP_COPY || kind[i] > GBG_REMAP_COLLAPSE ||
+            (kind[i] == GBG_REMAP_SPLIT && (s[1] < 0 || s[1] > 7))) {
+            set_error("bad remap kind or child index");
+            return GBG_ERR_ARG;
+        }
+        for (int k = 0; k < nsrc; ++k)
+            if (s[k] < 0 || s[k] >= h.amr.nb) {
+                set_error("remap source outside the current grid");
+                return GBG_ERR_ARG;
+            }
+        const int side = blocks[i].level >= 0 && blocks[i].level < 16 ? 1 << blocks[i].level : -1;
+        if (side < 0 || blocks[i].ix < 0 || blocks[i].iy < 0 || blocks[i].iz < 0 || blocks[i].ix >= side ||
+            blocks[i].iy >= side || blocks[i].iz >= side) {
+            set_error("block position outside its level");
+            return GBG_ERR_ARG;
+        }
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    return gbg::amr_remap(h, nbn, blocks, kind, src);
+}
+
+int gbg_amr_dump_uniform(gbg_handle *hh, int gpd, int reference_rules, double *out) {
+    if (int rc = check_amr(hh)) return rc;
+    if (gpd < 1 || gpd > 2048 || (gpd & (gpd - 1)) || !out || hh->h.amr.nb < 1) {
+        set_error("bad dump arguments (gpd a power of two)");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
+    return gbg::amr_dump_uniform(hh->h, gpd, reference_rules, out);
+}
+
 int gbg_launch_count(gbg_handle *hh, long long *count) {
     if (int rc = check_handle(hh)) return rc;
     if (!count) {

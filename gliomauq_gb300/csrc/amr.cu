@@ -22,6 +22,7 @@
 // largest magnitude (FWTReport::getOverAll_DetailMaxMag, :184-190).
 //
 // Compiled with -fmad=false: every operation rounds on its own.
+#include <utility>
 #include <vector>
 
 #include "gbg_internal.cuh"
@@ -197,6 +198,97 @@ __global__ void __launch_bounds__(512) k_amr_fwt(int nb, RegionTable rt, const R
     if (t == 0) detail[b] = red[0];
 }
 
+// New block i of a remap: kind 0 = copy of old block src[8i]; kind 1 = child
+// src[8i+1] (x + 2y + 4z) of old block src[8i], by Hs prediction
+// (BlockSplitter::_splitBlocks, source/MRAGcore/MRAGBlockSplitter.h:24-100):
+// fine point d takes parent lab points s with 2s - d in {-1, 0, 1}, weights
+// Hs = {1/2, 1, 1/2}, summed from 0 in (sz, sy, sx) ascending order; kind 2 =
+// collapse of the 8 old blocks src[8i..8i+7] (child x + 2y + 4z) by Ha = {1}
+// decimation (BlockCollapser::_filter, MRAGBlockCollapser.h:19-44), i.e. the
+// child's cell at even coordinates.
+template <typename Real>
+__global__ void k_amr_remap(int nbn, RegionTable rt, const int *__restrict__ kind, const int *__restrict__ src,
+                            const Real *__restrict__ f_old, const Real *__restrict__ g_old,
+                            Real *__restrict__ f_new) {
+    const long total = (long)nbn * BC;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / BC), c = (int)(i % BC);
+        const int x = c % BS, y = (c / BS) % BS, z = c / (BS * BS);
+        const int k = kind[b];
+        const int *sr = src + 8 * (size_t)b;
+        Real v = 0;
+        if (k == 0) {
+            v = f_old[(size_t)sr[0] * BC + c];
+        } else if (k == 1) {
+            const int p = sr[0], ch = sr[1];
+            const int d[3] = {(ch & 1) * BS + x, ((ch >> 1) & 1) * BS + y, ((ch >> 2) & 1) * BS + z};
+            int lo[3], n[3];
+            double w[3][2];
+            for (int a = 0; a < 3; ++a) {
+                if ((d[a] & 1) == 0) {
+                    lo[a] = d[a] / 2; n[a] = 1; w[a][0] = 1.0;
+                } else {
+                    lo[a] = (d[a] - 1) / 2; n[a] = 2; w[a][0] = 0.5; w[a][1] = 0.5;
+                }
+            }
+            Real acc = 0;
+            for (int iz = 0; iz < n[2]; ++iz)
+                for (int iy = 0; iy < n[1]; ++iy) {
+                    const double wZwY = w[2][iz] * w[1][iy];
+                    for (int ix = 0; ix < n[0]; ++ix) {
+                        const Real val = lab_at(rt, f_old, g_old, p, lo[0] + ix, lo[1] + iy, lo[2] + iz);
+                        acc = acc + val * (Real)(wZwY * w[0][ix]);
+                    }
+                }
+            v = acc;
+        } else {
+            const int ch = (x / 8) + 2 * (y / 8) + 4 * (z / 8);
+            const int sx = 2 * (x % 8), sy = 2 * (y % 8), sz = 2 * (z % 8);
+            v = (Real)0 + f_old[(size_t)sr[ch] * BC + sx + BS * (sy + BS * sz)] * (Real)1.0;
+        }
+        f_new[i] = v;
+    }
+}
+
+// Block cell values onto the finest uniform grid of gpd^3 cells
+// (Glioma_HG_UQ::_dumpUQoutput, source/Glioma/Glioma_HG_UQ.cpp:309-372):
+// cell (x, y, z) of a block with spacing h lands at floor(pos / hf), hf = 1/gpd,
+// replicated r^3 times. reference_rules: r = 1 if h == hf, 2 if h == 2 hf,
+// 3 if h == 3 hf, else 4 -- as the reference does, including its 4^3 for
+// coarser blocks; otherwise r = h / hf exactly. Blocks finer than hf are
+// sampled at their cells on the coarse grid points.
+template <typename Real>
+__global__ void k_amr_dump(int nb, const int *__restrict__ level, const int *__restrict__ bidx,
+                           const Real *__restrict__ phi, int gpd, int reference_rules, double *__restrict__ out) {
+    const long total = (long)nb * BC;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / BC), c = (int)(i % BC);
+        const int x = c % BS, y = (c / BS) % BS, z = c / (BS * BS);
+        const long cells_at_level = (long)BS << level[b];  // cells per side at this level
+        const long g[3] = {(long)bidx[3 * b] * BS + x, (long)bidx[3 * b + 1] * BS + y, (long)bidx[3 * b + 2] * BS + z};
+        long m[3];
+        int r;
+        if (cells_at_level >= gpd) {
+            const long ratio = cells_at_level / gpd;  // block cells per dump cell
+            if ((g[0] % ratio) || (g[1] % ratio) || (g[2] % ratio)) continue;
+            for (int a = 0; a < 3; ++a) m[a] = g[a] / ratio;
+            r = 1;
+        } else {
+            const long ratio = gpd / cells_at_level;  // dump cells per block cell
+            for (int a = 0; a < 3; ++a) m[a] = g[a] * ratio;
+            r = (int)ratio;
+            if (reference_rules) r = ratio == 1 ? 1 : (ratio == 2 ? 2 : (ratio == 3 ? 3 : 4));
+        }
+        const double v = (double)phi[i];
+        for (int cz = 0; cz < r; ++cz)
+            for (int cy = 0; cy < r; ++cy)
+                for (int cx = 0; cx < r; ++cx) {
+                    const long X = m[0] + cx, Y = m[1] + cy, Z = m[2] + cz;
+                    if (X < gpd && Y < gpd && Z < gpd) out[X + gpd * (Y + (long)gpd * Z)] = v;
+                }
+    }
+}
+
 RegionTable region_table() {
     RegionTable rt;
     for (int c = 0; c < 27; ++c) rt.start[c] = region_start(c);
@@ -225,13 +317,18 @@ int amr_alloc(Handle &h) {
     GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.level, (size_t)h.amr.max_blocks * sizeof(int)));
     GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.gstart, (ghosts + 1) * sizeof(long)));
     GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.detail, (size_t)h.amr.max_blocks * sizeof(double)));
+    GBG_CUDA_TRY(cudaMalloc(&h.amr.pw2, cells * sb));
+    GBG_CUDA_TRY(cudaMalloc(&h.amr.pg2, cells * sb));
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.bidx, (size_t)h.amr.max_blocks * 3 * sizeof(int)));
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.rkind, (size_t)h.amr.max_blocks * sizeof(int)));
+    GBG_CUDA_TRY(cudaMalloc((void **)&h.amr.rsrc, (size_t)h.amr.max_blocks * 8 * sizeof(int)));
     return GBG_OK;
 }
 
 void amr_free(Handle &h) {
     void *p[] = {h.amr.phi[0], h.amr.phi[1], h.amr.pw, h.amr.pg, h.amr.b0, h.amr.gphi, h.amr.gpw, h.amr.gpg,
                  h.amr.df, h.amr.level, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell, h.amr.gw,
-                 h.amr.detail};
+                 h.amr.detail, h.amr.pw2, h.amr.pg2, h.amr.bidx, h.amr.rkind, h.amr.rsrc};
     for (void *q : p)
         if (q) cudaFree(q);
 }
@@ -239,9 +336,15 @@ void amr_free(Handle &h) {
 int amr_set_grid(Handle &h, int nb, const gbg_block *blocks, const double *pw, const double *pg,
                  const double *phi) {
     const size_t n = (size_t)nb * BC;
-    std::vector<int> lv(nb);
-    for (int i = 0; i < nb; ++i) lv[i] = blocks[i].level;
+    std::vector<int> lv(nb), bi(3 * (size_t)nb);
+    for (int i = 0; i < nb; ++i) {
+        lv[i] = blocks[i].level;
+        bi[3 * i] = blocks[i].ix;
+        bi[3 * i + 1] = blocks[i].iy;
+        bi[3 * i + 2] = blocks[i].iz;
+    }
     GBG_CUDA_TRY(cudaMemcpyAsync(h.amr.level, lv.data(), nb * sizeof(int), cudaMemcpyHostToDevice, h.stream));
+    GBG_CUDA_TRY(cudaMemcpyAsync(h.amr.bidx, bi.data(), bi.size() * sizeof(int), cudaMemcpyHostToDevice, h.stream));
     const double *src[3] = {pw, pg, phi};
     void *dst[3] = {h.amr.pw, h.amr.pg, h.amr.phi[0]};
     if (h.prec == GBG_PREC_F64) {
@@ -403,6 +506,83 @@ int amr_fwt_detail(Handle &h, double *detail) {
     GBG_CUDA_TRY(cudaGetLastError());
     GBG_CUDA_TRY(cudaMemcpyAsync(detail, h.amr.detail, h.amr.nb * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
     GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    return GBG_OK;
+}
+
+int amr_remap(Handle &h, int nbn, const gbg_block *blocks, const int *kind, const int *src) {
+    if (!h.amr.ghosts_valid) {
+        set_error("the remap reads the current grid's ghosts: set its ghost tables first");
+        return GBG_ERR_STATE;
+    }
+    std::vector<int> lv(nbn), bi(3 * (size_t)nbn);
+    for (int i = 0; i < nbn; ++i) {
+        lv[i] = blocks[i].level;
+        bi[3 * i] = blocks[i].ix;
+        bi[3 * i + 1] = blocks[i].iy;
+        bi[3 * i + 2] = blocks[i].iz;
+    }
+    const RegionTable rt = region_table();
+    const long ng = (long)h.amr.nb * NG, cells = (long)nbn * BC;
+    const int gg = grid_blocks(h, ng), gc = grid_blocks(h, cells);
+    GBG_CUDA_TRY(cudaMemcpyAsync(h.amr.rkind, kind, nbn * sizeof(int), cudaMemcpyHostToDevice, h.stream));
+    GBG_CUDA_TRY(cudaMemcpyAsync(h.amr.rsrc, src, 8 * (size_t)nbn * sizeof(int), cudaMemcpyHostToDevice, h.stream));
+    void *pin = h.amr.phi[h.amr.cur], *pout = h.amr.phi[h.amr.cur ^ 1];
+    if (h.prec == GBG_PREC_F64) {
+        k_ghost_eval<double><<<gg, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell,
+                                                       h.amr.gw, (const double *)pin, (double *)h.amr.gphi);
+        k_amr_remap<double><<<gc, 256, 0, h.stream>>>(nbn, rt, h.amr.rkind, h.amr.rsrc, (const double *)pin,
+                                                      (const double *)h.amr.gphi, (double *)pout);
+        k_amr_remap<double><<<gc, 256, 0, h.stream>>>(nbn, rt, h.amr.rkind, h.amr.rsrc, (const double *)h.amr.pw,
+                                                      (const double *)h.amr.gpw, (double *)h.amr.pw2);
+        k_amr_remap<double><<<gc, 256, 0, h.stream>>>(nbn, rt, h.amr.rkind, h.amr.rsrc, (const double *)h.amr.pg,
+                                                      (const double *)h.amr.gpg, (double *)h.amr.pg2);
+    } else {
+        k_ghost_eval<float><<<gg, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell,
+                                                      h.amr.gw, (const float *)pin, (float *)h.amr.gphi);
+        k_amr_remap<float><<<gc, 256, 0, h.stream>>>(nbn, rt, h.amr.rkind, h.amr.rsrc, (const float *)pin,
+                                                     (const float *)h.amr.gphi, (float *)pout);
+        k_amr_remap<float><<<gc, 256, 0, h.stream>>>(nbn, rt, h.amr.rkind, h.amr.rsrc, (const float *)h.amr.pw,
+                                                     (const float *)h.amr.gpw, (float *)h.amr.pw2);
+        k_amr_remap<float><<<gc, 256, 0, h.stream>>>(nbn, rt, h.amr.rkind, h.amr.rsrc, (const float *)h.amr.pg,
+                                                     (const float *)h.amr.gpg, (float *)h.amr.pg2);
+    }
+    h.launches += 4;
+    GBG_CUDA_TRY(cudaGetLastError());
+    GBG_CUDA_TRY(cudaMemcpyAsync(h.amr.level, lv.data(), nbn * sizeof(int), cudaMemcpyHostToDevice, h.stream));
+    GBG_CUDA_TRY(cudaMemcpyAsync(h.amr.bidx, bi.data(), bi.size() * sizeof(int), cudaMemcpyHostToDevice, h.stream));
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    std::swap(h.amr.pw, h.amr.pw2);
+    std::swap(h.amr.pg, h.amr.pg2);
+    h.amr.cur ^= 1;
+    h.amr.nb = nbn;
+    h.amr.ghosts_valid = false;
+    h.amr.tables_valid = false;
+    return GBG_OK;
+}
+
+int amr_dump_uniform(Handle &h, int gpd, int reference_rules, double *out) {
+    const size_t n3 = (size_t)gpd * gpd * gpd;
+    double *d = nullptr;
+    GBG_CUDA_TRY(cudaMalloc((void **)&d, n3 * sizeof(double)));
+    cudaError_t e = cudaMemsetAsync(d, 0, n3 * sizeof(double), h.stream);
+    const long cells = (long)h.amr.nb * BC;
+    if (e == cudaSuccess) {
+        if (h.prec == GBG_PREC_F64)
+            k_amr_dump<double><<<grid_blocks(h, cells), 256, 0, h.stream>>>(
+                h.amr.nb, h.amr.level, h.amr.bidx, (const double *)h.amr.phi[h.amr.cur], gpd, reference_rules, d);
+        else
+            k_amr_dump<float><<<grid_blocks(h, cells), 256, 0, h.stream>>>(
+                h.amr.nb, h.amr.level, h.amr.bidx, (const float *)h.amr.phi[h.amr.cur], gpd, reference_rules, d);
+        h.launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, n3 * sizeof(double), cudaMemcpyDeviceToHost, h.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h.stream);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        set_error(std::string("amr dump: ") + cudaGetErrorString(e));
+        return GBG_ERR_CUDA;
+    }
     return GBG_OK;
 }
 

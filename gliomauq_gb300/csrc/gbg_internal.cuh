@@ -49,6 +49,9 @@ struct AmrState {
     int *gsrc_block = nullptr, *gsrc_cell = nullptr;
     double *gw = nullptr;
     double *detail = nullptr;  // FWT maxima per block
+    void *pw2 = nullptr, *pg2 = nullptr;  // remap targets
+    int *bidx = nullptr;       // block index (ix, iy, iz) per block
+    int *rkind = nullptr, *rsrc = nullptr;  // remap plan
     bool ghosts_valid = false, tables_valid = false;
     double tab_Dw = -1, tab_Dg = -1;
 };
@@ -162,6 +165,8 @@ int amr_set_ghosts(Handle &h, const long *start, const int *src_block, const int
 int amr_steps(Handle &h, double Dw, double Dg, double rho, double dt, long nsteps);
 int amr_get_phi(Handle &h, double *phi);
 int amr_fwt_detail(Handle &h, double *detail);
+int amr_remap(Handle &h, int nbn, const gbg_block *blocks, const int *kind, const int *src);
+int amr_dump_uniform(Handle &h, int gpd, int reference_rules, double *out);
 
 // ---- adjoint.cu ----
 int adjoint_grad(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_opts &o, double *loglik,

@@ -214,6 +214,28 @@ int gbg_amr_get_phi(gbg_handle *h, double *phi);
  * (source/MRAGcore/MRAGBlockFWT.h:184-190,219-298,447-468) -- the quantity
  * Science::AutomaticRefinement/Compression compare with their tolerances. */
 int gbg_amr_fwt_detail(gbg_handle *h, double *detail);
+/* Regrid data movement: build a new set of blocks from the current grid.
+ * New block i is kind[i] = GBG_REMAP_COPY of current block src[8i]; or
+ * GBG_REMAP_SPLIT, the child src[8i+1] (x + 2y + 4z) of current block src[8i]
+ * by interpolating-wavelet prediction (BlockSplitter::_splitBlocks,
+ * source/MRAGcore/MRAGBlockSplitter.h:24-100, using the current ghost
+ * tables); or GBG_REMAP_COLLAPSE of the eight current blocks src[8i..8i+7]
+ * (child x + 2y + 4z) by decimation (BlockCollapser::_collapseBlocks,
+ * source/MRAGcore/MRAGBlockCollapser.h:19-61). phi, p_w and p_g all move.
+ * The ghost tables of the new grid must be set before the next step. */
+#define GBG_REMAP_COPY 0
+#define GBG_REMAP_SPLIT 1
+#define GBG_REMAP_COLLAPSE 2
+int gbg_amr_remap(gbg_handle *h, int nblocks_new, const gbg_block *blocks_new, const int *kind,
+                  const int *src);
+/* phi on the uniform grid of gpd^3 cells, hf = 1/gpd, as
+ * Glioma_HG_UQ::_dumpUQoutput writes HGG_data.dat (Glioma_HG_UQ.cpp:309-372).
+ * reference_rules != 0 replicates a block cell r^3 times with r = 1, 2, 3 for
+ * h = hf, 2 hf, 3 hf and r = 4 otherwise, as the reference does (so blocks
+ * coarser than 4 hf leave cells unwritten: they are 0 here); reference_rules
+ * == 0 replicates h/hf exactly. Blocks finer than hf contribute the cells on
+ * the dump grid's points. */
+int gbg_amr_dump_uniform(gbg_handle *h, int gpd, int reference_rules, double *out);
 
 /* ---- introspection ---------------------------------------------------------- */
 /* number of kernels this handle has launched since creation */

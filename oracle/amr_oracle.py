@@ -153,3 +153,97 @@ def fwt_detail(phi, ghost_tables, real):
                     res = res + v * real(wZwY * wX)
         out = np.maximum(out, np.abs(res.astype(np.float64)).reshape(L.shape[0], -1).max(axis=1))
     return out
+
+
+def remap_plan(old_blocks, new_blocks):
+    """kind/src arrays of gbg_amr_remap that turn the grid `old_blocks` into
+    `new_blocks` ((n, 4) arrays of level, ix, iy, iz), found by position."""
+    pos = {tuple(b): i for i, b in enumerate(np.asarray(old_blocks).tolist())}
+    kind = np.zeros(len(new_blocks), dtype=np.int32)
+    src = np.zeros((len(new_blocks), 8), dtype=np.int32)
+    for i, (l, x, y, z) in enumerate(np.asarray(new_blocks).tolist()):
+        if (l, x, y, z) in pos:
+            kind[i], src[i, 0] = 0, pos[(l, x, y, z)]
+        elif (l - 1, x // 2, y // 2, z // 2) in pos:
+            kind[i] = 1
+            src[i, 0] = pos[(l - 1, x // 2, y // 2, z // 2)]
+            src[i, 1] = (x % 2) + 2 * (y % 2) + 4 * (z % 2)
+        else:
+            kids = [(l + 1, 2 * x + (c & 1), 2 * y + ((c >> 1) & 1), 2 * z + ((c >> 2) & 1))
+                    for c in range(8)]
+            if not all(k in pos for k in kids):
+                raise ValueError(f"block {(l, x, y, z)} is not a copy, split or collapse")
+            kind[i] = 2
+            src[i] = [pos[k] for k in kids]
+    return kind, src
+
+
+def remap(field, ghosts, kind, src, real):
+    """BlockSplitter / BlockCollapser data movement of one field
+    (source/MRAGcore/MRAGBlockSplitter.h:24-100, MRAGBlockCollapser.h:19-61)."""
+    real = np.dtype(real).type
+    f = np.asarray(field, dtype=real).reshape(-1, BS, BS, BS)
+    L = labs(f.reshape(-1, 4096), ghosts, real)
+    out = np.empty((len(kind), BS, BS, BS), dtype=real)
+    fine = np.arange(2 * BS)
+    for i, k in enumerate(kind):
+        if k == 0:
+            out[i] = f[src[i][0]]
+        elif k == 1:
+            p, ch = src[i][0], src[i][1]
+            off = [(ch & 1) * BS, ((ch >> 1) & 1) * BS, ((ch >> 2) & 1) * BS]
+            d = [fine[o:o + BS] for o in off]  # fine indices per axis
+            acc = np.zeros((BS, BS, BS), dtype=real)
+            # per axis: first parent point and its weight, second (odd d only)
+            lo = [dd // 2 for dd in d]
+            odd = [dd % 2 == 1 for dd in d]
+            for iz in (0, 1):
+                for iy in (0, 1):
+                    for ix in (0, 1):
+                        use = (odd[2] | (iz == 0))[:, None, None] & (odd[1] | (iy == 0))[None, :, None] \
+                            & (odd[0] | (ix == 0))[None, None, :]
+                        wz = np.where(odd[2], 0.5, 1.0)
+                        wy = np.where(odd[1], 0.5, 1.0)
+                        wx = np.where(odd[0], 0.5, 1.0)
+                        w = ((wz[:, None, None] * wy[None, :, None]) * wx[None, None, :]).astype(real)
+                        zz = (lo[2] + iz)[:, None, None] + 1
+                        yy = (lo[1] + iy)[None, :, None] + 1
+                        xx = (lo[0] + ix)[None, None, :] + 1
+                        v = L[p][np.minimum(zz, 17), np.minimum(yy, 17), np.minimum(xx, 17)]
+                        acc = np.where(use, acc + v * w, acc)
+            out[i] = acc
+        else:
+            for c in range(8):
+                cz, cy, cx = (c >> 2) & 1, (c >> 1) & 1, c & 1
+                out[i, cz * 8:(cz + 1) * 8, cy * 8:(cy + 1) * 8, cx * 8:(cx + 1) * 8] = \
+                    real(0) + f[src[i][c], ::2, ::2, ::2] * real(1.0)
+    return out
+
+
+def dump_uniform(blocks, phi, gpd, reference_rules=True):
+    """Glioma_HG_UQ::_dumpUQoutput (source/Glioma/Glioma_HG_UQ.cpp:309-372):
+    every block cell replicated r^3 times on the gpd^3 grid, r = 1 for h = hf,
+    2 for h = 2 hf, 3 for h = 3 hf and 4 otherwise (reference_rules), or
+    exactly h / hf; unwritten cells are 0."""
+    out = np.zeros((gpd, gpd, gpd))
+    f = np.asarray(phi, dtype=np.float64).reshape(-1, BS, BS, BS)
+    for i, (l, bx, by, bz) in enumerate(np.asarray(blocks).tolist()):
+        cells = BS << l
+        if cells >= gpd:
+            ratio = cells // gpd
+            sub = f[i][::ratio, ::ratio, ::ratio] if ratio > 1 else f[i]
+            # only the cells whose global index is a multiple of ratio
+            g0 = np.array([bz, by, bx]) * BS
+            first = (-g0) % ratio
+            sub = f[i][first[0]::ratio, first[1]::ratio, first[2]::ratio]
+            m = (g0 + first) // ratio
+            out[m[0]:m[0] + sub.shape[0], m[1]:m[1] + sub.shape[1], m[2]:m[2] + sub.shape[2]] = sub
+            continue
+        ratio = gpd // cells
+        r = ratio if not reference_rules else (ratio if ratio in (1, 2, 3) else 4)
+        for z in range(BS):
+            for y in range(BS):
+                for x in range(BS):
+                    mz, my, mx = ((bz * BS + z) * ratio, (by * BS + y) * ratio, (bx * BS + x) * ratio)
+                    out[mz:mz + r, my:my + r, mx:mx + r] = f[i, z, y, x]
+    return out

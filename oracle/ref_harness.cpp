@@ -32,6 +32,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -390,9 +391,10 @@ static void writeFwt(FILE *f, Grid<W, B> &grid) {
 
 // Adaptive state for the AMR fixtures: run the time loop (regridding at dump
 // times, without run()'s final refinement), then write S0 = blocks + ghost tables + FWT detail maxima; take
-// `extra` more steps without regridding and write S1 = blocks; then one
-// regrid (refinement then compression, as at a dump time) and write
-// S2 = blocks.
+// `extra` more steps without regridding and write S1 = blocks; then a
+// forced regrid (split every block below the maximum level, then collapse
+// the complete sibling groups among the other blocks in the upper half of x)
+// and write S2 = blocks.
 static int cmdState(const char *inp, const char *outp, int extra) {
     Input in = readInput(inp);
     Sim s(in.bpd);
@@ -412,7 +414,28 @@ static int cmdState(const char *inp, const char *outp, int extra) {
     for (int k = 0; k < extra; ++k)
         s.step(&s.grid->getBoundaryInfo(), gran, (Real)ri.Dw_unit, (Real)ri.Dg_unit, (Real)ri.rho, ri.dt);
     writeBlocks(f, *s.grid);
-    s.regrid();
+    // a forced regrid that both splits and collapses (Grid::refine with
+    // BlockSplitter, Grid::compress with BlockCollapser): refine every block
+    // below the maximum level, then offer for compression every block in the
+    // upper half of x
+    {
+        std::vector<BlockInfo> v = s.grid->getBlocksInfo();
+        std::set<int> toRefine, before;
+        for (const BlockInfo &b : v) {
+            before.insert(b.blockID);
+            if (b.level < maxLevel) toRefine.insert(b.blockID);
+        }
+        if (!toRefine.empty()) s.grid->refine(toRefine);
+        v = s.grid->getBlocksInfo();
+        std::set<int> toCompress;
+        for (const BlockInfo &b : v)
+            if (before.count(b.blockID) && b.index[0] >= (1 << b.level) / 2) toCompress.insert(b.blockID);
+        int nc = 0;
+        s.grid->compress(toCompress, nc);
+        if (getenv("GBG_HARNESS_VERBOSE"))
+            fprintf(stderr, "forced regrid: refined %zu, collapsed %d -> %zu blocks\n", toRefine.size(), nc,
+                    s.grid->getBlocksInfo().size());
+    }
     writeBlocks(f, *s.grid);
     fclose(f);
     return 0;

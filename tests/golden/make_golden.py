@@ -140,7 +140,8 @@ def region_starts():
 def amr_fixtures():
     """Adaptive 64^3-effective grid (4^3 blocks at level 2, maximum level 2):
     the reference time loop with a regrid every 25 days to T = 60, then its
-    blocks, ghost tables and FWT maxima, and the blocks after 10 more steps."""
+    blocks, ghost tables and FWT maxima, the blocks after 10 more steps, and
+    the blocks after a forced regrid that splits and collapses (S2)."""
     a = np.load(os.path.join(HERE, "anatomy64.npz"))
     pw, pg = a["p_w"].astype(np.float64), a["p_g"].astype(np.float64)
     an = S.Anatomy(n=64, p_w=pw, p_g=pg, psi=None)
@@ -172,7 +173,10 @@ def amr_fixtures():
             ghost_w=np.concatenate(w).astype(np.float32), fwt=st["fwt"],
             phi_after=np.stack([b["phi"] for b in st["s1"]]), steps_after=10,
             dt=st["dt"], Dw=st["Dw"], Dg=st["Dg"], rho=st["rho"],
-            s2_levels=np.array([b["level"] for b in st["s2"]], dtype=np.int32))
+            s2_blocks=np.array([[b["level"], *b["index"]] for b in st["s2"]], dtype=np.int32),
+            s2_phi=np.stack([b["phi"] for b in st["s2"]]),
+            s2_p_w=np.stack([b["p_w"] for b in st["s2"]]),
+            s2_p_g=np.stack([b["p_g"] for b in st["s2"]]))
 
 
 def patient_files(d, pat):

@@ -40,3 +40,31 @@ def test_amr_fwt_oracle_matches_reference(variant):
     d = golden_npz(f"amr64_{variant}.npz")
     got = A.fwt_detail(d["phi"].reshape(-1, 4096), tables(d), REAL[variant])
     assert np.array_equal(got, d["fwt"])
+
+
+@pytest.mark.parametrize("variant", ["f64", "f32"])
+def test_amr_remap_oracle_matches_reference(variant):
+    """BlockSplitter + BlockCollapser of the forced regrid S1 -> S2."""
+    d = golden_npz(f"amr64_{variant}.npz")
+    real = REAL[variant]
+    kind, src = A.remap_plan(d["blocks"], d["s2_blocks"])
+    assert {0, 1, 2} <= set(kind.tolist())
+    for name, key in (("phi_after", "s2_phi"), ("p_w", "s2_p_w"), ("p_g", "s2_p_g")):
+        f = d[name].reshape(-1, 4096)
+        g = A.ghost_values(f, *tables(d)[:3], tables(d)[3], real)
+        out = A.remap(f, g, kind, src, real)
+        assert np.array_equal(out.astype(np.float64), d[key]), name
+
+
+def test_amr_dump_rules():
+    d = golden_npz("amr64_f64.npz")
+    u = A.dump_uniform(d["blocks"], d["phi"], 64)
+    # level-2 blocks are copied, level-1 blocks replicated 2^3
+    b = [i for i, x in enumerate(d["blocks"].tolist()) if x[0] == 1][0]
+    l, bx, by, bz = d["blocks"][b]
+    assert u[bz * 32, by * 32, bx * 32] == d["phi"][b, 0, 0, 0]
+    assert u[bz * 32 + 1, by * 32 + 1, bx * 32 + 1] == d["phi"][b, 0, 0, 0]
+    assert np.count_nonzero(u) == np.count_nonzero(
+        np.concatenate([np.repeat(np.repeat(np.repeat(d["phi"][i], 2 ** (2 - d["blocks"][i][0]), 0),
+                                            2 ** (2 - d["blocks"][i][0]), 1),
+                                  2 ** (2 - d["blocks"][i][0]), 2).ravel() for i in range(len(d["blocks"]))]))

@@ -74,3 +74,28 @@ def test_amr_argument_errors(gbg):
         with pytest.raises(_lib.GbgError):
             h.set_ghosts(d["ghost_start"], bad, d["ghost_src_cell"].astype(np.int32),
                          d["ghost_w"].astype(np.float64))
+
+
+@pytest.mark.parametrize("variant", ["f64", "f32"])
+def test_amr_remap_matches_reference_regrid(gbg, variant):
+    """The forced regrid of the reference (3 blocks split by BlockSplitter, one
+    group collapsed by BlockCollapser) as one gbg_amr_remap on the GPU."""
+    d = golden_npz(f"amr64_{variant}.npz")
+    kind, src = A.remap_plan(d["blocks"], d["s2_blocks"])
+    with _lib.AmrHandle(96, PREC[variant]) as h:
+        load(h, d, d["phi_after"])
+        h.remap(d["s2_blocks"], kind, src)
+        out = h.get_phi()
+        with pytest.raises(_lib.GbgError):
+            h.step(1e-4, 1e-5, 0.1, 1.0, 1)  # the new grid needs its ghost tables
+    assert np.array_equal(out, d["s2_phi"])
+
+
+def test_amr_dump_matches_oracle(gbg):
+    d = golden_npz("amr64_f64.npz")
+    with _lib.AmrHandle(64, "f64") as h:
+        load(h, d)
+        u = h.dump_uniform(64)
+        u2 = h.dump_uniform(32, reference_rules=False)
+    assert np.array_equal(u, A.dump_uniform(d["blocks"], d["phi"], 64))
+    assert np.array_equal(u2, A.dump_uniform(d["blocks"], d["phi"], 32, reference_rules=False))
