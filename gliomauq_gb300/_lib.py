@@ -29,7 +29,10 @@ EXPORTS = [
     "gbg_population_variants", "gbg_set_population_variant", "gbg_population_variant_shape",
     "gbg_autotune", "gbg_amr_create", "gbg_amr_set_grid", "gbg_amr_set_ghosts", "gbg_amr_step",
     "gbg_amr_get_phi", "gbg_amr_fwt_detail", "gbg_adjoint_grad", "gbg_amr_remap",
-    "gbg_amr_dump_uniform",
+    "gbg_amr_dump_uniform", "gbg_surrogate_create", "gbg_surrogate_destroy",
+    "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
+    "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
+    "gbg_surrogate_loglik",
 ]
 
 
@@ -71,6 +74,13 @@ class AdjointOpts(C.Structure):
 
 class AmrConfig(C.Structure):
     _fields_ = [("max_blocks", C.c_int), ("precision", C.c_int), ("device", C.c_int)]
+
+
+class SurrogateConfig(C.Structure):
+    _fields_ = [("factor", C.c_int), ("batch_max", C.c_int), ("L", C.c_double),
+                ("dw_lo", C.c_double), ("dw_hi", C.c_double), ("rho_lo", C.c_double),
+                ("rho_hi", C.c_double), ("t_lo", C.c_double), ("t_hi", C.c_double),
+                ("seed", C.c_ulonglong)]
 
 
 class BatchOpts(C.Structure):
@@ -123,6 +133,16 @@ def load(path: str = LIB_PATH):
         "gbg_amr_fwt_detail": [vp, dp],
         "gbg_amr_remap": [vp, C.c_int, vp, vp, vp],
         "gbg_amr_dump_uniform": [vp, C.c_int, C.c_int, dp],
+        "gbg_surrogate_create": [vp, C.POINTER(SurrogateConfig), C.POINTER(vp)],
+        "gbg_surrogate_destroy": [vp],
+        "gbg_surrogate_nparams": [vp, lp],
+        "gbg_surrogate_get_params": [vp, fp],
+        "gbg_surrogate_set_params": [vp, fp],
+        "gbg_surrogate_train": [vp, C.POINTER(Sample), C.c_int, C.c_int, C.c_int, C.c_double,
+                                C.c_ulonglong, dp],
+        "gbg_surrogate_loss_grad": [vp, C.POINTER(Sample), C.c_int, fp, dp, fp],
+        "gbg_surrogate_features": [vp, C.POINTER(Sample), C.c_int, fp],
+        "gbg_surrogate_loglik": [vp, C.POINTER(Sample), C.c_int, C.POINTER(LikResult), fp],
         "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
                                C.POINTER(LikParams), vp, vp],
     }
@@ -372,4 +392,88 @@ class AmrHandle:
     def dump_uniform(self, gpd: int, reference_rules: bool = True) -> np.ndarray:
         out = np.empty((gpd, gpd, gpd), dtype=np.float64)
         check(self.lib.gbg_amr_dump_uniform(self._h, gpd, 1 if reference_rules else 0, dptr(out)))
+        return out
+
+
+def _samples(samples):
+    S = len(samples)
+    return S, (Sample * S)(*[Sample(*s) for s in samples])
+
+
+class Surrogate:
+    """bf16 3D U-Net surrogate of the final density, bound to a GBG_PREC_F32
+    Handle (its anatomy, observations and batched solver). Destroy it before
+    the handle it was created on."""
+
+    def __init__(self, handle: Handle, L: float, prior_lo, prior_hi, batch_max: int = 8,
+                 factor: int = 2, seed: int = 1):
+        self.lib = handle.lib
+        self.handle = handle
+        self.m = handle.n // factor
+        cfg = SurrogateConfig(factor, batch_max, L, prior_lo[0], prior_hi[0], prior_lo[1],
+                              prior_hi[1], prior_lo[2], prior_hi[2], seed)
+        self._s = C.c_void_p()
+        check(self.lib.gbg_surrogate_create(handle._h, C.byref(cfg), C.byref(self._s)))
+        self.batch_max = batch_max
+
+    def close(self):
+        if self._s:
+            self.lib.gbg_surrogate_destroy(self._s)
+            self._s = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def nparams(self) -> int:
+        c = C.c_long()
+        check(self.lib.gbg_surrogate_nparams(self._s, C.byref(c)))
+        return c.value
+
+    def get_params(self) -> np.ndarray:
+        p = np.empty(self.nparams(), dtype=np.float32)
+        check(self.lib.gbg_surrogate_get_params(self._s, fptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.size != self.nparams():
+            raise ValueError("parameter vector has the wrong length")
+        check(self.lib.gbg_surrogate_set_params(self._s, fptr(p)))
+
+    def train(self, samples, epochs: int, batch: int, lr: float = 1e-3, seed: int = 0) -> float:
+        S, arr = _samples(samples)
+        loss = C.c_double()
+        check(self.lib.gbg_surrogate_train(self._s, arr, S, epochs, batch, lr, seed,
+                                           C.byref(loss)))
+        return loss.value
+
+    def loss_grad(self, samples, targets, want_grad=True):
+        B, arr = _samples(samples)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        if t.size != B * self.m ** 3:
+            raise ValueError("targets must hold B fields of (n/factor)^3 values")
+        loss = C.c_double()
+        g = np.empty(self.nparams(), dtype=np.float32) if want_grad else None
+        check(self.lib.gbg_surrogate_loss_grad(self._s, arr, B, fptr(t), C.byref(loss),
+                                               fptr(g) if want_grad else None))
+        return loss.value, g
+
+    def features(self, samples) -> np.ndarray:
+        B, arr = _samples(samples)
+        out = np.empty((B, self.m, self.m, self.m, 16), dtype=np.float32)
+        check(self.lib.gbg_surrogate_features(self._s, arr, B, fptr(out)))
+        return out
+
+    def loglik(self, samples, want_phi=False):
+        B, arr = _samples(samples)
+        lik = (LikResult * B)()
+        n = self.handle.n
+        phi = np.empty((B, n, n, n), dtype=np.float32) if want_phi else None
+        check(self.lib.gbg_surrogate_loglik(self._s, arr, B, lik, fptr(phi) if want_phi else None))
+        out = dict(loglik=[lik[i].as_dict() for i in range(B)])
+        if want_phi:
+            out["phi"] = phi
         return out

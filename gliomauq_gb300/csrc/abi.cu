@@ -606,6 +606,151 @@ int gbg_amr_dump_uniform(gbg_handle *hh, int gpd, int reference_rules, double *o
     return gbg::amr_dump_uniform(hh->h, gpd, reference_rules, out);
 }
 
+}  // extern "C"
+
+struct gbg_surrogate {
+    gbg::Surrogate *s;
+    gbg_handle *owner;
+};
+
+extern "C" {
+
+int gbg_surrogate_create(gbg_handle *hh, const gbg_surrogate_config *cfg, gbg_surrogate **out) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!cfg || !out) {
+        set_error("null argument");
+        return GBG_ERR_ARG;
+    }
+    *out = nullptr;
+    if (h.is_amr || h.prec != GBG_PREC_F32 || h.max_samples < 1 || !h.anatomy_set) {
+        set_error("surrogate needs a GBG_PREC_F32 handle with max_samples >= 1 and its anatomy set");
+        return GBG_ERR_STATE;
+    }
+    if (!(cfg->L > 0) || !(cfg->dw_hi > cfg->dw_lo) || !(cfg->rho_hi > cfg->rho_lo) || !(cfg->t_hi > cfg->t_lo)) {
+        set_error("bad surrogate configuration");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    gbg::Surrogate *s = nullptr;
+    if (int rc = gbg::surrogate_create(h, *cfg, &s)) return rc;
+    *out = new gbg_surrogate{s, hh};
+    return GBG_OK;
+}
+
+int gbg_surrogate_destroy(gbg_surrogate *s) {
+    if (!s) return GBG_OK;
+    gbg::surrogate_destroy(s->s);
+    delete s;
+    return GBG_OK;
+}
+
+static int check_sur(gbg_surrogate *s) {
+    if (!s || !s->s) {
+        set_error("null surrogate");
+        return GBG_ERR_ARG;
+    }
+    cudaSetDevice(s->owner->h.device);
+    return GBG_OK;
+}
+
+int gbg_surrogate_nparams(gbg_surrogate *s, long *count) {
+    if (int rc = check_sur(s)) return rc;
+    if (!count) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    *count = gbg::surrogate_nparams(*s->s);
+    return GBG_OK;
+}
+
+int gbg_surrogate_get_params(gbg_surrogate *s, float *p) {
+    if (int rc = check_sur(s)) return rc;
+    if (!p) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    return gbg::surrogate_get_params(*s->s, p);
+}
+
+int gbg_surrogate_set_params(gbg_surrogate *s, const float *p) {
+    if (int rc = check_sur(s)) return rc;
+    if (!p) {
+        set_error("null input");
+        return GBG_ERR_ARG;
+    }
+    return gbg::surrogate_set_params(*s->s, p);
+}
+
+static int check_samples(const gbg_sample *smp, int n) {
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(smp[i].Dw) || !std::isfinite(smp[i].rho) || !std::isfinite(smp[i].x0) ||
+            !std::isfinite(smp[i].y0) || !std::isfinite(smp[i].z0) || !std::isfinite(smp[i].tend)) {
+            set_error("non-finite sample parameter");
+            return GBG_ERR_NONFINITE;
+        }
+    return GBG_OK;
+}
+
+int gbg_surrogate_train(gbg_surrogate *s, const gbg_sample *samples, int S, int epochs, int batch, double lr,
+                        unsigned long long seed, double *loss) {
+    if (int rc = check_sur(s)) return rc;
+    if (!samples || S < 1 || epochs < 0 || !(lr > 0)) {
+        set_error("bad training arguments");
+        return GBG_ERR_ARG;
+    }
+    if (int rc = check_samples(samples, S)) return rc;
+    return gbg::surrogate_train(*s->s, samples, S, epochs, batch, lr, seed, loss);
+}
+
+int gbg_surrogate_loss_grad(gbg_surrogate *s, const gbg_sample *samples, int B, const float *targets, double *loss,
+                            float *grad) {
+    if (int rc = check_sur(s)) return rc;
+    if (!samples || !targets || B < 1 || B > gbg::surrogate_batch_max(*s->s)) {
+        set_error("bad loss_grad arguments (1 <= B <= batch_max)");
+        return GBG_ERR_ARG;
+    }
+    if (int rc = check_samples(samples, B)) return rc;
+    return gbg::surrogate_loss_grad(*s->s, samples, B, targets, loss, grad);
+}
+
+int gbg_surrogate_features(gbg_surrogate *s, const gbg_sample *samples, int B, float *out) {
+    if (int rc = check_sur(s)) return rc;
+    if (!samples || !out || B < 1 || B > gbg::surrogate_batch_max(*s->s)) {
+        set_error("bad features arguments (1 <= B <= batch_max)");
+        return GBG_ERR_ARG;
+    }
+    return gbg::surrogate_features(*s->s, samples, B, out);
+}
+
+int gbg_surrogate_loglik(gbg_surrogate *s, const gbg_sample *samples, int B, gbg_lik_result *out, float *phi) {
+    if (int rc = check_sur(s)) return rc;
+    Handle &h = s->owner->h;
+    if (!samples || !out || B < 1 || B > gbg::surrogate_batch_max(*s->s)) {
+        set_error("bad loglik arguments (1 <= B <= batch_max)");
+        return GBG_ERR_ARG;
+    }
+    if (!h.obs.valid) {
+        set_error("observations not set");
+        return GBG_ERR_STATE;
+    }
+    if (int rc = check_samples(samples, B)) return rc;
+    if (int rc = ensure_lik_out(h, B)) return rc;
+    gbg_sample *d = gbg::batch_samples(h);
+    if (B > (h.max_samples > 1 ? h.max_samples : 1)) {
+        set_error("B exceeds the handle's sample capacity");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaMemcpyAsync(d, samples, B * sizeof(gbg_sample), cudaMemcpyHostToDevice, h.stream));
+    if (int rc = gbg::surrogate_predict(*s->s, d, B, (gbg_lik_result *)h.lik_out)) return rc;
+    GBG_CUDA_TRY(cudaMemcpyAsync(out, h.lik_out, B * sizeof(gbg_lik_result), cudaMemcpyDeviceToHost, h.stream));
+    if (phi)
+        GBG_CUDA_TRY(cudaMemcpyAsync(phi, gbg::surrogate_prediction(*s->s), (size_t)B * h.N * sizeof(float), cudaMemcpyDeviceToHost,
+                                     h.stream));
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    return GBG_OK;
+}
+
 int gbg_launch_count(gbg_handle *hh, long long *count) {
     if (int rc = check_handle(hh)) return rc;
     if (!count) {

@@ -172,6 +172,22 @@ int amr_dump_uniform(Handle &h, int gpd, int reference_rules, double *out);
 int adjoint_grad(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_opts &o, double *loglik,
                  double *grad);
 
+// ---- surrogate.cu ----
+struct Surrogate;
+int surrogate_create(Handle &h, const gbg_surrogate_config &c, Surrogate **out);
+void surrogate_destroy(Surrogate *s);
+long surrogate_nparams(const Surrogate &s);
+int surrogate_batch_max(const Surrogate &s);
+const float *surrogate_prediction(const Surrogate &s);  // last predicted densities, solver grid
+int surrogate_get_params(Surrogate &s, float *out);
+int surrogate_set_params(Surrogate &s, const float *in);
+int surrogate_loss_grad(Surrogate &s, const gbg_sample *samples, int B, const float *targets_host, double *loss,
+                        float *grad_host);
+int surrogate_features(Surrogate &s, const gbg_sample *samples, int B, float *out);
+int surrogate_train(Surrogate &s, const gbg_sample *samples, int S, int epochs, int batch, double lr,
+                    unsigned long long seed, double *loss_out);
+int surrogate_predict(Surrogate &s, const gbg_sample *samples_device, int B, gbg_lik_result *lik_device);
+
 // ---- likelihood.cu ----
 int lik_set_observations(Handle &h, const double *pet, const double *t1, const double *t2,
                          const double *points, long npoints, const gbg_lik_params &p);

@@ -177,6 +177,47 @@ typedef struct {
 int gbg_adjoint_grad(gbg_handle *h, const gbg_sample *samples, int S, const gbg_adjoint_opts *o,
                      double *loglik, double *grad);
 
+/* ---- learned surrogate (delayed-acceptance screening) ----------------------------
+ * No reference counterpart. A small 3D convolutional U-Net maps a sample's
+ * parameters (as input channels: the anatomy, a blob at the seed, the
+ * rescaled Dw, rho and tend, and the distance to a Fisher-KPP front of radius
+ * 2 sqrt(D rho) tend) to its final density on a grid `factor` (= 2) times
+ * coarser than the handle's. It is trained by the library's own bf16
+ * tensor-core kernels (forward and backward) on densities that the handle's
+ * batched solver computes for the given training samples, with Adam on fp32
+ * master weights. gbg_surrogate_loglik predicts densities (upsampled to the
+ * solver grid, zero off tissue) and evaluates the handle's likelihood on
+ * them: the cheap first stage of delayed-acceptance MCMC, whose second stage
+ * is the solver. The handle must be GBG_PREC_F32 with max_samples >= 1 and
+ * n a multiple of 8; gbg_surrogate_create copies its anatomy. */
+typedef struct gbg_surrogate gbg_surrogate;
+typedef struct {
+    int factor;      /* solver grid / surrogate grid, 2 */
+    int batch_max;   /* largest batch of train/loss_grad/loglik */
+    double L;        /* brain length in cm */
+    double dw_lo, dw_hi, rho_lo, rho_hi, t_lo, t_hi; /* prior ranges for input scaling */
+    unsigned long long seed; /* initial weights */
+} gbg_surrogate_config;
+
+int gbg_surrogate_create(gbg_handle *h, const gbg_surrogate_config *cfg, gbg_surrogate **out);
+int gbg_surrogate_destroy(gbg_surrogate *s);
+int gbg_surrogate_nparams(gbg_surrogate *s, long *count);
+int gbg_surrogate_get_params(gbg_surrogate *s, float *params);
+int gbg_surrogate_set_params(gbg_surrogate *s, const float *params);
+/* trains on S samples for `epochs` passes; *loss = mean loss of the last pass */
+int gbg_surrogate_train(gbg_surrogate *s, const gbg_sample *samples, int S, int epochs, int batch,
+                        double lr, unsigned long long seed, double *loss);
+/* loss and flat parameter gradient of one batch against host targets on the
+ * surrogate grid (B fields of (n/2)^3 floats); grad may be null */
+int gbg_surrogate_loss_grad(gbg_surrogate *s, const gbg_sample *samples, int B, const float *targets,
+                            double *loss, float *grad);
+/* the network's input channels of B samples, B x (n/2)^3 x 16 floats */
+int gbg_surrogate_features(gbg_surrogate *s, const gbg_sample *samples, int B, float *out);
+/* predicted log-likelihoods of B samples (host); phi, if non-null, receives
+ * the B predicted densities on the solver grid */
+int gbg_surrogate_loglik(gbg_surrogate *s, const gbg_sample *samples, int B, gbg_lik_result *out,
+                         float *phi);
+
 /* ---- multiresolution block grid ----------------------------------------------
  * MRAG's grid of 16^3 blocks at mixed levels (source/MRAGcore/MRAGrid.h:44-186):
  * block b at level l covers [index/2^l, (index+1)/2^l) of the unit cube with
