@@ -158,46 +158,139 @@ def cpu_baseline(an, prior, seconds=12.0):
                        f"{per_solve / N ** 3:.1f} steps per solve")
 
 
-def mcmc_comparison(device, mala_steps=120, mala_burn=40, rwm_steps=2000, rwm_burn=500,
-                    n=64, chains=64):
-    """Posterior ESS/s of plain single-solve MCMC (one random-walk chain,
-    one forward solve per step) against batched MALA (64 chains, one batched
-    forward + adjoint call per generation), same posterior, at n^3."""
+def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=16,
+                    plain_steps=3000, plain_burn=500, unet=True):
+    """Posterior effective samples per second at n^3 on one synthetic
+    patient: plain single-solve MCMC (one random-walk chain in theta, one
+    forward solve per step, the proposal scaled by the prior box and its
+    step adapted during burn-in) against the batched + adjoint + surrogate
+    pipeline (gliomauq_gb300.mcmc.sample_posterior: batched prior screen,
+    adjoint Newton mode and Hessian, profile-refined Gaussian, then delayed
+    acceptance with the affine tangent surrogate over `chains` lock-step
+    chains in the scaling symmetry's coordinates). Both target the same
+    posterior (smooth-time-grid forward model, dt0 from the prior's largest
+    Dw); the observations come from the same model. Diagnostics (multi-chain
+    and within-chain ESS, split R-hat) are taken in the invariant
+    coordinates (log c, log rho T, log Dw/rho, x0, y0, z0) for both samplers;
+    times exclude burn-in (setup and burn-in are reported separately). The
+    learned U-Net surrogate is measured as a stage-1 screen in the same
+    delayed-acceptance sampler."""
     from gliomauq_gb300 import _lib, mcmc, synthetic as Syn
     an = Syn.make_anatomy(n, seed=0)
     truth = Syn.draw_prior(an, 1, seed=10_000)[0]
     rng = np.random.default_rng(0)
-    h = _lib.Handle(n, "f32", device=device, max_samples=chains)
+    h = _lib.Handle(n, "f32", device=device, max_samples=512)
     h.set_anatomy(an.p_w, an.p_g)
-    u = h.batch_solve([truth.as_tuple()], an.L, with_loglik=False, want_phi=True)["phi"][0]
+    prior = mcmc.Prior.from_anatomy(an)
+    dt0 = Syn.reference_dt(n, prior.hi[0], an.L)[0]
+    # observations from the same forward model the samplers use
+    u = h.batch_solve([truth.as_tuple()], an.L, with_loglik=False, want_phi=True,
+                      dt0=dt0)["phi"][0]
     obs = Syn.make_observations(u.astype(np.float64), an, seed=3,
                                 centre_xyz=(truth.x0, truth.y0, truth.z0),
                                 radius_vox=27.0 * n / 128)
     h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2)
-    prior = mcmc.Prior.from_anatomy(an)
-    dt0 = Syn.reference_dt(n, prior.hi[0], an.L)[0]
-    th0 = np.array([truth.as_tuple()] * chains) + rng.normal(0, 1e-3, (chains, 6)) * prior.width
-    post = mcmc.Posterior(h, an.L, dt0, prior)
-    r = mcmc.mala(post, th0, mala_steps, 2e-3, rng, burn=mala_burn)
-    t_mala = r.seconds * (mala_steps - mala_burn) / mala_steps
-    e_mala = mcmc.ess(r.samples[mala_burn:])
+    screen = np.array([p.as_tuple() for p in Syn.draw_prior(an, 512, seed=99)])
+    res = mcmc.sample_posterior(h, an.L, prior, dt0, rng, chains=chains, generations=generations,
+                                burn=burn, inner=inner, screen_draws=screen)
+    lc = mcmc.LogCoords(mcmc.Posterior(h, an.L, dt0, prior), A=mcmc.INVARIANT_MAP)
+    names = ["log c (symmetry axis)", "log rho T", "log Dw/rho", "x0", "y0", "z0"]
+
+    def diagnostics(theta, seconds):
+        v = lc.to_u(theta)  # sampler-independent invariant coordinates
+        e, ew, rh = mcmc.ess(v), mcmc.ess(v, within=True), mcmc.rhat(v)
+        ident = slice(1, 6)
+        return {"ess": e.tolist(), "ess_within": ew.tolist(), "rhat": rh.tolist(),
+                "seconds": seconds,
+                "ess_per_s_identified": float(e[ident].min() / seconds),
+                "ess_per_s_symmetry_axis": float(e[0] / seconds),
+                "ess_per_s_all": float(e.min() / seconds),
+                "mean_theta": theta.reshape(-1, 6).mean(axis=0).tolist(),
+                "mean_v": v.reshape(-1, 6).mean(axis=0).tolist(),
+                "sd_v": v.reshape(-1, 6).std(axis=0).tolist()}
+
+    th = res.theta
+    d_pipe = diagnostics(th, res.sample_seconds)
+    half = chains // 2
+    va = lc.to_u(th[:, :half]).reshape(-1, 6).mean(axis=0)
+    vb = lc.to_u(th[:, half:]).reshape(-1, 6).mean(axis=0)
+    d_pipe["halves_mean_diff_in_sd"] = (np.abs(va - vb) / np.array(d_pipe["sd_v"])).tolist()
+    # plain single-solve chain, started at the same point as the pipeline's mode
     post1 = mcmc.Posterior(h, an.L, dt0, prior)
-    r1 = mcmc.rwm(post1, th0[:1], rwm_steps, 1e-3, rng, burn=rwm_burn)
-    t_rwm = r1.seconds * (rwm_steps - rwm_burn) / rwm_steps
-    e_rwm = mcmc.ess(r1.samples[rwm_burn:])
+    start = lc.to_theta(res.v_map[None])
+    r1 = mcmc.rwm(post1, start, plain_steps, 1e-3, rng, burn=plain_burn)
+    t_plain = r1.seconds * (plain_steps - plain_burn) / plain_steps
+    d_plain = diagnostics(r1.samples[plain_burn:], t_plain)
+    out = {
+        "grid": n, "dt0_days": dt0, "coordinates": names,
+        "posterior": "synthetic truth, PET/T1/T2 likelihood, smooth-time-grid model (data and "
+                     "inference)",
+        "truth": list(truth.as_tuple()),
+        "note": "the continuous model depends on (Dw/rho, rho T) only: along the scaling "
+                "symmetry (c Dw, c rho, T/c) only the time discretisation and the prior box "
+                "shape the posterior, which is long and flat there; ESS/s is reported for the "
+                "identified coordinates and for the symmetry axis separately",
+        "plain": dict(sampler="RWM, 1 chain in theta, 1 forward solve per step, "
+                              "prior-box-scaled proposal, step adapted in burn-in",
+                      steps=plain_steps - plain_burn, accept=float(r1.accept), **d_plain),
+        "pipeline": dict(sampler=f"delayed acceptance, tangent surrogate (affine + second order "
+                                 f"along the symmetry axis), {chains} chains x {inner} surrogate "
+                                 f"steps per solve, invariant coordinates",
+                         generations=generations - burn, accept=float(res.result.accept),
+                         stage1_accept=float(res.result.history["stage1_accept"]),
+                         stage2_accept=float(res.result.history["stage2_accept"]),
+                         setup_seconds=res.setup_seconds, burn_seconds=res.burn_seconds,
+                         **d_pipe),
+    }
+    for k in ("identified", "symmetry_axis", "all"):
+        a, b = d_pipe[f"ess_per_s_{k}"], d_plain[f"ess_per_s_{k}"]
+        out[f"ess_per_s_ratio_{k}"] = a / b if b > 0 else None
+    if unet:
+        out["learned_surrogate"] = unet_screen(h, an, prior, dt0, res, rng)
     h.close()
-    plain = float(e_rwm.min() / t_rwm)
-    mala = float(e_mala.min() / t_mala)
-    return {"grid": n, "posterior": "synthetic truth, PET/T1/T2 likelihood, smooth-time-grid model",
-            "plain": {"sampler": "RWM, 1 chain, 1 forward solve per step", "steps": rwm_steps - rwm_burn,
-                      "accept": float(r1.accept), "ess_min": float(e_rwm.min()),
-                      "seconds": t_rwm, "ess_per_s": plain},
-            "batched_adjoint": {"sampler": f"MALA, {chains} chains, batched forward+adjoint",
-                                "steps": mala_steps - mala_burn, "accept": float(r.accept),
-                                "ess_min": float(e_mala.min()), "seconds": t_mala,
-                                "ess_per_s": mala},
-            "ess_per_s_ratio": mala / plain if plain > 0 else None,
-            "surrogate": "not built"}
+    return out
+
+
+def unet_screen(h, an, prior, dt0, res, rng, train_n=256, epochs=6, gens=20, inner=8):
+    """The bf16 U-Net as the stage-1 screen: trained by the library's
+    kernels on `train_n` prior draws (batched solver targets), then its
+    held-out density error, its log-posterior error near the mode, and the
+    stage-2 acceptance of the same delayed-acceptance sampler with it in
+    place of the affine surrogate."""
+    from gliomauq_gb300 import _lib, mcmc, synthetic as Syn
+    lo = (Syn.PRIOR_DW_CM2[0], Syn.PRIOR_RHO[0], Syn.PRIOR_T[0])
+    hi = (Syn.PRIOR_DW_CM2[1], Syn.PRIOR_RHO[1], Syn.PRIOR_T[1])
+    sg = _lib.Surrogate(h, an.L, lo, hi, batch_max=64, seed=7)
+    try:
+        train = [p.as_tuple() for p in Syn.draw_prior(an, train_n, seed=21)]
+        t0 = time.perf_counter()
+        loss = sg.train(train, epochs=epochs, batch=8, lr=2e-3, seed=1)
+        t_train = time.perf_counter() - t0
+        test = [p.as_tuple() for p in Syn.draw_prior(an, 16, seed=22)]
+        pred = sg.loglik(test, want_phi=True)["phi"]
+        true = h.batch_solve(test, an.L, with_loglik=False, want_phi=True)["phi"]
+        dens = float(np.linalg.norm(pred - true) / np.linalg.norm(true))
+        post = mcmc.LogCoords(mcmc.Posterior(h, an.L, dt0, prior), A=mcmc.INVARIANT_MAP)
+        Lc = np.linalg.cholesky(res.cov)
+        near = res.v_map + rng.standard_normal((64, 6)) @ Lc.T
+        exact, _ = post.loglik(near, False)
+        sp = post.surrogate(mcmc.SurrogatePosterior(sg, prior))
+        t0 = time.perf_counter()
+        approx = sp.logpost(near)
+        t_eval = (time.perf_counter() - t0) / 64
+        aff = mcmc.AffineSurrogate(post, res.v_map, 0.5 * np.sqrt(np.diag(res.cov)))
+        aff_err = float(np.std(exact - aff.logpost(near)))
+        r = mcmc.da(post, sp, near, gens, 2.38 / np.sqrt(6), rng, inner=inner, burn=0, chol=Lc)
+        return {"params": sg.nparams(), "train_samples": train_n, "epochs": epochs,
+                "train_seconds": t_train, "train_loss": loss, "heldout_density_rel_l2": dens,
+                "seconds_per_eval": t_eval,
+                "logpost_error_sd_near_mode": float(np.std(exact - approx)),
+                "affine_logpost_error_sd_near_mode": aff_err,
+                "exact_logpost_sd_near_mode": float(np.std(exact)),
+                "da_stage2_accept": float(r.history["stage2_accept"]),
+                "da_generations": gens}
+    finally:
+        sg.close()
 
 
 def run_reference_arm(args):

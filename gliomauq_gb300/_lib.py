@@ -32,7 +32,7 @@ EXPORTS = [
     "gbg_amr_dump_uniform", "gbg_surrogate_create", "gbg_surrogate_destroy",
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
-    "gbg_surrogate_loglik",
+    "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik",
 ]
 
 
@@ -85,7 +85,7 @@ class SurrogateConfig(C.Structure):
 
 class BatchOpts(C.Structure):
     _fields_ = [("L", C.c_double), ("ic_peak", C.c_double), ("ic_sigma", C.c_double),
-                ("with_loglik", C.c_int)]
+                ("with_loglik", C.c_int), ("dt0", C.c_double)]
 
 
 _lib = None
@@ -143,6 +143,8 @@ def load(path: str = LIB_PATH):
         "gbg_surrogate_loss_grad": [vp, C.POINTER(Sample), C.c_int, fp, dp, fp],
         "gbg_surrogate_features": [vp, C.POINTER(Sample), C.c_int, fp],
         "gbg_surrogate_loglik": [vp, C.POINTER(Sample), C.c_int, C.POINTER(LikResult), fp],
+        "gbg_affine_set": [vp, C.c_int, fp, fp],
+        "gbg_affine_loglik": [vp, C.c_int, dp, C.POINTER(LikResult)],
         "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
                                C.POINTER(LikParams), vp, vp],
     }
@@ -181,6 +183,7 @@ class Handle:
         self.lib = load()
         self.n = n
         self.N = n ** 3
+        self.max_samples = max_samples
         self.precision = PREC_BY_NAME[precision] if isinstance(precision, str) else precision
         cfg = Config(n, self.precision, device, max_samples)
         h = C.c_void_p()
@@ -247,10 +250,12 @@ class Handle:
         return r.as_dict()
 
     def batch_solve(self, samples, L, ic_peak=0.1, ic_sigma=1.0, with_loglik=True,
-                    want_phi=False):
+                    want_phi=False, dt0=0.0):
+        """dt0 = 0: the reference's time loop per sample; dt0 > 0: the smooth
+        time grid of adjoint_grad (same forward model, bit for bit)."""
         S = len(samples)
         arr = (Sample * S)(*[Sample(*s) for s in samples])
-        opts = BatchOpts(L, ic_peak, ic_sigma, 1 if with_loglik else 0)
+        opts = BatchOpts(L, ic_peak, ic_sigma, 1 if with_loglik else 0, dt0)
         lik = (LikResult * S)()
         steps = np.zeros(S, dtype=np.int64)
         phi = np.empty((S, self.n, self.n, self.n), dtype=np.float32) if want_phi else None
@@ -266,8 +271,8 @@ class Handle:
         return out
 
     def batch_solve_device(self, samples_dev_ptr: int, S: int, L, lik_dev_ptr: int | None,
-                           ic_peak=0.1, ic_sigma=1.0):
-        opts = BatchOpts(L, ic_peak, ic_sigma, 1 if lik_dev_ptr else 0)
+                           ic_peak=0.1, ic_sigma=1.0, dt0=0.0):
+        opts = BatchOpts(L, ic_peak, ic_sigma, 1 if lik_dev_ptr else 0, dt0)
         check(self.lib.gbg_batch_solve_device(self._h, C.c_void_p(samples_dev_ptr), S,
                                               C.byref(opts),
                                               C.c_void_p(lik_dev_ptr) if lik_dev_ptr else None))
@@ -284,6 +289,23 @@ class Handle:
         check(self.lib.gbg_adjoint_grad(self._h, arr, S, C.byref(o), dptr(ll),
                                         dptr(g) if want_grad else None))
         return ll, (g if want_grad else None)
+
+    def affine_set(self, phi0, J):
+        """Affine density model phi0 + sum_p delta_p J[p] (float fields)."""
+        p0 = np.ascontiguousarray(phi0, dtype=np.float32).reshape(-1)
+        Jf = np.ascontiguousarray(J, dtype=np.float32).reshape(-1, self.N)
+        if p0.size != self.N:
+            raise ValueError("phi0 must have n^3 values")
+        check(self.lib.gbg_affine_set(self._h, Jf.shape[0], fptr(p0), fptr(Jf)))
+        self._aff_P = Jf.shape[0]
+
+    def affine_loglik(self, delta) -> np.ndarray:
+        """log L totals of the affine models at the rows of delta (B x P)."""
+        d = np.ascontiguousarray(np.atleast_2d(delta), dtype=np.float64)
+        B = d.shape[0]
+        lik = (LikResult * B)()
+        check(self.lib.gbg_affine_loglik(self._h, B, dptr(d), lik))
+        return np.array([lik[i].total for i in range(B)])
 
     def launch_count(self) -> int:
         c = C.c_longlong()

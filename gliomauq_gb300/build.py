@@ -20,7 +20,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr"]
 NOFMA = {"rd_exact.cu", "likelihood.cu", "amr.cu"}
 SOURCES = ["abi.cu", "rd_exact.cu", "rd_fast.cu", "likelihood.cu", "amr.cu", "adjoint.cu",
-           "surrogate.cu"]
+           "surrogate.cu", "affine.cu"]
 
 
 def nvcc() -> str:

@@ -78,7 +78,7 @@ void free_handle(Handle &h) {
     void *ptrs[] = {h.pw, h.pg, h.phi[0], h.phi[1], h.b0, h.dfx, h.dfy, h.dfz, h.cx, h.cy, h.cz,
                     h.msk, h.bphi[0], h.bphi[1], h.bwork, h.dev_status, h.barrier,
                     h.obs.pet_idx, h.obs.pet_val, h.obs.ti_idx, h.obs.t1_val, h.obs.t2_val,
-                    h.lik_partials, h.lik_out};
+                    h.lik_partials, h.lik_out, h.adj_ws, h.aff_phi0, h.aff_J, h.aff_out, h.aff_delta};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : h.ev_pop)
@@ -347,7 +347,7 @@ int gbg_loglik(gbg_handle *hh, gbg_lik_result *out) {
 
 static int validate_batch(Handle &h, int S, const gbg_batch_opts *o) {
     if (!o || S <= 0 || S > h.max_samples || !(o->L > 0) || !(o->ic_sigma > 0) ||
-        !std::isfinite(o->ic_peak)) {
+        !std::isfinite(o->ic_peak) || !(o->dt0 >= 0) || !std::isfinite(o->dt0)) {
         set_error("bad batch arguments");
         return GBG_ERR_ARG;
     }
@@ -604,6 +604,60 @@ int gbg_amr_dump_uniform(gbg_handle *hh, int gpd, int reference_rules, double *o
     }
     GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
     return gbg::amr_dump_uniform(hh->h, gpd, reference_rules, out);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int gbg_affine_set(gbg_handle *hh, int P, const float *phi0, const float *J) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!phi0 || !J) {
+        set_error("null field");
+        return GBG_ERR_ARG;
+    }
+    if (h.is_amr || h.prec != GBG_PREC_F32 || !h.anatomy_set) {
+        set_error("affine model needs a GBG_PREC_F32 handle with its anatomy set");
+        return GBG_ERR_STATE;
+    }
+    for (size_t i = 0; i < h.N; ++i)
+        if (!std::isfinite(phi0[i])) {
+            set_error("phi0 has NaN or Inf");
+            return GBG_ERR_NONFINITE;
+        }
+    if (P >= 1 && P <= 16)
+        for (size_t i = 0; i < (size_t)P * h.N; ++i)
+            if (!std::isfinite(J[i])) {
+                set_error("J has NaN or Inf");
+                return GBG_ERR_NONFINITE;
+            }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    return gbg::affine_set(h, P, phi0, J);
+}
+
+int gbg_affine_loglik(gbg_handle *hh, int B, const double *delta, gbg_lik_result *out) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!delta || !out || B < 1) {
+        set_error("bad affine arguments");
+        return GBG_ERR_ARG;
+    }
+    if (!h.obs.valid) {
+        set_error("observations not set");
+        return GBG_ERR_STATE;
+    }
+    for (size_t i = 0; i < (size_t)B * (h.aff_P > 0 ? h.aff_P : 0); ++i)
+        if (!std::isfinite(delta[i])) {
+            set_error("non-finite delta");
+            return GBG_ERR_NONFINITE;
+        }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    if (int rc = ensure_lik_out(h, B)) return rc;
+    if (int rc = gbg::affine_loglik(h, B, delta, (gbg_lik_result *)h.lik_out)) return rc;
+    GBG_CUDA_TRY(cudaMemcpyAsync(out, h.lik_out, B * sizeof(gbg_lik_result), cudaMemcpyDeviceToHost, h.stream));
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    return GBG_OK;
 }
 
 }  // extern "C"
@@ -903,7 +957,7 @@ int gbg_autotune(gbg_handle *hh, int probe_samples, const char *cache_path, int 
         gbg::reference_dt(h.n, Dw, L, false, &dt, &Dwu, &Dgu, &r);
         probe[i] = gbg_sample{Dw, 0.05, c + (i % 3) - 1.0, c, c + (i % 5) - 2.0, 23.5 * dt};
     }
-    gbg_batch_opts o{L, 0.1, 1.0, 0};
+    gbg_batch_opts o{L, 0.1, 1.0, 0, 0.0};
     int best = 0;
     float best_ms = 1e30f;
     const int saved = h.pop_variant;

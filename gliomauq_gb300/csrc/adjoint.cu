@@ -11,6 +11,9 @@
 // with a_k = dt_k Dw / (L^2 h^2), b_k = dt_k rho, unit face coefficients c_f
 // (Case2 harmonic means with Dg = 0.1 Dw) and the tissue mask m, from the
 // Gaussian initial density peak * exp(-|x - x0|^2 / (2 sigma^2)) on tissue.
+// With float states the forward pass is the batched solver's on its smooth
+// time grid (gbg_batch_opts.dt0): the same coefficient tables, schedule,
+// initial densities and operation order, so log L agrees bit for bit.
 //
 // Adjoint (L is symmetric, so L^T = L): with lambda = dlogL/dphi at step k+1,
 //   mu_c     = m_c [0 <= v_c < 1] lambda_c
@@ -55,7 +58,7 @@ __global__ void k_adj_tables(int n, const double *__restrict__ pw, const double 
         for (int i = 0; i < 7; ++i) {
             const double b = pw[nb[i]] + pg[nb[i]];
             all = all && b > 0.0;
-            if (i < 4) k[i] = b > 0.0 ? (pw[nb[i]] + 0.1 * pg[nb[i]]) / b : 0.0;
+            if (i < 4) k[i] = b > 0.0 ? (pw[nb[i]] + (double)0.1f * pg[nb[i]]) / b : 0.0;
         }
         Real *dst[3] = {cx, cy, cz};
         for (int f = 0; f < 3; ++f) {
@@ -83,6 +86,29 @@ __device__ __forceinline__ Real lap(const Real *f, const Real *cx, const Real *c
            cz[cB] * (f[cB] - f0) + cz[c] * (f[cF] - f0);
 }
 
+__device__ __forceinline__ float fma_r(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_r(double a, double b, double c) { return fma(a, b, c); }
+
+// pre-clamp update v = phi + a L(phi) + b phi (1 - phi), in the batched
+// solver's operation order (faces -x, +x, -y, +y, -z, +z)
+template <typename Real>
+__device__ __forceinline__ Real step_value(const Real *f, const Real *cx, const Real *cy, const Real *cz, int n,
+                                           size_t c, int x, int y, int z, Real a, Real b) {
+    const size_t nn = n, pl = nn * nn;
+    const size_t cW = c - x + wm(x, n), cE = c - x + wp(x, n);
+    const size_t cS = c + ((size_t)wm(y, n) - y) * nn, cN = c + ((size_t)wp(y, n) - y) * nn;
+    const size_t cB = c + ((size_t)wm(z, n) - z) * pl, cF = c + ((size_t)wp(z, n) - z) * pl;
+    const Real f0 = f[c];
+    Real lap = cx[cW] * (f[cW] - f0);
+    lap = fma_r(cx[c], f[cE] - f0, lap);
+    lap = fma_r(cy[cS], f[cS] - f0, lap);
+    lap = fma_r(cy[c], f[cN] - f0, lap);
+    lap = fma_r(cz[cB], f[cB] - f0, lap);
+    lap = fma_r(cz[c], f[cF] - f0, lap);
+    Real v = fma_r(a, lap, f0);
+    return fma_r(b * f0, (Real)1 - f0, v);
+}
+
 template <typename Real>
 __global__ void k_adj_ic(int n, int S, const gbg_sample *__restrict__ smp, double peak, double sigma,
                          const double *__restrict__ pw, const double *__restrict__ pg, Real *__restrict__ phi) {
@@ -93,7 +119,8 @@ __global__ void k_adj_ic(int n, int S, const gbg_sample *__restrict__ smp, doubl
         double v = 0.0;
         if (pw[c] + pg[c] > 0.0) {
             const double dx = x - smp[s].x0, dy = y - smp[s].y0, dz = z - smp[s].z0;
-            v = peak * exp(-(dx * dx + dy * dy + dz * dz) / (2.0 * sigma * sigma));
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            v = __dmul_rn(peak, exp(__ddiv_rn(-d2, __dmul_rn(__dmul_rn(2.0, sigma), sigma))));
         }
         phi[i] = (Real)v;
     }
@@ -114,8 +141,7 @@ __global__ void k_adj_fwd(int n, int S, const Real *__restrict__ in, Real *__res
             continue;
         }
         const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
-        const Real p = f[c];
-        Real v = p + (Real)a[s] * lap(f, cx, cy, cz, n, c, x, y, z) + (Real)b[s] * p * ((Real)1 - p);
+        Real v = step_value(f, cx, cy, cz, n, c, x, y, z, (Real)a[s], (Real)b[s]);
         v = v < (Real)0 ? (Real)0 : (v > (Real)1 ? (Real)1 : v);
         out[i] = m[c] != (Real)0 ? v : (Real)0;
     }
@@ -157,7 +183,7 @@ __global__ void k_adj_mu(int n, const Real *__restrict__ phi, const Real *__rest
         const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
         const Real p = f[c];
         const Real L = lap(f, cx, cy, cz, n, c, x, y, z);
-        const Real v = p + (Real)a[s] * L + (Real)b[s] * p * ((Real)1 - p);
+        const Real v = step_value(f, cx, cy, cz, n, c, x, y, z, (Real)a[s], (Real)b[s]);
         const Real g = (m[c] != (Real)0 && v >= (Real)0 && v < (Real)1) ? (Real)1 : (Real)0;
         const Real u = g * lam[i];
         mu[i] = u;
@@ -260,62 +286,104 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     const int n = h.n;
     const size_t N = h.N;
     const double hh = 1.0 / n, ih2 = 1.0 / (hh * hh), L2 = o.L * o.L;
-    // per-sample step counts on the smooth time grid
+    constexpr bool f32 = std::is_same<Real, float>::value;
+    // per-sample schedule on the smooth time grid, from the batched solver's
+    // schedule kernel (its float coefficients are the float path's a_k, b_k)
+    std::vector<SampleRec> recs(S);
+    {
+        void *d = nullptr;
+        const size_t bytes = S * (sizeof(gbg_sample) + sizeof(SampleRec)) + 256;
+        GBG_CUDA_TRY(cudaMalloc(&d, bytes));
+        gbg_sample *dsmp = (gbg_sample *)d;
+        SampleRec *drec = (SampleRec *)((char *)d + bwork_align(S * sizeof(gbg_sample)));
+        cudaError_t e = cudaMemcpyAsync(dsmp, samples, S * sizeof(gbg_sample), cudaMemcpyHostToDevice, h.stream);
+        int rc = e == cudaSuccess ? launch_schedule_smooth(h, dsmp, S, o.L, o.dt0, drec) : GBG_ERR_CUDA;
+        if (rc == GBG_OK &&
+            (cudaMemcpyAsync(recs.data(), drec, S * sizeof(SampleRec), cudaMemcpyDeviceToHost, h.stream) != cudaSuccess ||
+             cudaStreamSynchronize(h.stream) != cudaSuccess))
+            rc = GBG_ERR_CUDA;
+        cudaFree(d);
+        if (rc) {
+            set_error("adjoint: schedule failed");
+            return rc;
+        }
+    }
     std::vector<int> ns(S);
     std::vector<double> dtl(S);
     int nmax = 0;
     for (int s = 0; s < S; ++s) {
-        const double T = samples[s].tend;
-        int k = (int)std::ceil(T / o.dt0);
-        if (k < 1) k = 1;
+        const int k = recs[s].nsteps;
         ns[s] = k;
-        dtl[s] = T - (k - 1) * o.dt0;
+        dtl[s] = samples[s].tend - (k - 1) * o.dt0;
         nmax = std::max(nmax, k);
     }
-    const int K = o.checkpoint_every > 0 ? o.checkpoint_every : 50;
+    if (f32) {
+        if (int rc = fast_build_tables(h, (double)0.1f)) return rc;
+    }
+    int K = o.checkpoint_every;
+    if (K <= 0) K = std::max(1, (int)std::ceil(std::sqrt((double)nmax)));
+    // without a gradient only the forward pass runs: no checkpoints kept
+    if (!grad) K = nmax + 1;
     const int nck = nmax / K + 1;
-    // device buffers (freed at the end of the call)
-    std::vector<void *> owned;
-    auto alloc = [&](size_t bytes) -> void * {
-        void *p = nullptr;
-        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
-        owned.push_back(p);
-        return p;
-    };
-    auto release = [&]() {
-        for (void *p : owned) cudaFree(p);
-    };
-    Real *tab = (Real *)alloc(4 * N * sizeof(Real));
-    Real *ck = (Real *)alloc((size_t)nck * S * N * sizeof(Real));
-    Real *seg = (Real *)alloc((size_t)K * S * N * sizeof(Real));
-    Real *lam = (Real *)alloc(S * N * sizeof(Real));
-    Real *mu = (Real *)alloc(S * N * sizeof(Real));
-    Real *fin = (Real *)alloc(S * N * sizeof(Real));
-    double *da = (double *)alloc((size_t)nmax * S * sizeof(double));
-    double *db = (double *)alloc((size_t)nmax * S * sizeof(double));
-    double *gA = (double *)alloc((size_t)nmax * S * sizeof(double));
-    double *gB = (double *)alloc((size_t)nmax * S * sizeof(double));
-    double *gX = (double *)alloc(3 * S * sizeof(double));
-    gbg_sample *dsm = (gbg_sample *)alloc(S * sizeof(gbg_sample));
-    gbg_lik_result *dlik = (gbg_lik_result *)alloc(S * sizeof(gbg_lik_result));
-    for (void *p : owned)
-        if (!p) {
-            release();
+    const size_t segs = grad ? (size_t)K : 2;
+    // device working set: carved from the handle's grow-only workspace
+    const size_t SN = (size_t)S * N;
+    const size_t sizes[] = {f32 ? 0 : 4 * N * sizeof(Real), (size_t)nck * SN * sizeof(Real),
+                            segs * SN * sizeof(Real), SN * sizeof(Real), SN * sizeof(Real), SN * sizeof(Real),
+                            (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
+                            (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
+                            3 * S * sizeof(double), S * sizeof(gbg_sample), S * sizeof(gbg_lik_result)};
+    size_t total = 0;
+    for (size_t b : sizes) total += bwork_align(b);
+    if (h.adj_ws_bytes < total) {
+        if (h.adj_ws) cudaFree(h.adj_ws);
+        h.adj_ws = nullptr;
+        h.adj_ws_bytes = 0;
+        if (cudaMalloc(&h.adj_ws, total) != cudaSuccess) {
+            cudaGetLastError();
             set_error("adjoint: device allocation failed");
             return GBG_ERR_NOMEM;
         }
-    if (owned.size() != 13) {
-        release();
-        set_error("adjoint: device allocation failed");
-        return GBG_ERR_NOMEM;
+        h.adj_ws_bytes = total;
     }
+    void *parts[13];
+    {
+        char *q = (char *)h.adj_ws;
+        for (int i = 0; i < 13; ++i) {
+            parts[i] = q;
+            q += bwork_align(sizes[i]);
+        }
+    }
+    auto release = [] {};
+    Real *tab = (Real *)parts[0];
+    Real *ck = (Real *)parts[1];
+    Real *seg = (Real *)parts[2];
+    Real *lam = (Real *)parts[3];
+    Real *mu = (Real *)parts[4];
+    Real *fin = (Real *)parts[5];
+    double *da = (double *)parts[6];
+    double *db = (double *)parts[7];
+    double *gA = (double *)parts[8];
+    double *gB = (double *)parts[9];
+    double *gX = (double *)parts[10];
+    gbg_sample *dsm = (gbg_sample *)parts[11];
+    gbg_lik_result *dlik = (gbg_lik_result *)parts[12];
     // per-step coefficients; a < 0 marks a finished sample
     std::vector<double> ha((size_t)nmax * S), hb((size_t)nmax * S);
     for (int k = 0; k < nmax; ++k)
         for (int s = 0; s < S; ++s) {
-            const double dtk = k < ns[s] - 1 ? o.dt0 : (k == ns[s] - 1 ? dtl[s] : 0.0);
-            ha[(size_t)k * S + s] = k < ns[s] ? dtk * samples[s].Dw / L2 * ih2 : -1.0;
-            hb[(size_t)k * S + s] = k < ns[s] ? dtk * samples[s].rho : 0.0;
+            const bool last = k == ns[s] - 1;
+            if (k >= ns[s]) {
+                ha[(size_t)k * S + s] = -1.0;
+                hb[(size_t)k * S + s] = 0.0;
+            } else if (f32) {
+                ha[(size_t)k * S + s] = last ? recs[s].a2 : recs[s].a;
+                hb[(size_t)k * S + s] = last ? recs[s].b2 : recs[s].b;
+            } else {
+                const double dtk = last ? dtl[s] : o.dt0;
+                ha[(size_t)k * S + s] = dtk * (samples[s].Dw / L2) * ih2;
+                hb[(size_t)k * S + s] = dtk * samples[s].rho;
+            }
         }
     cudaStream_t st = h.stream;
     int rc = GBG_OK;
@@ -335,12 +403,30 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     ADJ_TRY(cudaMemsetAsync(gB, 0, (size_t)nmax * S * sizeof(double), st));
     ADJ_TRY(cudaMemsetAsync(gX, 0, 3 * S * sizeof(double), st));
     Tabs t{tab, tab + N, tab + 2 * N, tab + 3 * N};
-    k_adj_tables<Real><<<grid_of(h, N), 256, 0, st>>>(n, h.pw, h.pg, tab, tab + N, tab + 2 * N, tab + 3 * N);
-    k_adj_ic<Real><<<grid_of(h, N * S), 256, 0, st>>>(n, S, dsm, o.ic_peak, o.ic_sigma, h.pw, h.pg, ck);
-    h.launches += 2;
+    if (f32) {
+        t = Tabs{h.cx, h.cy, h.cz, h.msk};
+        rc = launch_gaussian_ic(h, dsm, S, o.ic_peak, o.ic_sigma, (float *)ck);
+        if (rc) {
+            release();
+            return rc;
+        }
+    } else {
+        k_adj_tables<Real><<<grid_of(h, N), 256, 0, st>>>(n, h.pw, h.pg, tab, tab + N, tab + 2 * N, tab + 3 * N);
+        k_adj_ic<Real><<<grid_of(h, N * S), 256, 0, st>>>(n, S, dsm, o.ic_peak, o.ic_sigma, h.pw, h.pg, ck);
+        h.launches += 2;
+    }
     // forward with checkpoints
     const int gS = grid_of(h, N * S);
-    {
+    if (!grad) {
+        // forward only: ping-pong through two segment slots, last state into fin
+        Real *cur = ck;
+        for (int k = 0; k < nmax; ++k) {
+            Real *nxt = (k + 1) == nmax ? fin : seg + (size_t)((k + 1) & 1) * S * N;
+            k_adj_fwd<Real><<<gS, 256, 0, st>>>(n, S, cur, nxt, t, da + (size_t)k * S, db + (size_t)k * S);
+            h.launches++;
+            cur = nxt;
+        }
+    } else {
         Real *cur = ck;
         for (int k = 0; k < nmax; ++k) {
             Real *nxt = ((k + 1) % K == 0) ? ck + (size_t)((k + 1) / K) * S * N

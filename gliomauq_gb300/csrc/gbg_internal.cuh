@@ -110,6 +110,17 @@ struct Handle {
     size_t lik_partials_cap = 0;
     void *lik_out = nullptr;         // device gbg_lik_result scratch
     int lik_out_cap = 0;
+
+    // adjoint working set, grow-only
+    void *adj_ws = nullptr;
+    size_t adj_ws_bytes = 0;
+
+    // affine density model phi0 + sum_p delta_p J_p (gbg_affine_*)
+    float *aff_phi0 = nullptr, *aff_J = nullptr, *aff_out = nullptr;
+    int aff_P = 0;
+    size_t aff_out_cap = 0;  // fields
+    double *aff_delta = nullptr;
+    size_t aff_delta_cap = 0;  // doubles
 };
 
 // ---- rd_exact.cu ----
@@ -121,9 +132,10 @@ int exact_steps(Handle &h, double Dw, double Dg, double rho, double dt, long nst
 // longest first, for the population kernel; unsorted for everything else).
 struct SampleRec {
     float a, b;   // dt*Dw/h^2 and dt*rho
-    int nsteps;   // reference step count
+    int nsteps;   // step count
     int order;    // sample index
     double dt;
+    float a2, b2; // coefficients of the last step (== a, b on the reference schedule)
 };
 // Layout of Handle::bwork, each region 256-byte aligned, cap = max(1, max_samples):
 // unsorted records | sorted records | rank_of ints | staged gbg_sample inputs.
@@ -146,6 +158,13 @@ inline gbg_sample *batch_samples(Handle &h) {
     return reinterpret_cast<gbg_sample *>((char *)h.bwork + bwork_off_samples(h));
 }
 int fast_build_tables(Handle &h, double ratio);
+// smooth time grid (fixed dt0, last step shortened): per-sample records into
+// dev_out (S entries, unsorted order)
+int launch_schedule_smooth(Handle &h, const gbg_sample *samples_device, int S, double L, double dt0,
+                           SampleRec *dev_out);
+// Gaussian initial densities of S samples (float fields, the batched solver's IC)
+int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, double peak, double sigma,
+                       float *phi);
 int fast_steps_single(Handle &h, double Dw, double rho, double dt, long nsteps);
 int population_variant_count(int n);
 int population_variant_shape(int n, int vi, int *ry, int *g, int *threads);
@@ -203,6 +222,10 @@ int lik_evaluate_population(Handle &h, const float *buf0, const float *buf1,
 void reference_dt(int n, double Dw_file, double L, bool f32, double *dt, double *Dw, double *Dg,
                   double *rho_in_out);
 long reference_num_steps(double dt, double tend);
+
+// ---- affine.cu ----
+int affine_set(Handle &h, int P, const float *phi0, const float *J);
+int affine_loglik(Handle &h, int B, const double *delta_host, gbg_lik_result *lik_device);
 
 }  // namespace gbg
 

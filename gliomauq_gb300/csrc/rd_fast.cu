@@ -114,6 +114,36 @@ __global__ void k_schedule(const gbg_sample *__restrict__ smp, int S, int n, dou
     r.nsteps = k;
     r.order = s;
     r.dt = dt;
+    r.a2 = r.a;
+    r.b2 = r.b;
+    unsorted[s] = r;
+}
+
+// Smooth time grid: fixed step dt0, k = ceil(tend/dt0) steps (at least one),
+// the last of length tend - (k-1) dt0. Dw in double (no float rounding of the
+// input); every operation rounded on its own so host code that restates it
+// gets the same coefficients.
+__global__ void k_schedule_smooth(const gbg_sample *__restrict__ smp, int S, int n, double L, double dt0,
+                                  SampleRec *__restrict__ unsorted) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const double h = __ddiv_rn(1.0, (double)n);
+    const double ih2 = __ddiv_rn(1., __dmul_rn(h, h));
+    const double Dw = __ddiv_rn(smp[s].Dw, __dmul_rn(L, L));
+    const double rho = smp[s].rho, tend = smp[s].tend;
+    double kk = ceil(__ddiv_rn(tend, dt0));
+    if (!(kk >= 1.0)) kk = 1.0;
+    if (kk > 1e8) kk = 1e8;
+    const int k = (int)kk;
+    const double dtl = __dadd_rn(tend, -__dmul_rn((double)(k - 1), dt0));
+    SampleRec r;
+    r.a = (float)__dmul_rn(__dmul_rn(dt0, Dw), ih2);
+    r.b = (float)__dmul_rn(dt0, rho);
+    r.a2 = (float)__dmul_rn(__dmul_rn(dtl, Dw), ih2);
+    r.b2 = (float)__dmul_rn(dtl, rho);
+    r.nsteps = k;
+    r.order = s;
+    r.dt = dt0;
     unsorted[s] = r;
 }
 
@@ -292,8 +322,9 @@ __global__ void __launch_bounds__(256, MINB) k_population1(PopArgs p) {
             const int r = (int)(it / p.tiles), t = (int)(it % p.tiles);
             const int ty = t % p.tiles_y, tz = t / p.tiles_y;
             const size_t off = (size_t)p.rec[r].order * p.stride;
+            const bool last = k == p.rec[r].nsteps - 1;
             march_tile<LR>(p.n, p.TZ, ty * rows, tz * p.TZ, in + off, out + off, p.cx, p.cy, p.cz,
-                           p.msk, p.rec[r].a, p.rec[r].b);
+                           p.msk, last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
         }
         if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
     }
@@ -346,8 +377,9 @@ __global__ void __launch_bounds__(LR *RY *G, (LR * RY * G >= 1024) ? 1 : 1024 / 
             float a = 0.f, b = 0.f;
             size_t off = 0;
             if (valid) {
-                a = p.rec[rank].a;
-                b = p.rec[rank].b;
+                const bool last = k == p.rec[rank].nsteps - 1;
+                a = last ? p.rec[rank].a2 : p.rec[rank].a;
+                b = last ? p.rec[rank].b2 : p.rec[rank].b;
                 off = (size_t)p.rec[rank].order * p.stride;
             }
             const float *src = in + off;
@@ -608,6 +640,23 @@ int check_device_status(Handle &h) {
     return GBG_OK;
 }
 
+int launch_schedule_smooth(Handle &h, const gbg_sample *samples_device, int S, double L, double dt0,
+                           SampleRec *dev_out) {
+    k_schedule_smooth<<<(S + 127) / 128, 128, 0, h.stream>>>(samples_device, S, h.n, L, dt0, dev_out);
+    h.launches++;
+    GBG_CUDA_TRY(cudaGetLastError());
+    return GBG_OK;
+}
+
+int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, double peak, double sigma,
+                       float *phi) {
+    k_gaussian_ic<<<grid_for(h, h.N * S), 256, 0, h.stream>>>(h.n, samples_device, S, peak, sigma, h.msk, h.pw,
+                                                               h.pg, phi);
+    h.launches++;
+    GBG_CUDA_TRY(cudaGetLastError());
+    return GBG_OK;
+}
+
 int fast_build_tables(Handle &h, double ratio) {
     if (h.fast_valid && h.fast_ratio == ratio) return GBG_OK;
     k_fast_tables<<<grid_for(h, h.N), 256, 0, h.stream>>>(h.n, h.pw, h.pg, ratio, h.cx, h.cy,
@@ -633,6 +682,8 @@ int fast_steps_single(Handle &h, double Dw, double rho, double dt, long nsteps) 
     r.nsteps = (int)nsteps;
     r.order = 0;
     r.dt = dt;
+    r.a2 = r.a;
+    r.b2 = r.b;
     SampleRec *d_rec = reinterpret_cast<SampleRec *>(h.bwork);
     GBG_CUDA_TRY(cudaMemcpyAsync(d_rec, &r, sizeof(r), cudaMemcpyHostToDevice, h.stream));
     int rc = launch_population(h, (float *)h.phi[h.cur], (float *)h.phi[h.cur ^ 1], d_rec, 1);
@@ -653,8 +704,11 @@ int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
     SampleRec *unsorted = batch_unsorted(h);
     SampleRec *sorted = batch_sorted(h);
     int *rank_of = batch_rank_of(h);
-    k_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(samples_device, S, h.n, o.L, f32ref ? 1 : 0,
-                                                      unsorted);
+    if (o.dt0 > 0)
+        k_schedule_smooth<<<(S + 127) / 128, 128, 0, h.stream>>>(samples_device, S, h.n, o.L, o.dt0, unsorted);
+    else
+        k_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(samples_device, S, h.n, o.L, f32ref ? 1 : 0,
+                                                          unsorted);
     k_sort_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(unsorted, S, sorted, rank_of);
     k_gaussian_ic<<<grid_for(h, h.N * S), 256, 0, h.stream>>>(h.n, samples_device, S, o.ic_peak,
                                                                o.ic_sigma, h.msk, h.pw, h.pg,

@@ -794,7 +794,7 @@ int surrogate_train(Surrogate &s, const gbg_sample *samples, int S, int epochs, 
     // training targets, in chunks of the handle's population capacity
     gbg_sample *dsm = batch_samples(h);
     int rc = GBG_OK;
-    gbg_batch_opts o{s.L, 0.1, 1.0, 0};
+    gbg_batch_opts o{s.L, 0.1, 1.0, 0, 0.0};
     for (int s0 = 0; s0 < S && rc == GBG_OK; s0 += h.max_samples) {
         const int cnt = std::min(h.max_samples, S - s0);
         if (cudaMemcpyAsync(dsm, samples + s0, cnt * sizeof(gbg_sample), cudaMemcpyHostToDevice, st) != cudaSuccess) {

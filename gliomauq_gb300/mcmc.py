@@ -12,10 +12,20 @@ uniform prior on a box for Dw, rho, T and on the interior seed region for
 
   * rwm  : random-walk Metropolis, Gaussian proposal
   * mala : Metropolis-adjusted Langevin, gradients from gbg_adjoint_grad
+  * da   : delayed acceptance (Christen & Fox 2005) in its surrogate-
+           transition form (Liu 2001, sec. 9.4): stage 1 runs `inner`
+           random-walk Metropolis steps on the learned surrogate's
+           posterior pi*, stage 2 accepts the end point y of that chain
+           with min(1, pi(y) pi*(x) / (pi(x) pi*(y))), pi from the solver.
+           The inner chain is reversible with respect to pi*, so the
+           composite kernel is reversible with respect to pi: the solver
+           judges every accepted sample and the chain targets the exact
+           posterior whatever the surrogate's error.
   * ess  : effective sample size per parameter (Geyer's initial monotone
            sequence on the chain-averaged autocorrelation)
-Both samplers use the adjoint's smooth-time-grid forward model for log L,
-so they target the same posterior.
+All samplers use the adjoint's smooth-time-grid forward model for log L,
+so they target the same posterior. Log densities and accept/reject are
+float64 throughout.
 """
 from __future__ import annotations
 
@@ -78,6 +88,10 @@ class Posterior:
     seconds: float = 0.0
 
     def loglik(self, theta: np.ndarray, with_grad: bool):
+        """log posterior (and its gradient) of each row of theta. Without the
+        gradient, log L comes from the batched population solver on the same
+        smooth time grid (bitwise the adjoint's forward model), in chunks of
+        the handle's max_samples."""
         th = np.atleast_2d(theta)
         lp = self.prior.logp(th)
         ll = np.full(th.shape[0], -np.inf)
@@ -85,16 +99,25 @@ class Posterior:
         ok = np.isfinite(lp)
         if ok.any():
             t0 = time.perf_counter()
-            l, gr = self.handle.adjoint_grad([tuple(x) for x in th[ok]], self.dt0, self.L,
-                                             ic_peak=self.ic_peak, ic_sigma=self.ic_sigma,
-                                             checkpoint_every=self.checkpoint_every,
-                                             state="f32", want_grad=with_grad)
+            rows = [tuple(x) for x in th[ok]]
+            if with_grad:
+                l, gr = self.handle.adjoint_grad(rows, self.dt0, self.L, ic_peak=self.ic_peak,
+                                                 ic_sigma=self.ic_sigma,
+                                                 checkpoint_every=self.checkpoint_every,
+                                                 state="f32", want_grad=True)
+                g[ok] = gr
+                self.calls += 1
+            else:
+                cap = max(1, self.handle.max_samples)
+                l = np.empty(len(rows))
+                for s0 in range(0, len(rows), cap):
+                    r = self.handle.batch_solve(rows[s0:s0 + cap], self.L, ic_peak=self.ic_peak,
+                                                ic_sigma=self.ic_sigma, dt0=self.dt0)
+                    l[s0:s0 + cap] = [d["total"] for d in r["loglik"]]
+                    self.calls += 1
             self.seconds += time.perf_counter() - t0
-            self.calls += 1
             self.solves += int(ok.sum())
             ll[ok] = l
-            if with_grad:
-                g[ok] = gr
         return ll + lp, g
 
 
@@ -108,17 +131,25 @@ class ChainResult:
     history: dict = field(default_factory=dict)
 
 
+def _chol(post, chol):
+    """Proposal scale: a Cholesky factor in parameter units (default: the
+    prior box widths on the diagonal)."""
+    return np.diag(post.prior.width) if chol is None else np.asarray(chol, dtype=np.float64)
+
+
 def rwm(post: Posterior, theta0: np.ndarray, steps: int, step: float, rng, burn: int = 0,
-        target: float = 0.234) -> ChainResult:
-    """Random-walk Metropolis in prior-width-scaled coordinates; the step is
-    adapted toward the target acceptance during the first `burn` steps."""
+        target: float = 0.234, chol=None) -> ChainResult:
+    """Random-walk Metropolis with proposal theta + step * chol xi (chol
+    defaults to the prior widths); the step is adapted toward the target
+    acceptance during the first `burn` steps."""
     th = np.array(theta0, dtype=np.float64)
+    Lc = _chol(post, chol)
     lp, _ = post.loglik(th, False)
     out = np.empty((steps,) + th.shape)
     acc = 0
     t0 = time.perf_counter()
     for k in range(steps):
-        prop = th + step * post.prior.width * rng.standard_normal(th.shape)
+        prop = th + step * rng.standard_normal(th.shape) @ Lc.T
         lq, _ = post.loglik(prop, False)
         a = np.log(rng.random(th.shape[0])) < lq - lp
         th[a], lp[a] = prop[a], lq[a]
@@ -132,29 +163,31 @@ def rwm(post: Posterior, theta0: np.ndarray, steps: int, step: float, rng, burn:
 
 
 def mala(post: Posterior, theta0: np.ndarray, steps: int, eps: float, rng, burn: int = 0,
-         target: float = 0.574) -> ChainResult:
-    """MALA in prior-width-scaled coordinates z = theta / width: proposal
-    z' = z + eps^2/2 grad_z log pi + eps xi, accepted with the Metropolis-
-    Hastings ratio of the two Langevin proposal densities."""
-    w = post.prior.width
+         target: float = 0.574, chol=None) -> ChainResult:
+    """Preconditioned MALA with metric M = chol chol^T (default: the prior
+    widths squared): theta' = theta + eps^2/2 M grad log pi + eps chol xi,
+    accepted with the Metropolis-Hastings ratio of the two Langevin proposal
+    densities (Gaussians of covariance eps^2 M)."""
     th = np.array(theta0, dtype=np.float64)
+    Lc = _chol(post, chol)
+    M = Lc @ Lc.T
+    Li = np.linalg.inv(Lc)
     lp, g = post.loglik(th, True)
-    gz = g * w
     out = np.empty((steps,) + th.shape)
     acc = 0
     t0 = time.perf_counter()
     for k in range(steps):
         xi = rng.standard_normal(th.shape)
-        zp = th / w + 0.5 * eps ** 2 * gz + eps * xi
-        prop = zp * w
+        mean_f = th + 0.5 * eps ** 2 * g @ M
+        prop = mean_f + eps * xi @ Lc.T
         lq, gq = post.loglik(prop, True)
-        gqz = gq * w
-        fwd = -np.sum((zp - th / w - 0.5 * eps ** 2 * gz) ** 2, axis=1) / (2 * eps ** 2)
-        bwd = -np.sum((th / w - zp - 0.5 * eps ** 2 * gqz) ** 2, axis=1) / (2 * eps ** 2)
+        mean_b = prop + 0.5 * eps ** 2 * gq @ M
+        fwd = -np.sum(((prop - mean_f) @ Li.T) ** 2, axis=1) / (2 * eps ** 2)
+        bwd = -np.sum(((th - mean_b) @ Li.T) ** 2, axis=1) / (2 * eps ** 2)
         with np.errstate(invalid="ignore"):
             logr = lq - lp + bwd - fwd
         a = np.isfinite(lq) & (np.log(rng.random(th.shape[0])) < logr)
-        th[a], lp[a], gz[a] = prop[a], lq[a], gqz[a]
+        th[a], lp[a], g[a] = prop[a], lq[a], gq[a]
         if k < burn:
             eps *= np.exp((a.mean() - target) / np.sqrt(k + 1.0))
         else:
@@ -164,6 +197,561 @@ def mala(post: Posterior, theta0: np.ndarray, steps: int, eps: float, rng, burn:
     return ChainResult(out, acc / n_acc, eps, time.perf_counter() - t0, post.solves)
 
 
+@dataclass
+class SurrogatePosterior:
+    """log pi*(theta) = the surrogate's predicted log L + log prior, in
+    batches of the surrogate's batch_max."""
+    surrogate: object
+    prior: Prior
+    calls: int = 0
+    evals: int = 0
+    seconds: float = 0.0
+
+    def logpost(self, theta: np.ndarray) -> np.ndarray:
+        th = np.atleast_2d(theta)
+        lp = self.prior.logp(th)
+        out = np.full(th.shape[0], -np.inf)
+        idx = np.nonzero(np.isfinite(lp))[0]
+        bm = self.surrogate.batch_max
+        t0 = time.perf_counter()
+        for s0 in range(0, idx.size, bm):
+            sl = idx[s0:s0 + bm]
+            r = self.surrogate.loglik([tuple(x) for x in th[sl]])["loglik"]
+            out[sl] = [d["total"] for d in r]
+            self.calls += 1
+        self.evals += idx.size
+        self.seconds += time.perf_counter() - t0
+        return out + lp
+
+
+def _chol_population(th: np.ndarray, w: np.ndarray) -> np.ndarray:
+    """Cholesky factor of the chains' covariance, in parameter units,
+    normalised so that its mean variance in prior-width-scaled coordinates is
+    one (its shape, not its size)."""
+    d = th.shape[1]
+    c = np.cov(th / w, rowvar=False) if th.shape[0] > d else np.eye(d)
+    c = c / max(np.trace(c) / d, 1e-300) + 1e-6 * np.eye(d)
+    return np.diag(w) @ np.linalg.cholesky(c)
+
+
+def _chol_cov(th: np.ndarray) -> np.ndarray:
+    """Cholesky factor of the chains' covariance in parameter units."""
+    c = np.cov(th, rowvar=False)
+    return np.linalg.cholesky(c + 1e-12 * np.diag(np.diag(c)) + 1e-300 * np.eye(c.shape[0]))
+
+
+def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: int, step: float,
+       rng, inner: int = 8, burn: int = 0, target: float = 0.3, chol=None, adapt: bool = False,
+       rebuild_every: int = 0, axis=None, axis_prob: float = 0.5) -> ChainResult:
+    """Delayed-acceptance MCMC, chains in lock-step: per generation `inner`
+    batched surrogate calls and one batched solver call for the chains whose
+    inner chain moved. The inner random-walk proposal is y + step * C xi:
+    C = chol if given, else the prior widths. During the first `burn`
+    generations the step is adapted toward the target inner acceptance and,
+    with adapt=True (or chol None), C follows the population covariance of
+    the chains; every `rebuild_every` burn-in generations a surrogate that
+    has rebuild(u_centre, steps) is re-linearised at the population mean
+    with half the population standard deviations as steps. With `axis` = a,
+    each inner step is, with probability axis_prob, instead a jump along
+    coordinate a alone of standard deviation 3x the population's spread in
+    a (at least 0.05): in the invariant coordinates a = 0 moves along the
+    scaling symmetry, the long direction of the posterior. Both moves are
+    symmetric random walks, so the inner chain stays reversible with respect
+    to the surrogate posterior. All of it is frozen after burn-in, so the
+    sampled chain is a fixed reversible kernel whose invariant law is the
+    exact posterior."""
+    w = post.prior.width
+    th = np.array(theta0, dtype=np.float64)
+    m, d = th.shape
+    lp, _ = post.loglik(th, False)
+    ls = spost.logpost(th)
+    Lc = _chol(post, chol)
+    out = np.empty((steps, m, d))
+    acc1 = acc2 = tried = 0
+    axis_sd = 0.05
+    t0 = time.perf_counter()
+    t_burn = 0.0
+    for k in range(steps):
+        if k == burn:
+            t_burn = time.perf_counter() - t0
+        if k < burn and m > 2 * d:
+            if chol is None:
+                Lc = _chol_population(th, w)
+            elif adapt and k >= max(1, burn // 4):
+                Lc = _chol_cov(th)
+            if axis is not None:
+                axis_sd = max(0.05, 3.0 * float(th[:, axis].std()))
+            if rebuild_every > 0 and k > 0 and k % rebuild_every == 0 and hasattr(spost, "rebuild"):
+                spost.rebuild(th.mean(axis=0), 0.5 * th.std(axis=0))
+                ls = spost.logpost(th)
+        y, ly = th.copy(), ls.copy()
+        a1 = 0.0
+        for _ in range(inner):
+            prop = y + step * rng.standard_normal((m, d)) @ Lc.T
+            if axis is not None:
+                jump = rng.random(m) < axis_prob
+                prop[jump] = y[jump]
+                prop[jump, axis] += axis_sd * rng.standard_normal(int(jump.sum()))
+            lq = spost.logpost(prop)
+            with np.errstate(invalid="ignore"):
+                a = np.isfinite(lq) & (np.log(rng.random(m)) < lq - ly)
+            y[a], ly[a] = prop[a], lq[a]
+            a1 += a.mean()
+        moved = np.any(y != th, axis=1)
+        if moved.any():
+            lpy = np.full(m, -np.inf)
+            lpy[moved], _ = post.loglik(y[moved], False)
+            with np.errstate(invalid="ignore"):
+                logr = (lpy - lp) - (ly - ls)
+            # a chain outside the support moves to any point inside it
+            logr = np.where(np.isneginf(lp) & np.isfinite(lpy), np.inf, logr)
+            a = moved & np.isfinite(lpy) & (np.log(rng.random(m)) < logr)
+            th[a], lp[a], ls[a] = y[a], lpy[a], ly[a]
+        else:
+            a = np.zeros(m, dtype=bool)
+        a1 /= inner
+        if k < burn:
+            step *= np.exp((a1 - target) / np.sqrt(k + 1.0))
+        else:
+            acc1 += a1 * m
+            acc2 += a.sum()
+            tried += moved.sum()
+        out[k] = th
+    n_gen = max(1, (steps - burn) * m)
+    return ChainResult(out, acc2 / n_gen, step, time.perf_counter() - t0, post.solves,
+                       history=dict(stage1_accept=acc1 / n_gen,
+                                    stage2_accept=acc2 / max(tried, 1),
+                                    surrogate_evals=spost.evals, inner=inner,
+                                    axis_sd=axis_sd if axis is not None else None,
+                                    burn_seconds=t_burn if burn < steps else time.perf_counter() - t0))
+
+
+def hessian(post: Posterior, theta: np.ndarray, steps: np.ndarray) -> np.ndarray:
+    """Hessian of log pi at each row of theta by central differences of
+    adjoint gradients, steps[j] along parameter j; all 12 gradients of every
+    row in one batched call. Symmetrised."""
+    th = np.atleast_2d(theta)
+    m, d = th.shape
+    pts = np.repeat(th, 2 * d, axis=0)
+    for j in range(d):
+        pts[2 * j::2 * d, j] += steps[j]
+        pts[2 * j + 1::2 * d, j] -= steps[j]
+    _, g = post.loglik(pts, True)
+    g = g.reshape(m, d, 2, d)
+    H = (g[:, :, 0, :] - g[:, :, 1, :]) / (2 * steps[None, :, None])  # H[r, j, i] = d g_i / d theta_j
+    return 0.5 * (H + H.transpose(0, 2, 1))
+
+
+def _posdef_cov(H: np.ndarray, w: np.ndarray) -> np.ndarray:
+    """Gaussian approximation of the posterior: covariance (|-H| + P)^{-1},
+    with |.| the absolute eigenvalues of -H in width-scaled coordinates (a
+    noisy or indefinite Hessian along a ridge stays positive) and P = 12 I
+    the precision of a uniform distribution on the prior box (it bounds the
+    variance along directions the likelihood does not constrain)."""
+    A = -H * np.outer(w, w)
+    ev, V = np.linalg.eigh(0.5 * (A + A.T))
+    ev = np.abs(ev) + 12.0
+    return (V / ev) @ V.T * np.outer(w, w)
+
+
+def find_mode(post: Posterior, starts: np.ndarray, iters: int = 10, hess_rel: float = 1e-5):
+    """Posterior mode from a few starting points by damped Newton steps:
+    per iteration one batched adjoint call for the gradients and Hessians
+    (central differences of gradients) of every start and one batched
+    forward call that tries every damping level; a start keeps its best
+    point. Returns (theta_map, log pi(theta_map), covariance (-H)^{-1} at the
+    mode, history of the best log pi)."""
+    w = post.prior.width
+    th = np.array(np.atleast_2d(starts), dtype=np.float64)
+    m, d = th.shape
+    lp, _ = post.loglik(th, False)
+    hist = [float(np.max(lp))]
+    lams = np.array([0.0, 1e-3, 1e-2, 1e-1, 1.0, 10.0, 100.0])
+    for _ in range(iters):
+        ok = np.isfinite(lp)
+        if not ok.any():
+            break
+        _, g = post.loglik(th, True)
+        H = hessian(post, th, hess_rel * w)
+        cands = []
+        for r in range(m):
+            A = -H[r] * np.outer(w, w)  # width-scaled coordinates
+            gz = g[r] * w
+            ev = np.abs(np.linalg.eigvalsh(0.5 * (A + A.T))).max() + 1e-300
+            for lam in lams:
+                try:
+                    dz = np.linalg.solve(A + lam * ev * np.eye(d), gz)
+                except np.linalg.LinAlgError:
+                    dz = gz / ev
+                cands.append(th[r] + dz * w)
+        cands = np.array(cands)
+        lc, _ = post.loglik(cands, False)
+        lc = lc.reshape(m, len(lams))
+        best = np.argmax(lc, axis=1)
+        for r in range(m):
+            if lc[r, best[r]] > lp[r]:
+                th[r] = cands[r * len(lams) + best[r]]
+                lp[r] = lc[r, best[r]]
+        hist.append(float(np.max(lp)))
+        if len(hist) > 2 and hist[-1] - hist[-2] < 1e-3:
+            break
+    r = int(np.argmax(lp))
+    H = hessian(post, th[r], hess_rel * w)[0]
+    cov = _posdef_cov(H, w)
+    # second pass with steps of half a posterior standard deviation (at most
+    # 1% of the prior width)
+    sd = np.minimum(np.sqrt(np.diag(cov)), 0.02 * w)
+    H = hessian(post, th[r], 0.5 * sd)[0]
+    cov = _posdef_cov(H, w)
+    return th[r].copy(), float(lp[r]), cov, hist
+
+
+# Coordinates in which the Fisher-KPP scaling symmetry is an axis: the
+# continuous model with this initial condition depends on (Dw / rho, rho T)
+# only, so (Dw, rho, T) -> (c Dw, c rho, T / c) leaves the density unchanged
+# and only the time discretisation and the prior box bound c. With
+# u = (log Dw, log rho, x0, y0, z0, log T), the invariant coordinates are
+# v = (log rho, log rho + log T, log Dw - log rho, x0, y0, z0): v_0 moves
+# along the symmetry, v_1 and v_2 are its invariants.
+INVARIANT_MAP = np.array([[0, 1, 0, 0, 0, 0],
+                          [0, 1, 0, 0, 0, 1],
+                          [1, -1, 0, 0, 0, 0],
+                          [0, 0, 1, 0, 0, 0],
+                          [0, 0, 0, 1, 0, 0],
+                          [0, 0, 0, 0, 1, 0]], dtype=np.float64)
+
+
+@dataclass
+class LogPrior:
+    """The prior of a LogCoords posterior, in its coordinates v = A u."""
+    base: Prior
+    log_idx: tuple
+    A: np.ndarray
+
+    def __post_init__(self):
+        self.Ai = np.linalg.inv(self.A)
+
+    def to_logu(self, v):
+        return np.asarray(v, dtype=np.float64) @ self.Ai.T
+
+    def to_theta(self, v):
+        th = self.to_logu(v)
+        th[..., list(self.log_idx)] = np.exp(th[..., list(self.log_idx)])
+        return th
+
+    def _ubox(self):
+        lo, hi = self.base.lo.copy(), self.base.hi.copy()
+        lo[list(self.log_idx)] = np.log(lo[list(self.log_idx)])
+        hi[list(self.log_idx)] = np.log(hi[list(self.log_idx)])
+        return lo, hi
+
+    @property
+    def width(self):
+        """Extent of the prior box's image along each v coordinate."""
+        lo, hi = self._ubox()
+        return np.abs(self.A) @ (hi - lo)
+
+    @property
+    def lo(self):
+        lo, hi = self._ubox()
+        return np.minimum(self.A, 0) @ (hi - lo) + self.A @ lo
+
+    @property
+    def hi(self):
+        return self.lo + self.width
+
+    def logp(self, v):
+        """Uniform prior on theta as a density in v: the log-Jacobian sum of
+        log theta_i over the log coordinates (the linear map's is a
+        constant), -inf outside the box."""
+        u = np.atleast_2d(self.to_logu(v))
+        th = u.copy()
+        th[:, list(self.log_idx)] = np.exp(th[:, list(self.log_idx)])
+        return self.base.logp(th) + u[:, list(self.log_idx)].sum(axis=1)
+
+
+@dataclass
+class LogCoords:
+    """A posterior in coordinates v = A u, u_i = log theta_i for i in
+    log_idx (Dw, rho and T by default) and u_i = theta_i otherwise; A = I
+    by default, INVARIANT_MAP for the scaling symmetry's coordinates. In u
+    the curved Dw-rho-T ridge of the posterior is straight, in the invariant
+    coordinates it is the v_0 axis. Densities include the Jacobian of the
+    map; gradients are transformed with it."""
+    post: object
+    log_idx: tuple = (0, 1, 5)
+    A: np.ndarray = None
+
+    def __post_init__(self):
+        if self.A is None:
+            self.A = np.eye(len(self.post.prior.lo))
+        self.A = np.asarray(self.A, dtype=np.float64)
+        self.prior = LogPrior(self.post.prior, self.log_idx, self.A)
+
+    def to_theta(self, v):
+        return self.prior.to_theta(v)
+
+    def to_u(self, th):
+        u = np.array(th, dtype=np.float64, copy=True)
+        u[..., list(self.log_idx)] = np.log(u[..., list(self.log_idx)])
+        return u @ self.A.T
+
+    @property
+    def solves(self):
+        return self.post.solves
+
+    @property
+    def seconds(self):
+        return self.post.seconds
+
+    def loglik(self, v, with_grad: bool):
+        v = np.atleast_2d(v)
+        u = self.prior.to_logu(v)
+        th = self.to_theta(v)
+        l, g = self.post.loglik(th, with_grad)
+        jac = u[:, list(self.log_idx)].sum(axis=1)
+        if with_grad:
+            g = np.array(g, dtype=np.float64, copy=True)
+            g[:, list(self.log_idx)] = g[:, list(self.log_idx)] * th[:, list(self.log_idx)] + 1.0
+            g = g @ self.prior.Ai  # d/dv = A^{-T} d/du, row-wise
+        return l + jac, g
+
+    def surrogate(self, spost: "SurrogatePosterior") -> "SurrogatePosterior":
+        """A theta-space surrogate posterior in the same coordinates."""
+        return _LogSurrogate(spost, self)
+
+
+class _LogSurrogate:
+    def __init__(self, spost, lc):
+        self.spost, self.lc = spost, lc
+
+    def __getattr__(self, k):
+        return getattr(self.spost, k)
+
+    def logpost(self, v):
+        v = np.atleast_2d(v)
+        u = self.lc.prior.to_logu(v)
+        return self.spost.logpost(self.lc.to_theta(v)) + u[:, list(self.lc.log_idx)].sum(axis=1)
+
+
+def refine_cov(post, u_map: np.ndarray, cov: np.ndarray, span: float = 8.0, npts: int = 33,
+               drop: float = 10.0):
+    """Gaussian approximation refined by profiles: log pi is evaluated along
+    each eigenvector of the Laplace precision (in prior-width-scaled
+    coordinates) at npts points out to +-span Laplace standard deviations,
+    all directions in one batched call, and a parabola fitted to the points
+    within `drop` of the centre gives that direction's standard deviation.
+    Directions whose profile stays within `drop` over the whole span are
+    rescanned 8x wider. A local Hessian misjudges directions along which log
+    pi is kinked or nearly flat (the Dw-rho-T ridge); the profile fit sees
+    the posterior's extent. Returns (covariance, per-direction sd ratio)."""
+    w = post.prior.width
+    d = u_map.size
+    A = np.linalg.inv(cov / np.outer(w, w))
+    ev, V = np.linalg.eigh(0.5 * (A + A.T))
+    sd = 1.0 / np.sqrt(ev)
+    ts = np.linspace(-1.0, 1.0, npts)
+    spans = np.full(d, span)
+    ratio = np.ones(d)
+    todo = list(range(d))
+    for _ in range(2):
+        if not todo:
+            break
+        pts = np.concatenate([u_map + np.outer(ts * spans[k] * sd[k], V[:, k] * w) for k in todo])
+        lp, _ = post.loglik(pts, False)
+        lp = lp.reshape(len(todo), npts)
+        again = []
+        for j, k in enumerate(todo):
+            x = ts * spans[k]
+            dl = lp[j] - lp[j, npts // 2]
+            sel = np.isfinite(dl) & (dl > -drop)
+            if sel.all() and spans[k] == span:
+                again.append(k)
+                spans[k] *= 8.0
+                continue
+            if sel.sum() >= 3:
+                c = np.polyfit(x[sel], dl[sel], 2)
+                ratio[k] = np.sqrt(-0.5 / c[0]) if c[0] < 0 else spans[k]
+            ratio[k] = min(max(ratio[k], 0.1), spans[k])
+        todo = again
+    sig = sd * ratio
+    return (V * sig ** 2) @ V.T * np.outer(w, w), ratio
+
+
+def stable_dt0(n: int, L: float, dw_max: float) -> float:
+    """Largest explicit step of the smooth time grid for diffusivities up to
+    dw_max [cm^2/day]: the reference's CFL rule dt = 0.99 h^2 / (6 Dw / L^2)."""
+    h = 1.0 / n
+    return 0.99 * h * h / (6.0 * dw_max / (L * L))
+
+
+def _base(post):
+    return post.post if isinstance(post, LogCoords) else post
+
+
+def _theta(post, u):
+    return post.to_theta(u) if isinstance(post, LogCoords) else np.array(u, dtype=np.float64)
+
+
+class AffineSurrogate:
+    """Screening density for delayed acceptance around a reference point
+    u_ref (normally the posterior mode): the final density is modelled as
+      phi(u) = phi(u_ref) + J delta  [+ K_aa delta_a^2 / 2 + sum_i K_ai delta_a delta_i]
+    with delta = u - u_ref, J from central differences of the batched
+    solver's densities (steps[p] along coordinate p) and, with quad_axis = a,
+    the second-order terms along coordinate a (the scaling symmetry's axis in
+    the invariant coordinates, along which the posterior ridge curves) from
+    the same central differences and 4 mixed-difference solves per other
+    coordinate; all solves of a build go through one batched call. log L of
+    the field comes from the library's affine model and likelihood kernel
+    (gbg_affine_loglik), whose basis fields are J and the K columns. A
+    handle holds one affine model: the latest build on it is the active one."""
+
+    def __init__(self, post, u_ref: np.ndarray, steps: np.ndarray, quad_axis=None):
+        self.post, self.base = post, _base(post)
+        self.prior = post.prior
+        self.quad_axis = quad_axis
+        self.evals = 0
+        self.calls = 0
+        self.seconds = 0.0
+        self.rebuild(u_ref, steps)
+
+    def _coeffs(self, delta: np.ndarray) -> np.ndarray:
+        if self.quad_axis is None:
+            return delta
+        a = self.quad_axis
+        others = [i for i in range(delta.shape[1]) if i != a]
+        return np.concatenate([delta, 0.5 * delta[:, a:a + 1] ** 2,
+                               delta[:, a:a + 1] * delta[:, others]], axis=1)
+
+    def rebuild(self, u_ref: np.ndarray, steps: np.ndarray):
+        """Re-build at u_ref with finite-difference steps `steps`."""
+        post, base = self.post, self.base
+        self.u_ref = np.array(u_ref, dtype=np.float64)
+        d = self.u_ref.size
+        steps = np.asarray(steps, dtype=np.float64)
+        pts = np.repeat(self.u_ref[None], 2 * d + 1, axis=0)
+        for p in range(d):
+            pts[1 + 2 * p, p] += steps[p]
+            pts[2 + 2 * p, p] -= steps[p]
+        a = self.quad_axis
+        others = [] if a is None else [i for i in range(d) if i != a]
+        mixed = []
+        for i in others:
+            for sa, si in ((1, 1), (1, -1), (-1, 1), (-1, -1)):
+                q = self.u_ref.copy()
+                q[a] += sa * steps[a]
+                q[i] += si * steps[i]
+                mixed.append(q)
+        if mixed:
+            pts = np.concatenate([pts, np.array(mixed)])
+        th = _theta(post, pts)
+        h = base.handle
+        cap = max(1, h.max_samples)
+        phis = []
+        for s0 in range(0, len(th), cap):
+            r = h.batch_solve([tuple(x) for x in th[s0:s0 + cap]], base.L, ic_peak=base.ic_peak,
+                              ic_sigma=base.ic_sigma, with_loglik=False, want_phi=True, dt0=base.dt0)
+            phis.append(r["phi"].reshape(r["phi"].shape[0], -1))
+        phis = np.concatenate(phis).astype(np.float64)
+        self.phi0 = phis[0].astype(np.float32)
+        basis = [(phis[1 + 2 * p] - phis[2 + 2 * p]) / (2 * steps[p]) for p in range(d)]
+        if a is not None:
+            basis.append((phis[1 + 2 * a] + phis[2 + 2 * a] - 2 * phis[0]) / steps[a] ** 2)
+            for j, i in enumerate(others):
+                f = phis[2 * d + 1 + 4 * j: 2 * d + 5 + 4 * j]
+                basis.append((f[0] - f[1] - f[2] + f[3]) / (4 * steps[a] * steps[i]))
+        self.J = np.stack(basis)
+        h.affine_set(self.phi0, self.J.astype(np.float32))
+
+    def logpost(self, u: np.ndarray) -> np.ndarray:
+        u = np.atleast_2d(u)
+        lp = self.prior.logp(u)
+        out = np.full(u.shape[0], -np.inf)
+        ok = np.isfinite(lp)
+        if ok.any():
+            t0 = time.perf_counter()
+            out[ok] = self.base.handle.affine_loglik(self._coeffs(u[ok] - self.u_ref))
+            self.seconds += time.perf_counter() - t0
+            self.calls += 1
+            self.evals += int(ok.sum())
+        return out + lp
+
+
+@dataclass
+class PipelineResult:
+    result: ChainResult      # the DA chains (sampler coordinates)
+    theta: np.ndarray        # post-burn-in draws in theta, (steps, chains, 6)
+    v_map: np.ndarray
+    cov: np.ndarray
+    setup_seconds: float     # prior screen + mode + profiles + surrogate
+    sample_seconds: float    # the post-burn-in generations
+    burn_seconds: float
+
+
+def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: int = 64,
+                     generations: int = 300, burn: int = 100, inner: int = 16,
+                     screen: int = 512, screen_draws=None, ic_peak: float = 0.1,
+                     ic_sigma: float = 1.0) -> PipelineResult:
+    """The batched + adjoint + surrogate posterior sampler:
+      1. log pi of `screen` prior draws in batched solves; the best four start
+      2. damped Newton with batched adjoint gradients and Hessians (find_mode)
+         in the scaling symmetry's coordinates (INVARIANT_MAP)
+      3. the Laplace covariance refined by batched profiles (refine_cov)
+      4. delayed acceptance with the affine (tangent) surrogate around the
+         mode, `chains` chains started from the refined Gaussian, proposal
+         covariance and surrogate adapted to the population during burn-in
+         and frozen after it.
+    screen_draws: theta rows to screen instead of drawing from the prior
+    (the caller's prior sampler)."""
+    post = LogCoords(Posterior(handle, L, dt0, prior, ic_peak=ic_peak, ic_sigma=ic_sigma),
+                     A=INVARIANT_MAP)
+    t0 = time.perf_counter()
+    if screen_draws is None:
+        raise ValueError("screen_draws: theta rows drawn from the prior")
+    dv = post.to_u(np.asarray(screen_draws, dtype=np.float64))
+    ld, _ = post.loglik(dv, False)
+    starts = dv[np.argsort(ld)[::-1][:4]]
+    v_map, _, cov0, _ = find_mode(post, starts, iters=10)
+    cov, _ = refine_cov(post, v_map, cov0)
+    sd = np.sqrt(np.diag(cov))
+    Lc = np.linalg.cholesky(cov)
+    sur = AffineSurrogate(post, v_map, 0.5 * sd, quad_axis=0)
+    setup = time.perf_counter() - t0
+    # starting points from the refined Gaussian, spread along the symmetry
+    # axis over +-0.3 (the posterior's long direction), redrawn until inside
+    # the prior
+    def draw(k):
+        v = v_map + rng.standard_normal((k, v_map.size)) @ Lc.T
+        v[:, 0] += rng.uniform(-0.3, 0.3, k)
+        return v
+    v0 = draw(chains)
+    for _ in range(100):
+        bad = ~np.isfinite(post.prior.logp(v0))
+        if not bad.any():
+            break
+        v0[bad] = draw(int(bad.sum()))
+    v0[~np.isfinite(post.prior.logp(v0))] = v_map
+    run = Posterior(handle, L, dt0, prior, ic_peak=ic_peak, ic_sigma=ic_sigma)
+    r = da(LogCoords(run, A=INVARIANT_MAP), sur, v0, generations, 2.38 / np.sqrt(v_map.size), rng,
+           inner=inner, burn=burn, chol=Lc, adapt=True, rebuild_every=25, axis=0)
+    burn_s = r.history["burn_seconds"]
+    return PipelineResult(r, post.to_theta(r.samples[burn:]), v_map, cov, setup, r.seconds - burn_s,
+                          burn_s)
+
+
+def rhat(samples: np.ndarray) -> np.ndarray:
+    """Split-R-hat per parameter of (steps, chains, d) draws (Gelman-Rubin
+    on the chains cut in halves): near 1 when the chains agree, well above
+    1 while they still sample different regions."""
+    n = samples.shape[0] // 2
+    x = np.concatenate([samples[:n], samples[n:2 * n]], axis=1)
+    w = x.var(axis=0, ddof=1).mean(axis=0)
+    b = n * x.mean(axis=0).var(axis=0, ddof=1)
+    var_plus = (n - 1) / n * w + b / n
+    return np.sqrt(var_plus / np.maximum(w, 1e-300))
+
+
 def _autocov(x: np.ndarray) -> np.ndarray:
     n = x.size
     f = np.fft.rfft(x - x.mean(), n=2 * n)
@@ -171,10 +759,14 @@ def _autocov(x: np.ndarray) -> np.ndarray:
     return ac / n
 
 
-def ess(samples: np.ndarray) -> np.ndarray:
+def ess(samples: np.ndarray, within: bool = False) -> np.ndarray:
     """Effective sample size per parameter of (steps, chains, d) draws:
     chain-averaged autocorrelation (split-free version of the multi-chain
-    estimator) with Geyer's initial monotone sequence truncation."""
+    estimator) with Geyer's initial monotone sequence truncation. With
+    within=True only the chains' own autocorrelation counts (the pooled
+    within-chain autocorrelation, rho_t = mean acov_t / mean acov_0): a
+    conservative figure that gives no credit for the spread of the chains'
+    starting points."""
     n, m, d = samples.shape
     out = np.zeros(d)
     for j in range(d):
@@ -183,10 +775,14 @@ def ess(samples: np.ndarray) -> np.ndarray:
         w = acov[:, 0].mean() * n / max(n - 1, 1)
         b = n * x.mean(axis=0).var(ddof=1) if m > 1 else 0.0
         var_plus = (n - 1) / n * w + b / n
+        if within:
+            var_plus = acov[:, 0].mean()
         if var_plus <= 0:
             out[j] = float(n * m)
             continue
         rho = 1.0 - (w - acov.mean(axis=0)) / var_plus
+        if within:
+            rho = acov.mean(axis=0) / var_plus
         rho[0] = 1.0
         s, prev = 0.0, np.inf
         for t in range(0, n - 1, 2):

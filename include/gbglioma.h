@@ -138,6 +138,13 @@ typedef struct {
     double ic_peak;    /* initial peak density */
     double ic_sigma;   /* initial width in voxels */
     int with_loglik;   /* evaluate the likelihood per sample */
+    double dt0;        /* 0: the reference's time loop per sample (dt from Dw,
+                          steps while t <= tend). > 0: the smooth time grid of
+                          gbg_adjoint_grad -- fixed step dt0, ceil(tend/dt0)
+                          steps, the last one shortened to end at tend; the
+                          densities and log L equal gbg_adjoint_grad's forward
+                          model bit for bit (GBG_PREC_F32 state). dt0 must
+                          satisfy the CFL limit of the largest Dw. */
 } gbg_batch_opts;
 
 /* Host entry: copies the S samples in, solves, copies loglik (S results, may
@@ -162,10 +169,13 @@ int gbg_batch_solve_device(gbg_handle *h, const gbg_sample *samples_device, int 
  * (Dw, rho, x0, y0, z0, tend), in the units of gbg_sample, written as
  * grad[6*s + 0..5]; loglik[s] receives log L of the same forward model
  * (either pointer may be null; with grad null no adjoint sweep runs).
- * States are checkpointed every checkpoint_every steps (0: 50) and each
- * segment is recomputed for its backward sweep; state_precision is
- * GBG_PREC_F32 (float states) or GBG_PREC_F64 (double states). Works on
- * any handle made by gbg_create; allocates its working set per call. */
+ * States are checkpointed every checkpoint_every steps (<= 0: about
+ * sqrt(steps), which minimises the stored states) and each segment is
+ * recomputed for its backward sweep; state_precision is GBG_PREC_F32 (float
+ * states) or GBG_PREC_F64 (double states). Works on any handle made by
+ * gbg_create; the working set (checkpoints, one segment of states, adjoint
+ * fields) is kept by the handle between calls and grows when a call needs
+ * more, until gbg_destroy. */
 typedef struct {
     double dt0;            /* step in days; e.g. 0.99 h^2 / (6 Dw_max / L^2) */
     int checkpoint_every;
@@ -176,6 +186,19 @@ typedef struct {
 
 int gbg_adjoint_grad(gbg_handle *h, const gbg_sample *samples, int S, const gbg_adjoint_opts *o,
                      double *loglik, double *grad);
+
+/* ---- affine density model (tangent screening) ------------------------------------
+ * No reference counterpart. phi(delta) = m * clamp(phi0 + sum_p delta_p J_p, 0, 1)
+ * with m the fast path's tissue mask and 1 <= P <= 16 basis fields:
+ * gbg_affine_set copies phi0 (n^3 floats) and J (P x n^3 floats, field-
+ * major; e.g. J_p = d phi / d u_p at the reference sample in the sampler's
+ * coordinates u, plus second-order fields); gbg_affine_loglik writes log L
+ * (the handle's observations) of B models given by their coefficients delta
+ * (B x P doubles; e.g. u - u_ref and products of its components). The cheap first stage
+ * of delayed-acceptance MCMC around a posterior mode. GBG_PREC_F32 handles;
+ * the handle keeps the fields until gbg_destroy. */
+int gbg_affine_set(gbg_handle *h, int P, const float *phi0, const float *J);
+int gbg_affine_loglik(gbg_handle *h, int B, const double *delta, gbg_lik_result *out);
 
 /* ---- learned surrogate (delayed-acceptance screening) ----------------------------
  * No reference counterpart. A small 3D convolutional U-Net maps a sample's

@@ -83,3 +83,28 @@ def test_adjoint_argument_errors(gbg):
         bad = [(np.nan,) + samples[0][1:]]
         with pytest.raises(_lib.GbgError):
             h.adjoint_grad(bad, dt0, an.L)
+
+
+def test_batched_smooth_grid_equals_adjoint_forward(gbg):
+    """The batched population solver on the smooth time grid (dt0 > 0) and
+    the adjoint's float forward pass are the same model: log L bit for bit;
+    the last, shortened step is taken (log L differs between tend and a tend
+    a fraction of a step later)."""
+    an, obs, samples, dt0 = _problem()
+    extra = [(0.0009, 0.03, 16.1, 15.2, 15.8, 3.0 * dt0), (0.0017, 0.09, 15.0, 16.0, 15.0, 0.4 * dt0)]
+    smp = samples + extra
+    with _lib.Handle(an.n, "f32", max_samples=8) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=1, step_ti=1)
+        ll_adj, _ = h.adjoint_grad(smp, dt0, an.L, state="f32", want_grad=False)
+        r = h.batch_solve(smp, an.L, dt0=dt0)
+        ll_pop = np.array([d["total"] for d in r["loglik"]])
+        assert np.array_equal(ll_adj, ll_pop), (ll_adj, ll_pop)
+        assert list(r["nsteps"]) == [int(np.ceil(s[5] / dt0)) for s in smp]
+        later = [s[:5] + (s[5] + 0.3 * dt0,) for s in smp]
+        ll_later = np.array([d["total"] for d in h.batch_solve(later, an.L, dt0=dt0)["loglik"]])
+        assert np.all(ll_later != ll_pop)
+        # the reference schedule is still the default
+        r0 = h.batch_solve(smp, an.L)
+        k_ref = [S.num_steps(S.reference_dt(an.n, s[0], an.L)[0], s[5]) for s in smp]
+        assert list(r0["nsteps"]) == k_ref

@@ -51,3 +51,229 @@ def test_mala_and_rwm_recover_a_gaussian():
     s2 = r2.samples[500:].reshape(-1, 6)
     assert 0.1 < r2.accept < 0.4
     assert np.all(np.abs(s2.mean(axis=0) - post.mu) < 0.3 * post.sd)
+
+
+class BiasedSurrogateStub:
+    """Surrogate with the library binding's interface whose log L is the
+    Gaussian stub's with a shifted mean, a 30% wider spread and a constant
+    offset: delayed acceptance must still sample the stub exactly."""
+
+    def __init__(self, post):
+        self.post = post
+        self.batch_max = 8
+        self.calls = 0
+
+    def loglik(self, samples):
+        th = np.asarray(samples, dtype=np.float64)
+        self.calls += 1
+        assert th.shape[0] <= self.batch_max
+        z = (th - self.post.mu - 0.5 * self.post.sd) / (1.3 * self.post.sd)
+        ll = -0.5 * np.sum(z * z, axis=1) - 1234.5
+        return dict(loglik=[dict(total=v) for v in ll])
+
+
+def test_delayed_acceptance_targets_the_exact_posterior():
+    rng = np.random.default_rng(3)
+    post = GaussianStub()
+    sur = BiasedSurrogateStub(post)
+    spost = mcmc.SurrogatePosterior(sur, post.prior)
+    th0 = post.mu + post.sd * rng.standard_normal((32, 6))
+    r = mcmc.da(post, spost, th0, 1200, 0.02, rng, inner=6, burn=200)
+    s = r.samples[200:].reshape(-1, 6)
+    assert np.all(np.abs(s.mean(axis=0) - post.mu) < 0.15 * post.sd)
+    assert np.all(np.abs(s.std(axis=0) / post.sd - 1) < 0.15)
+    h = r.history
+    assert 0.15 < h["stage1_accept"] < 0.5
+    assert 0.2 < h["stage2_accept"] <= 1.0
+    # one solver call per generation for the moved chains, `inner` surrogate
+    # passes in batches of batch_max
+    assert sur.calls >= 6 * 1200 * 32 // 8
+    assert post.solves <= 32 * 1201
+    # with adaptation and jumps along one axis the target is still exact
+    r = mcmc.da(post, spost, th0, 1200, 0.02, rng, inner=6, burn=200, chol=np.diag(post.sd),
+                adapt=True, axis=0)
+    s = r.samples[200:].reshape(-1, 6)
+    assert np.all(np.abs(s.mean(axis=0) - post.mu) < 0.15 * post.sd)
+    assert np.all(np.abs(s.std(axis=0) / post.sd - 1) < 0.15)
+    assert np.all(mcmc.rhat(r.samples[200:]) < 1.05)
+
+
+class CorrelatedStub(GaussianStub):
+    """Gaussian posterior with strong correlations (Dw-rho-T), as the front
+    position 2 sqrt(Dw rho) T makes them in the tumour model."""
+
+    def __init__(self):
+        super().__init__()
+        rng = np.random.default_rng(7)
+        Q, _ = np.linalg.qr(rng.standard_normal((6, 6)))
+        ev = np.array([1.0, 0.5, 0.2, 0.05, 0.01, 0.002])
+        C = Q @ np.diag(ev) @ Q.T
+        self.cov = C * np.outer(self.sd, self.sd)
+        self.prec = np.linalg.inv(self.cov)
+
+    def loglik(self, th, with_grad):
+        th = np.atleast_2d(th)
+        self.solves += th.shape[0]
+        r = th - self.mu
+        lp = self.prior.logp(th)
+        return -0.5 * np.einsum("ij,jk,ik->i", r, self.prec, r) + lp, -r @ self.prec
+
+
+def test_find_mode_hessian_and_preconditioned_samplers():
+    rng = np.random.default_rng(5)
+    post = CorrelatedStub()
+    starts = post.mu + 3 * post.sd * rng.standard_normal((3, 6))
+    th, lp, cov, hist = mcmc.find_mode(post, starts, iters=6)
+    assert np.all(np.abs(th - post.mu) < 1e-6 * post.sd)
+    # the Gaussian approximation adds the prior box's precision 12 / width^2
+    w = post.prior.width
+    expect = np.linalg.inv(post.prec + np.diag(12.0 / w ** 2))
+    assert np.allclose(cov, expect, rtol=1e-5, atol=1e-8 * np.abs(expect).max())
+    assert hist[-1] >= hist[0]
+    L = np.linalg.cholesky(cov)
+    th0 = th + rng.standard_normal((16, 6)) @ L.T
+    r = mcmc.mala(post, th0, 800, 1.0, rng, burn=200, chol=L)
+    s = r.samples[200:].reshape(-1, 6)
+    assert 0.4 < r.accept < 0.75
+    assert np.all(np.abs(s.mean(axis=0) - post.mu) < 0.15 * post.sd)
+    assert np.all(np.abs(np.sqrt(np.diag(np.cov(s, rowvar=False))) / np.sqrt(np.diag(post.cov)) - 1) < 0.15)
+    r2 = mcmc.rwm(post, th0, 2000, 1.0, rng, burn=400, chol=L)
+    assert 0.15 < r2.accept < 0.35
+    # preconditioning makes the ill-conditioned target easy: ESS per step
+    # is far above that of the width-scaled random walk
+    r3 = mcmc.rwm(post, th0, 2000, 1e-3, rng, burn=400)
+    assert mcmc.ess(r2.samples[400:]).min() > 5 * mcmc.ess(r3.samples[400:]).min()
+
+
+def test_log_coordinates_density_gradient_and_prior():
+    post = GaussianStub()
+    post.prior = mcmc.Prior(lo=0.5 * post.mu, hi=1.5 * post.mu, seed_mask=post.prior.seed_mask)
+    lc = mcmc.LogCoords(post)
+    th = post.mu + 0.3 * post.sd
+    u = lc.to_u(th)
+    assert np.allclose(lc.to_theta(u), th)
+    l, g = lc.loglik(u[None], True)
+    l0, g0 = post.loglik(th[None], True)
+    assert np.isclose(l[0], l0[0] + np.log(th[[0, 1, 5]]).sum())
+    # gradient in u against central differences of the u-density
+    for i in range(6):
+        e = np.zeros(6)
+        e[i] = 1e-6 * max(1.0, abs(u[i]))
+        fd = (lc.loglik((u + e)[None], False)[0][0] - lc.loglik((u - e)[None], False)[0][0]) / (2 * e[i])
+        assert abs(fd - g[0, i]) <= 1e-5 * max(1.0, abs(fd))
+    # the prior box maps to a box in u; outside it the density is -inf
+    assert np.allclose(lc.prior.lo[[0, 1, 5]], np.log(post.prior.lo[[0, 1, 5]]))
+    out = u.copy()
+    out[0] = lc.prior.hi[0] + 0.1
+    assert lc.prior.logp(out[None])[0] == -np.inf and np.isfinite(lc.prior.logp(u[None])[0])
+
+
+def test_within_chain_ess_gives_no_credit_for_spread_starts():
+    # stuck chains started at independent points: the multi-chain ESS counts
+    # the starting spread (about m/2), the within-chain ESS does not
+    rng = np.random.default_rng(2)
+    x = np.repeat(rng.standard_normal((1, 64, 1)), 500, axis=0) + 1e-3 * rng.standard_normal((500, 64, 1))
+    assert mcmc.ess(x)[0] > 20
+    assert mcmc.ess(x, within=True)[0] > 1e4  # white noise within each chain
+    # AR(1) chains started in stationarity: both agree
+    phi = 0.8
+    y = np.zeros((4000, 8, 1))
+    y[0] = rng.standard_normal((8, 1)) / np.sqrt(1 - phi ** 2)
+    for t in range(1, y.shape[0]):
+        y[t] = phi * y[t - 1] + rng.standard_normal((8, 1))
+    a, b = mcmc.ess(y)[0], mcmc.ess(y, within=True)[0]
+    assert abs(a - b) < 0.15 * a
+
+
+def test_refine_cov_recovers_a_wider_direction():
+    """Laplace covariance too narrow along one direction: the profile fit
+    restores the true standard deviation."""
+    post = CorrelatedStub()
+    wrong = post.cov.copy()
+    ev, V = np.linalg.eigh(np.linalg.inv(post.cov / np.outer(post.prior.width, post.prior.width)))
+    # shrink the softest direction's variance 4x
+    ev2 = ev.copy()
+    ev2[0] *= 16.0
+    w = post.prior.width
+    wrong = np.linalg.inv((V * ev2) @ V.T) * np.outer(w, w)
+    cov, ratio = mcmc.refine_cov(post, post.mu, wrong)
+    r = np.sort(ratio)
+    assert abs(r[-1] - 4.0) < 0.05 and np.all(np.abs(r[:-1] - 1.0) < 0.05)
+    assert np.allclose(cov, post.cov, rtol=1e-2, atol=1e-3 * np.abs(post.cov).max())
+
+
+def test_invariant_coordinates_map_gradient_and_symmetry():
+    post = GaussianStub()
+    post.prior = mcmc.Prior(lo=0.5 * post.mu, hi=1.5 * post.mu, seed_mask=post.prior.seed_mask)
+    lc = mcmc.LogCoords(post, A=mcmc.INVARIANT_MAP)
+    th = post.mu * (1 + 0.05 * np.arange(6) / 6)
+    v = lc.to_u(th)
+    assert np.allclose(lc.to_theta(v), th)
+    # the scaling (c Dw, c rho, T / c) moves v_0 only
+    c = 1.07
+    th2 = th.copy()
+    th2[0] *= c
+    th2[1] *= c
+    th2[5] /= c
+    dv = lc.to_u(th2) - v
+    assert abs(dv[0] - np.log(c)) < 1e-12 and np.all(np.abs(dv[1:]) < 1e-12)
+    l, g = lc.loglik(v[None], True)
+    for i in range(6):
+        e = np.zeros(6)
+        e[i] = 1e-6
+        fd = (lc.loglik((v + e)[None], False)[0][0] - lc.loglik((v - e)[None], False)[0][0]) / 2e-6
+        assert abs(fd - g[0, i]) <= 1e-4 * max(1.0, abs(fd)), (i, fd, g[0, i])
+    # prior: inside the box finite, the image box bounds contain the point
+    assert np.isfinite(lc.prior.logp(v[None])[0])
+    assert np.all(lc.prior.lo <= v) and np.all(v <= lc.prior.hi)
+
+
+class FieldModelStub:
+    """Posterior-like object whose 'solver' returns fields of a known
+    second-order model phi(u) = f0 + sum_i a_i u_i + b u_0^2 / 2 + sum_i c_i u_0 u_i
+    (no clamping), and a handle whose affine model is evaluated in NumPy."""
+
+    def __init__(self, n_cells=50, seed=0):
+        rng = np.random.default_rng(seed)
+        self.f0 = rng.uniform(0.3, 0.6, n_cells)
+        self.a = rng.normal(0, 0.1, (6, n_cells))
+        self.b = rng.normal(0, 0.2, n_cells)
+        self.c = rng.normal(0, 0.1, (6, n_cells))
+        self.c[0] = 0.0
+        self.target = self.field(np.full(6, 0.01)) + 0.001 * rng.standard_normal(n_cells)
+        self.prior = mcmc.Prior(lo=np.full(6, -1.0), hi=np.full(6, 1.0),
+                                seed_mask=np.ones((4, 4, 4), dtype=bool))
+        self.prior.logp = lambda th: np.zeros(np.atleast_2d(th).shape[0])
+        self.handle, self.L, self.dt0, self.ic_peak, self.ic_sigma = self, 1.0, 1.0, 0.1, 1.0
+        self.max_samples = 7
+
+    def field(self, u):
+        return (self.f0 + u @ self.a + 0.5 * self.b * u[0] ** 2 + u[0] * (u @ self.c))
+
+    def loglik_exact(self, u):
+        return -0.5 * np.sum((self.field(u) - self.target) ** 2) / 1e-4
+
+    def batch_solve(self, rows, L, ic_peak, ic_sigma, with_loglik, want_phi, dt0):
+        return {"phi": np.array([self.field(np.array(r)) for r in rows])}
+
+    def affine_set(self, phi0, J):
+        self._phi0, self._J = phi0.astype(np.float64), J.astype(np.float64)
+
+    def affine_loglik(self, coeffs):
+        f = self._phi0[None] + coeffs @ self._J
+        return -0.5 * np.sum((f - self.target) ** 2, axis=1) / 1e-4
+
+
+def test_tangent_surrogate_second_order_terms_along_the_axis():
+    m = FieldModelStub()
+    ref = np.zeros(6)
+    rng = np.random.default_rng(4)
+    us = 0.2 * rng.standard_normal((20, 6))
+    exact = np.array([m.loglik_exact(u) for u in us])
+    # a handle holds one affine model: the latest build is the active one
+    lin = mcmc.AffineSurrogate(m, ref, np.full(6, 0.05))
+    err_lin = np.abs(lin.logpost(us) - exact).max()
+    quad = mcmc.AffineSurrogate(m, ref, np.full(6, 0.05), quad_axis=0)
+    assert np.allclose(quad.logpost(us), exact, rtol=1e-6, atol=1e-6 * np.abs(exact).max())
+    assert err_lin > 100 * np.abs(quad.logpost(us) - exact).max()
+    assert quad.J.shape == (12, m.f0.size)
