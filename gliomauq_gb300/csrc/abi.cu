@@ -347,7 +347,7 @@ int gbg_loglik(gbg_handle *hh, gbg_lik_result *out) {
 
 static int validate_batch(Handle &h, int S, const gbg_batch_opts *o) {
     if (!o || S <= 0 || S > h.max_samples || !(o->L > 0) || !(o->ic_sigma > 0) ||
-        !std::isfinite(o->ic_peak) || !(o->dt0 >= 0) || !std::isfinite(o->dt0)) {
+        !std::isfinite(o->ic_peak) || !std::isfinite(o->dt0) || o->dt0 < -1.0) {
         set_error("bad batch arguments");
         return GBG_ERR_ARG;
     }
@@ -428,14 +428,18 @@ int gbg_adjoint_grad(gbg_handle *hh, const gbg_sample *samples, int S, const gbg
         set_error("the adjoint runs on uniform-grid handles");
         return GBG_ERR_STATE;
     }
-    if (!samples || S < 1 || !o || !(o->dt0 > 0) || !(o->L > 0) || !(o->ic_sigma > 0) ||
+    if (!samples || S < 1 || !o || !(o->dt0 != 0) || !std::isfinite(o->dt0) || o->dt0 < -1.0 || !(o->L > 0) ||
+        !(o->ic_sigma > 0) ||
         o->checkpoint_every < 0 || (o->state_precision != GBG_PREC_F32 && o->state_precision != GBG_PREC_F64)) {
         set_error("bad adjoint arguments");
         return GBG_ERR_ARG;
     }
     for (int s = 0; s < S; ++s)
         if (!std::isfinite(samples[s].Dw) || !std::isfinite(samples[s].rho) || !std::isfinite(samples[s].tend) ||
-            !(samples[s].tend > 0) || samples[s].tend / o->dt0 > 1e6) {
+            !(samples[s].Dw > 0) || !(samples[s].tend > 0) ||
+            samples[s].tend / (o->dt0 > 0 ? o->dt0
+                                          : -o->dt0 * 0.99 / (6.0 * h.n * h.n * samples[s].Dw / (o->L * o->L))) >
+                1e6) {
             set_error("non-finite or out-of-range sample parameter");
             return GBG_ERR_NONFINITE;
         }

@@ -311,10 +311,12 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     std::vector<int> ns(S);
     std::vector<double> dtl(S);
     int nmax = 0;
+    std::vector<double> dts(S);
     for (int s = 0; s < S; ++s) {
         const int k = recs[s].nsteps;
         ns[s] = k;
-        dtl[s] = samples[s].tend - (k - 1) * o.dt0;
+        dts[s] = recs[s].dt;
+        dtl[s] = samples[s].tend - (k - 1) * dts[s];
         nmax = std::max(nmax, k);
     }
     if (f32) {
@@ -380,7 +382,7 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
                 ha[(size_t)k * S + s] = last ? recs[s].a2 : recs[s].a;
                 hb[(size_t)k * S + s] = last ? recs[s].b2 : recs[s].b;
             } else {
-                const double dtk = last ? dtl[s] : o.dt0;
+                const double dtk = last ? dtl[s] : dts[s];
                 ha[(size_t)k * S + s] = dtk * (samples[s].Dw / L2) * ih2;
                 hb[(size_t)k * S + s] = dtk * samples[s].rho;
             }
@@ -498,12 +500,28 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     ADJ_TRY(cudaStreamSynchronize(st));
     release();
 #undef ADJ_TRY
+    // chain rule from the per-step sensitivities dlogL/da_k, dlogL/db_k,
+    // a_k = dt_k Dw / (L^2 h^2), b_k = dt_k rho. Fixed grid: only the last
+    // step's length depends on the parameters (through tend). Scaled grid:
+    // dt = C / Dw, so full steps have da/dDw = 0 and db/dDw = -dt rho / Dw,
+    // and the last step (length tend - (k-1) dt) has da/dDw = tend / (L^2 h^2)
+    // and db/dDw = rho (k-1) dt / Dw.
+    const bool scaled = o.dt0 < 0;
     for (int s = 0; s < S; ++s) {
         double gDw = 0.0, gRho = 0.0;
+        const double Dw = samples[s].Dw, rho = samples[s].rho, dt = dts[s];
         for (int k = 0; k < ns[s]; ++k) {
-            const double dtk = k < ns[s] - 1 ? o.dt0 : dtl[s];
-            gDw += hA[(size_t)k * S + s] * dtk / L2 * ih2;
-            gRho += hB[(size_t)k * S + s] * dtk;
+            const bool last = k == ns[s] - 1;
+            const double dtk = last ? dtl[s] : dt;
+            const double gA = hA[(size_t)k * S + s], gB = hB[(size_t)k * S + s];
+            if (!scaled) {
+                gDw += gA * dtk / L2 * ih2;
+            } else if (!last) {
+                gDw += gB * (-dt * rho / Dw);
+            } else {
+                gDw += gA * samples[s].tend / L2 * ih2 + gB * rho * (ns[s] - 1) * dt / Dw;
+            }
+            gRho += gB * dtk;
         }
         const int kl = ns[s] - 1;
         const double gT = hA[(size_t)kl * S + s] * samples[s].Dw / L2 * ih2 + hB[(size_t)kl * S + s] * samples[s].rho;

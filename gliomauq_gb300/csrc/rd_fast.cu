@@ -119,10 +119,16 @@ __global__ void k_schedule(const gbg_sample *__restrict__ smp, int S, int n, dou
     unsorted[s] = r;
 }
 
-// Smooth time grid: fixed step dt0, k = ceil(tend/dt0) steps (at least one),
-// the last of length tend - (k-1) dt0. Dw in double (no float rounding of the
-// input); every operation rounded on its own so host code that restates it
-// gets the same coefficients.
+// Smooth time grids: a step dt, k = ceil(tend/dt) steps (at least one), the
+// last of length tend - (k-1) dt, so the final state is continuous in tend.
+//   dt0 > 0: dt = dt0 for every sample (fixed grid)
+//   dt0 < 0: dt = |dt0| * 0.99 h^2 / (6 Dw / L^2), the reference's step rule
+//            per sample (scaled grid). a = dt Dw / h^2 is then the same for
+//            every sample, b = dt rho depends on Dw / rho only and the step
+//            count on tend Dw only: the discrete model keeps the continuous
+//            one's symmetry (Dw, rho, tend) -> (c Dw, c rho, tend / c).
+// Dw in double (no float rounding of the input); every operation rounded on
+// its own so host code that restates it gets the same coefficients.
 __global__ void k_schedule_smooth(const gbg_sample *__restrict__ smp, int S, int n, double L, double dt0,
                                   SampleRec *__restrict__ unsorted) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -131,19 +137,22 @@ __global__ void k_schedule_smooth(const gbg_sample *__restrict__ smp, int S, int
     const double ih2 = __ddiv_rn(1., __dmul_rn(h, h));
     const double Dw = __ddiv_rn(smp[s].Dw, __dmul_rn(L, L));
     const double rho = smp[s].rho, tend = smp[s].tend;
-    double kk = ceil(__ddiv_rn(tend, dt0));
+    double dt = dt0;
+    if (dt0 < 0)
+        dt = __dmul_rn(-dt0, __ddiv_rn(__dmul_rn(__dmul_rn(0.99, h), h), __dmul_rn(6.0, Dw)));
+    double kk = ceil(__ddiv_rn(tend, dt));
     if (!(kk >= 1.0)) kk = 1.0;
     if (kk > 1e8) kk = 1e8;
     const int k = (int)kk;
-    const double dtl = __dadd_rn(tend, -__dmul_rn((double)(k - 1), dt0));
+    const double dtl = __dadd_rn(tend, -__dmul_rn((double)(k - 1), dt));
     SampleRec r;
-    r.a = (float)__dmul_rn(__dmul_rn(dt0, Dw), ih2);
-    r.b = (float)__dmul_rn(dt0, rho);
+    r.a = (float)__dmul_rn(__dmul_rn(dt, Dw), ih2);
+    r.b = (float)__dmul_rn(dt, rho);
     r.a2 = (float)__dmul_rn(__dmul_rn(dtl, Dw), ih2);
     r.b2 = (float)__dmul_rn(dtl, rho);
     r.nsteps = k;
     r.order = s;
-    r.dt = dt0;
+    r.dt = dt;
     unsorted[s] = r;
 }
 
@@ -704,7 +713,7 @@ int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
     SampleRec *unsorted = batch_unsorted(h);
     SampleRec *sorted = batch_sorted(h);
     int *rank_of = batch_rank_of(h);
-    if (o.dt0 > 0)
+    if (o.dt0 != 0)
         k_schedule_smooth<<<(S + 127) / 128, 128, 0, h.stream>>>(samples_device, S, h.n, o.L, o.dt0, unsorted);
     else
         k_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(samples_device, S, h.n, o.L, f32ref ? 1 : 0,

@@ -846,8 +846,11 @@ int surrogate_train(Surrogate &s, const gbg_sample *samples, int S, int epochs, 
             ++s.adam_t;
             const float b1 = 0.9f, b2 = 0.999f;
             const float c1 = 1.f - (float)std::pow(b1, (double)s.adam_t), c2 = 1.f - (float)std::pow(b2, (double)s.adam_t);
+            // linear learning-rate warm-up over the first 100 updates of the
+            // network's life: large early Adam steps switch ReLUs off for good
+            const double lr_t = lr * std::min(1.0, (double)s.adam_t / 100.0);
             sg::k_adam<<<sg::grid_n(s.net.nparams), 256, 0, st>>>(s.net.nparams, s.w32, s.g32, s.am, s.av, s.wb,
-                                                                   (float)lr, b1, b2, 1e-8f, c1, c2, 1.f);
+                                                                   (float)lr_t, b1, b2, 1e-8f, c1, c2, 1.f);
             h.launches++;
             sum += l;
             ++nb;

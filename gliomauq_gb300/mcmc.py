@@ -234,9 +234,23 @@ def _chol_population(th: np.ndarray, w: np.ndarray) -> np.ndarray:
     return np.diag(w) @ np.linalg.cholesky(c)
 
 
-def _chol_cov(th: np.ndarray) -> np.ndarray:
+def _decoupled(c: np.ndarray, axis) -> np.ndarray:
+    """Covariance with coordinate `axis` made independent of the others (its
+    own variance kept): random-walk moves of the other coordinates then use
+    their marginal covariance."""
+    if axis is None:
+        return c
+    c = np.array(c, dtype=np.float64, copy=True)
+    var = c[axis, axis]
+    c[axis, :] = 0.0
+    c[:, axis] = 0.0
+    c[axis, axis] = var if var > 0 else 1.0
+    return c
+
+
+def _chol_cov(th: np.ndarray, axis=None) -> np.ndarray:
     """Cholesky factor of the chains' covariance in parameter units."""
-    c = np.cov(th, rowvar=False)
+    c = _decoupled(np.cov(th, rowvar=False), axis)
     return np.linalg.cholesky(c + 1e-12 * np.diag(np.diag(c)) + 1e-300 * np.eye(c.shape[0]))
 
 
@@ -251,13 +265,15 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
     with adapt=True (or chol None), C follows the population covariance of
     the chains; every `rebuild_every` burn-in generations a surrogate that
     has rebuild(u_centre, steps) is re-linearised at the population mean
-    with half the population standard deviations as steps. With `axis` = a,
-    each inner step is, with probability axis_prob, instead a jump along
-    coordinate a alone of standard deviation 3x the population's spread in
-    a (at least 0.05): in the invariant coordinates a = 0 moves along the
-    scaling symmetry, the long direction of the posterior. Both moves are
-    symmetric random walks, so the inner chain stays reversible with respect
-    to the surrogate posterior. All of it is frozen after burn-in, so the
+    with half the population standard deviations as steps. With `axis` = a
+    (the scaling symmetry's coordinate in the invariant coordinates, along
+    which the likelihood of the scaled time grid is flat), random-walk moves
+    leave coordinate a fixed and each inner step is, with probability
+    axis_prob, instead a redraw of coordinate a from its prior conditional
+    (post.prior.redraw_axis), an independence proposal accepted with the
+    ratio of the surrogate's likelihoods (its prior terms cancel the
+    proposal's). Both moves keep the inner chain reversible with respect to
+    the surrogate posterior. All of it is frozen after burn-in, so the
     sampled chain is a fixed reversible kernel whose invariant law is the
     exact posterior."""
     w = post.prior.width
@@ -266,9 +282,10 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
     lp, _ = post.loglik(th, False)
     ls = spost.logpost(th)
     Lc = _chol(post, chol)
+    if axis is not None:
+        Lc = np.linalg.cholesky(_decoupled(Lc @ Lc.T, axis))
     out = np.empty((steps, m, d))
     acc1 = acc2 = tried = 0
-    axis_sd = 0.05
     t0 = time.perf_counter()
     t_burn = 0.0
     for k in range(steps):
@@ -278,25 +295,31 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
             if chol is None:
                 Lc = _chol_population(th, w)
             elif adapt and k >= max(1, burn // 4):
-                Lc = _chol_cov(th)
-            if axis is not None:
-                axis_sd = max(0.05, 3.0 * float(th[:, axis].std()))
+                Lc = _chol_cov(th, axis)
             if rebuild_every > 0 and k > 0 and k % rebuild_every == 0 and hasattr(spost, "rebuild"):
                 spost.rebuild(th.mean(axis=0), 0.5 * th.std(axis=0))
                 ls = spost.logpost(th)
         y, ly = th.copy(), ls.copy()
-        a1 = 0.0
+        a1 = 0.0   # random-walk acceptances (the step adapts to these)
+        n1 = 0
         for _ in range(inner):
             prop = y + step * rng.standard_normal((m, d)) @ Lc.T
+            corr = np.zeros(m)
+            jump = np.zeros(m, dtype=bool)
             if axis is not None:
+                prop[:, axis] = y[:, axis]
                 jump = rng.random(m) < axis_prob
-                prop[jump] = y[jump]
-                prop[jump, axis] += axis_sd * rng.standard_normal(int(jump.sum()))
+                if jump.any():
+                    prop[jump] = post.prior.redraw_axis(y[jump], axis, rng)
+                    # independence proposal from the prior conditional: the
+                    # prior factors cancel, leaving the likelihood ratio
+                    corr[jump] = post.prior.logp(y[jump]) - post.prior.logp(prop[jump])
             lq = spost.logpost(prop)
             with np.errstate(invalid="ignore"):
-                a = np.isfinite(lq) & (np.log(rng.random(m)) < lq - ly)
+                a = np.isfinite(lq) & (np.log(rng.random(m)) < lq - ly + corr)
             y[a], ly[a] = prop[a], lq[a]
-            a1 += a.mean()
+            a1 += a[~jump].sum()
+            n1 += int((~jump).sum())
         moved = np.any(y != th, axis=1)
         if moved.any():
             lpy = np.full(m, -np.inf)
@@ -309,7 +332,7 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
             th[a], lp[a], ls[a] = y[a], lpy[a], ly[a]
         else:
             a = np.zeros(m, dtype=bool)
-        a1 /= inner
+        a1 /= max(n1, 1)
         if k < burn:
             step *= np.exp((a1 - target) / np.sqrt(k + 1.0))
         else:
@@ -319,10 +342,9 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
         out[k] = th
     n_gen = max(1, (steps - burn) * m)
     return ChainResult(out, acc2 / n_gen, step, time.perf_counter() - t0, post.solves,
-                       history=dict(stage1_accept=acc1 / n_gen,
+                       history=dict(stage1_accept=acc1 / n_gen,  # random-walk moves
                                     stage2_accept=acc2 / max(tried, 1),
                                     surrogate_evals=spost.evals, inner=inner,
-                                    axis_sd=axis_sd if axis is not None else None,
                                     burn_seconds=t_burn if burn < steps else time.perf_counter() - t0))
 
 
@@ -459,6 +481,42 @@ class LogPrior:
     @property
     def hi(self):
         return self.lo + self.width
+
+    def redraw_axis(self, v: np.ndarray, a: int, rng) -> np.ndarray:
+        """Exact draw of coordinate a from the prior conditional given the
+        others (rows of v): along the line v + t e_a every log coordinate is
+        linear in t, the box gives an interval for t and the density (the
+        log-Jacobian) is exp(alpha t) there, alpha = sum over log coordinates
+        of (A^{-1})_{i,a}. Rows whose line moves a non-log coordinate (the
+        seed, whose prior is a voxel mask) are returned unchanged."""
+        v = np.array(np.atleast_2d(v), dtype=np.float64, copy=True)
+        col = self.Ai[:, a]
+        logs = list(self.log_idx)
+        if np.any(np.abs(np.delete(col, logs)) > 0):
+            return v
+        lo_u, hi_u = self._ubox()
+        u = self.to_logu(v)
+        t_lo = np.full(v.shape[0], -np.inf)
+        t_hi = np.full(v.shape[0], np.inf)
+        for i in logs:
+            if col[i] == 0:
+                continue
+            b1 = (lo_u[i] - u[:, i]) / col[i]
+            b2 = (hi_u[i] - u[:, i]) / col[i]
+            t_lo = np.maximum(t_lo, np.minimum(b1, b2))
+            t_hi = np.minimum(t_hi, np.maximum(b1, b2))
+        ok = np.isfinite(t_lo) & np.isfinite(t_hi) & (t_hi > t_lo)
+        alpha = float(col[logs].sum())
+        q = rng.random(v.shape[0])
+        t = np.zeros(v.shape[0])
+        if abs(alpha) < 1e-12:
+            t[ok] = t_lo[ok] + q[ok] * (t_hi[ok] - t_lo[ok])
+        else:
+            # inverse CDF of exp(alpha t) on [t_lo, t_hi], in a stable form
+            span = alpha * (t_hi[ok] - t_lo[ok])
+            t[ok] = t_lo[ok] + np.log1p(q[ok] * np.expm1(span)) / alpha
+        v[ok, a] += t[ok]
+        return v
 
     def logp(self, v):
         """Uniform prior on theta as a density in v: the log-Jacobian sum of
@@ -693,7 +751,10 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
                      generations: int = 300, burn: int = 100, inner: int = 16,
                      screen: int = 512, screen_draws=None, ic_peak: float = 0.1,
                      ic_sigma: float = 1.0) -> PipelineResult:
-    """The batched + adjoint + surrogate posterior sampler:
+    """The batched + adjoint + surrogate posterior sampler (dt0 < 0, the
+    scaled time grid, makes the likelihood invariant along the scaling
+    symmetry, whose coordinate is then drawn exactly from its prior
+    conditional; dt0 > 0 works too, with that move an ordinary MH step):
       1. log pi of `screen` prior draws in batched solves; the best four start
       2. damped Newton with batched adjoint gradients and Hessians (find_mode)
          in the scaling symmetry's coordinates (INVARIANT_MAP)
@@ -718,13 +779,11 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
     Lc = np.linalg.cholesky(cov)
     sur = AffineSurrogate(post, v_map, 0.5 * sd, quad_axis=0)
     setup = time.perf_counter() - t0
-    # starting points from the refined Gaussian, spread along the symmetry
-    # axis over +-0.3 (the posterior's long direction), redrawn until inside
-    # the prior
+    # starting points from the refined Gaussian, the symmetry axis redrawn
+    # from its prior conditional, redrawn until inside the prior
     def draw(k):
         v = v_map + rng.standard_normal((k, v_map.size)) @ Lc.T
-        v[:, 0] += rng.uniform(-0.3, 0.3, k)
-        return v
+        return post.prior.redraw_axis(v, 0, rng)
     v0 = draw(chains)
     for _ in range(100):
         bad = ~np.isfinite(post.prior.logp(v0))

@@ -138,13 +138,11 @@ typedef struct {
     double ic_peak;    /* initial peak density */
     double ic_sigma;   /* initial width in voxels */
     int with_loglik;   /* evaluate the likelihood per sample */
-    double dt0;        /* 0: the reference's time loop per sample (dt from Dw,
-                          steps while t <= tend). > 0: the smooth time grid of
-                          gbg_adjoint_grad -- fixed step dt0, ceil(tend/dt0)
-                          steps, the last one shortened to end at tend; the
-                          densities and log L equal gbg_adjoint_grad's forward
-                          model bit for bit (GBG_PREC_F32 state). dt0 must
-                          satisfy the CFL limit of the largest Dw. */
+    double dt0;        /* time grid. 0: the reference's time loop per sample
+                          (dt from Dw, steps while t <= tend). Otherwise a
+                          smooth grid of gbg_adjoint_grad (see there): the
+                          densities and log L equal its forward model bit for
+                          bit (GBG_PREC_F32 state). */
 } gbg_batch_opts;
 
 /* Host entry: copies the S samples in, solves, copies loglik (S results, may
@@ -161,10 +159,15 @@ int gbg_batch_solve_device(gbg_handle *h, const gbg_sample *samples_device, int 
 
 /* ---- gradients for MALA: discrete adjoint ----------------------------------------
  * No reference counterpart for the adjoint itself; the forward model it
- * differentiates is the fast-path step with a smooth time grid: one fixed
- * step dt0 for every sample of the call, n = ceil(tend/dt0) steps, the last
- * one shortened to end exactly at tend (the reference's dt(Dw) and integer
- * step count make its output piecewise constant in Dw and tend). Gradients
+ * differentiates is the fast-path step on a smooth time grid: a step dt,
+ * n = ceil(tend/dt) steps, the last one shortened to end exactly at tend
+ * (the reference's integer step count makes its output piecewise constant
+ * in Dw and tend). dt0 > 0: dt = dt0 for every sample (fixed grid; dt0 must
+ * satisfy the CFL limit of the largest Dw, e.g. 0.99 h^2 / (6 Dw_max / L^2)).
+ * dt0 < 0: dt = |dt0| * 0.99 h^2 / (6 Dw / L^2), the reference's step rule per
+ * sample (scaled grid, stable for |dt0| <= 1): the discrete model then keeps
+ * the continuous model's symmetry (Dw, rho, tend) -> (c Dw, c rho, tend / c),
+ * under which the density at tend is unchanged. Gradients
  * are of the log-likelihood (gbg_set_observations) with respect to
  * (Dw, rho, x0, y0, z0, tend), in the units of gbg_sample, written as
  * grad[6*s + 0..5]; loglik[s] receives log L of the same forward model
@@ -177,7 +180,7 @@ int gbg_batch_solve_device(gbg_handle *h, const gbg_sample *samples_device, int 
  * fields) is kept by the handle between calls and grows when a call needs
  * more, until gbg_destroy. */
 typedef struct {
-    double dt0;            /* step in days; e.g. 0.99 h^2 / (6 Dw_max / L^2) */
+    double dt0;            /* > 0: fixed step in days; < 0: scaled grid, -1 = reference rule */
     int checkpoint_every;
     double L;              /* brain length in cm */
     double ic_peak, ic_sigma;

@@ -42,9 +42,12 @@ def _rel_err(ga, gf, samples):
     return np.linalg.norm(a - f, axis=1) / np.linalg.norm(f, axis=1), a, f
 
 
-@pytest.mark.parametrize("state,tol", [("f64", 1e-5), ("f32", 1e-3)])
-def test_adjoint_gradient_matches_central_differences(gbg, state, tol):
+@pytest.mark.parametrize("state,tol,grid", [("f64", 1e-5, "fixed"), ("f32", 1e-3, "fixed"),
+                                            ("f64", 1e-5, "scaled"), ("f32", 1e-3, "scaled")])
+def test_adjoint_gradient_matches_central_differences(gbg, state, tol, grid):
     an, obs, samples, dt0 = _problem()
+    if grid == "scaled":
+        dt0 = -1.0  # the reference's step rule per sample, last step shortened
     with _lib.Handle(an.n, "f32") as h:
         h.set_anatomy(an.p_w, an.p_g)
         h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=1, step_ti=1)
@@ -52,7 +55,7 @@ def test_adjoint_gradient_matches_central_differences(gbg, state, tol):
         gf = _fd(h, samples, dt0, an.L, "f64")
     err, a, f = _rel_err(ga, gf, samples)
     for s in range(len(samples)):
-        print(f"{state} sample {s}: rel err {err[s]:.2e}")
+        print(f"{state} {grid} sample {s}: rel err {err[s]:.2e}")
         for i in range(6):
             print(f"   {NAMES[i]:4s} adjoint {a[s, i]: .6e}  fd {f[s, i]: .6e}")
     assert np.all(np.isfinite(ll)) and np.all(err <= tol)
@@ -78,8 +81,9 @@ def test_adjoint_argument_errors(gbg):
         assert e.value.status == -5
         h.set_anatomy(an.p_w, an.p_g)
         h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK)
-        with pytest.raises(_lib.GbgError):
-            h.adjoint_grad(samples, -1.0, an.L)
+        for bad_dt0 in (0.0, -2.0):  # no grid; scaled grid beyond the stability limit
+            with pytest.raises(_lib.GbgError):
+                h.adjoint_grad(samples, bad_dt0, an.L)
         bad = [(np.nan,) + samples[0][1:]]
         with pytest.raises(_lib.GbgError):
             h.adjoint_grad(bad, dt0, an.L)
@@ -108,3 +112,26 @@ def test_batched_smooth_grid_equals_adjoint_forward(gbg):
         r0 = h.batch_solve(smp, an.L)
         k_ref = [S.num_steps(S.reference_dt(an.n, s[0], an.L)[0], s[5]) for s in smp]
         assert list(r0["nsteps"]) == k_ref
+
+
+def test_scaled_grid_keeps_the_scaling_symmetry(gbg):
+    """(Dw, rho, tend) -> (c Dw, c rho, tend / c) leaves the continuous
+    model's density at tend unchanged; on the scaled grid (dt0 < 0) the
+    discrete model keeps it up to float rounding of the coefficients, on the
+    fixed grid it does not. Also: the batched solver equals the adjoint's
+    forward pass bit for bit on the scaled grid."""
+    an, obs, samples, dt0 = _problem()
+    with _lib.Handle(an.n, "f32", max_samples=8) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=1, step_ti=1)
+        base = samples[0]
+        scaled = [base] + [(c * base[0], c * base[1], *base[2:5], base[5] / c) for c in (0.8, 1.25)]
+        phi = h.batch_solve(scaled, an.L, with_loglik=False, want_phi=True, dt0=-1.0)["phi"]
+        for k in (1, 2):
+            rel = np.linalg.norm(phi[k] - phi[0]) / np.linalg.norm(phi[0])
+            assert rel < 1e-5, rel
+        phi_f = h.batch_solve(scaled, an.L, with_loglik=False, want_phi=True, dt0=dt0)["phi"]
+        assert np.linalg.norm(phi_f[1] - phi_f[0]) / np.linalg.norm(phi_f[0]) > 1e-4
+        ll_adj, _ = h.adjoint_grad(scaled, -1.0, an.L, state="f32", want_grad=False)
+        ll_pop = np.array([d["total"] for d in h.batch_solve(scaled, an.L, dt0=-1.0)["loglik"]])
+        assert np.array_equal(ll_adj, ll_pop)

@@ -89,13 +89,88 @@ def test_delayed_acceptance_targets_the_exact_posterior():
     # passes in batches of batch_max
     assert sur.calls >= 6 * 1200 * 32 // 8
     assert post.solves <= 32 * 1201
-    # with adaptation and jumps along one axis the target is still exact
+    # with adaptation the target is still exact
     r = mcmc.da(post, spost, th0, 1200, 0.02, rng, inner=6, burn=200, chol=np.diag(post.sd),
-                adapt=True, axis=0)
+                adapt=True)
     s = r.samples[200:].reshape(-1, 6)
     assert np.all(np.abs(s.mean(axis=0) - post.mu) < 0.15 * post.sd)
     assert np.all(np.abs(s.std(axis=0) / post.sd - 1) < 0.15)
     assert np.all(mcmc.rhat(r.samples[200:]) < 1.05)
+
+
+class InvariantStub(GaussianStub):
+    """Likelihood that depends on (log rho T, log Dw/rho, x0, y0, z0) only
+    (Gaussian there), prior box on theta: the tumour model's symmetry."""
+
+    def __init__(self):
+        super().__init__()
+        self.prior = mcmc.Prior(lo=np.array([2e-4, 0.01, 20, 20, 20, 100.0]),
+                                hi=np.array([2.5e-3, 0.2, 44, 44, 44, 500.0]),
+                                seed_mask=np.ones((64, 64, 64), dtype=bool))
+        self.c = np.array([np.log(0.15 * 260.0), np.log(6e-4 / 0.15), 30.0, 32.0, 31.0])
+        self.s = np.array([0.01, 0.02, 0.5, 0.5, 0.5])
+
+    def inv(self, th):
+        th = np.atleast_2d(th)
+        return np.stack([np.log(th[:, 1] * th[:, 5]), np.log(th[:, 0] / th[:, 1]),
+                         th[:, 2], th[:, 3], th[:, 4]], axis=1)
+
+    def loglik(self, th, with_grad):
+        th = np.atleast_2d(th)
+        self.solves += th.shape[0]
+        z = (self.inv(th) - self.c) / self.s
+        return -0.5 * np.sum(z * z, axis=1) + self.prior.logp(th), None
+
+
+class InvariantSurrogate:
+    """The invariant stub's log L with a shifted centre (a biased screen)."""
+    batch_max = 16
+
+    def __init__(self, post):
+        self.post = post
+
+    def loglik(self, samples):
+        th = np.asarray(samples, dtype=np.float64)
+        z = (self.post.inv(th) - self.post.c - 0.3 * self.post.s) / (1.2 * self.post.s)
+        return dict(loglik=[dict(total=v) for v in -0.5 * np.sum(z * z, axis=1)])
+
+
+def test_delayed_acceptance_with_symmetry_axis_redraw():
+    rng = np.random.default_rng(8)
+    base = InvariantStub()
+    lc = mcmc.LogCoords(base, A=mcmc.INVARIANT_MAP)
+    sp = lc.surrogate(mcmc.SurrogatePosterior(InvariantSurrogate(base), base.prior))
+    v_c = np.concatenate([[np.log(0.15)], base.c])
+    v0 = v_c + np.concatenate([[0.0], base.s]) * rng.standard_normal((32, 6))
+    v0 = lc.prior.redraw_axis(v0, 0, rng)
+    chol = np.diag(np.concatenate([[0.1], base.s]))
+    r = mcmc.da(lc, sp, v0, 1500, 1.0, rng, inner=6, burn=300, chol=chol, adapt=True, axis=0)
+    v = r.samples[300:]
+    flat = v.reshape(-1, 6)
+    # seed coordinates: the Gaussian (the prior box is far from it)
+    assert np.all(np.abs(flat[:, 3:].mean(axis=0) - base.c[2:]) < 0.1 * base.s[2:])
+    assert np.all(np.abs(flat[:, 3:].std(axis=0) / base.s[2:] - 1) < 0.1)
+    # (v1, v2): the Gaussian times the prior volume along the symmetry axis,
+    # Z(v1, v2) = integral of exp(v0) over the allowed interval, on a grid
+    g1 = base.c[0] + base.s[0] * np.linspace(-6, 6, 241)
+    g2 = base.c[1] + base.s[1] * np.linspace(-6, 6, 241)
+    V1, V2 = np.meshgrid(g1, g2, indexing="ij")
+    lo = np.maximum.reduce([np.full_like(V1, np.log(0.01)), np.log(2e-4) - V2, V1 - np.log(500.0)])
+    hi = np.minimum.reduce([np.full_like(V1, np.log(0.2)), np.log(2.5e-3) - V2, V1 - np.log(100.0)])
+    w = np.exp(-0.5 * (((V1 - base.c[0]) / base.s[0]) ** 2 + ((V2 - base.c[1]) / base.s[1]) ** 2))
+    w *= np.clip(np.exp(hi) - np.exp(lo), 0, None)
+    w /= w.sum()
+    m1, m2 = (w * V1).sum(), (w * V2).sum()
+    s1 = np.sqrt((w * (V1 - m1) ** 2).sum())
+    s2 = np.sqrt((w * (V2 - m2) ** 2).sum())
+    assert abs(flat[:, 1].mean() - m1) < 0.1 * s1 and abs(flat[:, 2].mean() - m2) < 0.1 * s2
+    assert abs(flat[:, 1].std() / s1 - 1) < 0.1 and abs(flat[:, 2].std() / s2 - 1) < 0.1
+    # the symmetry axis: given the rest, exp(v0) on the allowed interval; its
+    # mean matches the mean of exact prior-conditional redraws of the same rows
+    ref = lc.prior.redraw_axis(flat[::7], 0, rng)[:, 0]
+    assert abs(flat[:, 0].mean() - ref.mean()) < 0.05 * flat[:, 0].std() + 0.01
+    assert np.all(mcmc.rhat(v) < 1.05)
+    assert r.history["stage2_accept"] > 0.3
 
 
 class CorrelatedStub(GaussianStub):
@@ -277,3 +352,27 @@ def test_tangent_surrogate_second_order_terms_along_the_axis():
     assert np.allclose(quad.logpost(us), exact, rtol=1e-6, atol=1e-6 * np.abs(exact).max())
     assert err_lin > 100 * np.abs(quad.logpost(us) - exact).max()
     assert quad.J.shape == (12, m.f0.size)
+
+
+def test_redraw_axis_samples_the_prior_conditional():
+    """Along the scaling symmetry (v_0 of the invariant coordinates) the
+    prior conditional is exp(v_0) on the interval the box allows; the redraw
+    reproduces it (Kolmogorov distance of 20000 draws) and stays in the box."""
+    post = GaussianStub()
+    post.prior = mcmc.Prior(lo=np.array([2e-4, 0.01, 0, 0, 0, 100.0]),
+                            hi=np.array([2.5e-3, 0.2, 64, 64, 64, 500.0]),
+                            seed_mask=np.ones((64, 64, 64), dtype=bool))
+    lc = mcmc.LogCoords(post, A=mcmc.INVARIANT_MAP)
+    v = lc.to_u(np.array([6e-4, 0.15, 30.0, 32.0, 31.0, 260.0]))
+    rng = np.random.default_rng(0)
+    draws = lc.prior.redraw_axis(np.repeat(v[None], 20000, axis=0), 0, rng)
+    assert np.all(draws[:, 1:] == v[1:])
+    assert np.all(np.isfinite(lc.prior.logp(draws)))
+    # interval: log rho in [log .01, log .2], log Dw = v2 + v0 in box, log T = v1 - v0 in box
+    lo = max(np.log(0.01), np.log(2e-4) - v[2], v[1] - np.log(500.0))
+    hi = min(np.log(0.2), np.log(2.5e-3) - v[2], v[1] - np.log(100.0))
+    x = np.sort(draws[:, 0])
+    cdf = (np.exp(x) - np.exp(lo)) / (np.exp(hi) - np.exp(lo))
+    emp = np.arange(1, x.size + 1) / x.size
+    assert x[0] >= lo - 1e-12 and x[-1] <= hi + 1e-12
+    assert np.abs(cdf - emp).max() < 0.015
