@@ -458,7 +458,8 @@ class LogPrior:
 
     def to_theta(self, v):
         th = self.to_logu(v)
-        th[..., list(self.log_idx)] = np.exp(th[..., list(self.log_idx)])
+        with np.errstate(over="ignore"):  # far proposals map to inf, outside the prior
+            th[..., list(self.log_idx)] = np.exp(th[..., list(self.log_idx)])
         return th
 
     def _ubox(self):
