@@ -440,7 +440,7 @@ def main():
                                                    "chosen_by": "gbg_autotune"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
-                         "kernel": "k_population2", "kernel_ms": kern_ms,
+                         "kernel": f"k_population (autotuned variant {variant})", "kernel_ms": kern_ms,
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "peak_source": f"{peak_kind} hbm_gbs"},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 48 * S,

@@ -183,7 +183,12 @@ __global__ void k_gaussian_ic(int n, const gbg_sample *__restrict__ smp, int S, 
         const size_t s = i / N, c = i % N;
         const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
         float v = 0.0f;
-        if (pw[c] + pg[c] > 0.0) {
+        // float screen: cells with d^2 > 2 sigma^2 * 120 (+1 voxel^2 margin for the
+        // float rounding) have exponent < -110 and get 0 below; skip their FP64 work
+        const float fx = (float)x - (float)smp[s].x0, fy = (float)y - (float)smp[s].y0,
+                    fz = (float)z - (float)smp[s].z0;
+        const bool near = peak > 1.0 || fx * fx + fy * fy + fz * fz <= (float)(two_s2 * 120.0) + 1.0f;
+        if (near && pw[c] + pg[c] > 0.0) {
             // d2 and the exponent rounded operation by operation (no FMA), as
             // peak * exp(-d2 / (2 sigma^2)) evaluates in plain double arithmetic
             const double dx = x - smp[s].x0, dy = y - smp[s].y0, dz = z - smp[s].z0;
@@ -257,7 +262,9 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // the z-1, z, z+1 planes of its four cells in registers; the y-neighbour
 // rows and the anatomy come through L2 (density, __ldcg) and L1 (anatomy,
 // __ldg).
-template <int LR>  // lanes per x-row = n/4
+// PF = 1: the z+2 density plane (the DRAM stream) is loaded one plane ahead,
+// so two planes of each thread's new data are in flight at once.
+template <int LR, int PF = 0>  // lanes per x-row = n/4
 __device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
                                            const float *__restrict__ in, float *__restrict__ out,
                                            const float *__restrict__ cx, const float *__restrict__ cy,
@@ -274,10 +281,18 @@ __device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
     float4 Pp = __ldcg(reinterpret_cast<const float4 *>(in + at(y, zs)));
     float4 Pc = __ldcg(reinterpret_cast<const float4 *>(in + at(y, tz0)));
     float4 CZp = __ldg(reinterpret_cast<const float4 *>(cz + at(y, zs)));
+    float4 Pahead;
+    if (PF) Pahead = __ldcg(reinterpret_cast<const float4 *>(in + at(y, wrapp(tz0, n))));
     for (int dz = 0; dz < TZ; ++dz) {
         const int z = tz0 + dz;
         const int zn = wrapp(z, n);
-        const float4 Pn = __ldcg(reinterpret_cast<const float4 *>(in + at(y, zn)));
+        float4 Pn;
+        if (PF) {
+            Pn = Pahead;
+            if (dz + 1 < TZ) Pahead = __ldcg(reinterpret_cast<const float4 *>(in + at(y, wrapp(zn, n))));
+        } else {
+            Pn = __ldcg(reinterpret_cast<const float4 *>(in + at(y, zn)));
+        }
         const float4 PS = __ldcg(reinterpret_cast<const float4 *>(in + at(ym, z)));
         const float4 PN = __ldcg(reinterpret_cast<const float4 *>(in + at(yp, z)));
         const float4 CX = __ldg(reinterpret_cast<const float4 *>(cx + at(y, z)));
@@ -317,7 +332,11 @@ __device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
     }
 }
 
-template <int LR, int MINB>
+// Items of a round are ordered tile-major (item = tile * active + sample):
+// CTAs running at the same time work on the same tile of different samples,
+// so each tile's anatomy comes from DRAM once per round and is then shared
+// through L2.
+template <int LR, int MINB, int PF = 0>
 __global__ void __launch_bounds__(256, MINB) k_population1(PopArgs p) {
     const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
     int active = p.S;
@@ -328,11 +347,11 @@ __global__ void __launch_bounds__(256, MINB) k_population1(PopArgs p) {
         float *out = (k & 1) ? p.buf0 : p.buf1;
         const long items = (long)active * p.tiles;
         for (long it = blockIdx.x; it < items; it += gridDim.x) {
-            const int r = (int)(it / p.tiles), t = (int)(it % p.tiles);
+            const int r = (int)(it % active), t = (int)(it / active);
             const int ty = t % p.tiles_y, tz = t / p.tiles_y;
             const size_t off = (size_t)p.rec[r].order * p.stride;
             const bool last = k == p.rec[r].nsteps - 1;
-            march_tile<LR>(p.n, p.TZ, ty * rows, tz * p.TZ, in + off, out + off, p.cx, p.cy, p.cz,
+            march_tile<LR, PF>(p.n, p.TZ, ty * rows, tz * p.TZ, in + off, out + off, p.cx, p.cy, p.cz,
                            p.msk, last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
         }
         if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
@@ -504,10 +523,10 @@ struct PopVariant {
     size_t smem;
 };
 
-template <int LR, int MINB = 1>
+template <int LR, int MINB = 1, int PF = 0>
 PopVariant make_register_variant(int tz) {
     PopVariant v;
-    v.fn = (const void *)k_population1<LR, MINB>;
+    v.fn = (const void *)k_population1<LR, MINB, PF>;
     v.ry = 256 / LR;
     v.g = 1;
     v.threads = 256;
@@ -540,6 +559,9 @@ int variants_for(int n, PopVariant *out) {
             out[k++] = make_register_variant<32, 5>(16);
             out[k++] = make_register_variant<32, 6>(16);
             out[k++] = make_register_variant<32, 6>(32);
+            out[k++] = make_register_variant<32, 4, 1>(16);
+            out[k++] = make_register_variant<32, 5, 1>(16);
+            out[k++] = make_register_variant<32, 5, 1>(32);
             out[k++] = make_variant<32, 8, 2>(32);
             out[k++] = make_variant<32, 8, 1>(32);
             out[k++] = make_variant<32, 8, 2>(16);
@@ -551,6 +573,7 @@ int variants_for(int n, PopVariant *out) {
         case 64:
             out[k++] = make_register_variant<16>(16);
             out[k++] = make_register_variant<16, 6>(16);
+            out[k++] = make_register_variant<16, 5, 1>(16);
             out[k++] = make_variant<16, 16, 2>(16);
             out[k++] = make_variant<16, 16, 1>(16);
             out[k++] = make_variant<16, 8, 2>(16);
@@ -595,7 +618,7 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
         set_error("fast path supports n = 32, 64 or 128");
         return GBG_ERR_UNSUPPORTED;
     }
-    PopVariant vs[16];
+    PopVariant vs[32];
     const int nv = variants_for(h.n, vs);
     int vi = h.pop_variant;
     if (vi < 0 || vi >= nv) vi = 0;
@@ -622,12 +645,12 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
 }  // namespace
 
 int population_variant_count(int n) {
-    PopVariant vs[16];
+    PopVariant vs[32];
     return variants_for(n, vs);
 }
 
 int population_variant_shape(int n, int vi, int *ry, int *g, int *threads) {
-    PopVariant vs[16];
+    PopVariant vs[32];
     const int nv = variants_for(n, vs);
     if (vi < 0 || vi >= nv) return GBG_ERR_ARG;
     *ry = vs[vi].ry;
