@@ -54,6 +54,23 @@ def rank_info():
             int(os.environ.get("WORLD_SIZE", "1")))
 
 
+def max_over_ranks(value: float, world: int, device) -> float:
+    """The largest of every rank's value (the job's time is its slowest
+    rank's); a no-op on one rank."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(samples_per_rank: int, world: int, seconds_per_step: float) -> float:
+    """Whole-job solves/s: every rank solves its own population (weak scaling,
+    no collective on the data path), the step lasts as long as the slowest."""
+    return world * samples_per_rank / seconds_per_step
+
+
 def make_workload(seed_offset=0):
     from gliomauq_gb300 import synthetic as Syn
     an = Syn.make_anatomy(N, seed=0)
@@ -397,11 +414,8 @@ def main():
     launches = h.launch_count() - launches0
     total_ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
-    t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local_rank}")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_per_step = float(t.item()) / args.steps
-    value = world * S / (ms_per_step / 1000.0)
+    ms_per_step = max_over_ranks(total_ms, world, f"cuda:{local_rank}") / args.steps
+    value = job_rate(S, world, ms_per_step / 1000.0)
 
     # ---- end to end through the host C ABI ----
     host_samples = [p.as_tuple() for p in prior]
@@ -411,10 +425,7 @@ def main():
         res = h.batch_solve(host_samples, an.L, with_loglik=True)
     barrier()
     e2e_s = (time.perf_counter() - t0) / args.steps
-    te = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local_rank}")
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * S / float(te.item())
+    e2e_value = job_rate(S, world, max_over_ranks(e2e_s, world, f"cuda:{local_rank}"))
     assert np.all(res["nsteps"] == np.array(steps_list))
     assert all(np.isfinite(r["total"]) for r in res["loglik"])
 

@@ -22,7 +22,7 @@ void set_error(const std::string &msg);
     } while (0)
 
 // Device-side error codes written to the handle's status word.
-enum DeviceStatus : int { DEV_OK = 0, DEV_BARRIER_TIMEOUT = 1 };
+enum DeviceStatus : int { DEV_OK = 0, DEV_BARRIER_TIMEOUT = 1, DEV_COPY_TIMEOUT = 2 };
 
 // Compact observation lists for the likelihood (see likelihood.cu).
 struct ObsDevice {

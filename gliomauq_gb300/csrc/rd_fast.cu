@@ -34,6 +34,15 @@
 // sample by one step per round, rounds separated by a bounded grid barrier.
 // Samples are ordered by step count, longest first, so the active samples of
 // round k are a prefix of that order.
+//
+// Kernel families (the autotuner times them per grid size): registers
+// (k_population1: planes carried in registers, loads through L1/L2, optional
+// one-plane-ahead prefetch), cp.async rings (k_population3), and bulk-copy
+// rings fed by the TMA unit with mbarrier completion (k_population5: one
+// elected thread issues, a block barrier per plane; k_population6: a
+// producer warp and full/empty barriers per slot, no block barriers). All
+// run the same per-cell operation sequence, so every variant gives the same
+// bits.
 #include <vector>
 
 #include "gbg_internal.cuh"
@@ -505,6 +514,446 @@ __global__ void __launch_bounds__(LR *RY *G, (LR * RY * G >= 1024) ? 1 : 1024 / 
     }
 }
 
+// ---- population kernel, bulk-copy (TMA) staged family --------------------------
+// Same arithmetic and operation order as march_tile. One elected thread
+// copies each z-plane of a tile into a ring of D shared-memory slots with
+// cp.async.bulk (the TMA unit; one mbarrier per slot, completion by byte
+// count), up to D planes ahead of the plane being computed, so a CTA keeps
+// D planes of loads in flight without holding registers for them. A slot
+// holds, for one plane: density rows y0-1 .. y0+RY (periodic), cy rows
+// y0-1 .. y0+RY-1 and cx, cz, mask rows y0 .. y0+RY-1 (8 copies, rows of
+// n floats; the RY-row blocks are contiguous in memory). Every wait is
+// bounded; on a timeout the kernel records DEV_COPY_TIMEOUT, waits (bounded)
+// for the copies it has in flight and leaves.
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+// bounded wait for the given phase parity; false on timeout
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+    const unsigned addr = smem_u32(bar);
+    for (long long spins = 0; spins < (1ll << 24); ++spins) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (spins > 64) __nanosleep(32);
+    }
+    return false;
+}
+
+template <int LR, int RY, int D>
+struct TmaRing {
+    static constexpr int n = 4 * LR;
+    static constexpr int ROW = n * 4;                  // bytes per row
+    static constexpr int DEN = (RY + 2) * n;           // floats: density rows y0-1 .. y0+RY
+    static constexpr int CYR = (RY + 1) * n;           // cy rows y0-1 .. y0+RY-1
+    static constexpr int BLK = RY * n;                 // cx, cz, mask rows y0 .. y0+RY-1
+    static constexpr int SLOT = DEN + CYR + 3 * BLK;   // floats per slot
+    static constexpr unsigned BYTES = SLOT * 4;
+    static constexpr size_t smem() { return (size_t)D * BYTES + 64 * D; }
+};
+
+template <int LR, int RY, int D, int MINB>
+__global__ void __launch_bounds__(LR *RY, MINB) k_population5(PopArgs p) {
+    using R = TmaRing<LR, RY, D>;
+    constexpr int n = R::n;
+    constexpr int plane = n * n;
+    extern __shared__ __align__(128) float smem5[];
+    float *ring = smem5;
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem5 + (size_t)D * R::SLOT);
+    const int r = threadIdx.x / LR, li = threadIdx.x % LR, x0 = 4 * li;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < D; ++i) mbar_init(bar + i, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    // Planes form one sequence per CTA: plane q goes to slot q % D and
+    // completes phase (q / D) & 1 of that slot's barrier. Within a round the
+    // CTA's items (blockIdx.x, + gridDim.x, ...) are known in advance, so the
+    // producer (thread 0) runs ahead across item boundaries: plane q is
+    // issued once plane q - D is no longer read. Producer and consumers walk
+    // the sequence with incremental cursors (no divisions per plane).
+    struct Cursor {
+        int slot;
+        unsigned phase;
+        __device__ void step() {
+            if (++slot == D) {
+                slot = 0;
+                phase ^= 1u;
+            }
+        }
+    };
+    Cursor prod{0, 0u}, cons{0, 0u};  // next plane to issue / to wait for
+    int n_issued = 0;                 // within the round
+    unsigned used = 0, last_phase = 0;  // per slot (bit s): ever issued, phase of its latest copy
+    bool okw = true;                  // this thread's last copy wait succeeded
+    bool ok = true;                   // CTA-uniform
+    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
+    const int nplanes = p.TZ + 2;     // planes tz0-1 .. tz0+TZ of an item
+    int active = p.S;
+    for (int k = 0; k < maxsteps && ok; ++k) {
+        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
+        const float *in = (k & 1) ? p.buf1 : p.buf0;
+        float *out = (k & 1) ? p.buf0 : p.buf1;
+        const int items = active * p.tiles;
+        const int my_items = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+        const int round_planes = my_items * nplanes;
+        auto item_of = [&](int m, int &y0, int &tz0, size_t &off, int &smp) {
+            const int it = (int)blockIdx.x + m * (int)gridDim.x;
+            smp = it % active;
+            const int t = it / active;
+            y0 = (t % p.tiles_y) * RY;
+            tz0 = (t / p.tiles_y) * p.TZ;
+            off = (size_t)p.rec[smp].order * p.stride;
+        };
+        // producer cursor within the round
+        int pm = 0, pj = 0, py0 = 0, ptz0 = 0, psmp = 0;
+        size_t poff = 0;
+        if (threadIdx.x == 0 && my_items > 0) item_of(0, py0, ptz0, poff, psmp);
+        n_issued = 0;
+        // issue planes up to (not including) round-local index lim
+        auto issue_upto = [&](int lim) {
+            if (lim > round_planes) lim = round_planes;
+            if (threadIdx.x == 0) {
+                while (n_issued < lim) {
+                    unsigned long long *mb = bar + prod.slot;
+                    float *slot = ring + (size_t)prod.slot * R::SLOT;
+                    int zz = ptz0 - 1 + pj;
+                    zz = zz < 0 ? zz + n : (zz >= n ? zz - n : zz);
+                    const int ym = py0 == 0 ? n - 1 : py0 - 1, yp = py0 + RY == n ? 0 : py0 + RY;
+                    const float *pl = in + poff + (size_t)zz * plane;
+                    const size_t ao = (size_t)zz * plane;
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                    mbar_expect_tx(mb, R::BYTES);
+                    bulk_g2s(slot, pl + (size_t)ym * n, R::ROW, mb);
+                    bulk_g2s(slot + n, pl + (size_t)py0 * n, RY * R::ROW, mb);
+                    bulk_g2s(slot + (RY + 1) * n, pl + (size_t)yp * n, R::ROW, mb);
+                    float *cyb = slot + R::DEN;
+                    bulk_g2s(cyb, p.cy + ao + (size_t)ym * n, R::ROW, mb);
+                    bulk_g2s(cyb + n, p.cy + ao + (size_t)py0 * n, RY * R::ROW, mb);
+                    float *cxb = cyb + R::CYR, *czb = cxb + R::BLK, *mkb = czb + R::BLK;
+                    bulk_g2s(cxb, p.cx + ao + (size_t)py0 * n, RY * R::ROW, mb);
+                    bulk_g2s(czb, p.cz + ao + (size_t)py0 * n, RY * R::ROW, mb);
+                    bulk_g2s(mkb, p.msk + ao + (size_t)py0 * n, RY * R::ROW, mb);
+                    used |= 1u << prod.slot;
+                    last_phase = (last_phase & ~(1u << prod.slot)) | (prod.phase << prod.slot);
+                    prod.step();
+                    ++n_issued;
+                    if (++pj == nplanes) {
+                        pj = 0;
+                        if (++pm < my_items) item_of(pm, py0, ptz0, poff, psmp);
+                    }
+                }
+            } else if (lim > n_issued) {
+                n_issued = lim;
+            }
+        };
+        for (int m = 0; m < my_items; ++m) {
+            const int base = m * nplanes;  // round-local index of plane j = 0
+            int y0, tz0, smp;
+            size_t off;
+            item_of(m, y0, tz0, off, smp);
+            const bool last = k == p.rec[smp].nsteps - 1;
+            const float a = last ? p.rec[smp].a2 : p.rec[smp].a;
+            const float b = last ? p.rec[smp].b2 : p.rec[smp].b;
+            // the previous item is fully read: planes < base are free; a failed
+            // wait anywhere in the CTA ends the launch (a CTA-uniform decision)
+            if (__syncthreads_or(!okw)) {
+                ok = false;
+                break;
+            }
+            issue_upto(base + D);
+            const float *s0 = ring + (size_t)cons.slot * R::SLOT;
+            okw = mbar_wait(bar + cons.slot, cons.phase);
+            cons.step();
+            const float *sc = ring + (size_t)cons.slot * R::SLOT;  // plane tz0 (j = 1)
+            okw = mbar_wait(bar + cons.slot, cons.phase) && okw;
+            cons.step();
+            if (__syncthreads_or(!okw)) {
+                ok = false;
+                break;
+            }
+            const int y = y0 + r;
+            float4 Pp = *reinterpret_cast<const float4 *>(s0 + (r + 1) * n + x0);
+            float4 Pc = *reinterpret_cast<const float4 *>(sc + (r + 1) * n + x0);
+            float4 CZp = *reinterpret_cast<const float4 *>(s0 + R::DEN + R::CYR + R::BLK + r * n + x0);
+            for (int dz = 0; dz < p.TZ; ++dz) {
+                const int z = tz0 + dz;
+                // iteration dz - 1 (or the reads above) is done: planes j <= dz
+                // of this item are free, so planes up to j = dz + D may go out
+                if (__syncthreads_or(!okw)) {
+                    ok = false;
+                    break;
+                }
+                issue_upto(base + dz + 1 + D);
+                // plane z + 1 (j = dz + 2). After a failed wait the values read
+                // below are stale; the launch ends at the next barrier.
+                const float *sn = ring + (size_t)cons.slot * R::SLOT;
+                okw = mbar_wait(bar + cons.slot, cons.phase);
+                cons.step();
+                const float4 Pn = *reinterpret_cast<const float4 *>(sn + (r + 1) * n + x0);
+                const float4 PS = *reinterpret_cast<const float4 *>(sc + r * n + x0);
+                const float4 PN = *reinterpret_cast<const float4 *>(sc + (r + 2) * n + x0);
+                const float *cyb = sc + R::DEN, *cxb = cyb + R::CYR, *czb = cxb + R::BLK, *mkb = czb + R::BLK;
+                const float4 CYm = *reinterpret_cast<const float4 *>(cyb + r * n + x0);
+                const float4 CY = *reinterpret_cast<const float4 *>(cyb + (r + 1) * n + x0);
+                const float4 CX = *reinterpret_cast<const float4 *>(cxb + r * n + x0);
+                const float4 CZ = *reinterpret_cast<const float4 *>(czb + r * n + x0);
+                const float4 M = *reinterpret_cast<const float4 *>(mkb + r * n + x0);
+                const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
+                const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
+                const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
+                const float pv[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
+                const float cxa[5] = {cxl, CX.x, CX.y, CX.z, CX.w};
+                const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
+                const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
+                const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
+                const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
+                const float m4[4] = {M.x, M.y, M.z, M.w};
+                float o[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float f0 = pv[i + 1];
+                    float lap = cxa[i] * (pv[i] - f0);
+                    lap = fmaf(cxa[i + 1], pv[i + 2] - f0, lap);
+                    lap = fmaf(cym4[i], ps[i] - f0, lap);
+                    lap = fmaf(cy4[i], pn[i] - f0, lap);
+                    lap = fmaf(czp4[i], pp[i] - f0, lap);
+                    lap = fmaf(cz4[i], pq[i] - f0, lap);
+                    float v = fmaf(a, lap, f0);
+                    v = fmaf(b * f0, 1.0f - f0, v);
+                    v = fminf(fmaxf(v, 0.0f), 1.0f);
+                    o[i] = m4[i] != 0.0f ? v : 0.0f;
+                }
+                __stcg(reinterpret_cast<float4 *>(out + off + (size_t)x0 + (size_t)n * y + (size_t)plane * z),
+                       make_float4(o[0], o[1], o[2], o[3]));
+                Pp = Pc;
+                Pc = Pn;
+                CZp = CZ;
+                sc = sn;
+            }
+            if (!ok) break;
+        }
+        // this round's stores (generic proxy) before the next round's bulk
+        // copies (async proxy) read them, across the grid barrier
+        asm volatile("fence.proxy.async.global;\n" ::: "memory");
+        if (ok && __syncthreads_or(!okw)) ok = false;
+        if (!ok) break;
+        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
+        asm volatile("fence.proxy.async.global;\n" ::: "memory");
+    }
+    if (!ok && threadIdx.x == 0) {
+        // a copy never completed: record it and let the copies this CTA has in
+        // flight land (bounded) before its shared memory is released; the other
+        // CTAs see the status word at their next grid barrier and leave
+        atomicExch(p.status, (int)DEV_COPY_TIMEOUT);
+        // the latest copy of a slot completes after all earlier ones of that slot
+        for (int sl = 0; sl < D; ++sl)
+            if (used >> sl & 1u) mbar_wait(bar + sl, last_phase >> sl & 1u);
+    }
+}
+
+// Warp-specialised variant of the bulk-copy family: warp NC (after the NC
+// consumer warps) produces, the consumer warps compute. Each slot has a
+// "full" barrier (completed by the copies' byte count) and an "empty"
+// barrier (one arrival per consumer warp once the plane is no longer read),
+// so consumers never synchronise as a block: a consumer warp waits only for
+// the planes it reads, the producer only for a slot to be released. All
+// waits are bounded; a timeout sets a shared flag and the status word, and
+// every warp leaves at its next wait.
+template <int LR, int RY, int D, int MINB>
+__global__ void __launch_bounds__(LR *RY + 32, MINB) k_population6(PopArgs p) {
+    using R = TmaRing<LR, RY, D>;
+    constexpr int n = R::n;
+    constexpr int plane = n * n;
+    constexpr int NC = LR * RY / 32;  // consumer warps
+    extern __shared__ __align__(128) float smem6[];
+    float *ring = smem6;
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(smem6 + (size_t)D * R::SLOT);
+    unsigned long long *empty = full + D;
+    __shared__ int abort_flag;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool producer = warp == NC;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < D; ++i) {
+            mbar_init(full + i, 1);
+            mbar_init(empty + i, NC);
+        }
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto fail = [&]() {
+        atomicExch(&abort_flag, 1);
+        atomicExch(p.status, (int)DEV_COPY_TIMEOUT);
+    };
+    const int r = producer ? 0 : threadIdx.x / LR, li = threadIdx.x % LR, x0 = 4 * li;
+    int slot = 0;
+    unsigned phase = 0;  // this warp's cursor: next plane's slot and full/empty phase
+    unsigned used = 0, last_phase = 0;  // producer: per-slot latest copy (drain)
+    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
+    const int nplanes = p.TZ + 2;
+    int active = p.S;
+    long long q = 0;  // plane sequence number of the next plane (both roles)
+    for (int k = 0; k < maxsteps; ++k) {
+        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
+        const float *in = (k & 1) ? p.buf1 : p.buf0;
+        float *out = (k & 1) ? p.buf0 : p.buf1;
+        const int items = active * p.tiles;
+        const int my_items = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+        for (int m = 0; m < my_items; ++m) {
+            const int it = (int)blockIdx.x + m * (int)gridDim.x;
+            const int smp = it % active, t = it / active;
+            const int y0 = (t % p.tiles_y) * RY, tz0 = (t / p.tiles_y) * p.TZ;
+            const size_t off = (size_t)p.rec[smp].order * p.stride;
+            if (producer) {
+                for (int j = 0; j < nplanes; ++j, ++q) {
+                    if (lane == 0 && !*(volatile int *)&abort_flag) {
+                        // the slot's previous plane (q - D) released by every consumer warp
+                        if (q >= D && !mbar_wait(empty + slot, phase ^ 1u)) fail();
+                        if (!*(volatile int *)&abort_flag) {
+                            unsigned long long *mb = full + slot;
+                            float *dst = ring + (size_t)slot * R::SLOT;
+                            int zz = tz0 - 1 + j;
+                            zz = zz < 0 ? zz + n : (zz >= n ? zz - n : zz);
+                            const int ym = y0 == 0 ? n - 1 : y0 - 1, yp = y0 + RY == n ? 0 : y0 + RY;
+                            const float *pl = in + off + (size_t)zz * plane;
+                            const size_t ao = (size_t)zz * plane;
+                            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                            mbar_expect_tx(mb, R::BYTES);
+                            bulk_g2s(dst, pl + (size_t)ym * n, R::ROW, mb);
+                            bulk_g2s(dst + n, pl + (size_t)y0 * n, RY * R::ROW, mb);
+                            bulk_g2s(dst + (RY + 1) * n, pl + (size_t)yp * n, R::ROW, mb);
+                            float *cyb = dst + R::DEN;
+                            bulk_g2s(cyb, p.cy + ao + (size_t)ym * n, R::ROW, mb);
+                            bulk_g2s(cyb + n, p.cy + ao + (size_t)y0 * n, RY * R::ROW, mb);
+                            float *cxb = cyb + R::CYR, *czb = cxb + R::BLK, *mkb = czb + R::BLK;
+                            bulk_g2s(cxb, p.cx + ao + (size_t)y0 * n, RY * R::ROW, mb);
+                            bulk_g2s(czb, p.cz + ao + (size_t)y0 * n, RY * R::ROW, mb);
+                            bulk_g2s(mkb, p.msk + ao + (size_t)y0 * n, RY * R::ROW, mb);
+                            used |= 1u << slot;
+                            last_phase = (last_phase & ~(1u << slot)) | (phase << slot);
+                        }
+                    }
+                    if (++slot == D) {
+                        slot = 0;
+                        phase ^= 1u;
+                    }
+                }
+                continue;
+            }
+            // consumers
+            const bool last = k == p.rec[smp].nsteps - 1;
+            const float a = last ? p.rec[smp].a2 : p.rec[smp].a;
+            const float b = last ? p.rec[smp].b2 : p.rec[smp].b;
+            const int y = y0 + r;
+            auto advance = [&]() {
+                if (++slot == D) {
+                    slot = 0;
+                    phase ^= 1u;
+                }
+                ++q;
+            };
+            auto release = [&](int sl) {  // this warp no longer reads slot sl
+                __syncwarp();
+                if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(empty + sl)) : "memory");
+            };
+            // planes j = 0 (z = tz0 - 1) and j = 1 (z = tz0)
+            const int s0 = slot;
+            if (!mbar_wait(full + slot, phase)) fail();
+            advance();
+            int sc = slot;
+            if (!mbar_wait(full + slot, phase)) fail();
+            advance();
+            if (*(volatile int *)&abort_flag) break;
+            const float *b0 = ring + (size_t)s0 * R::SLOT;
+            float4 Pp = *reinterpret_cast<const float4 *>(b0 + (r + 1) * n + x0);
+            float4 CZp = *reinterpret_cast<const float4 *>(b0 + R::DEN + R::CYR + R::BLK + r * n + x0);
+            float4 Pc = *reinterpret_cast<const float4 *>(ring + (size_t)sc * R::SLOT + (r + 1) * n + x0);
+            release(s0);
+            for (int dz = 0; dz < p.TZ; ++dz) {
+                const int z = tz0 + dz;
+                const int sn = slot;  // plane z + 1
+                if (!mbar_wait(full + slot, phase)) fail();
+                advance();
+                if (*(volatile int *)&abort_flag) break;
+                const float *pc = ring + (size_t)sc * R::SLOT, *pn = ring + (size_t)sn * R::SLOT;
+                const float4 Pn = *reinterpret_cast<const float4 *>(pn + (r + 1) * n + x0);
+                const float4 PS = *reinterpret_cast<const float4 *>(pc + r * n + x0);
+                const float4 PN = *reinterpret_cast<const float4 *>(pc + (r + 2) * n + x0);
+                const float *cyb = pc + R::DEN, *cxb = cyb + R::CYR, *czb = cxb + R::BLK, *mkb = czb + R::BLK;
+                const float4 CYm = *reinterpret_cast<const float4 *>(cyb + r * n + x0);
+                const float4 CY = *reinterpret_cast<const float4 *>(cyb + (r + 1) * n + x0);
+                const float4 CX = *reinterpret_cast<const float4 *>(cxb + r * n + x0);
+                const float4 CZ = *reinterpret_cast<const float4 *>(czb + r * n + x0);
+                const float4 M = *reinterpret_cast<const float4 *>(mkb + r * n + x0);
+                release(sc);  // plane z is read for the last time above
+                const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
+                const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
+                const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
+                const float pv[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
+                const float cxa[5] = {cxl, CX.x, CX.y, CX.z, CX.w};
+                const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pnn[4] = {PN.x, PN.y, PN.z, PN.w};
+                const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
+                const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
+                const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
+                const float m4[4] = {M.x, M.y, M.z, M.w};
+                float o[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float f0 = pv[i + 1];
+                    float lap = cxa[i] * (pv[i] - f0);
+                    lap = fmaf(cxa[i + 1], pv[i + 2] - f0, lap);
+                    lap = fmaf(cym4[i], ps[i] - f0, lap);
+                    lap = fmaf(cy4[i], pnn[i] - f0, lap);
+                    lap = fmaf(czp4[i], pp[i] - f0, lap);
+                    lap = fmaf(cz4[i], pq[i] - f0, lap);
+                    float v = fmaf(a, lap, f0);
+                    v = fmaf(b * f0, 1.0f - f0, v);
+                    v = fminf(fmaxf(v, 0.0f), 1.0f);
+                    o[i] = m4[i] != 0.0f ? v : 0.0f;
+                }
+                __stcg(reinterpret_cast<float4 *>(out + off + (size_t)x0 + (size_t)n * y + (size_t)plane * z),
+                       make_float4(o[0], o[1], o[2], o[3]));
+                Pp = Pc;
+                Pc = Pn;
+                CZp = CZ;
+                sc = sn;
+            }
+            if (*(volatile int *)&abort_flag) break;
+            release(sc);  // plane tz0 + TZ (j = TZ + 1): read as z + 1 only
+        }
+        // this round's stores before the next round's bulk copies read them
+        asm volatile("fence.proxy.async.global;\n" ::: "memory");
+        __syncthreads();
+        if (*(volatile int *)&abort_flag) break;
+        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
+        asm volatile("fence.proxy.async.global;\n" ::: "memory");
+    }
+    if (abort_flag && producer && lane == 0) {
+        // let this CTA's copies in flight land (bounded) before leaving
+        for (int sl = 0; sl < D; ++sl)
+            if (used >> sl & 1u) mbar_wait(full + sl, last_phase >> sl & 1u);
+    }
+}
+
 int grid_for(const Handle &h, size_t work) {
     const size_t blocks = (work + 255) / 256;
     const size_t cap = (size_t)h.num_sms * 8;
@@ -548,6 +997,30 @@ PopVariant make_variant(int tz) {
     return v;
 }
 
+template <int LR, int RY, int D, int MINB>
+PopVariant make_ws_variant(int tz) {
+    PopVariant v;
+    v.fn = (const void *)k_population6<LR, RY, D, MINB>;
+    v.ry = RY;
+    v.g = 1;
+    v.threads = LR * RY + 32;
+    v.tz = tz;
+    v.smem = TmaRing<LR, RY, D>::smem();
+    return v;
+}
+
+template <int LR, int RY, int D, int MINB>
+PopVariant make_tma_variant(int tz) {
+    PopVariant v;
+    v.fn = (const void *)k_population5<LR, RY, D, MINB>;
+    v.ry = RY;
+    v.g = 1;
+    v.threads = LR * RY;
+    v.tz = tz;
+    v.smem = TmaRing<LR, RY, D>::smem();
+    return v;
+}
+
 // Candidate shapes per grid size; index 0 is the default.
 int variants_for(int n, PopVariant *out) {
     int k = 0;
@@ -562,6 +1035,9 @@ int variants_for(int n, PopVariant *out) {
             out[k++] = make_register_variant<32, 4, 1>(16);
             out[k++] = make_register_variant<32, 5, 1>(16);
             out[k++] = make_register_variant<32, 5, 1>(32);
+            out[k++] = make_tma_variant<32, 8, 3, 3>(32);
+            out[k++] = make_ws_variant<32, 8, 3, 3>(16);
+            out[k++] = make_ws_variant<32, 8, 3, 3>(32);
             out[k++] = make_variant<32, 8, 2>(32);
             out[k++] = make_variant<32, 8, 1>(32);
             out[k++] = make_variant<32, 8, 2>(16);
@@ -574,6 +1050,7 @@ int variants_for(int n, PopVariant *out) {
             out[k++] = make_register_variant<16>(16);
             out[k++] = make_register_variant<16, 6>(16);
             out[k++] = make_register_variant<16, 5, 1>(16);
+            out[k++] = make_tma_variant<16, 16, 3, 3>(16);
             out[k++] = make_variant<16, 16, 2>(16);
             out[k++] = make_variant<16, 16, 1>(16);
             out[k++] = make_variant<16, 8, 2>(16);
@@ -666,7 +1143,8 @@ int check_device_status(Handle &h) {
     if (st != DEV_OK) {
         const int zero = 0;
         cudaMemcpy(h.dev_status, &zero, sizeof(int), cudaMemcpyHostToDevice);
-        set_error("device-side grid barrier timed out");
+        set_error(st == DEV_COPY_TIMEOUT ? "device-side bulk copy did not complete"
+                                         : "device-side grid barrier timed out");
         return GBG_ERR_TIMEOUT;
     }
     return GBG_OK;

@@ -101,14 +101,17 @@ def test_batch_argument_errors(gbg):
         assert e.value.status == -5
 
 
-def test_every_population_shape_gives_identical_results(gbg):
-    """The per-cell arithmetic does not depend on the tile shape: all
-    population-kernel variants agree bitwise."""
-    an, samples = _setup(n=64, seed=6)
-    sm = [S.SampleParams(Dw=0.0013, rho=0.03, x0=30.2, y0=33.1, z0=31.5, T=40.0),
-          S.SampleParams(Dw=0.0021, rho=0.1, x0=28.0, y0=31.0, z0=33.0, T=25.0),
-          S.SampleParams(Dw=0.0009, rho=0.05, x0=33.4, y0=30.6, z0=29.9, T=60.0)]
-    with _lib.Handle(64, "f32", max_samples=3) as h:
+@pytest.mark.parametrize("n", [64, 128])
+def test_every_population_shape_gives_identical_results(gbg, n):
+    """The per-cell arithmetic does not depend on the tile shape or the
+    staging (registers, cp.async rings, bulk-copy rings): all population-kernel
+    variants agree bitwise."""
+    an, samples = _setup(n=n, seed=6)
+    c = n / 64.0
+    sm = [S.SampleParams(Dw=0.0013, rho=0.03, x0=30.2 * c, y0=33.1 * c, z0=31.5 * c, T=40.0),
+          S.SampleParams(Dw=0.0021, rho=0.1, x0=28.0 * c, y0=31.0 * c, z0=33.0 * c, T=25.0),
+          S.SampleParams(Dw=0.0009, rho=0.05, x0=33.4 * c, y0=30.6 * c, z0=29.9 * c, T=60.0)]
+    with _lib.Handle(n, "f32", max_samples=3) as h:
         h.set_anatomy(an.p_w, an.p_g)
         shapes = h.population_variants()
         assert len(shapes) >= 2
