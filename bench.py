@@ -316,6 +316,64 @@ def unet_screen(h, an, prior, dt0, res, rng, train_n=256, epochs=10, gens=20, in
         sg.close()
 
 
+def amr_measurement(device, level=4, steps=20, err_steps=60):
+    """The multiresolution-grid kernels (gbg_amr_*) at the size of the
+    adaptive configuration: 16^3 blocks of 16^3 cells (256^3), in both exact
+    modes (FP64, and the reference's default FP32 storage) and the fast FP32
+    mode. All blocks sit
+    at one level, with periodic same-level ghost tables (grids with
+    resolution jumps take MRAG's own tables); the step evaluates every ghost
+    through the tables like any grid. Reports cell-steps/s, algorithmic
+    GB/s and the FP32 modes' density error against FP64 after err_steps."""
+    from gliomauq_gb300 import _lib, amr, synthetic as Syn
+    n = 16 << level
+    an = Syn.make_anatomy(n, seed=0)
+    phi = np.clip(Syn.gaussian_ic(an, n / 2 + 0.3, n / 2 - 0.6, n / 2 + 0.2, peak=0.1, sigma=1.0), 0, 1)
+    L = n * 0.1
+    Dw_cm2, rho = 0.0013, 0.025
+    Dw = Dw_cm2 / L ** 2
+    Dg = 0.1 * Dw
+    dt = 0.99 * (1.0 / n) ** 2 / (6.0 * Dw)
+    blocks = amr.uniform_blocks(level)
+    tables = amr.same_level_ghosts(blocks)
+    pw, pg = amr.to_block_major(an.p_w, level), amr.to_block_major(an.p_g, level)
+    out = {"grid": f"{len(blocks)} blocks of 16^3 at level {level} ({n}^3), periodic "
+                   f"same-level ghost tables", "steps_timed": steps}
+    fields = {}
+    for mode in ("f64", "f32ref", "f32"):
+        real = 8 if mode == "f64" else 4
+        d, g = (Dw, Dg) if mode == "f64" else (float(np.float32(Dw)),
+                                               float(np.float32(np.float32(0.1) * np.float32(Dw))))
+        with _lib.AmrHandle(len(blocks), mode, device=device) as h:
+            h.set_grid(blocks, pw, pg, amr.to_block_major(phi, level))
+            h.set_ghosts(*tables)
+            h.step(d, g, rho, dt, 2)
+            h.sync()
+            t0 = time.perf_counter()
+            h.step(d, g, rho, dt, steps)
+            h.sync()
+            sec = time.perf_counter() - t0
+            h.step(d, g, rho, dt, err_steps - 2 - steps)
+            fields[mode] = amr.from_block_major(h.get_phi(), level)
+        cells = len(blocks) * 4096
+        # per cell-step: phi read + write and the cell's tables (exact modes:
+        # brain sum and six double face diffusivities; fast mode: six float
+        # face coefficients and the mask); per ghost (1736 per block): source
+        # value, weight (double), source block and cell (int), CSR start
+        # (long), ghost write
+        tab_bytes = 7 * 4 if mode == "f32" else real + 48
+        per_cell = 2 * real + tab_bytes + (1736 / 4096) * (real + 8 + 4 + 4 + 8 + real)
+        rate = cells * steps / sec
+        out[mode] = {"cell_steps_per_s": rate, "seconds_per_step": sec / steps,
+                     "algorithmic_bytes_per_cell_step": per_cell,
+                     "algorithmic_gb_per_s": rate * per_cell / 1e9}
+    b = fields["f64"]
+    for mode in ("f32ref", "f32"):
+        out[f"{mode}_vs_f64_rel_l2"] = float(np.linalg.norm(fields[mode] - b) / np.linalg.norm(b))
+    out["error_after_steps"] = err_steps
+    return out
+
+
 def run_reference_arm(args):
     rank, _, world = rank_info()
     if rank != 0:
@@ -349,6 +407,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mcmc", action="store_true",
                     help="skip the ESS/s comparison of plain and batched MALA sampling")
+    ap.add_argument("--no-amr", action="store_true",
+                    help="skip the multiresolution-grid measurement")
     ap.add_argument("--samples", type=int, default=S,
                     help="population size (profiling runs use a smaller one)")
     args = ap.parse_args()
@@ -463,6 +523,8 @@ def main():
             line["cpu_baseline"] = cpu_baseline(an, prior)
         if not args.no_mcmc:
             line["mcmc"] = mcmc_comparison(local_rank)
+        if not args.no_amr:
+            line["amr"] = amr_measurement(local_rank)
         print(json.dumps(line))
     h.close()
     if world > 1:

@@ -390,7 +390,11 @@ class AmrHandle:
                                           dptr(ww), int(ww.size)))
 
     def step(self, Dw, Dg, rho, dt, nsteps=1):
+        """Enqueues the steps on the handle's stream (returns before they finish)."""
         check(self.lib.gbg_amr_step(self._h, Dw, Dg, rho, dt, nsteps))
+
+    def sync(self):
+        check(self.lib.gbg_sync(self._h))
 
     def get_phi(self) -> np.ndarray:
         out = np.empty((self.nb, 16, 16, 16), dtype=np.float64)

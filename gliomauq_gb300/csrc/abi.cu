@@ -457,8 +457,9 @@ int gbg_amr_create(const gbg_amr_config *cfg, gbg_handle **out) {
         return GBG_ERR_ARG;
     }
     *out = nullptr;
-    if (cfg->max_blocks < 1 || (cfg->precision != GBG_PREC_F64 && cfg->precision != GBG_PREC_F32REF)) {
-        set_error("bad AMR configuration (max_blocks >= 1; GBG_PREC_F64 or GBG_PREC_F32REF)");
+    if (cfg->max_blocks < 1 || (cfg->precision != GBG_PREC_F64 && cfg->precision != GBG_PREC_F32REF &&
+                                cfg->precision != GBG_PREC_F32)) {
+        set_error("bad AMR configuration (max_blocks >= 1; GBG_PREC_F64, GBG_PREC_F32REF or GBG_PREC_F32)");
         return GBG_ERR_ARG;
     }
     int ndev = 0;

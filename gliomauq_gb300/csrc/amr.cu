@@ -22,6 +22,7 @@
 // largest magnitude (FWTReport::getOverAll_DetailMaxMag, :184-190).
 //
 // Compiled with -fmad=false: every operation rounds on its own.
+#include <algorithm>
 #include <utility>
 #include <vector>
 
@@ -153,6 +154,87 @@ __global__ void k_amr_step(int nb, RegionTable rt, const int *__restrict__ level
         v = ((Real)0 < v) ? v : (Real)0;
         v = (v < (Real)1) ? v : (Real)1;
         out[i] = v;
+    }
+}
+
+// ---- fast FP32 mode (GBG_PREC_F32 handles) ------------------------------------
+// The uniform fast path's arithmetic on the block grid: unit face
+// coefficients c_f = 2 k_c k_n / (k_c + k_n), k = (p_w + r p_g) / (p_w + p_g)
+// (double, rounded to float), a tissue mask (cell and its six lab
+// neighbours have tissue), and per step
+//   phi' = m * clamp(phi + a_l sum_f c_f (phi_f - phi) + b phi (1 - phi), 0, 1)
+// in float, faces in the order W E S N B F, a_l = dt Dw / h_l^2 per block
+// level. On a one-level grid this is the uniform fast path bit for bit.
+// Table per cell: 7 floats (c_W, c_E, c_S, c_N, c_B, c_F, mask).
+__global__ void k_amr_fast_tables(int nb, RegionTable rt, const float *__restrict__ pw, const float *__restrict__ pg,
+                                  const float *__restrict__ gpw, const float *__restrict__ gpg, double ratio,
+                                  float *__restrict__ tab) {
+    const long total = (long)nb * BC;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / BC), c = (int)(i % BC);
+        const int x = c % BS, y = (c / BS) % BS, z = c / (BS * BS);
+        const int nx[7] = {x, x - 1, x + 1, x, x, x, x};
+        const int ny[7] = {y, y, y, y - 1, y + 1, y, y};
+        const int nz[7] = {z, z, z, z, z, z - 1, z + 1};
+        double k[7];
+        bool all = true;
+        for (int q = 0; q < 7; ++q) {
+            const double a = (double)lab_at(rt, pw, gpw, b, nx[q], ny[q], nz[q]);
+            const double g = (double)lab_at(rt, pg, gpg, b, nx[q], ny[q], nz[q]);
+            const double br = a + g;
+            all = all && (br > 0.0);
+            k[q] = br > 0.0 ? (a + ratio * g) / br : 0.0;
+        }
+        float *t = tab + (size_t)i * 7;
+        for (int f = 0; f < 6; ++f) {
+            // the face's two cells in the uniform tables' order: (cell, +neighbour)
+            const bool minus = (f % 2) == 0;
+            const double k0 = minus ? k[f + 1] : k[0], k1 = minus ? k[0] : k[f + 1];
+            const double sum = k0 + k1;
+            t[f] = (k0 > 0.0 && k1 > 0.0 && sum > 0.0) ? (float)(2.0 * k0 * k1 / sum) : 0.0f;
+        }
+        t[6] = all ? 1.0f : 0.0f;
+    }
+}
+
+// One CTA per block: the block and its ghosts go to an 18^3 lab in shared
+// memory, then 256 threads update 16 cells each.
+__global__ void __launch_bounds__(256) k_amr_fast_step(int nb, RegionTable rt, const int *__restrict__ level,
+                                                       const float *__restrict__ phi,
+                                                       const float *__restrict__ gphi,
+                                                       const float *__restrict__ tab, float *__restrict__ out,
+                                                       double Dw, double rho, double dt) {
+    constexpr int LS = BS + 2;
+    __shared__ float lab[LS * LS * LS];
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        __syncthreads();
+        const float *pb = phi + (size_t)b * BC;
+        const float *gb = gphi + (size_t)b * NG;
+        for (int l = threadIdx.x; l < LS * LS * LS; l += blockDim.x) {
+            const int x = l % LS - 1, y = (l / LS) % LS - 1, z = l / (LS * LS) - 1;
+            const bool inside = x >= 0 && x < BS && y >= 0 && y < BS && z >= 0 && z < BS;
+            lab[l] = inside ? pb[x + BS * (y + BS * z)] : gb[ghost_slot(rt, x, y, z)];
+        }
+        __syncthreads();
+        const double h = 1.0 / (double)((1 << level[b]) * BS);
+        const float a = (float)(dt * Dw * (1. / (h * h)));
+        const float bb = (float)(dt * rho);
+        for (int c = threadIdx.x; c < BC; c += blockDim.x) {
+            const int x = c % BS, y = (c / BS) % BS, z = c / (BS * BS);
+            const int l = (x + 1) + LS * ((y + 1) + LS * (z + 1));
+            const float f0 = lab[l];
+            const float *t = tab + ((size_t)b * BC + c) * 7;
+            float lap = t[0] * (lab[l - 1] - f0);
+            lap = fmaf(t[1], lab[l + 1] - f0, lap);
+            lap = fmaf(t[2], lab[l - LS] - f0, lap);
+            lap = fmaf(t[3], lab[l + LS] - f0, lap);
+            lap = fmaf(t[4], lab[l - LS * LS] - f0, lap);
+            lap = fmaf(t[5], lab[l + LS * LS] - f0, lap);
+            float v = fmaf(a, lap, f0);
+            v = fmaf(bb * f0, 1.0f - f0, v);
+            v = fminf(fmaxf(v, 0.0f), 1.0f);
+            out[(size_t)b * BC + c] = t[6] != 0.0f ? v : 0.0f;
+        }
     }
 }
 
@@ -427,6 +509,32 @@ int amr_steps(Handle &h, double Dw, double Dg, double rho, double dt, long nstep
     const long cells = (long)h.amr.nb * BC, ng = (long)h.amr.nb * NG;
     const int gc = grid_blocks(h, cells), gg = grid_blocks(h, ng);
     const bool f64 = h.prec == GBG_PREC_F64;
+    if (h.prec == GBG_PREC_F32) {
+        // fast mode: unit coefficients for the ratio Dg/Dw (rounded to float, as
+        // the uniform fast path does), the 7-float table in the df storage
+        float *tab = reinterpret_cast<float *>(h.amr.df);
+        if (!h.amr.tables_valid || h.amr.tab_Dw != Dw || h.amr.tab_Dg != Dg) {
+            k_amr_fast_tables<<<gc, 256, 0, h.stream>>>(h.amr.nb, rt, (const float *)h.amr.pw,
+                                                        (const float *)h.amr.pg, (const float *)h.amr.gpw,
+                                                        (const float *)h.amr.gpg, (double)(float)(Dg / Dw), tab);
+            h.launches++;
+            h.amr.tab_Dw = Dw;
+            h.amr.tab_Dg = Dg;
+            h.amr.tables_valid = true;
+        }
+        const int gb = std::min(h.amr.nb, h.num_sms * 8);
+        for (long s = 0; s < nsteps; ++s) {
+            void *in = h.amr.phi[h.amr.cur], *out = h.amr.phi[h.amr.cur ^ 1];
+            k_ghost_eval<float><<<gg, 256, 0, h.stream>>>(h.amr.nb, h.amr.gstart, h.amr.gsrc_block, h.amr.gsrc_cell,
+                                                          h.amr.gw, (const float *)in, (float *)h.amr.gphi);
+            k_amr_fast_step<<<gb, 256, 0, h.stream>>>(h.amr.nb, rt, h.amr.level, (const float *)in,
+                                                      (const float *)h.amr.gphi, tab, (float *)out, Dw, rho, dt);
+            h.launches += 2;
+            h.amr.cur ^= 1;
+        }
+        GBG_CUDA_TRY(cudaGetLastError());
+        return GBG_OK;
+    }
     if (!h.amr.tables_valid || h.amr.tab_Dw != Dw || h.amr.tab_Dg != Dg) {
         if (f64)
             k_amr_tables<double><<<gc, 256, 0, h.stream>>>(h.amr.nb, rt, (const double *)h.amr.pw,

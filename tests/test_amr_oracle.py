@@ -68,3 +68,27 @@ def test_amr_dump_rules():
         np.concatenate([np.repeat(np.repeat(np.repeat(d["phi"][i], 2 ** (2 - d["blocks"][i][0]), 0),
                                             2 ** (2 - d["blocks"][i][0]), 1),
                                   2 ** (2 - d["blocks"][i][0]), 2).ravel() for i in range(len(d["blocks"]))]))
+
+
+def test_same_level_ghost_tables_are_periodic_copies():
+    """gliomauq_gb300.amr.same_level_ghosts in the oracle's ghost order: every
+    ghost of a one-level grid equals the periodic neighbour cell of the
+    uniform field."""
+    from gliomauq_gb300 import amr
+    assert np.array_equal(amr.ghost_lab_coords()[:, ::-1] + 1,
+                          np.argwhere(A.LAB_SLOTS >= 0)[np.argsort(A.LAB_SLOTS[A.LAB_SLOTS >= 0])])
+    level = 1
+    n = 16 << level
+    rng = np.random.default_rng(0)
+    u = rng.random((n, n, n))
+    blocks = amr.uniform_blocks(level)
+    f = amr.to_block_major(u, level)
+    assert np.array_equal(amr.from_block_major(f, level), u)
+    st, sb, sc, w = amr.same_level_ghosts(blocks)
+    gv = A.ghost_values(f.reshape(-1, 4096), st, sb, sc, w, np.float64).reshape(-1, 1736)
+    lab = amr.ghost_lab_coords()
+    for bi, (lv, ix, iy, iz) in enumerate(blocks):
+        gx = (ix * 16 + lab[:, 0]) % n
+        gy = (iy * 16 + lab[:, 1]) % n
+        gz = (iz * 16 + lab[:, 2]) % n
+        assert np.array_equal(gv[bi], u[gz, gy, gx])

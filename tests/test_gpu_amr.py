@@ -99,3 +99,78 @@ def test_amr_dump_matches_oracle(gbg):
         u2 = h.dump_uniform(32, reference_rules=False)
     assert np.array_equal(u, A.dump_uniform(d["blocks"], d["phi"], 64))
     assert np.array_equal(u2, A.dump_uniform(d["blocks"], d["phi"], 32, reference_rules=False))
+
+
+@pytest.mark.parametrize("variant", ["f64", "f32"])
+def test_one_level_block_grid_equals_uniform_solver(gbg, variant):
+    """A grid of 4^3 blocks at level 2 with periodic same-level ghost tables
+    (gliomauq_gb300.amr) steps to the same bits as the uniform 64^3 exact
+    solver: both restate the reference's operator, and a one-level MRAG grid
+    is a periodic uniform grid."""
+    from gliomauq_gb300 import amr, synthetic as S
+    level, n = 2, 64
+    an = S.make_anatomy(n, seed=3)
+    phi = np.clip(S.gaussian_ic(an, 30.2, 33.1, 31.5, peak=0.8, sigma=3.0), 0, 1)
+    Dw, rho, dt, steps = 0.0013 / (n * 0.1) ** 2, 0.03, 0.7, 12
+    Dg = 0.1 * Dw
+    if variant == "f32":
+        Dw, Dg = float(np.float32(Dw)), float(np.float32(np.float32(0.1) * np.float32(Dw)))
+        phi = phi.astype(np.float32).astype(np.float64)
+    with _lib.Handle(n, PREC[variant]) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        h.set_phi(phi)
+        h.rd_step(Dw, Dg, rho, dt, steps)
+        ref = h.get_phi()
+    blocks = amr.uniform_blocks(level)
+    with _lib.AmrHandle(len(blocks), PREC[variant]) as h:
+        h.set_grid(blocks, amr.to_block_major(an.p_w, level), amr.to_block_major(an.p_g, level),
+                   amr.to_block_major(phi, level))
+        h.set_ghosts(*amr.same_level_ghosts(blocks))
+        h.step(Dw, Dg, rho, dt, steps)
+        out = amr.from_block_major(h.get_phi(), level)
+    assert np.array_equal(out, ref)
+
+
+def test_fast_f32_one_level_grid_equals_uniform_fast_path(gbg):
+    """The fast FP32 block-grid mode (GBG_PREC_F32) on a one-level grid is
+    the uniform fast path bit for bit (same coefficients, same operation
+    order); the anatomy is given in float-representable values so that both
+    paths start from the same numbers."""
+    from gliomauq_gb300 import amr, synthetic as S
+    level, n = 2, 64
+    an = S.make_anatomy(n, seed=3)
+    pw = an.p_w.astype(np.float32).astype(np.float64)
+    pg = an.p_g.astype(np.float32).astype(np.float64)
+    phi = np.clip(S.gaussian_ic(an, 30.2, 33.1, 31.5, peak=0.8, sigma=3.0), 0, 1)
+    phi = phi.astype(np.float32).astype(np.float64)
+    Dw, rho, dt, steps = 0.0013 / (n * 0.1) ** 2, 0.03, 0.7, 12
+    with _lib.Handle(n, "f32") as h:
+        h.set_anatomy(pw, pg)
+        h.set_phi(phi)
+        h.rd_step(Dw, 0.1 * Dw, rho, dt, steps)
+        ref = h.get_phi()
+    blocks = amr.uniform_blocks(level)
+    with _lib.AmrHandle(len(blocks), "f32") as h:
+        h.set_grid(blocks, amr.to_block_major(pw, level), amr.to_block_major(pg, level),
+                   amr.to_block_major(phi, level))
+        h.set_ghosts(*amr.same_level_ghosts(blocks))
+        h.step(Dw, 0.1 * Dw, rho, dt, steps)
+        out = amr.from_block_major(h.get_phi(), level)
+    assert np.array_equal(out, ref)
+
+
+def test_fast_f32_mixed_level_grid_error_against_f64(gbg):
+    """Fast FP32 mode on the reference's mixed-level grid (resolution-jump
+    ghosts from MRAG's tables): relative L2 error against the FP64 mode after
+    the fixture's steps below 1e-5 (float arithmetic, as the uniform fast
+    path's 3.5e-7)."""
+    d = golden_npz("amr64_f64.npz")
+    outs = {}
+    for prec in ("f64", "f32"):
+        with _lib.AmrHandle(64, prec) as h:
+            load(h, d)
+            h.step(float(d["Dw"]), float(d["Dg"]), float(d["rho"]), float(d["dt"]), int(d["steps_after"]))
+            outs[prec] = h.get_phi()
+    err = np.linalg.norm(outs["f32"] - outs["f64"]) / np.linalg.norm(outs["f64"])
+    print("fast f32 vs f64 relative L2", err)
+    assert 0 < err < 1e-5
