@@ -32,7 +32,7 @@ EXPORTS = [
     "gbg_amr_dump_uniform", "gbg_surrogate_create", "gbg_surrogate_destroy",
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
-    "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik",
+    "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_surrogate_set_engine",
 ]
 
 
@@ -143,6 +143,7 @@ def load(path: str = LIB_PATH):
         "gbg_surrogate_loss_grad": [vp, C.POINTER(Sample), C.c_int, fp, dp, fp],
         "gbg_surrogate_features": [vp, C.POINTER(Sample), C.c_int, fp],
         "gbg_surrogate_loglik": [vp, C.POINTER(Sample), C.c_int, C.POINTER(LikResult), fp],
+        "gbg_surrogate_set_engine": [vp, C.c_int],
         "gbg_affine_set": [vp, C.c_int, fp, fp],
         "gbg_affine_loglik": [vp, C.c_int, dp, C.POINTER(LikResult)],
         "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
@@ -457,6 +458,10 @@ class Surrogate:
         c = C.c_long()
         check(self.lib.gbg_surrogate_nparams(self._s, C.byref(c)))
         return c.value
+
+    def set_engine(self, engine: str):
+        """Convolution kernels: "tcgen05" or "mma.sync"."""
+        check(self.lib.gbg_surrogate_set_engine(self._s, {"mma.sync": 0, "tcgen05": 1}[engine]))
 
     def get_params(self) -> np.ndarray:
         p = np.empty(self.nparams(), dtype=np.float32)

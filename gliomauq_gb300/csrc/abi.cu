@@ -807,7 +807,12 @@ int gbg_surrogate_loglik(gbg_surrogate *s, const gbg_sample *samples, int B, gbg
         GBG_CUDA_TRY(cudaMemcpyAsync(phi, gbg::surrogate_prediction(*s->s), (size_t)B * h.N * sizeof(float), cudaMemcpyDeviceToHost,
                                      h.stream));
     GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
-    return GBG_OK;
+    return gbg::check_device_status(h);
+}
+
+int gbg_surrogate_set_engine(gbg_surrogate *s, int engine) {
+    if (int rc = check_sur(s)) return rc;
+    return gbg::surrogate_set_engine(*s->s, engine);
 }
 
 int gbg_launch_count(gbg_handle *hh, long long *count) {

@@ -22,7 +22,7 @@ void set_error(const std::string &msg);
     } while (0)
 
 // Device-side error codes written to the handle's status word.
-enum DeviceStatus : int { DEV_OK = 0, DEV_BARRIER_TIMEOUT = 1, DEV_COPY_TIMEOUT = 2 };
+enum DeviceStatus : int { DEV_OK = 0, DEV_BARRIER_TIMEOUT = 1, DEV_COPY_TIMEOUT = 2, DEV_MMA_TIMEOUT = 3 };
 
 // Compact observation lists for the likelihood (see likelihood.cu).
 struct ObsDevice {
@@ -197,6 +197,7 @@ int surrogate_create(Handle &h, const gbg_surrogate_config &c, Surrogate **out);
 void surrogate_destroy(Surrogate *s);
 long surrogate_nparams(const Surrogate &s);
 int surrogate_batch_max(const Surrogate &s);
+int surrogate_set_engine(Surrogate &s, int engine);
 const float *surrogate_prediction(const Surrogate &s);  // last predicted densities, solver grid
 int surrogate_get_params(Surrogate &s, float *out);
 int surrogate_set_params(Surrogate &s, const float *in);

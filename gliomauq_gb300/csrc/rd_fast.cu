@@ -1143,8 +1143,9 @@ int check_device_status(Handle &h) {
     if (st != DEV_OK) {
         const int zero = 0;
         cudaMemcpy(h.dev_status, &zero, sizeof(int), cudaMemcpyHostToDevice);
-        set_error(st == DEV_COPY_TIMEOUT ? "device-side bulk copy did not complete"
-                                         : "device-side grid barrier timed out");
+        set_error(st == DEV_COPY_TIMEOUT  ? "device-side bulk copy did not complete"
+                  : st == DEV_MMA_TIMEOUT ? "device-side tensor-core MMA did not complete"
+                                          : "device-side grid barrier timed out");
         return GBG_ERR_TIMEOUT;
     }
     return GBG_OK;

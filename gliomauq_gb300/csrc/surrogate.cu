@@ -1,5 +1,7 @@
 // Learned surrogate of the forward solve: a small 3D convolutional U-Net,
-// trained and evaluated with the kernels in this file.
+// trained and evaluated with the kernels in this file. Forward and
+// data-gradient convolutions run on tcgen05 (k_conv_fwd_tc) by default, or
+// on mma.sync tiles (k_conv_fwd); the weight gradient on mma.sync.
 //
 // Tensors are channels-last, [batch][z][y][x][channel], bf16 activations and
 // weights with fp32 accumulation; a layer reads or writes a channel slice
@@ -121,6 +123,225 @@ __global__ void __launch_bounds__(128) k_conv_fwd(Geom g, Slice in, int Cin, con
                 if (out.p) out.p[v * out.stride + out.off + co] = __float2bfloat16(val);
             }
         }
+}
+
+// ---- forward convolution on the 5th-generation tensor cores (tcgen05) ----------
+// Same GEMM as k_conv_fwd: D[v, co] = sum_{tap, ci} in[v + tap, ci] w[co, tap, ci],
+// M = 128 voxels per tile, N = Cout, K = 27 Cin in chunks of 16. The weights
+// (N x K, bf16) sit in shared memory for the whole launch; the A operand of
+// each K-chunk (128 voxels x 16 channels of one tap, zero outside the grid)
+// is gathered by the 128 threads into one of S shared-memory stages; one
+// thread issues tcgen05.mma (bf16 x bf16 -> fp32 accumulator in tensor
+// memory) and commits it to the stage's mbarrier, which frees the stage when
+// the MMA has read it. Operands use the no-swizzle K-major layout: 8-row x
+// 16-byte core matrices, the two core matrices of a 16-wide K-chunk 128 B
+// apart (leading byte offset), 8-row groups 256 B apart (stride byte
+// offset). The epilogue reads the accumulator with tcgen05.ld (warp w owns
+// tensor-memory lanes 32w..32w+31 = voxels), adds the bias, applies ReLU and
+// stores bf16 and/or fp32. Every mbarrier wait is bounded; on a timeout the
+// kernel records an error, waits (bounded) for its MMAs and frees its
+// tensor memory before leaving.
+namespace tc {
+constexpr int S = 3;              // A stages
+constexpr int G = 3;              // K-chunks per stage (27 Cin / 16 is a multiple of 3)
+constexpr int STAGE = G * 4096;   // bytes per stage
+
+__device__ __forceinline__ unsigned saddr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, leading and stride byte
+// offsets (16-byte units), descriptor version 1, no swizzle
+__device__ __forceinline__ unsigned long long sdesc(unsigned addr, unsigned lbo, unsigned sbo) {
+    return (unsigned long long)((addr >> 4) & 0x3FFFu) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor, kind::f16: fp32 accumulator, bf16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr unsigned idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void bar_init(unsigned long long *b) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(b)) : "memory");
+}
+__device__ __forceinline__ bool bar_wait(unsigned long long *b, unsigned parity) {
+    for (long long spins = 0; spins < (1ll << 24); ++spins) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(saddr(b)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (spins > 64) __nanosleep(32);
+    }
+    return false;
+}
+__device__ __forceinline__ void mma(unsigned tmem, unsigned long long a, unsigned long long b, unsigned idesc,
+                                    int accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void commit(unsigned long long *b) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(saddr(b))
+                 : "memory");
+}
+__device__ __forceinline__ void ld16(unsigned taddr, unsigned (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+
+__host__ __device__ constexpr int ncols(int N) { return N < 32 ? 32 : N; }
+inline size_t smem_bytes(int Cin, int N) {
+    return (size_t)(27 * Cin / 16) * N * 32 + (size_t)S * STAGE + 8 * (S + 1) + 16;
+}
+}  // namespace tc
+
+template <int N>
+__global__ void __launch_bounds__(128) k_conv_fwd_tc(Geom g, Slice in, int Cin, const __nv_bfloat16 *__restrict__ w,
+                                                     const float *__restrict__ bias, Slice out,
+                                                     float *__restrict__ out_f32, int relu, int *status) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int K = 27 * Cin, KC = K / 16, CC = Cin / 16;
+    unsigned char *Bs = sm;                            // KC chunks of N x 16 bf16
+    unsigned char *As = sm + (size_t)KC * N * 32;      // S stages of G x (128 x 16 bf16)
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(As + tc::S * tc::STAGE);  // stages + done
+    unsigned *tslot = reinterpret_cast<unsigned *>(bars + tc::S + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights into the core-matrix layout, 16-byte pieces (8 consecutive k of one n)
+    for (int pc = tid; pc < N * (K / 8); pc += 128) {
+        const int n = pc / (K / 8), k8 = pc % (K / 8);
+        unsigned char *dst = Bs + (size_t)(k8 >> 1) * N * 32 + (n >> 3) * 256 + (k8 & 1) * 128 + (n & 7) * 16;
+        *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(w + (size_t)n * K + (size_t)k8 * 8);
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    if (tid == 0) {
+        for (int i = 0; i <= tc::S; ++i) tc::bar_init(bars + i);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::saddr(tslot)),
+                     "r"(tc::ncols(N))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const unsigned tmem = *tslot;
+    constexpr unsigned IDESC = tc::idesc_bf16(128, N);
+    const long nv = g.voxels();
+    const long tiles = (nv + 127) / 128;
+    long gc = 0;             // K-chunks issued by this CTA (stage = gc % S)
+    unsigned done_phase = 0;
+    bool ok = true;
+    for (long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const long v = tile * 128 + tid;
+        const bool valid = v < nv;
+        int bb = 0, z = 0, y = 0, x = 0;
+        unflat(g, valid ? v : 0, bb, z, y, x);
+        // K-chunks in groups of G per stage; the next group's global loads are
+        // issued before the barrier that hands the current group to the MMA
+        uint4 pre[2 * tc::G];
+        auto load_group = [&](int gi) {
+#pragma unroll
+            for (int j = 0; j < tc::G; ++j) {
+                const int c = gi * tc::G + j;
+                const int tap = c / CC, ci0 = (c % CC) * 16;
+                const int zz = z + tap / 9 - 1, yy = y + (tap / 3) % 3 - 1, xx = x + tap % 3 - 1;
+                uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
+                if (valid && zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W) {
+                    const __nv_bfloat16 *src =
+                        in.p + ((((long)bb * g.D + zz) * g.H + yy) * g.W + xx) * in.stride + in.off + ci0;
+                    lo = *reinterpret_cast<const uint4 *>(src);
+                    hi = *reinterpret_cast<const uint4 *>(src + 8);
+                }
+                pre[2 * j] = lo;
+                pre[2 * j + 1] = hi;
+            }
+        };
+        const int NGRP = KC / tc::G;
+        load_group(0);
+        for (int gi = 0; gi < NGRP; ++gi, ++gc) {
+            const int s = (int)(gc % tc::S);
+            bool okw = true;
+            if (gc >= tc::S) okw = tc::bar_wait(bars + s, (unsigned)((gc / tc::S - 1) & 1));
+            unsigned char *stage = As + (size_t)s * tc::STAGE;
+#pragma unroll
+            for (int j = 0; j < tc::G; ++j) {
+                unsigned char *a = stage + j * 4096 + (tid >> 3) * 256 + (tid & 7) * 16;
+                *reinterpret_cast<uint4 *>(a) = pre[2 * j];
+                *reinterpret_cast<uint4 *>(a + 128) = pre[2 * j + 1];
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            if (gi + 1 < NGRP) load_group(gi + 1);
+            if (__syncthreads_or(!okw)) {
+                ok = false;
+                break;
+            }
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+                for (int j = 0; j < tc::G; ++j) {
+                    const int c = gi * tc::G + j;
+                    const unsigned long long ad = tc::sdesc(tc::saddr(stage + j * 4096), 128, 256);
+                    const unsigned long long bd = tc::sdesc(tc::saddr(Bs + (size_t)c * N * 32), 128, 256);
+                    tc::mma(tmem, ad, bd, IDESC, c > 0 ? 1 : 0);
+                }
+                tc::commit(bars + s);
+            }
+        }
+        if (!ok) break;
+        if (tid == 0) tc::commit(bars + tc::S);
+        const bool okd = tc::bar_wait(bars + tc::S, done_phase);
+        done_phase ^= 1u;
+        if (__syncthreads_or(!okd)) {
+            ok = false;
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        unsigned r[N];
+#pragma unroll
+        for (int q = 0; q < N / 16; ++q) {
+            unsigned part[16];
+            tc::ld16(tmem + ((unsigned)(32 * warp) << 16) + 16 * q, part);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) r[16 * q + e] = part[e];
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (valid) {
+#pragma unroll
+            for (int co = 0; co < N; ++co) {
+                float val = __uint_as_float(r[co]) + (bias ? bias[co] : 0.f);
+                if (relu) val = fmaxf(val, 0.f);
+                if (out_f32) out_f32[v * N + co] = val;
+                if (out.p) out.p[v * out.stride + out.off + co] = __float2bfloat16(val);
+            }
+        }
+        // every warp has read the accumulator before the next tile's first MMA
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+    }
+    if (!ok) {
+        if (tid == 0) {
+            atomicExch(status, (int)DEV_MMA_TIMEOUT);
+            tc::commit(bars + tc::S);
+        }
+        tc::bar_wait(bars + tc::S, done_phase);  // the MMAs issued so far (bounded)
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(tc::ncols(N))
+                     : "memory");
 }
 
 // Weight gradient for one tap: dw[co][tap][ci] += sum_v dout[v][co] * in[v+tap][ci].
@@ -431,8 +652,23 @@ inline int grid_n(long work, int cap = 4096) {
     return (int)(g < cap ? g : cap);
 }
 
+// engine 1: tcgen05 kernel (Cout 16, 32 or 64); engine 0: mma.sync kernel
 void conv_fwd(cudaStream_t st, Geom g, Slice in, int cin, const __nv_bfloat16 *w, const float *b, Slice out,
-              float *out32, int cout, bool relu) {
+              float *out32, int cout, bool relu, int engine = 0, int num_sms = 0, int *status = nullptr) {
+    if (engine == 1 && (cout == 16 || cout == 32 || cout == 64) && status) {
+        const size_t sm = tc::smem_bytes(cin, cout);
+        const long tiles = (g.voxels() + 127) / 128;
+        const int grid = (int)std::min<long>(tiles, (long)num_sms * 8);
+        const void *fn = cout == 16 ? (const void *)k_conv_fwd_tc<16>
+                                    : (cout == 32 ? (const void *)k_conv_fwd_tc<32> : (const void *)k_conv_fwd_tc<64>);
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        switch (cout) {
+            case 16: k_conv_fwd_tc<16><<<grid, 128, sm, st>>>(g, in, cin, w, b, out, out32, relu, status); break;
+            case 32: k_conv_fwd_tc<32><<<grid, 128, sm, st>>>(g, in, cin, w, b, out, out32, relu, status); break;
+            case 64: k_conv_fwd_tc<64><<<grid, 128, sm, st>>>(g, in, cin, w, b, out, out32, relu, status); break;
+        }
+        return;
+    }
     const long warps = (g.voxels() + 15) / 16;
     const int ctas = (int)((warps + 3) / 4);
     switch (cout / 8) {
@@ -454,6 +690,7 @@ void conv_wgrad(cudaStream_t st, Geom g, Slice in, int cin, Slice dout, int cout
 
 struct Surrogate {
     Handle *h = nullptr;
+    int engine = 1;  // forward and data-gradient convolutions: 0 mma.sync, 1 tcgen05
     int n_solver = 0, factor = 2, m = 0, batch_max = 0;
     double L = 0;
     sg::FeatParams fp{};
@@ -495,18 +732,18 @@ void forward(Surrogate &s, int B) {
     const auto &Ly = s.net.L;
     auto W = [&](int i) { return s.wb + Ly[i].w_off; };
     auto Bi = [&](int i) { return s.w32 + Ly[i].b_off; };
-    sg::conv_fwd(st, g0, Slice{s.x0, 16, 0}, 16, W(0), Bi(0), Slice{s.t0, 16, 0}, nullptr, 16, true);
-    sg::conv_fwd(st, g0, Slice{s.t0, 16, 0}, 16, W(1), Bi(1), Slice{s.c0, 32, 16}, nullptr, 16, true);
+    sg::conv_fwd(st, g0, Slice{s.x0, 16, 0}, 16, W(0), Bi(0), Slice{s.t0, 16, 0}, nullptr, 16, true, s.engine, s.h->num_sms, s.h->dev_status);
+    sg::conv_fwd(st, g0, Slice{s.t0, 16, 0}, 16, W(1), Bi(1), Slice{s.c0, 32, 16}, nullptr, 16, true, s.engine, s.h->num_sms, s.h->dev_status);
     sg::k_pool2<<<sg::grid_n(g1.voxels() * 16), 256, 0, st>>>(g1, 16, Slice{s.c0, 32, 16}, Slice{s.p1, 16, 0});
-    sg::conv_fwd(st, g1, Slice{s.p1, 16, 0}, 16, W(2), Bi(2), Slice{s.t1, 32, 0}, nullptr, 32, true);
-    sg::conv_fwd(st, g1, Slice{s.t1, 32, 0}, 32, W(3), Bi(3), Slice{s.c1, 64, 32}, nullptr, 32, true);
+    sg::conv_fwd(st, g1, Slice{s.p1, 16, 0}, 16, W(2), Bi(2), Slice{s.t1, 32, 0}, nullptr, 32, true, s.engine, s.h->num_sms, s.h->dev_status);
+    sg::conv_fwd(st, g1, Slice{s.t1, 32, 0}, 32, W(3), Bi(3), Slice{s.c1, 64, 32}, nullptr, 32, true, s.engine, s.h->num_sms, s.h->dev_status);
     sg::k_pool2<<<sg::grid_n(g2.voxels() * 32), 256, 0, st>>>(g2, 32, Slice{s.c1, 64, 32}, Slice{s.p2, 32, 0});
-    sg::conv_fwd(st, g2, Slice{s.p2, 32, 0}, 32, W(4), Bi(4), Slice{s.q2, 32, 0}, nullptr, 32, true);
+    sg::conv_fwd(st, g2, Slice{s.p2, 32, 0}, 32, W(4), Bi(4), Slice{s.q2, 32, 0}, nullptr, 32, true, s.engine, s.h->num_sms, s.h->dev_status);
     sg::k_up2<<<sg::grid_n(g1.voxels() * 32), 256, 0, st>>>(g1, 32, Slice{s.q2, 32, 0}, Slice{s.c1, 64, 0});
-    sg::conv_fwd(st, g1, Slice{s.c1, 64, 0}, 64, W(5), Bi(5), Slice{s.u1, 16, 0}, nullptr, 16, true);
+    sg::conv_fwd(st, g1, Slice{s.c1, 64, 0}, 64, W(5), Bi(5), Slice{s.u1, 16, 0}, nullptr, 16, true, s.engine, s.h->num_sms, s.h->dev_status);
     sg::k_up2<<<sg::grid_n(g0.voxels() * 16), 256, 0, st>>>(g0, 16, Slice{s.u1, 16, 0}, Slice{s.c0, 32, 0});
-    sg::conv_fwd(st, g0, Slice{s.c0, 32, 0}, 32, W(6), Bi(6), Slice{s.u0, 16, 0}, nullptr, 16, true);
-    sg::conv_fwd(st, g0, Slice{s.u0, 16, 0}, 16, W(7), Bi(7), Slice{nullptr, 0, 0}, s.logits, 16, false);
+    sg::conv_fwd(st, g0, Slice{s.c0, 32, 0}, 32, W(6), Bi(6), Slice{s.u0, 16, 0}, nullptr, 16, true, s.engine, s.h->num_sms, s.h->dev_status);
+    sg::conv_fwd(st, g0, Slice{s.u0, 16, 0}, 16, W(7), Bi(7), Slice{nullptr, 0, 0}, s.logits, 16, false, s.engine, s.h->num_sms, s.h->dev_status);
     s.h->launches += 12;
 }
 
@@ -515,7 +752,8 @@ void data_grad(Surrogate &s, Geom g, int i, Slice dout, Slice din) {
     const auto &l = s.net.L[i];
     const long n = (long)l.cout * 27 * l.cin;
     sg::k_flip_weights<<<sg::grid_n(n), 256, 0, s.h->stream>>>(s.wb + l.w_off, l.cout, l.cin, s.wflip);
-    sg::conv_fwd(s.h->stream, g, dout, l.cout, s.wflip, nullptr, din, nullptr, l.cin, false);
+    sg::conv_fwd(s.h->stream, g, dout, l.cout, s.wflip, nullptr, din, nullptr, l.cin, false, s.engine, s.h->num_sms,
+                 s.h->dev_status);
     s.h->launches += 2;
 }
 
@@ -733,6 +971,14 @@ void surrogate_destroy(Surrogate *s) {
 
 long surrogate_nparams(const Surrogate &s) { return s.net.nparams; }
 int surrogate_batch_max(const Surrogate &s) { return s.batch_max; }
+int surrogate_set_engine(Surrogate &s, int engine) {
+    if (engine != 0 && engine != 1) {
+        set_error("convolution engine: 0 (mma.sync) or 1 (tcgen05)");
+        return GBG_ERR_ARG;
+    }
+    s.engine = engine;
+    return GBG_OK;
+}
 const float *surrogate_prediction(const Surrogate &s) { return s.up_pred; }
 
 int surrogate_get_params(Surrogate &s, float *out) {
@@ -762,7 +1008,7 @@ int surrogate_loss_grad(Surrogate &s, const gbg_sample *samples, int B, const fl
         GBG_CUDA_TRY(cudaMemcpyAsync(grad_host, s.g32, s.net.nparams * sizeof(float), cudaMemcpyDeviceToHost, st));
         GBG_CUDA_TRY(cudaStreamSynchronize(st));
     }
-    return GBG_OK;
+    return check_device_status(*s.h);
 }
 
 // features of B samples (host copy, [B][m^3][16] as float) for the oracle
@@ -860,6 +1106,7 @@ int surrogate_train(Surrogate &s, const gbg_sample *samples, int S, int epochs, 
     cudaFree(targets);
     if (rc) return rc;
     GBG_CUDA_TRY(cudaGetLastError());
+    if (int st_rc = check_device_status(h)) return st_rc;
     if (loss_out) *loss_out = last;
     return GBG_OK;
 }

@@ -243,6 +243,11 @@ int gbg_surrogate_features(gbg_surrogate *s, const gbg_sample *samples, int B, f
  * the B predicted densities on the solver grid */
 int gbg_surrogate_loglik(gbg_surrogate *s, const gbg_sample *samples, int B, gbg_lik_result *out,
                          float *phi);
+/* the kernels of the forward and data-gradient convolutions: 0 = mma.sync
+ * (m16n8k16 bf16 tiles in registers), 1 = tcgen05 (128 x Cout tiles,
+ * accumulator in tensor memory, operands in shared memory). The weight
+ * gradient always runs on mma.sync. Default 1. */
+int gbg_surrogate_set_engine(gbg_surrogate *s, int engine);
 
 /* ---- multiresolution block grid ----------------------------------------------
  * MRAG's grid of 16^3 blocks at mixed levels (source/MRAGcore/MRAGrid.h:44-186):
