@@ -374,6 +374,46 @@ def amr_measurement(device, level=4, steps=20, err_steps=60):
     return out
 
 
+def surrogate_measurement(device, n=128, batch=32, reps=5):
+    """Forward throughput of the bf16 U-Net surrogate at n^3 (its grid is
+    (n/2)^3): milliseconds per sample of gbg_surrogate_loglik (features,
+    network, upsampling, likelihood) on each convolution engine, and the
+    network's effective TFLOP/s (2 * 27 * Cin * Cout per voxel and layer)."""
+    from gliomauq_gb300 import _lib, synthetic as Syn
+    an = Syn.make_anatomy(n, seed=0)
+    lo = (Syn.PRIOR_DW_CM2[0], Syn.PRIOR_RHO[0], Syn.PRIOR_T[0])
+    hi = (Syn.PRIOR_DW_CM2[1], Syn.PRIOR_RHO[1], Syn.PRIOR_T[1])
+    h = _lib.Handle(n, "f32", device=device, max_samples=batch)
+    h.set_anatomy(an.p_w, an.p_g)
+    truth = Syn.draw_prior(an, 1, seed=10_000)[0]
+    u = h.batch_solve([truth.as_tuple()], an.L, with_loglik=False, want_phi=True)["phi"][0]
+    obs = Syn.make_observations(u.astype(np.float64), an, seed=3,
+                                centre_xyz=(truth.x0, truth.y0, truth.z0), radius_vox=27.0 * n / 128)
+    h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2)
+    sg = _lib.Surrogate(h, an.L, lo, hi, batch_max=batch, seed=7)
+    smp = [p.as_tuple() for p in Syn.draw_prior(an, batch, seed=5)]
+    m = n // 2
+    layers = [(16, 16, m), (16, 16, m), (16, 32, m // 2), (32, 32, m // 2), (32, 32, m // 4),
+              (64, 16, m // 2), (32, 16, m), (16, 16, m)]
+    flops = float(sum(2 * 27 * ci * co * v ** 3 for ci, co, v in layers))
+    out = {"grid": f"{n}^3 (network on {m}^3)", "batch": batch, "params": sg.nparams(),
+           "flops_per_sample": flops}
+    try:
+        for eng in ("tcgen05", "mma.sync"):
+            sg.set_engine(eng)
+            sg.loglik(smp)
+            h.sync()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                sg.loglik(smp)
+            t = (time.perf_counter() - t0) / reps / batch
+            out[eng] = {"ms_per_sample": 1e3 * t, "effective_tflops": flops / t / 1e12}
+    finally:
+        sg.close()
+        h.close()
+    return out
+
+
 def run_reference_arm(args):
     rank, _, world = rank_info()
     if rank != 0:
@@ -409,11 +449,18 @@ def main():
                     help="skip the ESS/s comparison of plain and batched MALA sampling")
     ap.add_argument("--no-amr", action="store_true",
                     help="skip the multiresolution-grid measurement")
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="skip the surrogate-network measurement")
+    ap.add_argument("--only-surrogate", action="store_true",
+                    help="print the surrogate-network measurement alone (profiling runs)")
     ap.add_argument("--samples", type=int, default=S,
                     help="population size (profiling runs use a smaller one)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.only_surrogate:
+        print(json.dumps({"surrogate": surrogate_measurement(int(os.environ.get("LOCAL_RANK", "0")))}))
+        return
     set_population(args.samples)
 
     import torch
@@ -525,6 +572,8 @@ def main():
             line["mcmc"] = mcmc_comparison(local_rank)
         if not args.no_amr:
             line["amr"] = amr_measurement(local_rank)
+        if not args.no_surrogate:
+            line["surrogate"] = surrogate_measurement(local_rank)
         print(json.dumps(line))
     h.close()
     if world > 1:

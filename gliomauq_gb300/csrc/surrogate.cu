@@ -344,6 +344,175 @@ __global__ void __launch_bounds__(128) k_conv_fwd_tc(Geom g, Slice in, int Cin, 
                      : "memory");
 }
 
+// Halo-tile variant (grids with W % 8 == 0 and H % 16 == 0): an output tile
+// is 8 (x) x 16 (y) voxels of one z-plane of one sample, M = 128 rows ordered
+// x-fastest. Its input halo, 10 (x) x 18 (y) x 3 (z) voxels, is loaded into
+// shared memory once, one array per 8-channel chunk, voxels x-fastest at 16
+// bytes each: 8 consecutive x-voxels of a chunk are one 128-byte core matrix.
+// The A operand of tap (dx, dy, dz) is then a descriptor into the halo tile
+// (start = the tap's offset, stride byte offset = one halo row = 160 B,
+// leading byte offset = one chunk array), so all 27 Cin / 16 MMAs of a tile
+// are issued back to back without gathering.
+namespace tc {
+constexpr int HX = 10, HY = 18, HZ = 3;
+constexpr int HALO_CHUNK = HX * HY * HZ * 16;  // bytes per 8-channel chunk array (8640)
+inline size_t halo_smem_bytes(int Cin, int N) {  // weights, two halo buffers, barrier, tmem slot
+    return (size_t)(27 * Cin / 16) * N * 32 + 2 * (size_t)(Cin / 8) * HALO_CHUNK + 8 * 2 + 16;
+}
+}  // namespace tc
+
+template <int N>
+__global__ void __launch_bounds__(128) k_conv_fwd_tc_halo(Geom g, Slice in, int Cin, const __nv_bfloat16 *__restrict__ w,
+                                                          const float *__restrict__ bias, Slice out,
+                                                          float *__restrict__ out_f32, int relu, int *status) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int K = 27 * Cin, KC = K / 16, CC = Cin / 16, C8 = Cin / 8;
+    unsigned char *Bs = sm;                                   // KC chunks of N x 16 bf16
+    unsigned char *Hs = sm + (size_t)KC * N * 32;             // two halo tiles of C8 chunk arrays
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(Hs + 2 * (size_t)C8 * tc::HALO_CHUNK);
+    unsigned *tslot = reinterpret_cast<unsigned *>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int pc = tid; pc < N * (K / 8); pc += 128) {
+        const int n = pc / (K / 8), k8 = pc % (K / 8);
+        unsigned char *dst = Bs + (size_t)(k8 >> 1) * N * 32 + (n >> 3) * 256 + (k8 & 1) * 128 + (n & 7) * 16;
+        *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(w + (size_t)n * K + (size_t)k8 * 8);
+    }
+    if (tid == 0) {
+        tc::bar_init(bars);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::saddr(tslot)),
+                     "r"(tc::ncols(N))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const unsigned tmem = *tslot;
+    constexpr unsigned IDESC = tc::idesc_bf16(128, N);
+    const int tx = g.W / 8, ty = g.H / 16;
+    const long tiles = (long)g.B * g.D * ty * tx;
+    const size_t halo_bytes = (size_t)C8 * tc::HALO_CHUNK;
+    // halo tile of `tile` into buffer `buf` (each thread fences its own stores)
+    auto load_tile = [&](long tile, int buf) {
+        const int x0 = (int)(tile % tx) * 8;
+        long t = tile / tx;
+        const int y0 = (int)(t % ty) * 16;
+        t /= ty;
+        const int z = (int)(t % g.D);
+        const int bb = (int)(t / g.D);
+        unsigned char *H = Hs + (size_t)buf * halo_bytes;
+        const int entries = C8 * tc::HX * tc::HY * tc::HZ;
+        for (int e = tid; e < entries; e += 128) {
+            const int hx = e % tc::HX;
+            int r = e / tc::HX;
+            const int hy = r % tc::HY;
+            r /= tc::HY;
+            const int hz = r % tc::HZ, k8 = r / tc::HZ;
+            const int xx = x0 + hx - 1, yy = y0 + hy - 1, zz = z + hz - 1;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (xx >= 0 && xx < g.W && yy >= 0 && yy < g.H && zz >= 0 && zz < g.D)
+                v = *reinterpret_cast<const uint4 *>(
+                    in.p + ((((long)bb * g.D + zz) * g.H + yy) * g.W + xx) * in.stride + in.off + k8 * 8);
+            *reinterpret_cast<uint4 *>(H + (size_t)k8 * tc::HALO_CHUNK + ((hz * tc::HY + hy) * tc::HX + hx) * 16) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    };
+    unsigned done_phase = 0;
+    bool ok = true;
+    int buf = 0;
+    if (blockIdx.x < tiles) load_tile(blockIdx.x, 0);
+    __syncthreads();
+    for (long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, buf ^= 1) {
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const unsigned char *H = Hs + (size_t)buf * halo_bytes;
+            for (int tap = 0; tap < 27; ++tap) {
+                const int dx = tap % 3, dy = (tap / 3) % 3, dz = tap / 9;  // halo offsets of the tap
+                const unsigned toff = ((dz * tc::HY + dy) * tc::HX + dx) * 16;
+                for (int cc = 0; cc < CC; ++cc) {
+                    const int c = tap * CC + cc;
+                    // K-chunk cc = channel chunks 2cc and 2cc+1: leading byte offset = one chunk array
+                    const unsigned long long ad =
+                        tc::sdesc(tc::saddr(H + (size_t)(2 * cc) * tc::HALO_CHUNK + toff), tc::HALO_CHUNK, tc::HX * 16);
+                    const unsigned long long bd = tc::sdesc(tc::saddr(Bs + (size_t)c * N * 32), 128, 256);
+                    tc::mma(tmem, ad, bd, IDESC, c > 0 ? 1 : 0);
+                }
+            }
+            tc::commit(bars);
+        }
+        // the next tile's halo goes to the other buffer while the MMAs run
+        // (that buffer's previous MMAs completed before the last epilogue)
+        if (tile + gridDim.x < tiles) load_tile(tile + gridDim.x, buf ^ 1);
+        const bool okd = tc::bar_wait(bars, done_phase);
+        done_phase ^= 1u;
+        if (__syncthreads_or(!okd)) {
+            ok = false;
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        unsigned r[N];
+#pragma unroll
+        for (int q = 0; q < N / 16; ++q) {
+            unsigned part[16];
+            tc::ld16(tmem + ((unsigned)(32 * warp) << 16) + 16 * q, part);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) r[16 * q + e] = part[e];
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        // row m = tid: x = x0 + m % 8, y = y0 + m / 8
+        {
+            const int x0 = (int)(tile % tx) * 8;
+            long t = tile / tx;
+            const int y0 = (int)(t % ty) * 16;
+            t /= ty;
+            const int z = (int)(t % g.D);
+            const int bb = (int)(t / g.D);
+            const long v = (((long)bb * g.D + z) * g.H + (y0 + tid / 8)) * g.W + (x0 + tid % 8);
+            float val[N];
+#pragma unroll
+            for (int co = 0; co < N; ++co) {
+                val[co] = __uint_as_float(r[co]) + (bias ? bias[co] : 0.f);
+                if (relu) val[co] = fmaxf(val[co], 0.f);
+            }
+            if (out_f32) {
+#pragma unroll
+                for (int q = 0; q < N / 4; ++q)
+                    *reinterpret_cast<float4 *>(out_f32 + v * N + 4 * q) =
+                        make_float4(val[4 * q], val[4 * q + 1], val[4 * q + 2], val[4 * q + 3]);
+            }
+            if (out.p) {
+                // 8 channels per 16-byte store (the slice offset and stride are multiples of 8)
+#pragma unroll
+                for (int q = 0; q < N / 8; ++q) {
+                    uint4 pk;
+                    pk.x = pack2(__float2bfloat16(val[8 * q]), __float2bfloat16(val[8 * q + 1]));
+                    pk.y = pack2(__float2bfloat16(val[8 * q + 2]), __float2bfloat16(val[8 * q + 3]));
+                    pk.z = pack2(__float2bfloat16(val[8 * q + 4]), __float2bfloat16(val[8 * q + 5]));
+                    pk.w = pack2(__float2bfloat16(val[8 * q + 6]), __float2bfloat16(val[8 * q + 7]));
+                    *reinterpret_cast<uint4 *>(out.p + v * out.stride + out.off + 8 * q) = pk;
+                }
+            }
+        }
+        // the accumulator is read, and the next halo stored, before the next tile's MMAs
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+    }
+    if (!ok) {
+        if (tid == 0) atomicExch(status, (int)DEV_MMA_TIMEOUT);
+        tc::bar_wait(bars, done_phase);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(tc::ncols(N))
+                     : "memory");
+}
+
 // Weight gradient for one tap: dw[co][tap][ci] += sum_v dout[v][co] * in[v+tap][ci].
 // M = Cout (16-row tiles), N = Cin (8-col tiles), K = voxels in chunks of 16.
 // Each warp handles one (m-tile, n-tile) over a voxel range.
@@ -465,14 +634,17 @@ __global__ void k_pool2_bwd(Geom gi, int C, Slice dout, Slice din) {
 
 // 2x nearest upsampling: out (fine) <- in (coarse); and its transpose (sum of 8)
 __global__ void k_up2(Geom gf, int C, Slice in, Slice out) {
-    const long n = gf.voxels() * C;
+    // 8 channels (16 bytes) per item: C, the strides and offsets are multiples of 8
+    const int C8 = C / 8;
+    const long n = gf.voxels() * C8;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const long v = i / C;
-        const int c = (int)(i % C);
+        const long v = i / C8;
+        const int c = (int)(i % C8) * 8;
         int b, z, y, x;
         unflat(gf, v, b, z, y, x);
         const long vc = (((long)b * (gf.D / 2) + z / 2) * (gf.H / 2) + y / 2) * (gf.W / 2) + x / 2;
-        out.p[v * out.stride + out.off + c] = in.p[vc * in.stride + in.off + c];
+        *reinterpret_cast<uint4 *>(out.p + v * out.stride + out.off + c) =
+            *reinterpret_cast<const uint4 *>(in.p + vc * in.stride + in.off + c);
     }
 }
 
@@ -553,18 +725,27 @@ __global__ void k_features(int S, int n, int factor, const gbg_sample *__restric
         const long s = i / N, c = i % N;
         const int xx = (int)(c % n), yy = (int)((c / n) % n), zz = (int)(c / ((long)n * n));
         const gbg_sample q = smp[s];
-        // cell centre in solver voxel units
-        const double px = (xx + 0.5) * factor - 0.5, py = (yy + 0.5) * factor - 0.5, pz = (zz + 0.5) * factor - 0.5;
-        const double d2 = (px - q.x0) * (px - q.x0) + (py - q.y0) * (py - q.y0) + (pz - q.z0) * (pz - q.z0);
-        const double blob = exp(-d2 / (2.0 * fp.blob_sigma * fp.blob_sigma));
+        // per-sample scalars in double; per-cell geometry in float (the
+        // features are rounded to bf16)
         // front speed 2 sqrt(D rho) in voxels/day: D in voxel^2/day = Dw / L^2 * n_solver^2
         const double dvox = q.Dw / (fp.L * fp.L) * fp.n_solver * fp.n_solver;
-        const double front = 2.0 * sqrt(dvox * q.rho) * q.tend;
-        const float f[7] = {pw[c], pg[c], (float)blob, (float)((q.Dw - fp.dw_lo) / (fp.dw_hi - fp.dw_lo)),
+        const float front = (float)(2.0 * sqrt(dvox * q.rho) * q.tend);
+        const float inv2s2 = (float)(1.0 / (2.0 * fp.blob_sigma * fp.blob_sigma));
+        // cell centre in solver voxel units
+        const float dx = (float)((xx + 0.5) * factor - 0.5 - q.x0), dy = (float)((yy + 0.5) * factor - 0.5 - q.y0),
+                    dz = (float)((zz + 0.5) * factor - 0.5 - q.z0);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float f[7] = {pw[c], pg[c], expf(-d2 * inv2s2), (float)((q.Dw - fp.dw_lo) / (fp.dw_hi - fp.dw_lo)),
                             (float)((q.rho - fp.rho_lo) / (fp.rho_hi - fp.rho_lo)),
-                            (float)((q.tend - fp.t_lo) / (fp.t_hi - fp.t_lo)), (float)((sqrt(d2) - front) / 16.0)};
-        __nv_bfloat16 *o = x + i * 16;
-        for (int k = 0; k < 16; ++k) o[k] = __float2bfloat16(k < 7 ? f[k] : 0.f);
+                            (float)((q.tend - fp.t_lo) / (fp.t_hi - fp.t_lo)), (sqrtf(d2) - front) * (1.0f / 16.0f)};
+        uint4 lo, hi = make_uint4(0, 0, 0, 0);
+        lo.x = pack2(__float2bfloat16(f[0]), __float2bfloat16(f[1]));
+        lo.y = pack2(__float2bfloat16(f[2]), __float2bfloat16(f[3]));
+        lo.z = pack2(__float2bfloat16(f[4]), __float2bfloat16(f[5]));
+        lo.w = pack2(__float2bfloat16(f[6]), __float2bfloat16(0.f));
+        uint4 *o = reinterpret_cast<uint4 *>(x + i * 16);
+        o[0] = lo;
+        o[1] = hi;
     }
 }
 
@@ -655,6 +836,21 @@ inline int grid_n(long work, int cap = 4096) {
 // engine 1: tcgen05 kernel (Cout 16, 32 or 64); engine 0: mma.sync kernel
 void conv_fwd(cudaStream_t st, Geom g, Slice in, int cin, const __nv_bfloat16 *w, const float *b, Slice out,
               float *out32, int cout, bool relu, int engine = 0, int num_sms = 0, int *status = nullptr) {
+    if (engine == 1 && (cout == 16 || cout == 32 || cout == 64) && status && g.W % 8 == 0 && g.H % 16 == 0) {
+        const size_t sm = tc::halo_smem_bytes(cin, cout);
+        const long tiles = (long)g.B * g.D * (g.H / 16) * (g.W / 8);
+        const int grid = (int)std::min<long>(tiles, (long)num_sms * 8);
+        const void *fn = cout == 16 ? (const void *)k_conv_fwd_tc_halo<16>
+                                    : (cout == 32 ? (const void *)k_conv_fwd_tc_halo<32>
+                                                  : (const void *)k_conv_fwd_tc_halo<64>);
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        switch (cout) {
+            case 16: k_conv_fwd_tc_halo<16><<<grid, 128, sm, st>>>(g, in, cin, w, b, out, out32, relu, status); break;
+            case 32: k_conv_fwd_tc_halo<32><<<grid, 128, sm, st>>>(g, in, cin, w, b, out, out32, relu, status); break;
+            case 64: k_conv_fwd_tc_halo<64><<<grid, 128, sm, st>>>(g, in, cin, w, b, out, out32, relu, status); break;
+        }
+        return;
+    }
     if (engine == 1 && (cout == 16 || cout == 32 || cout == 64) && status) {
         const size_t sm = tc::smem_bytes(cin, cout);
         const long tiles = (g.voxels() + 127) / 128;
