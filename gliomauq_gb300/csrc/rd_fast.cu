@@ -40,9 +40,11 @@
 // one-plane-ahead prefetch), cp.async rings (k_population3), and bulk-copy
 // rings fed by the TMA unit with mbarrier completion (k_population5: one
 // elected thread issues, a block barrier per plane; k_population6: a
-// producer warp and full/empty barriers per slot, no block barriers). All
-// run the same per-cell operation sequence, so every variant gives the same
-// bits.
+// producer warp and full/empty barriers per slot, no block barriers), and
+// temporal blocking (k_population7: two steps per round through a
+// shared-memory ring of first-step planes, density read and written once per
+// two steps). All run the same per-cell operation sequence, so every variant
+// gives the same bits.
 #include <vector>
 
 #include "gbg_internal.cuh"
@@ -180,10 +182,14 @@ __global__ void k_sort_schedule(const SampleRec *__restrict__ unsorted, int S,
     rank_of[s] = r;
 }
 
+// phi1 and recs non-null (temporally blocked population kernels): sample s
+// starts in phi1 when (nsteps_s / 2) is odd, so that its final state lands in
+// buffer nsteps_s & 1 like every other population kernel's.
 __global__ void k_gaussian_ic(int n, const gbg_sample *__restrict__ smp, int S, double peak,
                               double sigma, const float *__restrict__ msk_tissue,
                               const double *__restrict__ pw, const double *__restrict__ pg,
-                              float *__restrict__ phi) {
+                              float *__restrict__ phi, float *__restrict__ phi1 = nullptr,
+                              const SampleRec *__restrict__ recs = nullptr) {
     const size_t N = (size_t)n * n * n;
     const size_t total = N * S;
     const double two_s2 = __dmul_rn(__dmul_rn(2.0, sigma), sigma);
@@ -207,7 +213,8 @@ __global__ void k_gaussian_ic(int n, const gbg_sample *__restrict__ smp, int S, 
             // rounds to float 0 for any peak <= 1e+0: skip the FP64 exp there
             if (e > -110.0 || peak > 1.0) v = (float)__dmul_rn(peak, exp(e));
         }
-        phi[i] = v;
+        float *dst = (phi1 && recs && ((recs[s].nsteps / 2) & 1)) ? phi1 : phi;
+        dst[i] = v;
     }
 }
 
@@ -954,6 +961,168 @@ __global__ void __launch_bounds__(LR *RY + 32, MINB) k_population6(PopArgs p) {
     }
 }
 
+// ---- population kernel, two time steps per sweep (temporal blocking) -------------
+// A CTA of 10 warps owns a tile of 8 rows (y0 .. y0+7) x TZ planes. Warp w
+// computes the first step for row y0-1+w (the tile's rows and one halo row
+// on each side) while marching z from tz0-1 to tz0+TZ, with the same
+// per-cell operation sequence as march_tile; the first-step rows go through a
+// 3-plane ring in shared memory, from which warps 1..8 compute the second
+// step of plane z-1 (own row's z-2, z-1, z in registers, rows y-1 and y+1
+// from the ring, x-neighbours by shuffle). Each round advances every active
+// sample by two steps (one when a single step is left), so phi is read and
+// written once per two steps. Rounds alternate the buffers; a sample starts
+// in buffer (nsteps / 2) & 1 (k_gaussian_ic) and ends in nsteps & 1.
+// RELOAD: the second step re-reads its cell's anatomy (an L1/L2 hit: the
+// warp read it one plane earlier) instead of carrying it in registers.
+template <int MINB, bool RELOAD>
+__global__ void __launch_bounds__(320, MINB) k_population7(PopArgs p) {
+    constexpr int LR = 32, n = 128, RY = 8, NW = RY + 2;
+    constexpr size_t plane = (size_t)n * n;
+    __shared__ __align__(16) float ring[3][NW][n];
+    const int w = threadIdx.x / LR, li = threadIdx.x % LR, x0 = 4 * li;
+    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
+    const int rounds = (maxsteps + 1) / 2;
+    int active = p.S;
+    for (int j = 0; j < rounds; ++j) {
+        const int k = 2 * j;  // first step of the round
+        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
+        const long items = (long)active * p.tiles;
+        for (long it = blockIdx.x; it < items; it += gridDim.x) {
+            const int r = (int)(it % active), t = (int)(it / active);
+            const SampleRec rec = p.rec[r];
+            const int y0 = (t % p.tiles_y) * RY, tz0 = (t / p.tiles_y) * p.TZ;
+            const bool two = rec.nsteps - k >= 2;
+            const bool last1 = k == rec.nsteps - 1, last2 = k + 1 == rec.nsteps - 1;
+            const float a1 = last1 ? rec.a2 : rec.a, b1 = last1 ? rec.b2 : rec.b;
+            const float a2 = last2 ? rec.a2 : rec.a, b2 = last2 ? rec.b2 : rec.b;
+            const int s0 = (rec.nsteps / 2) & 1;
+            const float *in = (((j + s0) & 1) ? p.buf1 : p.buf0) + (size_t)rec.order * p.stride;
+            float *out = (((j + s0) & 1) ? p.buf0 : p.buf1) + (size_t)rec.order * p.stride;
+            const int y = (y0 - 1 + w + n) % n;        // this warp's first-step row
+            const int ym = y == 0 ? n - 1 : y - 1, yp = y == n - 1 ? 0 : y + 1;
+            const bool inner = w >= 1 && w <= RY;      // rows of the tile (second step, output)
+            auto at = [&](int yy, int zz) -> unsigned { return (unsigned)(x0 + n * yy) + (unsigned)plane * (unsigned)zz; };
+            auto wz = [&](int zz) { return zz < 0 ? zz + n : (zz >= n ? zz - n : zz); };
+            // first-step state: planes z-1, z in registers; anatomy carried for the second step
+            const int zstart = tz0 - 1;
+            float4 Pp = __ldcg(reinterpret_cast<const float4 *>(in + at(y, wz(zstart - 1))));
+            float4 Pc = __ldcg(reinterpret_cast<const float4 *>(in + at(y, wz(zstart))));
+            float4 CZp = __ldg(reinterpret_cast<const float4 *>(p.cz + at(y, wz(zstart - 1))));
+            // second-step inputs of this row: first-step values of planes z-2, z-1
+            float4 Q2 = make_float4(0, 0, 0, 0), Q1 = Q2;
+            // anatomy of plane z-1 of this row (the second step's cell), and cz of z-2
+            float4 AX = Q2, AY = Q2, AYm = Q2, AZ = Q2, AM = Q2, AZp = Q2;
+            for (int step = 0; step < p.TZ + 2; ++step) {
+                const int z = wz(zstart + step);
+                const int zn = wz(zstart + step + 1);
+                // ---- first step, plane z, row y ----
+                const float4 Pn = __ldcg(reinterpret_cast<const float4 *>(in + at(y, zn)));
+                const float4 PS = __ldcg(reinterpret_cast<const float4 *>(in + at(ym, z)));
+                const float4 PN = __ldcg(reinterpret_cast<const float4 *>(in + at(yp, z)));
+                const float4 CX = __ldg(reinterpret_cast<const float4 *>(p.cx + at(y, z)));
+                const float4 CY = __ldg(reinterpret_cast<const float4 *>(p.cy + at(y, z)));
+                const float4 CYm = __ldg(reinterpret_cast<const float4 *>(p.cy + at(ym, z)));
+                const float4 CZ = __ldg(reinterpret_cast<const float4 *>(p.cz + at(y, z)));
+                const float4 M = __ldg(reinterpret_cast<const float4 *>(p.msk + at(y, z)));
+                float4 F;
+                {
+                    const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
+                    const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
+                    const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
+                    const float pv[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
+                    const float cxa[5] = {cxl, CX.x, CX.y, CX.z, CX.w};
+                    const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
+                    const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
+                    const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
+                    const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
+                    const float m4[4] = {M.x, M.y, M.z, M.w};
+                    float o[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float f0 = pv[i + 1];
+                        float lap = cxa[i] * (pv[i] - f0);
+                        lap = fmaf(cxa[i + 1], pv[i + 2] - f0, lap);
+                        lap = fmaf(cym4[i], ps[i] - f0, lap);
+                        lap = fmaf(cy4[i], pn[i] - f0, lap);
+                        lap = fmaf(czp4[i], pp[i] - f0, lap);
+                        lap = fmaf(cz4[i], pq[i] - f0, lap);
+                        float v = fmaf(a1, lap, f0);
+                        v = fmaf(b1 * f0, 1.0f - f0, v);
+                        v = fminf(fmaxf(v, 0.0f), 1.0f);
+                        o[i] = m4[i] != 0.0f ? v : 0.0f;
+                    }
+                    F = make_float4(o[0], o[1], o[2], o[3]);
+                }
+                const int zo = zstart + step;  // unwrapped plane of F
+                if (!two) {
+                    // one step left: the first step is the output
+                    if (inner && zo >= tz0 && zo < tz0 + p.TZ)
+                        __stcg(reinterpret_cast<float4 *>(out + at(y, z)), F);
+                } else {
+                    *reinterpret_cast<float4 *>(&ring[step % 3][w][x0]) = F;
+                }
+                __syncthreads();
+                // ---- second step, plane z-1 (unwrapped zo-1), rows of the tile ----
+                if (two && step >= 2 && inner) {
+                    const int zc = wz(zo - 1);
+                    if (RELOAD) {
+                        AX = __ldg(reinterpret_cast<const float4 *>(p.cx + at(y, zc)));
+                        AY = __ldg(reinterpret_cast<const float4 *>(p.cy + at(y, zc)));
+                        AYm = __ldg(reinterpret_cast<const float4 *>(p.cy + at(ym, zc)));
+                        AZ = __ldg(reinterpret_cast<const float4 *>(p.cz + at(y, zc)));
+                        AZp = __ldg(reinterpret_cast<const float4 *>(p.cz + at(y, wz(zo - 2))));
+                        AM = __ldg(reinterpret_cast<const float4 *>(p.msk + at(y, zc)));
+                    }
+                    const float4 S1 = *reinterpret_cast<const float4 *>(&ring[(step - 1) % 3][w - 1][x0]);
+                    const float4 N1 = *reinterpret_cast<const float4 *>(&ring[(step - 1) % 3][w + 1][x0]);
+                    const float left = __shfl_sync(0xffffffffu, Q1.w, (li + LR - 1) % LR, LR);
+                    const float right = __shfl_sync(0xffffffffu, Q1.x, (li + 1) % LR, LR);
+                    const float cxl = __shfl_sync(0xffffffffu, AX.w, (li + LR - 1) % LR, LR);
+                    const float pv[6] = {left, Q1.x, Q1.y, Q1.z, Q1.w, right};
+                    const float cxa[5] = {cxl, AX.x, AX.y, AX.z, AX.w};
+                    const float ps[4] = {S1.x, S1.y, S1.z, S1.w}, pn[4] = {N1.x, N1.y, N1.z, N1.w};
+                    const float pp[4] = {Q2.x, Q2.y, Q2.z, Q2.w}, pq[4] = {F.x, F.y, F.z, F.w};
+                    const float cy4[4] = {AY.x, AY.y, AY.z, AY.w}, cym4[4] = {AYm.x, AYm.y, AYm.z, AYm.w};
+                    const float cz4[4] = {AZ.x, AZ.y, AZ.z, AZ.w}, czp4[4] = {AZp.x, AZp.y, AZp.z, AZp.w};
+                    const float m4[4] = {AM.x, AM.y, AM.z, AM.w};
+                    float o[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float f0 = pv[i + 1];
+                        float lap = cxa[i] * (pv[i] - f0);
+                        lap = fmaf(cxa[i + 1], pv[i + 2] - f0, lap);
+                        lap = fmaf(cym4[i], ps[i] - f0, lap);
+                        lap = fmaf(cy4[i], pn[i] - f0, lap);
+                        lap = fmaf(czp4[i], pp[i] - f0, lap);
+                        lap = fmaf(cz4[i], pq[i] - f0, lap);
+                        float v = fmaf(a2, lap, f0);
+                        v = fmaf(b2 * f0, 1.0f - f0, v);
+                        v = fminf(fmaxf(v, 0.0f), 1.0f);
+                        o[i] = m4[i] != 0.0f ? v : 0.0f;
+                    }
+                    __stcg(reinterpret_cast<float4 *>(out + at(y, zc)), make_float4(o[0], o[1], o[2], o[3]));
+                }
+                // shift: this plane's first-step values and anatomy serve the next
+                // iteration's second step (its cell plane is this z)
+                Q2 = Q1;
+                Q1 = F;
+                if (!RELOAD) {
+                    AZp = AZ;
+                    AX = CX;
+                    AY = CY;
+                    AYm = CYm;
+                    AZ = CZ;
+                    AM = M;
+                }
+                Pp = Pc;
+                Pc = Pn;
+                CZp = CZ;
+            }
+        }
+        if (j + 1 < rounds && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
+    }
+}
+
 int grid_for(const Handle &h, size_t work) {
     const size_t blocks = (work + 255) / 256;
     const size_t cap = (size_t)h.num_sms * 8;
@@ -970,6 +1139,7 @@ struct PopVariant {
     const void *fn;
     int ry, g, threads, tz;
     size_t smem;
+    bool tb = false;  // two steps per round (start buffer per sample, see k_gaussian_ic)
 };
 
 template <int LR, int MINB = 1, int PF = 0>
@@ -994,6 +1164,19 @@ PopVariant make_variant(int tz) {
     v.tz = tz;
     const int n = 4 * LR;
     v.smem = (size_t)(4 * (4 * RY + 1) * n + G * 4 * (RY + 2) * n) * sizeof(float);
+    return v;
+}
+
+template <int MINB, bool RELOAD>
+PopVariant make_tb_variant(int tz) {
+    PopVariant v;
+    v.fn = (const void *)k_population7<MINB, RELOAD>;
+    v.ry = 8;
+    v.g = 1;
+    v.threads = 320;
+    v.tz = tz;
+    v.smem = 0;
+    v.tb = true;
     return v;
 }
 
@@ -1035,6 +1218,8 @@ int variants_for(int n, PopVariant *out) {
             out[k++] = make_register_variant<32, 4, 1>(16);
             out[k++] = make_register_variant<32, 5, 1>(16);
             out[k++] = make_register_variant<32, 5, 1>(32);
+            out[k++] = make_tb_variant<2, true>(16);
+            out[k++] = make_tb_variant<2, true>(32);
             out[k++] = make_tma_variant<32, 8, 3, 3>(32);
             out[k++] = make_ws_variant<32, 8, 3, 3>(16);
             out[k++] = make_ws_variant<32, 8, 3, 3>(32);
@@ -1089,7 +1274,17 @@ int launch_population_v(Handle &h, PopArgs &a, const PopVariant &v) {
     return GBG_OK;
 }
 
-int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_sorted, int S) {
+bool variant_is_tb(const Handle &h) {
+    PopVariant vs[32];
+    const int nv = variants_for(h.n, vs);
+    const int vi = h.pop_variant;
+    return vi >= 0 && vi < nv && vs[vi].tb;
+}
+
+// allow_tb = false (the single-solve path, whose state must start in buf0)
+// runs the default variant in place of a temporally blocked one
+int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_sorted, int S,
+                      bool allow_tb = true) {
     const int LR = lanes_per_row(h.n);
     if (!LR) {
         set_error("fast path supports n = 32, 64 or 128");
@@ -1098,7 +1293,7 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
     PopVariant vs[32];
     const int nv = variants_for(h.n, vs);
     int vi = h.pop_variant;
-    if (vi < 0 || vi >= nv) vi = 0;
+    if (vi < 0 || vi >= nv || (vs[vi].tb && !allow_tb)) vi = 0;
     const PopVariant &v = vs[vi];
     PopArgs a;
     a.n = h.n;
@@ -1197,7 +1392,7 @@ int fast_steps_single(Handle &h, double Dw, double rho, double dt, long nsteps) 
     r.b2 = r.b;
     SampleRec *d_rec = reinterpret_cast<SampleRec *>(h.bwork);
     GBG_CUDA_TRY(cudaMemcpyAsync(d_rec, &r, sizeof(r), cudaMemcpyHostToDevice, h.stream));
-    int rc = launch_population(h, (float *)h.phi[h.cur], (float *)h.phi[h.cur ^ 1], d_rec, 1);
+    int rc = launch_population(h, (float *)h.phi[h.cur], (float *)h.phi[h.cur ^ 1], d_rec, 1, false);
     if (rc) return rc;
     rc = check_device_status(h);
     if (rc) return rc;
@@ -1221,9 +1416,11 @@ int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
         k_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(samples_device, S, h.n, o.L, f32ref ? 1 : 0,
                                                           unsorted);
     k_sort_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(unsorted, S, sorted, rank_of);
+    const bool tb = variant_is_tb(h);
     k_gaussian_ic<<<grid_for(h, h.N * S), 256, 0, h.stream>>>(h.n, samples_device, S, o.ic_peak,
                                                                o.ic_sigma, h.msk, h.pw, h.pg,
-                                                               h.bphi[0]);
+                                                               h.bphi[0], tb ? h.bphi[1] : nullptr,
+                                                               tb ? unsorted : nullptr);
     h.launches += 3;
     GBG_CUDA_TRY(cudaGetLastError());
     if (f32ref) {
