@@ -437,6 +437,12 @@ def run_reference_arm(args):
     print(json.dumps(line))
 
 
+# DRAM bytes per cell-step of the population kernel measured by ncu
+# (profiles/k_population8_128_pop64_ncu.md: 268.87 GB read + written for
+# 3.2076e10 cell-steps); traffic grows with the cell-steps of a launch.
+NCU_BYTES_PER_CELL_STEP = 268.869814e9 / 32075939840.0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -557,7 +563,12 @@ def main():
                                                    "threads": shape[2],
                                                    "chosen_by": "gbg_autotune"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": NCU_BYTES_PER_CELL_STEP * cell_steps,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                           "k_population8<32, 4> (TZ 16) on the 64-sample population "
+                                           f"({NCU_BYTES_PER_CELL_STEP:.3f} B per cell-step), scaled "
+                                           "by this launch's cell-steps",
                          "kernel": f"k_population (autotuned variant {variant})", "kernel_ms": kern_ms,
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "peak_source": f"{peak_kind} hbm_gbs"},

@@ -76,7 +76,7 @@ bool all_finite(const double *a, size_t n) {
 
 void free_handle(Handle &h) {
     void *ptrs[] = {h.pw, h.pg, h.phi[0], h.phi[1], h.b0, h.dfx, h.dfy, h.dfz, h.cx, h.cy, h.cz,
-                    h.msk, h.bphi[0], h.bphi[1], h.bwork, h.dev_status, h.barrier,
+                    h.msk, h.cxs, h.bphi[0], h.bphi[1], h.bwork, h.dev_status, h.barrier,
                     h.obs.pet_idx, h.obs.pet_val, h.obs.ti_idx, h.obs.t1_val, h.obs.t2_val,
                     h.lik_partials, h.lik_out, h.adj_ws, h.aff_phi0, h.aff_J, h.aff_out, h.aff_delta};
     for (void *p : ptrs)
@@ -163,6 +163,7 @@ int gbg_create(const gbg_config *cfg, gbg_handle **out) {
         TRY_ALLOC(h.cy, h.N * sizeof(float));
         TRY_ALLOC(h.cz, h.N * sizeof(float));
         TRY_ALLOC(h.msk, h.N * sizeof(float));
+        TRY_ALLOC(h.cxs, h.N * sizeof(float));
         if (h.max_samples > 0) {
             TRY_ALLOC(h.bphi[0], h.N * (size_t)h.max_samples * sizeof(float));
             TRY_ALLOC(h.bphi[1], h.N * (size_t)h.max_samples * sizeof(float));

@@ -83,6 +83,7 @@ struct Handle {
 
     // fast mode: unit-diffusivity face coefficients and tissue mask (float SoA)
     float *cx = nullptr, *cy = nullptr, *cz = nullptr, *msk = nullptr;
+    float *cxs = nullptr;  // cx with the sign bit set where msk is 0 (population kernels)
     double fast_ratio = -1;  // Dg/Dw the fast coefficients were built for
     bool fast_valid = false;
 

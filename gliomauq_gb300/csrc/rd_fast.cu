@@ -36,8 +36,11 @@
 // round k are a prefix of that order.
 //
 // Kernel families (the autotuner times them per grid size): registers
-// (k_population1: planes carried in registers, loads through L1/L2, optional
-// one-plane-ahead prefetch), cp.async rings (k_population3), and bulk-copy
+// (k_population8, the default: planes carried in registers, the mask in the
+// sign bit of the x-face table, 32-bit offsets; k_population9: the same with
+// two samples of one tile per warp sharing the anatomy loads; k_population1:
+// a separate mask table, optional one-plane-ahead loads or L2 prefetches),
+// cp.async rings (k_population3), and bulk-copy
 // rings fed by the TMA unit with mbarrier completion (k_population5: one
 // elected thread issues, a block barrier per plane; k_population6: a
 // producer warp and full/empty barriers per slot, no block barriers), and
@@ -58,7 +61,8 @@ __device__ __forceinline__ int wrapp(int i, int n) { return i == n - 1 ? 0 : i +
 
 __global__ void k_fast_tables(int n, const double *__restrict__ pw, const double *__restrict__ pg,
                               double ratio, float *__restrict__ cx, float *__restrict__ cy,
-                              float *__restrict__ cz, float *__restrict__ msk) {
+                              float *__restrict__ cz, float *__restrict__ msk,
+                              float *__restrict__ cxs) {
     const size_t N = (size_t)n * n * n;
     for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
          c += (size_t)gridDim.x * blockDim.x) {
@@ -84,6 +88,9 @@ __global__ void k_fast_tables(int n, const double *__restrict__ pw, const double
             dst[f][c] = (k[0] > 0.0 && k[f + 1] > 0.0 && s > 0.0) ? (float)(2.0 * k[0] * k[f + 1] / s) : 0.0f;
         }
         msk[c] = all ? 1.0f : 0.0f;
+        // every coefficient is +0 or positive, so the sign bit is free to carry
+        // the mask: |cxs| = cx exactly, signbit(cxs) = (msk == 0)
+        cxs[c] = all ? cx[c] : -cx[c];
     }
 }
 
@@ -185,37 +192,71 @@ __global__ void k_sort_schedule(const SampleRec *__restrict__ unsorted, int S,
 // phi1 and recs non-null (temporally blocked population kernels): sample s
 // starts in phi1 when (nsteps_s / 2) is odd, so that its final state lands in
 // buffer nsteps_s & 1 like every other population kernel's.
+__device__ __forceinline__ float gaussian_ic_value(int x, int y, int z, double x0, double y0, double z0,
+                                                   double peak, double two_s2, float screen,
+                                                   const double *__restrict__ pw, const double *__restrict__ pg,
+                                                   unsigned c) {
+    // float screen: cells with d^2 > 2 sigma^2 * 120 (+1 voxel^2 margin for the
+    // float rounding) have exponent < -110 and get 0 below; skip their FP64 work
+    const float fx = (float)x - (float)x0, fy = (float)y - (float)y0, fz = (float)z - (float)z0;
+    const bool near = peak > 1.0 || fx * fx + fy * fy + fz * fz <= screen;
+    float v = 0.0f;
+    if (near && pw[c] + pg[c] > 0.0) {
+        // d2 and the exponent rounded operation by operation (no FMA), as
+        // peak * exp(-d2 / (2 sigma^2)) evaluates in plain double arithmetic
+        const double dx = x - x0, dy = y - y0, dz = z - z0;
+        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+        const double e = __ddiv_rn(-d2, two_s2);
+        // below -745 exp underflows to 0; below -110 peak*exp(e) <= 1e-47
+        // rounds to float 0 for any peak <= 1e+0: skip the FP64 exp there
+        if (e > -110.0 || peak > 1.0) v = (float)__dmul_rn(peak, exp(e));
+    }
+    return v;
+}
+
+// Grid: y over samples, x over groups of four consecutive cells of one
+// sample (float4 stores when n is a multiple of 4, cell by cell otherwise).
+// 32-bit index arithmetic inside a sample (n <= 1024, n^3 < 2^32).
 __global__ void k_gaussian_ic(int n, const gbg_sample *__restrict__ smp, int S, double peak,
-                              double sigma, const float *__restrict__ msk_tissue,
-                              const double *__restrict__ pw, const double *__restrict__ pg,
+                              double sigma, const double *__restrict__ pw, const double *__restrict__ pg,
                               float *__restrict__ phi, float *__restrict__ phi1 = nullptr,
                               const SampleRec *__restrict__ recs = nullptr) {
-    const size_t N = (size_t)n * n * n;
-    const size_t total = N * S;
+    const unsigned un = (unsigned)n, N = un * un * un, groups = (N + 3) / 4;
     const double two_s2 = __dmul_rn(__dmul_rn(2.0, sigma), sigma);
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-         i += (size_t)gridDim.x * blockDim.x) {
-        const size_t s = i / N, c = i % N;
-        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
-        float v = 0.0f;
-        // float screen: cells with d^2 > 2 sigma^2 * 120 (+1 voxel^2 margin for the
-        // float rounding) have exponent < -110 and get 0 below; skip their FP64 work
-        const float fx = (float)x - (float)smp[s].x0, fy = (float)y - (float)smp[s].y0,
-                    fz = (float)z - (float)smp[s].z0;
-        const bool near = peak > 1.0 || fx * fx + fy * fy + fz * fz <= (float)(two_s2 * 120.0) + 1.0f;
-        if (near && pw[c] + pg[c] > 0.0) {
-            // d2 and the exponent rounded operation by operation (no FMA), as
-            // peak * exp(-d2 / (2 sigma^2)) evaluates in plain double arithmetic
-            const double dx = x - smp[s].x0, dy = y - smp[s].y0, dz = z - smp[s].z0;
-            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-            const double e = __ddiv_rn(-d2, two_s2);
-            // below -745 exp underflows to 0; below -110 peak*exp(e) <= 1e-47
-            // rounds to float 0 for any peak <= 1e+0: skip the FP64 exp there
-            if (e > -110.0 || peak > 1.0) v = (float)__dmul_rn(peak, exp(e));
+    const float screen = (float)(two_s2 * 120.0) + 1.0f;
+    for (unsigned s = blockIdx.y; s < (unsigned)S; s += gridDim.y) {
+        const double x0 = smp[s].x0, y0 = smp[s].y0, z0 = smp[s].z0;
+        float *dst = ((phi1 && recs && ((recs[s].nsteps / 2) & 1)) ? phi1 : phi) + (size_t)s * N;
+        for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += gridDim.x * blockDim.x) {
+            const unsigned c = 4 * g;
+            if ((un & 3u) == 0) {
+                const unsigned row = c / un;
+                const int x = (int)(c - row * un), y = (int)(row % un), z = (int)(row / un);
+                float v[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    v[j] = gaussian_ic_value(x + j, y, z, x0, y0, z0, peak, two_s2, screen, pw, pg, c + j);
+                *reinterpret_cast<float4 *>(dst + c) = make_float4(v[0], v[1], v[2], v[3]);
+            } else {
+                for (unsigned cj = c; cj < c + 4 && cj < N; ++cj) {
+                    const unsigned row = cj / un;
+                    dst[cj] = gaussian_ic_value((int)(cj - row * un), (int)(row % un), (int)(row / un), x0, y0, z0,
+                                                peak, two_s2, screen, pw, pg, cj);
+                }
+            }
         }
-        float *dst = (phi1 && recs && ((recs[s].nsteps / 2) & 1)) ? phi1 : phi;
-        dst[i] = v;
     }
+}
+
+dim3 ic_grid(const Handle &h, int S) {
+    const unsigned groups = (unsigned)((h.N + 3) / 4);
+    unsigned gx = (groups + 255) / 256;
+    if (gx > 128) gx = 128;
+    unsigned gy = (unsigned)h.num_sms * 16 / gx;
+    if (gy < 1) gy = 1;
+    if (gy > (unsigned)S) gy = (unsigned)S;
+    if (gy > 65535) gy = 65535;
+    return dim3(gx, gy);
 }
 
 // Bounded grid barrier for the cooperative persistent kernel. Returns false
@@ -261,6 +302,7 @@ struct PopArgs {
     size_t stride;                 // cells per sample field
     float *buf0, *buf1;
     const float *cx, *cy, *cz, *msk;
+    const float *cxs;              // cx, sign bit = not msk
     const SampleRec *rec;          // sorted by nsteps descending
     unsigned *barrier;
     int *status;
@@ -280,7 +322,14 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // __ldg).
 // PF = 1: the z+2 density plane (the DRAM stream) is loaded one plane ahead,
 // so two planes of each thread's new data are in flight at once.
-template <int LR, int PF = 0>  // lanes per x-row = n/4
+// D > 0: every lane asks for its own 16 bytes of density D planes ahead to be
+// brought into L2 (prefetch.global.L2; no registers held), so the z+1 load
+// the march waits on is an L2 hit.
+__device__ __forceinline__ void l2_prefetch_lane(const float *p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));
+}
+
+template <int LR, int PF = 0, int D = 0>  // lanes per x-row = n/4
 __device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
                                            const float *__restrict__ in, float *__restrict__ out,
                                            const float *__restrict__ cx, const float *__restrict__ cy,
@@ -299,9 +348,17 @@ __device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
     float4 CZp = __ldg(reinterpret_cast<const float4 *>(cz + at(y, zs)));
     float4 Pahead;
     if (PF) Pahead = __ldcg(reinterpret_cast<const float4 *>(in + at(y, wrapp(tz0, n))));
+    // planes tz0 + 1 .. tz0 + TZ are this tile's DRAM stream (tz0 - 1 and tz0
+    // were just loaded); rows start at x = 0, 16-byte aligned, n * 4 bytes
+    auto prefetch = [&](int zu) {
+        if (zu <= tz0 + TZ) l2_prefetch_lane(in + at(y, zu % n));
+    };
+    if (D > 1)
+        for (int d = 1; d < D; ++d) prefetch(tz0 + d);
     for (int dz = 0; dz < TZ; ++dz) {
         const int z = tz0 + dz;
         const int zn = wrapp(z, n);
+        if (D > 0) prefetch(z + D);
         float4 Pn;
         if (PF) {
             Pn = Pahead;
@@ -352,7 +409,7 @@ __device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
 // CTAs running at the same time work on the same tile of different samples,
 // so each tile's anatomy comes from DRAM once per round and is then shared
 // through L2.
-template <int LR, int MINB, int PF = 0>
+template <int LR, int MINB, int PF = 0, int D = 0>
 __global__ void __launch_bounds__(256, MINB) k_population1(PopArgs p) {
     const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
     int active = p.S;
@@ -367,13 +424,229 @@ __global__ void __launch_bounds__(256, MINB) k_population1(PopArgs p) {
             const int ty = t % p.tiles_y, tz = t / p.tiles_y;
             const size_t off = (size_t)p.rec[r].order * p.stride;
             const bool last = k == p.rec[r].nsteps - 1;
-            march_tile<LR, PF>(p.n, p.TZ, ty * rows, tz * p.TZ, in + off, out + off, p.cx, p.cy, p.cz,
+            march_tile<LR, PF, D>(p.n, p.TZ, ty * rows, tz * p.TZ, in + off, out + off, p.cx, p.cy, p.cz,
                            p.msk, last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
         }
         if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
     }
 }
 
+
+// Register variant with fewer loads and cheaper addressing: the mask comes
+// from the sign bit of the x-face table (one float4 load less per plane), and
+// offsets inside a sample are 32-bit, formed once per tile and advanced by a
+// plane per step. Same operation sequence as march_tile on |cxs| = cx.
+template <int LR>
+__device__ __forceinline__ void march_tile_s(int n, int TZ, int ty0, int tz0,
+                                             const float *__restrict__ in, float *__restrict__ out,
+                                             const float *__restrict__ cxs, const float *__restrict__ cy,
+                                             const float *__restrict__ cz, float a, float b) {
+    const int lane = threadIdx.x & 31;
+    const int li = lane % LR;
+    const int y = ty0 + (int)(threadIdx.x / LR);
+    const int x0 = 4 * li;
+    const int ym = wrapm(y, n), yp = wrapp(y, n);
+    const unsigned plane = (unsigned)n * (unsigned)n;
+    const unsigned oy = (unsigned)(x0 + n * y), oym = (unsigned)(x0 + n * ym), oyp = (unsigned)(x0 + n * yp);
+    auto ld = [](const float *base, unsigned off) { return __ldcg(reinterpret_cast<const float4 *>(base + off)); };
+    auto lg = [](const float *base, unsigned off) { return __ldg(reinterpret_cast<const float4 *>(base + off)); };
+    const unsigned zso = plane * (unsigned)wrapm(tz0, n);
+    unsigned zo = plane * (unsigned)tz0;
+    float4 Pp = ld(in, oy + zso);
+    float4 Pc = ld(in, oy + zo);
+    float4 CZp = lg(cz, oy + zso);
+    const unsigned last = plane * (unsigned)(n - 1);
+    for (int dz = 0; dz < TZ; ++dz) {
+        const unsigned zno = zo == last ? 0u : zo + plane;
+        const float4 Pn = ld(in, oy + zno);
+        const float4 PS = ld(in, oym + zo);
+        const float4 PN = ld(in, oyp + zo);
+        const float4 CX = lg(cxs, oy + zo);
+        const float4 CY = lg(cy, oy + zo);
+        const float4 CYm = lg(cy, oym + zo);
+        const float4 CZ = lg(cz, oy + zo);
+        const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
+        const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
+        const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
+        const float p[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
+        const float cxa[5] = {fabsf(cxl), fabsf(CX.x), fabsf(CX.y), fabsf(CX.z), fabsf(CX.w)};
+        const bool off4[4] = {signbit(CX.x), signbit(CX.y), signbit(CX.z), signbit(CX.w)};
+        const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
+        const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
+        const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
+        const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
+        float o[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float f0 = p[i + 1];
+            float lap = cxa[i] * (p[i] - f0);
+            lap = fmaf(cxa[i + 1], p[i + 2] - f0, lap);
+            lap = fmaf(cym4[i], ps[i] - f0, lap);
+            lap = fmaf(cy4[i], pn[i] - f0, lap);
+            lap = fmaf(czp4[i], pp[i] - f0, lap);
+            lap = fmaf(cz4[i], pq[i] - f0, lap);
+            float v = fmaf(a, lap, f0);
+            v = fmaf(b * f0, 1.0f - f0, v);
+            v = fminf(fmaxf(v, 0.0f), 1.0f);
+            o[i] = off4[i] ? 0.0f : v;
+        }
+        *reinterpret_cast<float4 *>(out + oy + zo) = make_float4(o[0], o[1], o[2], o[3]);
+        Pp = Pc;
+        Pc = Pn;
+        CZp = CZ;
+        zo = zno;
+    }
+}
+
+template <int LR, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_population8(PopArgs p) {
+    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
+    int active = p.S;
+    const int rows = 256 / LR;
+    for (int k = 0; k < maxsteps; ++k) {
+        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
+        const float *in = (k & 1) ? p.buf1 : p.buf0;
+        float *out = (k & 1) ? p.buf0 : p.buf1;
+        const long items = (long)active * p.tiles;
+        for (long it = blockIdx.x; it < items; it += gridDim.x) {
+            const int r = (int)(it % active), t = (int)(it / active);
+            const int ty = t % p.tiles_y, tz = t / p.tiles_y;
+            const size_t off = (size_t)p.rec[r].order * p.stride;
+            const bool last = k == p.rec[r].nsteps - 1;
+            march_tile_s<LR>(p.n, p.TZ, ty * rows, tz * p.TZ, in + off, out + off, p.cxs, p.cy, p.cz,
+                             last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
+        }
+        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
+    }
+}
+
+// Two samples on one tile per warp: the anatomy (cxs, cy, cz) is loaded once
+// for both, so a plane costs 6 density + 4 anatomy loads for two samples
+// (5 per sample in place of 7), and each round trip of loads feeds twice the
+// arithmetic. The second slot is idle (two = false) for the odd sample of a
+// round. Per-sample operation sequence as march_tile.
+template <int LR>
+__device__ __forceinline__ void stencil4(const float4 &Pc, const float4 &Pp, const float4 &Pn, const float4 &PS,
+                                         const float4 &PN, const float4 &CX, const float4 &CY,
+                                         const float4 &CYm, const float4 &CZ, const float4 &CZp, float cxl,
+                                         int li, float a, float b, float4 &res) {
+    const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
+    const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
+    const float p[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
+    const float cxa[5] = {fabsf(cxl), fabsf(CX.x), fabsf(CX.y), fabsf(CX.z), fabsf(CX.w)};
+    const bool off4[4] = {signbit(CX.x), signbit(CX.y), signbit(CX.z), signbit(CX.w)};
+    const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
+    const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
+    const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
+    const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
+    float o[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float f0 = p[i + 1];
+        float lap = cxa[i] * (p[i] - f0);
+        lap = fmaf(cxa[i + 1], p[i + 2] - f0, lap);
+        lap = fmaf(cym4[i], ps[i] - f0, lap);
+        lap = fmaf(cy4[i], pn[i] - f0, lap);
+        lap = fmaf(czp4[i], pp[i] - f0, lap);
+        lap = fmaf(cz4[i], pq[i] - f0, lap);
+        float v = fmaf(a, lap, f0);
+        v = fmaf(b * f0, 1.0f - f0, v);
+        v = fminf(fmaxf(v, 0.0f), 1.0f);
+        o[i] = off4[i] ? 0.0f : v;
+    }
+    res = make_float4(o[0], o[1], o[2], o[3]);
+}
+
+template <int LR>
+__device__ __forceinline__ void march_tile_pair(int n, int TZ, int ty0, int tz0, bool two,
+                                                const float *__restrict__ in0, float *__restrict__ out0,
+                                                const float *__restrict__ in1, float *__restrict__ out1,
+                                                const float *__restrict__ cxs, const float *__restrict__ cy,
+                                                const float *__restrict__ cz, float a0, float b0, float a1,
+                                                float b1) {
+    const int lane = threadIdx.x & 31;
+    const int li = lane % LR;
+    const int y = ty0 + (int)(threadIdx.x / LR);
+    const int x0 = 4 * li;
+    const int ym = wrapm(y, n), yp = wrapp(y, n);
+    const unsigned plane = (unsigned)n * (unsigned)n;
+    const unsigned oy = (unsigned)(x0 + n * y), oym = (unsigned)(x0 + n * ym), oyp = (unsigned)(x0 + n * yp);
+    auto ld = [](const float *base, unsigned off) { return __ldcg(reinterpret_cast<const float4 *>(base + off)); };
+    auto lg = [](const float *base, unsigned off) { return __ldg(reinterpret_cast<const float4 *>(base + off)); };
+    const unsigned zso = plane * (unsigned)wrapm(tz0, n);
+    unsigned zo = plane * (unsigned)tz0;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 Pp0 = ld(in0, oy + zso), Pc0 = ld(in0, oy + zo);
+    float4 Pp1 = two ? ld(in1, oy + zso) : zero, Pc1 = two ? ld(in1, oy + zo) : zero;
+    float4 CZp = lg(cz, oy + zso);
+    const unsigned last = plane * (unsigned)(n - 1);
+    for (int dz = 0; dz < TZ; ++dz) {
+        const unsigned zno = zo == last ? 0u : zo + plane;
+        const float4 Pn0 = ld(in0, oy + zno), PS0 = ld(in0, oym + zo), PN0 = ld(in0, oyp + zo);
+        float4 Pn1 = zero, PS1 = zero, PN1 = zero;
+        if (two) {
+            Pn1 = ld(in1, oy + zno);
+            PS1 = ld(in1, oym + zo);
+            PN1 = ld(in1, oyp + zo);
+        }
+        const float4 CX = lg(cxs, oy + zo);
+        const float4 CY = lg(cy, oy + zo);
+        const float4 CYm = lg(cy, oym + zo);
+        const float4 CZ = lg(cz, oy + zo);
+        const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
+        float4 r0, r1;
+        stencil4<LR>(Pc0, Pp0, Pn0, PS0, PN0, CX, CY, CYm, CZ, CZp, cxl, li, a0, b0, r0);
+        *reinterpret_cast<float4 *>(out0 + oy + zo) = r0;
+        if (two) {
+            stencil4<LR>(Pc1, Pp1, Pn1, PS1, PN1, CX, CY, CYm, CZ, CZp, cxl, li, a1, b1, r1);
+            *reinterpret_cast<float4 *>(out1 + oy + zo) = r1;
+        }
+        Pp0 = Pc0;
+        Pc0 = Pn0;
+        Pp1 = Pc1;
+        Pc1 = Pn1;
+        CZp = CZ;
+        zo = zno;
+    }
+}
+
+// Items of a round: item = tile * pairs + pair, pair q = sorted samples 2q and
+// 2q + 1 (tile-major, as k_population1).
+template <int LR, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_population9(PopArgs p) {
+    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
+    int active = p.S;
+    const int rows = 256 / LR;
+    for (int k = 0; k < maxsteps; ++k) {
+        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
+        const float *in = (k & 1) ? p.buf1 : p.buf0;
+        float *out = (k & 1) ? p.buf0 : p.buf1;
+        const unsigned pairs = (unsigned)(active + 1) / 2;
+        const unsigned items = pairs * (unsigned)p.tiles;
+        for (unsigned it = blockIdx.x; it < items; it += gridDim.x) {
+            const unsigned q = it % pairs, t = it / pairs;
+            const int r0 = 2 * (int)q, r1 = r0 + 1;
+            const bool two = r1 < active;
+            const int ty = (int)t % p.tiles_y, tz = (int)t / p.tiles_y;
+            const SampleRec &s0 = p.rec[r0];
+            const size_t off0 = (size_t)s0.order * p.stride;
+            const bool last0 = k == s0.nsteps - 1;
+            const float a0 = last0 ? s0.a2 : s0.a, b0 = last0 ? s0.b2 : s0.b;
+            size_t off1 = off0;
+            float a1 = a0, b1 = b0;
+            if (two) {
+                const SampleRec &s1 = p.rec[r1];
+                off1 = (size_t)s1.order * p.stride;
+                const bool last1 = k == s1.nsteps - 1;
+                a1 = last1 ? s1.a2 : s1.a;
+                b1 = last1 ? s1.b2 : s1.b;
+            }
+            march_tile_pair<LR>(p.n, p.TZ, ty * rows, tz * p.TZ, two, in + off0, out + off0, in + off1,
+                                out + off1, p.cxs, p.cy, p.cz, a0, b0, a1, b1);
+        }
+        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
+    }
+}
 
 // Population kernel.
 //   LR lanes per x-row (n = 4 LR), RY rows per sample slot, G sample slots per
@@ -1142,12 +1415,36 @@ struct PopVariant {
     bool tb = false;  // two steps per round (start buffer per sample, see k_gaussian_ic)
 };
 
-template <int LR, int MINB = 1, int PF = 0>
+template <int LR, int MINB = 1, int PF = 0, int D = 0>
 PopVariant make_register_variant(int tz) {
     PopVariant v;
-    v.fn = (const void *)k_population1<LR, MINB, PF>;
+    v.fn = (const void *)k_population1<LR, MINB, PF, D>;
     v.ry = 256 / LR;
     v.g = 1;
+    v.threads = 256;
+    v.tz = tz;
+    v.smem = 0;
+    return v;
+}
+
+template <int LR, int MINB>
+PopVariant make_signmask_variant(int tz) {
+    PopVariant v;
+    v.fn = (const void *)k_population8<LR, MINB>;
+    v.ry = 256 / LR;
+    v.g = 1;
+    v.threads = 256;
+    v.tz = tz;
+    v.smem = 0;
+    return v;
+}
+
+template <int LR, int MINB>
+PopVariant make_pair_variant(int tz) {
+    PopVariant v;
+    v.fn = (const void *)k_population9<LR, MINB>;
+    v.ry = 256 / LR;
+    v.g = 2;
     v.threads = 256;
     v.tz = tz;
     v.smem = 0;
@@ -1209,15 +1506,17 @@ int variants_for(int n, PopVariant *out) {
     int k = 0;
     switch (n) {
         case 128:
-            out[k++] = make_register_variant<32>(16);
-            out[k++] = make_register_variant<32>(32);
+            out[k++] = make_signmask_variant<32, 4>(16);
+            out[k++] = make_signmask_variant<32, 4>(32);
+            out[k++] = make_signmask_variant<32, 3>(16);
+            out[k++] = make_signmask_variant<32, 5>(16);
+            out[k++] = make_pair_variant<32, 3>(16);
+            out[k++] = make_pair_variant<32, 3>(32);
             out[k++] = make_register_variant<32, 4>(16);
             out[k++] = make_register_variant<32, 5>(16);
-            out[k++] = make_register_variant<32, 6>(16);
-            out[k++] = make_register_variant<32, 6>(32);
+            out[k++] = make_register_variant<32>(16);
             out[k++] = make_register_variant<32, 4, 1>(16);
-            out[k++] = make_register_variant<32, 5, 1>(16);
-            out[k++] = make_register_variant<32, 5, 1>(32);
+            out[k++] = make_register_variant<32, 4, 0, 2>(16);
             out[k++] = make_tb_variant<2, true>(16);
             out[k++] = make_tb_variant<2, true>(32);
             out[k++] = make_tma_variant<32, 8, 3, 3>(32);
@@ -1225,13 +1524,11 @@ int variants_for(int n, PopVariant *out) {
             out[k++] = make_ws_variant<32, 8, 3, 3>(32);
             out[k++] = make_variant<32, 8, 2>(32);
             out[k++] = make_variant<32, 8, 1>(32);
-            out[k++] = make_variant<32, 8, 2>(16);
             out[k++] = make_variant<32, 4, 4>(32);
-            out[k++] = make_variant<32, 8, 1>(64);
-            out[k++] = make_variant<32, 4, 2>(32);
-            out[k++] = make_variant<32, 16, 1>(32);
             break;
         case 64:
+            out[k++] = make_signmask_variant<16, 4>(16);
+            out[k++] = make_signmask_variant<16, 5>(16);
             out[k++] = make_register_variant<16>(16);
             out[k++] = make_register_variant<16, 6>(16);
             out[k++] = make_register_variant<16, 5, 1>(16);
@@ -1242,6 +1539,7 @@ int variants_for(int n, PopVariant *out) {
             out[k++] = make_variant<16, 8, 4>(32);
             break;
         case 32:
+            out[k++] = make_signmask_variant<8, 4>(8);
             out[k++] = make_register_variant<8>(8);
             out[k++] = make_variant<8, 32, 1>(8);
             out[k++] = make_variant<8, 32, 2>(8);
@@ -1308,6 +1606,7 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
     a.cy = h.cy;
     a.cz = h.cz;
     a.msk = h.msk;
+    a.cxs = h.cxs;
     a.rec = rec_sorted;
     a.barrier = h.barrier;
     a.status = h.dev_status;
@@ -1356,8 +1655,7 @@ int launch_schedule_smooth(Handle &h, const gbg_sample *samples_device, int S, d
 
 int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, double peak, double sigma,
                        float *phi) {
-    k_gaussian_ic<<<grid_for(h, h.N * S), 256, 0, h.stream>>>(h.n, samples_device, S, peak, sigma, h.msk, h.pw,
-                                                               h.pg, phi);
+    k_gaussian_ic<<<ic_grid(h, S), 256, 0, h.stream>>>(h.n, samples_device, S, peak, sigma, h.pw, h.pg, phi);
     h.launches++;
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
@@ -1366,7 +1664,7 @@ int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, doubl
 int fast_build_tables(Handle &h, double ratio) {
     if (h.fast_valid && h.fast_ratio == ratio) return GBG_OK;
     k_fast_tables<<<grid_for(h, h.N), 256, 0, h.stream>>>(h.n, h.pw, h.pg, ratio, h.cx, h.cy,
-                                                           h.cz, h.msk);
+                                                           h.cz, h.msk, h.cxs);
     h.launches++;
     GBG_CUDA_TRY(cudaGetLastError());
     h.fast_ratio = ratio;
@@ -1417,10 +1715,9 @@ int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
                                                           unsorted);
     k_sort_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(unsorted, S, sorted, rank_of);
     const bool tb = variant_is_tb(h);
-    k_gaussian_ic<<<grid_for(h, h.N * S), 256, 0, h.stream>>>(h.n, samples_device, S, o.ic_peak,
-                                                               o.ic_sigma, h.msk, h.pw, h.pg,
-                                                               h.bphi[0], tb ? h.bphi[1] : nullptr,
-                                                               tb ? unsorted : nullptr);
+    k_gaussian_ic<<<ic_grid(h, S), 256, 0, h.stream>>>(h.n, samples_device, S, o.ic_peak, o.ic_sigma, h.pw,
+                                                        h.pg, h.bphi[0], tb ? h.bphi[1] : nullptr,
+                                                        tb ? unsorted : nullptr);
     h.launches += 3;
     GBG_CUDA_TRY(cudaGetLastError());
     if (f32ref) {
