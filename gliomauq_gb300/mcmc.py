@@ -254,18 +254,48 @@ def _chol_cov(th: np.ndarray, axis=None) -> np.ndarray:
     return np.linalg.cholesky(c + 1e-12 * np.diag(np.diag(c)) + 1e-300 * np.eye(c.shape[0]))
 
 
+STRANDED_NATS = 25.0  # a chain this far below the population's median log pi is stranded
+
+
+def _stranded(lp: np.ndarray) -> np.ndarray:
+    """Chains whose log pi is not finite or lies more than STRANDED_NATS below
+    the population median (far outside the bulk of a posterior with a few
+    identified parameters: chi^2_5 / 2 exceeds 10.3 with probability 1e-3)."""
+    ok = np.isfinite(lp)
+    if not ok.any():
+        return ~ok
+    return ~ok | (lp < np.median(lp[ok]) - STRANDED_NATS)
+
+
+def _discrepancy(lp: np.ndarray, ls: np.ndarray) -> float:
+    """Spread of log pi - log pi_surrogate over the population: what the
+    second stage's acceptance depends on (a constant offset cancels)."""
+    ok = np.isfinite(lp) & np.isfinite(ls)
+    return float(np.std(lp[ok] - ls[ok])) if ok.sum() >= 3 else np.inf
+
+
 def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: int, step: float,
        rng, inner: int = 8, burn: int = 0, target: float = 0.3, chol=None, adapt: bool = False,
-       rebuild_every: int = 0, axis=None, axis_prob: float = 0.5) -> ChainResult:
+       rebuild_every: int = 0, axis=None, axis_prob: float = 0.5,
+       adapt_pool: bool = True, reset_stranded: bool = True) -> ChainResult:
     """Delayed-acceptance MCMC, chains in lock-step: per generation `inner`
     batched surrogate calls and one batched solver call for the chains whose
     inner chain moved. The inner random-walk proposal is y + step * C xi:
     C = chol if given, else the prior widths. During the first `burn`
     generations the step is adapted toward the target inner acceptance and,
     with adapt=True (or chol None), C follows the population covariance of
-    the chains; every `rebuild_every` burn-in generations a surrogate that
-    has rebuild(u_centre, steps) is re-linearised at the population mean
-    with half the population standard deviations as steps. With `axis` = a
+    the chains (adapt_pool: pooled over the chains and the latter half of the
+    generations so far, a far steadier estimate than one generation's
+    `chains` points, stranded chain-generations left out); every
+    `rebuild_every` burn-in generations a surrogate that has
+    rebuild(u_centre, steps) is re-linearised at the population median with
+    half the population standard deviations as steps, and kept only if it
+    lowers the spread of log pi - log pi_surrogate over the population
+    (state()/restore() put the previous build back otherwise). With
+    reset_stranded, chains stranded far below the population (_stranded) are
+    moved to copies of randomly chosen other chains at those points and once
+    more when burn-in ends; burn-in output is discarded, so this only
+    changes where the fixed post-burn-in kernel starts. With `axis` = a
     (the scaling symmetry's coordinate in the invariant coordinates, along
     which the likelihood of the scaled time grid is flat), random-walk moves
     leave coordinate a fixed and each inner step is, with probability
@@ -285,20 +315,50 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
     if axis is not None:
         Lc = np.linalg.cholesky(_decoupled(Lc @ Lc.T, axis))
     out = np.empty((steps, m, d))
+    lp_out = np.empty((steps, m))
     acc1 = acc2 = tried = 0
+    resets = rebuilds_kept = rebuilds_tried = 0
     t0 = time.perf_counter()
     t_burn = 0.0
+
+    def reset():
+        nonlocal resets
+        bad = _stranded(lp)
+        if bad.any() and not bad.all():
+            src = rng.choice(np.flatnonzero(~bad), size=int(bad.sum()))
+            th[bad], lp[bad], ls[bad] = th[src], lp[src], ls[src]
+            resets += int(bad.sum())
+
     for k in range(steps):
         if k == burn:
+            if reset_stranded and burn > 0:
+                reset()
             t_burn = time.perf_counter() - t0
         if k < burn and m > 2 * d:
+            if rebuild_every > 0 and k > 0 and k % rebuild_every == 0:
+                if reset_stranded:
+                    reset()
+                if hasattr(spost, "rebuild"):
+                    good = ~_stranded(lp)
+                    old = spost.state() if hasattr(spost, "state") else None
+                    spost.rebuild(np.median(th[good], axis=0), 0.5 * th[good].std(axis=0))
+                    ls_new = spost.logpost(th)
+                    rebuilds_tried += 1
+                    if old is not None and _discrepancy(lp, ls_new) > _discrepancy(lp, ls):
+                        spost.restore(old)
+                    else:
+                        ls = ls_new
+                        rebuilds_kept += 1
             if chol is None:
                 Lc = _chol_population(th, w)
             elif adapt and k >= max(1, burn // 4):
-                Lc = _chol_cov(th, axis)
-            if rebuild_every > 0 and k > 0 and k % rebuild_every == 0 and hasattr(spost, "rebuild"):
-                spost.rebuild(th.mean(axis=0), 0.5 * th.std(axis=0))
-                ls = spost.logpost(th)
+                if adapt_pool:
+                    win = slice(k // 2, k)
+                    keep = np.stack([~_stranded(r) for r in lp_out[win]])
+                    pts = out[win][keep]
+                    Lc = _chol_cov(pts if len(pts) > 2 * d else th, axis)
+                else:
+                    Lc = _chol_cov(th, axis)
         y, ly = th.copy(), ls.copy()
         a1 = 0.0   # random-walk acceptances (the step adapts to these)
         n1 = 0
@@ -340,11 +400,14 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
             acc2 += a.sum()
             tried += moved.sum()
         out[k] = th
+        lp_out[k] = lp
     n_gen = max(1, (steps - burn) * m)
     return ChainResult(out, acc2 / n_gen, step, time.perf_counter() - t0, post.solves,
                        history=dict(stage1_accept=acc1 / n_gen,  # random-walk moves
                                     stage2_accept=acc2 / max(tried, 1),
                                     surrogate_evals=spost.evals, inner=inner,
+                                    stranded_resets=resets, rebuilds_kept=rebuilds_kept,
+                                    rebuilds_tried=rebuilds_tried,
                                     burn_seconds=t_burn if burn < steps else time.perf_counter() - t0))
 
 
@@ -594,7 +657,7 @@ class _LogSurrogate:
 
 
 def refine_cov(post, u_map: np.ndarray, cov: np.ndarray, span: float = 8.0, npts: int = 33,
-               drop: float = 10.0):
+               drop: float = 10.0, with_best: bool = False):
     """Gaussian approximation refined by profiles: log pi is evaluated along
     each eigenvector of the Laplace precision (in prior-width-scaled
     coordinates) at npts points out to +-span Laplace standard deviations,
@@ -603,7 +666,10 @@ def refine_cov(post, u_map: np.ndarray, cov: np.ndarray, span: float = 8.0, npts
     Directions whose profile stays within `drop` over the whole span are
     rescanned 8x wider. A local Hessian misjudges directions along which log
     pi is kinked or nearly flat (the Dw-rho-T ridge); the profile fit sees
-    the posterior's extent. Returns (covariance, per-direction sd ratio)."""
+    the posterior's extent. Returns (covariance, per-direction sd ratio),
+    and with with_best also the profile point of highest log pi and its
+    value (above log pi(u_map) when u_map is short of the mode, e.g. part
+    way along a narrow curved ridge)."""
     w = post.prior.width
     d = u_map.size
     A = np.linalg.inv(cov / np.outer(w, w))
@@ -613,11 +679,16 @@ def refine_cov(post, u_map: np.ndarray, cov: np.ndarray, span: float = 8.0, npts
     spans = np.full(d, span)
     ratio = np.ones(d)
     todo = list(range(d))
+    best_u, best_lp = np.array(u_map, dtype=np.float64), -np.inf
     for _ in range(2):
         if not todo:
             break
         pts = np.concatenate([u_map + np.outer(ts * spans[k] * sd[k], V[:, k] * w) for k in todo])
         lp, _ = post.loglik(pts, False)
+        fin = np.where(np.isfinite(lp), lp, -np.inf)
+        if fin.max() > best_lp:
+            best_lp = float(fin.max())
+            best_u = pts[int(np.argmax(fin))].copy()
         lp = lp.reshape(len(todo), npts)
         again = []
         for j, k in enumerate(todo):
@@ -634,7 +705,10 @@ def refine_cov(post, u_map: np.ndarray, cov: np.ndarray, span: float = 8.0, npts
             ratio[k] = min(max(ratio[k], 0.1), spans[k])
         todo = again
     sig = sd * ratio
-    return (V * sig ** 2) @ V.T * np.outer(w, w), ratio
+    cov_r = (V * sig ** 2) @ V.T * np.outer(w, w)
+    if with_best:
+        return cov_r, ratio, best_u, best_lp
+    return cov_r, ratio
 
 
 def stable_dt0(n: int, L: float, dw_max: float) -> float:
@@ -723,6 +797,15 @@ class AffineSurrogate:
         self.J = np.stack(basis)
         h.affine_set(self.phi0, self.J.astype(np.float32))
 
+    def state(self):
+        """The current build (for restore)."""
+        return (self.u_ref.copy(), self.phi0.copy(), self.J.copy())
+
+    def restore(self, state):
+        """Make an earlier build the active one again."""
+        self.u_ref, self.phi0, self.J = (np.array(x) for x in state)
+        self.base.handle.affine_set(self.phi0, self.J.astype(np.float32))
+
     def logpost(self, u: np.ndarray) -> np.ndarray:
         u = np.atleast_2d(u)
         lp = self.prior.logp(u)
@@ -751,7 +834,9 @@ class PipelineResult:
 def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: int = 64,
                      generations: int = 300, burn: int = 100, inner: int = 16,
                      screen: int = 512, screen_draws=None, ic_peak: float = 0.1,
-                     ic_sigma: float = 1.0) -> PipelineResult:
+                     ic_sigma: float = 1.0, adapt_pool: bool = True, adapt: bool = True,
+                     rebuild_every: int = 25, reset_stranded: bool = True,
+                     polish: int = 8) -> PipelineResult:
     """The batched + adjoint + surrogate posterior sampler (dt0 < 0, the
     scaled time grid, makes the likelihood invariant along the scaling
     symmetry, whose coordinate is then drawn exactly from its prior
@@ -759,7 +844,9 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
       1. log pi of `screen` prior draws in batched solves; the best four start
       2. damped Newton with batched adjoint gradients and Hessians (find_mode)
          in the scaling symmetry's coordinates (INVARIANT_MAP)
-      3. the Laplace covariance refined by batched profiles (refine_cov)
+      3. the Laplace covariance refined by batched profiles (refine_cov);
+         while a profile point lies more than 1 nat above the mode estimate,
+         Newton restarts from it (at most `polish` times)
       4. delayed acceptance with the affine (tangent) surrogate around the
          mode, `chains` chains started from the refined Gaussian, proposal
          covariance and surrogate adapted to the population during burn-in
@@ -774,8 +861,17 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
     dv = post.to_u(np.asarray(screen_draws, dtype=np.float64))
     ld, _ = post.loglik(dv, False)
     starts = dv[np.argsort(ld)[::-1][:4]]
-    v_map, _, cov0, _ = find_mode(post, starts, iters=10)
-    cov, _ = refine_cov(post, v_map, cov0)
+    v_map, lp_map, cov0, _ = find_mode(post, starts, iters=10)
+    # the posterior is a narrow curved ridge in (log rho T, log Dw/rho), along
+    # which damped Newton can stop short of the mode: while a profile point
+    # lies above the current point, restart Newton from it
+    for _ in range(polish):
+        cov, _, v_best, lp_best = refine_cov(post, v_map, cov0, with_best=True)
+        if not lp_best > lp_map + 1.0:
+            break
+        v_map, lp_map, cov0, _ = find_mode(post, v_best[None], iters=5)
+    else:
+        cov, _ = refine_cov(post, v_map, cov0)
     sd = np.sqrt(np.diag(cov))
     Lc = np.linalg.cholesky(cov)
     sur = AffineSurrogate(post, v_map, 0.5 * sd, quad_axis=0)
@@ -794,7 +890,8 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
     v0[~np.isfinite(post.prior.logp(v0))] = v_map
     run = Posterior(handle, L, dt0, prior, ic_peak=ic_peak, ic_sigma=ic_sigma)
     r = da(LogCoords(run, A=INVARIANT_MAP), sur, v0, generations, 2.38 / np.sqrt(v_map.size), rng,
-           inner=inner, burn=burn, chol=Lc, adapt=True, rebuild_every=25, axis=0)
+           inner=inner, burn=burn, chol=Lc, adapt=adapt, rebuild_every=rebuild_every, axis=0,
+           adapt_pool=adapt_pool, reset_stranded=reset_stranded)
     burn_s = r.history["burn_seconds"]
     return PipelineResult(r, post.to_theta(r.samples[burn:]), v_map, cov, setup, r.seconds - burn_s,
                           burn_s)

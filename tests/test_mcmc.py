@@ -277,6 +277,36 @@ def test_refine_cov_recovers_a_wider_direction():
     assert np.allclose(cov, post.cov, rtol=1e-2, atol=1e-3 * np.abs(post.cov).max())
 
 
+def test_refine_cov_reports_a_higher_profile_point():
+    """Centre short of the mode along the soft direction of a correlated
+    Gaussian (as damped Newton can stop part way along a narrow ridge): the
+    profiles return a point above the centre, closer to the mode; at the
+    mode none is higher."""
+    post = CorrelatedStub()
+    w = post.prior.width
+    A = np.linalg.inv(post.cov / np.outer(w, w))
+    ev, V = np.linalg.eigh(A)
+    soft = V[:, 0] * w / np.sqrt(ev[0])   # one sd along the softest direction
+    start = post.mu + 5.0 * soft
+    l0 = post.loglik(start[None], False)[0][0]
+    _, _, best, lb = mcmc.refine_cov(post, start, post.cov, with_best=True)
+    assert lb > l0 + 1.0
+    z = lambda u: (u - post.mu) / w
+    assert np.linalg.norm(z(best)) < 0.5 * np.linalg.norm(z(start))
+    lm = post.loglik(post.mu[None], False)[0][0]
+    _, _, _, lbm = mcmc.refine_cov(post, post.mu, post.cov, with_best=True)
+    assert lbm <= lm + 1e-9
+
+
+def test_stranded_chains_and_discrepancy():
+    lp = np.array([0.0, -1.0, -2.0, -3.0, -40.0, -np.inf])
+    assert mcmc._stranded(lp).tolist() == [False, False, False, False, True, True]
+    assert mcmc._stranded(np.full(3, -np.inf)).all()
+    # a constant offset between exact and surrogate costs nothing
+    assert mcmc._discrepancy(lp[:4], lp[:4] - 7.0) == 0.0
+    assert mcmc._discrepancy(lp[:2], lp[:2]) == np.inf  # too few finite pairs
+
+
 def test_invariant_coordinates_map_gradient_and_symmetry():
     post = GaussianStub()
     post.prior = mcmc.Prior(lo=0.5 * post.mu, hi=1.5 * post.mu, seed_mask=post.prior.seed_mask)
