@@ -568,7 +568,8 @@ def main():
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
                                            "k_population8<32, 4> (TZ 16) on the 64-sample population "
                                            f"({NCU_BYTES_PER_CELL_STEP:.3f} B per cell-step), scaled "
-                                           "by this launch's cell-steps",
+                                           "by this launch's cell-steps; the register-family variants "
+                                           "the autotuner picks between move the same density stream",
                          "kernel": f"k_population (autotuned variant {variant})", "kernel_ms": kern_ms,
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "peak_source": f"{peak_kind} hbm_gbs"},
