@@ -378,7 +378,8 @@ def surrogate_measurement(device, n=128, batch=32, reps=5):
     """Forward throughput of the bf16 U-Net surrogate at n^3 (its grid is
     (n/2)^3): milliseconds per sample of gbg_surrogate_loglik (features,
     network, upsampling, likelihood) on each convolution engine, and the
-    network's effective TFLOP/s (2 * 27 * Cin * Cout per voxel and layer)."""
+    network's effective TFLOP/s (2 * 27 * Cin * Cout per voxel and layer);
+    the same for one training step (loss and parameter gradient)."""
     from gliomauq_gb300 import _lib, synthetic as Syn
     an = Syn.make_anatomy(n, seed=0)
     lo = (Syn.PRIOR_DW_CM2[0], Syn.PRIOR_RHO[0], Syn.PRIOR_T[0])
@@ -408,6 +409,16 @@ def surrogate_measurement(device, n=128, batch=32, reps=5):
                 sg.loglik(smp)
             t = (time.perf_counter() - t0) / reps / batch
             out[eng] = {"ms_per_sample": 1e3 * t, "effective_tflops": flops / t / 1e12}
+            # one training step (forward, data and weight gradients, loss):
+            # three times the forward's convolution flops
+            targ = np.random.default_rng(1).uniform(0, 1, (batch, m, m, m)).astype(np.float32)
+            sg.loss_grad(smp, targ)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                sg.loss_grad(smp, targ)
+            t = (time.perf_counter() - t0) / reps / batch
+            out[eng]["train_step_ms_per_sample"] = 1e3 * t
+            out[eng]["train_effective_tflops"] = 3 * flops / t / 1e12
     finally:
         sg.close()
         h.close()

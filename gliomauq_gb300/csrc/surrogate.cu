@@ -1,7 +1,9 @@
 // Learned surrogate of the forward solve: a small 3D convolutional U-Net,
 // trained and evaluated with the kernels in this file. Forward and
 // data-gradient convolutions run on tcgen05 (k_conv_fwd_tc) by default, or
-// on mma.sync tiles (k_conv_fwd); the weight gradient on mma.sync.
+// on mma.sync tiles (k_conv_fwd); the weight gradient on mma.sync over
+// staged tiles (k_conv_wgrad_tiled: its GEMM has M, N = channels <= 64 and
+// K = voxels, below tcgen05's smallest M of 64).
 //
 // Tensors are channels-last, [batch][z][y][x][channel], bf16 activations and
 // weights with fp32 accumulation; a layer reads or writes a channel slice
@@ -569,6 +571,120 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(Geom g, Slice in, int Cin, S
         }
 }
 
+// Weight gradient on staged tiles. A persistent CTA (8 warps) walks voxel
+// tiles of 8 (x) x 8 (y) of one z-plane; per tile it stages the input's
+// 10 x 10 x 3 halo and the tile's output gradient in shared memory (16-byte
+// loads, rows padded by 8 channels so that ldmatrix rows fall in distinct
+// banks) and accumulates, for every (tap, 16 output channels, 8 input
+// channels) block it owns, dw += dout^T(16 x 16 voxels) in_tap(16 voxels x 8)
+// with mma.sync m16n8k16. Fragments come from ldmatrix.trans (both operands
+// are stored voxel-major, channels contiguous); the tap's shift is the row
+// addresses of the B fragment. Accumulators stay in registers over all of a
+// CTA's tiles and are added to dw (fp32 atomics) once at the end.
+// Needs W % 8 == 0, H % 8 == 0, slice strides and offsets multiples of 8.
+__device__ __forceinline__ void ldsm_x4_trans(unsigned r[4], const void *p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+__device__ __forceinline__ void ldsm_x2_trans(unsigned r[2], const void *p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
+                 : "=r"(r[0]), "=r"(r[1])
+                 : "r"(a));
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_conv_wgrad_tiled(Geom g, Slice in, Slice dout, float *__restrict__ dw) {
+    constexpr int TX = 8, TY = 8, TV = TX * TY;
+    constexpr int HX = TX + 2, HY = TY + 2, HV = 3 * HY * HX;
+    constexpr int CP = CIN + 8, OP = COUT + 8;  // padded voxel strides (elements)
+    // a warp owns the (tap, 8 input channels) blocks warp, warp + 8, ... for
+    // every group of 16 output channels (the B fragment serves them all)
+    constexpr int CT = COUT / 16, NT = CIN / 8, TN = 27 * NT, NW = 8;
+    constexpr int TPW = (TN + NW - 1) / NW;
+    __shared__ __align__(16) __nv_bfloat16 sh_in[HV * CP];
+    __shared__ __align__(16) __nv_bfloat16 sh_out[TV * OP];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int q = lane >> 3, i8 = lane & 7;
+    float acc[CT][TPW][4];
+#pragma unroll
+    for (int ct = 0; ct < CT; ++ct)
+#pragma unroll
+        for (int j = 0; j < TPW; ++j) acc[ct][j][0] = acc[ct][j][1] = acc[ct][j][2] = acc[ct][j][3] = 0.f;
+    const int tx_n = g.W / TX, ty_n = g.H / TY;
+    const long ntiles = (long)g.B * g.D * ty_n * tx_n;
+    for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int xt = (int)(t % tx_n);
+        long r = t / tx_n;
+        const int yt = (int)(r % ty_n);
+        r /= ty_n;
+        const int z = (int)(r % g.D), b = (int)(r / g.D);
+        const int x0 = xt * TX, y0 = yt * TY;
+        __syncthreads();  // the previous tile's fragments are read
+        for (int k = threadIdx.x; k < HV * (CIN / 8); k += blockDim.x) {
+            const int c8 = k % (CIN / 8), hv = k / (CIN / 8);
+            const int hx = hv % HX, hy = (hv / HX) % HY, hz = hv / (HX * HY);
+            const int X = x0 + hx - 1, Y = y0 + hy - 1, Z = z + hz - 1;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (X >= 0 && X < g.W && Y >= 0 && Y < g.H && Z >= 0 && Z < g.D)
+                v = *reinterpret_cast<const uint4 *>(in.p + ((((long)b * g.D + Z) * g.H + Y) * g.W + X) * in.stride +
+                                                     in.off + c8 * 8);
+            *reinterpret_cast<uint4 *>(sh_in + hv * CP + c8 * 8) = v;
+        }
+        for (int k = threadIdx.x; k < TV * (COUT / 8); k += blockDim.x) {
+            const int c8 = k % (COUT / 8), vv = k / (COUT / 8);
+            const int X = x0 + vv % TX, Y = y0 + vv / TX;
+            *reinterpret_cast<uint4 *>(sh_out + vv * OP + c8 * 8) = *reinterpret_cast<const uint4 *>(
+                dout.p + ((((long)b * g.D + z) * g.H + Y) * g.W + X) * dout.stride + dout.off + c8 * 8);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < TV / 16; ++ks) {
+            // A = dout^T for 16 voxels (rows 2ks, 2ks+1 of the tile): matrix q
+            // covers channels (q & 1) * 8 .. +7 and voxels (q >> 1) * 8 .. +7
+            unsigned a[CT][4];
+#pragma unroll
+            for (int ct = 0; ct < CT; ++ct)
+                ldsm_x4_trans(a[ct], sh_out + (ks * 16 + (q >> 1) * 8 + i8) * OP + ct * 16 + (q & 1) * 8);
+            // B rows: voxel (x = i8, y = 2ks + (q & 1)) shifted by the tap
+            const int vy = 2 * ks + (q & 1);
+#pragma unroll
+            for (int j = 0; j < TPW; ++j) {
+                const int tl = warp + j * NW;
+                if (tl < TN) {
+                    const int tap = tl / NT, nt = tl % NT;
+                    const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
+                    const int hidx = ((dz + 1) * HY + (vy + dy + 1)) * HX + (i8 + dx + 1);
+                    unsigned bf[2];
+                    ldsm_x2_trans(bf, sh_in + hidx * CP + nt * 8);
+#pragma unroll
+                    for (int ct = 0; ct < CT; ++ct) mma16816(acc[ct][j], a[ct], bf);
+                }
+            }
+        }
+    }
+    const int K = 27 * CIN, r0 = lane >> 2, kq = (lane & 3) * 2;
+#pragma unroll
+    for (int j = 0; j < TPW; ++j) {
+        const int tl = warp + j * NW;
+        if (tl < TN) {
+            const int tap = tl / NT, nt = tl % NT;
+#pragma unroll
+            for (int ct = 0; ct < CT; ++ct)
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int co = ct * 16 + r0 + 8 * h, ci = nt * 8 + kq + e;
+                        atomicAdd(dw + (long)co * K + tap * CIN + ci, acc[ct][j][2 * h + e]);
+                    }
+        }
+    }
+}
+
 // flipped/transposed weights for the data gradient: wt[ci][26-tap][co] = w[co][tap][ci]
 __global__ void k_flip_weights(const __nv_bfloat16 *__restrict__ w, int Cout, int Cin, __nv_bfloat16 *__restrict__ wt) {
     const long n = (long)Cout * 27 * Cin;
@@ -875,7 +991,26 @@ void conv_fwd(cudaStream_t st, Geom g, Slice in, int cin, const __nv_bfloat16 *w
     }
 }
 
-void conv_wgrad(cudaStream_t st, Geom g, Slice in, int cin, Slice dout, int cout, float *dw) {
+template <int CIN, int COUT>
+void wgrad_tiled(cudaStream_t st, Geom g, Slice in, Slice dout, float *dw, int num_sms) {
+    const long ntiles = (long)g.B * g.D * (g.H / 8) * (g.W / 8);
+    int bps = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_conv_wgrad_tiled<CIN, COUT>, 256, 0);
+    long grid = (long)(bps > 0 ? bps : 1) * num_sms;
+    if (grid > ntiles) grid = ntiles;
+    k_conv_wgrad_tiled<CIN, COUT><<<(unsigned)grid, 256, 0, st>>>(g, in, dout, dw);
+}
+
+void conv_wgrad(cudaStream_t st, Geom g, Slice in, int cin, Slice dout, int cout, float *dw, int num_sms) {
+    const bool tiled = g.W % 8 == 0 && g.H % 8 == 0 && in.stride % 8 == 0 && in.off % 8 == 0 &&
+                       dout.stride % 8 == 0 && dout.off % 8 == 0;
+    if (tiled) {
+        if (cin == 16 && cout == 16) return wgrad_tiled<16, 16>(st, g, in, dout, dw, num_sms);
+        if (cin == 16 && cout == 32) return wgrad_tiled<16, 32>(st, g, in, dout, dw, num_sms);
+        if (cin == 32 && cout == 16) return wgrad_tiled<32, 16>(st, g, in, dout, dw, num_sms);
+        if (cin == 32 && cout == 32) return wgrad_tiled<32, 32>(st, g, in, dout, dw, num_sms);
+        if (cin == 64 && cout == 16) return wgrad_tiled<64, 16>(st, g, in, dout, dw, num_sms);
+    }
     const long chunk = 2048;
     const int tiles = 27 * (cout / 16) * (cin / 8);
     dim3 grid((unsigned)((g.voxels() + chunk - 1) / chunk), (unsigned)((tiles + 3) / 4));
@@ -955,7 +1090,7 @@ void data_grad(Surrogate &s, Geom g, int i, Slice dout, Slice din) {
 
 void param_grad(Surrogate &s, Geom g, int i, Slice in, Slice dout) {
     const auto &l = s.net.L[i];
-    sg::conv_wgrad(s.h->stream, g, in, l.cin, dout, l.cout, s.g32 + l.w_off);
+    sg::conv_wgrad(s.h->stream, g, in, l.cin, dout, l.cout, s.g32 + l.w_off, s.h->num_sms);
     dim3 gb(64, l.cout);
     sg::k_bias_grad<<<gb, 256, 0, s.h->stream>>>(g.voxels(), l.cout, dout, s.g32 + l.b_off);
     s.h->launches += 2;
