@@ -33,6 +33,7 @@ EXPORTS = [
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
     "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_surrogate_set_engine",
+    "gbg_set_slopes", "gbg_get_slopes", "gbg_mala_step", "gbg_run_mala",
 ]
 
 
@@ -109,6 +110,10 @@ def load(path: str = LIB_PATH):
         "gbg_set_phi": [vp, dp],
         "gbg_get_phi": [vp, dp],
         "gbg_rd_step": [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_long],
+        "gbg_set_slopes": [vp, dp, dp],
+        "gbg_get_slopes": [vp, dp, dp],
+        "gbg_mala_step": [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_long],
+        "gbg_run_mala": [vp, C.c_double, C.c_double, C.c_double, C.c_double, lp, dp],
         "gbg_run": [vp, C.c_double, C.c_double, C.c_double, C.c_double, lp, dp],
         "gbg_set_observations": [vp, dp, dp, dp, dp, C.c_long, C.POINTER(LikParams)],
         "gbg_loglik": [vp, C.POINTER(LikResult)],
@@ -229,6 +234,28 @@ class Handle:
 
     def rd_step(self, Dw, Dg, rho, dt, nsteps=1):
         check(self.lib.gbg_rd_step(self._h, Dw, Dg, rho, dt, nsteps))
+
+    def set_slopes(self, sRho=None, sD=None):
+        """MALA variant: the slope fields (None = zero)."""
+        a = None if sRho is None else self._field(sRho)
+        b = None if sD is None else self._field(sD)
+        check(self.lib.gbg_set_slopes(self._h, dptr(a) if a is not None else None,
+                                      dptr(b) if b is not None else None))
+
+    def get_slopes(self):
+        sr = np.empty((self.n,) * 3, dtype=np.float64)
+        sd = np.empty((self.n,) * 3, dtype=np.float64)
+        check(self.lib.gbg_get_slopes(self._h, dptr(sr), dptr(sd)))
+        return sr, sd
+
+    def mala_step(self, Dw, Dg, rho, dt, nsteps=1):
+        check(self.lib.gbg_mala_step(self._h, Dw, Dg, rho, dt, nsteps))
+
+    def run_mala(self, Dw_file, rho, tend, L):
+        ns = C.c_long()
+        dt = C.c_double()
+        check(self.lib.gbg_run_mala(self._h, Dw_file, rho, tend, L, C.byref(ns), C.byref(dt)))
+        return ns.value, dt.value
 
     def run(self, Dw_file, rho, tend, L):
         ns = C.c_long()

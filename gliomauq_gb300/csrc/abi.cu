@@ -76,7 +76,7 @@ bool all_finite(const double *a, size_t n) {
 
 void free_handle(Handle &h) {
     void *ptrs[] = {h.pw, h.pg, h.phi[0], h.phi[1], h.b0, h.dfx, h.dfy, h.dfz, h.cx, h.cy, h.cz,
-                    h.msk, h.cxs, h.bphi[0], h.bphi[1], h.bwork, h.dev_status, h.barrier,
+                    h.msk, h.cxs, h.sr[0], h.sr[1], h.sd[0], h.sd[1], h.mala_tt, h.bphi[0], h.bphi[1], h.bwork, h.dev_status, h.barrier,
                     h.obs.pet_idx, h.obs.pet_val, h.obs.ti_idx, h.obs.t1_val, h.obs.t2_val,
                     h.lik_partials, h.lik_out, h.adj_ws, h.aff_phi0, h.aff_J, h.aff_out, h.aff_delta};
     for (void *p : ptrs)
@@ -215,6 +215,7 @@ int gbg_set_anatomy(gbg_handle *hh, const double *p_w, const double *p_g) {
     h.anatomy_set = true;
     h.tables_valid = false;
     h.fast_valid = false;
+    h.mala_valid = false;
     return GBG_OK;
 }
 
@@ -287,6 +288,126 @@ int gbg_rd_step(gbg_handle *hh, double Dw, double Dg, double rho, double dt, lon
         return gbg::fast_steps_single(h, Dw, rho, dt, nsteps);
     }
     return gbg::exact_steps(h, Dw, Dg, rho, dt, nsteps);
+}
+
+namespace {
+
+// slopes and the slopes' tissue tensor, allocated on first use (exact modes)
+int ensure_mala(Handle &h) {
+    if (h.prec == GBG_PREC_F32) {
+        set_error("the MALA variant runs in GBG_PREC_F64 or GBG_PREC_F32REF");
+        return GBG_ERR_UNSUPPORTED;
+    }
+    const size_t sb = storage_bytes(h.prec);
+    for (int k = 0; k < 2; ++k) {
+        if (!h.sr[k]) GBG_CUDA_TRY(cudaMalloc(&h.sr[k], h.N * sb));
+        if (!h.sd[k]) GBG_CUDA_TRY(cudaMalloc(&h.sd[k], h.N * sb));
+    }
+    if (!h.mala_tt) GBG_CUDA_TRY(cudaMalloc((void **)&h.mala_tt, 6 * h.N * sizeof(double)));
+    return GBG_OK;
+}
+
+}  // namespace
+
+int gbg_set_slopes(gbg_handle *hh, const double *sRho, const double *sD) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if ((sRho && !all_finite(sRho, h.N)) || (sD && !all_finite(sD, h.N))) {
+        set_error("slopes have NaN or Inf");
+        return GBG_ERR_NONFINITE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    if (int rc = ensure_mala(h)) return rc;
+    const size_t sb = storage_bytes(h.prec);
+    const double *src[2] = {sRho, sD};
+    void *dst[2] = {h.sr[h.cur], h.sd[h.cur]};
+    for (int k = 0; k < 2; ++k) {
+        if (!src[k]) {
+            GBG_CUDA_TRY(cudaMemsetAsync(dst[k], 0, h.N * sb, h.stream));
+        } else if (h.prec == GBG_PREC_F64) {
+            GBG_CUDA_TRY(cudaMemcpyAsync(dst[k], src[k], h.N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+            GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        } else {
+            std::vector<float> tmp(h.N);
+            for (size_t i = 0; i < h.N; ++i) tmp[i] = (float)src[k][i];
+            GBG_CUDA_TRY(cudaMemcpyAsync(dst[k], tmp.data(), h.N * sizeof(float), cudaMemcpyHostToDevice, h.stream));
+            GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        }
+    }
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    h.slopes_set = true;
+    return GBG_OK;
+}
+
+int gbg_get_slopes(gbg_handle *hh, double *sRho, double *sD) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!sRho || !sD) {
+        set_error("null field");
+        return GBG_ERR_ARG;
+    }
+    if (!h.slopes_set) {
+        set_error("slopes not set");
+        return GBG_ERR_STATE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    double *dst[2] = {sRho, sD};
+    void *src[2] = {h.sr[h.cur], h.sd[h.cur]};
+    for (int k = 0; k < 2; ++k) {
+        if (h.prec == GBG_PREC_F64) {
+            GBG_CUDA_TRY(cudaMemcpyAsync(dst[k], src[k], h.N * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+            GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        } else {
+            std::vector<float> tmp(h.N);
+            GBG_CUDA_TRY(cudaMemcpyAsync(tmp.data(), src[k], h.N * sizeof(float), cudaMemcpyDeviceToHost, h.stream));
+            GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+            for (size_t i = 0; i < h.N; ++i) dst[k][i] = (double)tmp[i];
+        }
+    }
+    return GBG_OK;
+}
+
+int gbg_mala_step(gbg_handle *hh, double Dw, double Dg, double rho, double dt, long nsteps) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!h.anatomy_set || !h.phi_set) {
+        set_error("set anatomy and phi before stepping");
+        return GBG_ERR_STATE;
+    }
+    if (nsteps < 0 || !std::isfinite(Dw) || !std::isfinite(Dg) || !std::isfinite(rho) ||
+        !std::isfinite(dt) || !(Dw > 0) || !(Dg >= 0) || !(dt > 0)) {
+        set_error("bad step parameters");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    if (!h.slopes_set)
+        if (int rc = gbg_set_slopes(hh, nullptr, nullptr)) return rc;
+    if (int rc = ensure_mala(h)) return rc;
+    return gbg::mala_steps(h, Dw, Dg, rho, dt, nsteps);
+}
+
+int gbg_run_mala(gbg_handle *hh, double Dw_file, double rho, double tend, double L, long *nsteps_out,
+                 double *dt_out) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!std::isfinite(Dw_file) || !std::isfinite(rho) || !std::isfinite(tend) || !(L > 0) ||
+        !(Dw_file > 0)) {
+        set_error("bad run parameters");
+        return GBG_ERR_ARG;
+    }
+    if (h.prec == GBG_PREC_F32) {
+        set_error("the MALA variant runs in GBG_PREC_F64 or GBG_PREC_F32REF");
+        return GBG_ERR_UNSUPPORTED;
+    }
+    double dt, Dw, Dg, r = rho;
+    gbg::reference_dt(h.n, Dw_file, L, h.prec == GBG_PREC_F32REF, &dt, &Dw, &Dg, &r);
+    const long ns = gbg::reference_num_steps(dt, tend);
+    if (nsteps_out) *nsteps_out = ns;
+    if (dt_out) *dt_out = dt;
+    int rc = gbg_mala_step(hh, Dw, Dg, r, dt, ns);
+    if (rc) return rc;
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    return GBG_OK;
 }
 
 int gbg_run(gbg_handle *hh, double Dw_file, double rho, double tend, double L, long *nsteps_out,

@@ -81,6 +81,15 @@ struct Handle {
     double tab_Dw = -1, tab_Dg = -1;  // (Dw, Dg) the tables were built for
     bool tables_valid = false;
 
+    // MALA variant (exact modes): slopes sRho, sD ping-pong in the storage
+    // type (index cur, with phi), and the slopes' tissue tensor, 6 doubles per
+    // cell (SoA, faces W, E, S, N, B, F) for the ratio Dg/Dw it was built for
+    void *sr[2] = {nullptr, nullptr}, *sd[2] = {nullptr, nullptr};
+    bool slopes_set = false;
+    double *mala_tt = nullptr;
+    double mala_ratio = -1;
+    bool mala_valid = false;
+
     // fast mode: unit-diffusivity face coefficients and tissue mask (float SoA)
     float *cx = nullptr, *cy = nullptr, *cz = nullptr, *msk = nullptr;
     float *cxs = nullptr;  // cx with the sign bit set where msk is 0 (population kernels)
@@ -127,6 +136,9 @@ struct Handle {
 // ---- rd_exact.cu ----
 int exact_build_tables(Handle &h, double Dw, double Dg);
 int exact_steps(Handle &h, double Dw, double Dg, double rho, double dt, long nsteps);
+// nsteps steps of the MALA variant: phi (exact_steps) and the slopes; the
+// slopes must be allocated and set
+int mala_steps(Handle &h, double Dw, double Dg, double rho, double dt, long nsteps);
 
 // ---- rd_fast.cu ----
 // Per-sample schedule record of the batched solver (stored sorted by nsteps,

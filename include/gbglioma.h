@@ -96,6 +96,35 @@ int gbg_rd_step(gbg_handle *h, double Dw, double Dg, double rho, double dt, long
 int gbg_run(gbg_handle *h, double Dw_file, double rho, double tend, double L, long *nsteps_out,
             double *dt_out);
 
+/* ---- the MALA variant (exact modes) ------------------------------------------
+ * Glioma_HG_UQ_MALA carries two more cell fields, the slopes sRho = dphi/drho
+ * and sD = dphi/dDw (CCell_extended::sRho, sD,
+ * source/Glioma/Glioma_Types.h:61-62), zero at the start.
+ *
+ * gbg_set_slopes: n^3 doubles each, converted to the storage type; NULL sets
+ * that field to zero. gbg_get_slopes reads both back. GBG_PREC_F64 and
+ * GBG_PREC_F32REF only (GBG_ERR_UNSUPPORTED otherwise). */
+int gbg_set_slopes(gbg_handle *h, const double *sRho, const double *sD);
+int gbg_get_slopes(gbg_handle *h, double *sRho, double *sD);
+
+/* nsteps steps of Glioma_HG_UQ_MALA::_reactionDiffusionMALAStep
+ * (source/Glioma/Glioma_HG_UQ_MALA.cpp:575-591): the RD right-hand side and
+ * the slopes' right-hand side (Glioma_MALAslopesRHS<3>,
+ * source/Glioma/Glioma_MALA_SlopesOperator.h:13-188) from the state before
+ * the step, then UpdateTumor and UpdateMALAslopes (:190-226). Arguments as
+ * gbg_rd_step. The slopes operator is the reference's as written: its
+ * tissue tensor is the non-Case2 harmonic mean with Neumann doubling, and
+ * its sources are phi (1 - phi) and div(T grad phi) without the linearised
+ * reaction term, so sRho and sD are the reference's slopes, not exact
+ * derivatives of phi (gbg_adjoint gives those). Slopes not set are zero. */
+int gbg_mala_step(gbg_handle *h, double Dw, double Dg, double rho, double dt, long nsteps);
+
+/* The MALA variant's whole loop (Glioma_HG_UQ_MALA::run,
+ * source/Glioma/Glioma_HG_UQ_MALA.cpp:717-758): arguments, parameter rescale,
+ * step rule and loop as gbg_run. */
+int gbg_run_mala(gbg_handle *h, double Dw_file, double rho, double tend, double L, long *nsteps_out,
+                 double *dt_out);
+
 /* ---- imaging log-likelihood (source/Likelihood/source/HGG_Likelihood.cpp) --
  * Observations: PET, T1, T2 fields (n^3 doubles each, PET_data.dat,
  * T1_data.dat, T2_data.dat) and the Sphere.dat point set, npoints x 3 voxel

@@ -195,6 +195,99 @@ void orc_rd_solve_f32ref(int n, const float *pw, const float *pg, float *phi, fl
     free(tmp);
 }
 
+/* ---------------- MALA slopes (Glioma_MALA_SlopesOperator.h) -------------
+ * Tissue tensor of one cell, :131-148: tt[f] = 2/(1/a_c + 1/a_f) with
+ * a = p_w + p_g * ratioD (1/0 = inf makes a face to a cell outside the
+ * tissue 0), all zero outside the tissue, then the Neumann doubling in order.
+ * a_c, a_f are computed by the caller (double; from float fields in the
+ * default build). */
+static void slopes_tt(int inside, const double a[7], double tt[6]) {
+    for (int f = 0; f < 6; ++f) tt[f] = 0.0;
+    if (inside) {
+        for (int f = 0; f < 6; ++f) tt[f] = 2.0 * (1.0 / ((1.0 / a[0]) + (1.0 / a[f + 1])));
+        if (tt[0] == 0) tt[1] *= 2.0;
+        if (tt[1] == 0) tt[0] *= 2.0;
+        if (tt[2] == 0) tt[3] *= 2.0;
+        if (tt[3] == 0) tt[2] *= 2.0;
+        if (tt[4] == 0) tt[5] *= 2.0;
+        if (tt[5] == 0) tt[4] *= 2.0;
+    }
+}
+
+/* :152-182: the two rates, in the reference's evaluation order; s, d, p are
+ * sRho, sD and phi at (c, W, E, S, N, B, F) widened to double, DwR = Dw as
+ * stored (Real). */
+static void slopes_rates(const double tt[6], const double s[7], const double d[7], const double p[7],
+                         double DwR, double ih2, double *dsr, double *dsd) {
+    const double tsum = tt[0] + tt[1] + tt[2] + tt[3] + tt[4] + tt[5];
+    const double inR = ih2 * DwR * (tt[0] * s[1] + tt[1] * s[2] + tt[2] * s[3] + tt[3] * s[4] +
+                                    tt[4] * s[5] + tt[5] * s[6]);
+    const double outR = -ih2 * DwR * tsum * s[0];
+    const double reR = p[0] * (1. - p[0]);
+    *dsr = outR + inR + reR;
+    const double inD = ih2 * DwR * (tt[0] * d[1] + tt[1] * d[2] + tt[2] * d[3] + tt[3] * d[4] +
+                                    tt[4] * d[5] + tt[5] * d[6]);
+    const double outD = -ih2 * DwR * tsum * d[0];
+    const double rin = ih2 * (tt[0] * p[1] + tt[1] * p[2] + tt[2] * p[3] + tt[3] * p[4] +
+                              tt[4] * p[5] + tt[5] * p[6]);
+    const double rout = -ih2 * tsum * p[0];
+    *dsd = outD + inD + rin + rout;
+}
+
+void orc_mala_step_f64(int n, const double *pw, const double *pg, const double *phi_in,
+                       const double *sr_in, const double *sd_in, double *phi_out,
+                       double *sr_out, double *sd_out, double Dw, double Dg, double rho,
+                       double dt, double h) {
+    orc_rd_step_f64(n, pw, pg, phi_in, phi_out, Dw, Dg, rho, dt, h, 1);
+    const double ih2 = 1. / (h * h), ratioD = Dg / Dw;
+    for (int z = 0; z < n; ++z)
+        for (int y = 0; y < n; ++y)
+            for (int x = 0; x < n; ++x) {
+                const size_t id[7] = {IDX(x, y, z), IDX((x + n - 1) % n, y, z), IDX((x + 1) % n, y, z),
+                                      IDX(x, (y + n - 1) % n, z), IDX(x, (y + 1) % n, z),
+                                      IDX(x, y, (z + n - 1) % n), IDX(x, y, (z + 1) % n)};
+                double a[7], s[7], d[7], p[7], tt[6], dsr, dsd;
+                for (int k = 0; k < 7; ++k) {
+                    a[k] = pw[id[k]] + pg[id[k]] * ratioD;
+                    s[k] = sr_in[id[k]];
+                    d[k] = sd_in[id[k]];
+                    p[k] = phi_in[id[k]];
+                }
+                slopes_tt(pw[id[0]] > 0.0 || pg[id[0]] > 0.0, a, tt);
+                slopes_rates(tt, s, d, p, Dw, ih2, &dsr, &dsd);
+                sr_out[id[0]] = s[0] + dt * dsr;
+                sd_out[id[0]] = d[0] + dt * dsd;
+            }
+}
+
+void orc_mala_step_f32ref(int n, const float *pw, const float *pg, const float *phi_in,
+                          const float *sr_in, const float *sd_in, float *phi_out, float *sr_out,
+                          float *sd_out, float Dw, float Dg, float rho, double dt, double h) {
+    orc_rd_step_f32ref(n, pw, pg, phi_in, phi_out, Dw, Dg, rho, dt, h, 1);
+    const double ih2 = 1. / (h * h);
+    const double ratioD = (double)(Dg / Dw); /* Real / Real, then widened (:117) */
+    for (int z = 0; z < n; ++z)
+        for (int y = 0; y < n; ++y)
+            for (int x = 0; x < n; ++x) {
+                const size_t id[7] = {IDX(x, y, z), IDX((x + n - 1) % n, y, z), IDX((x + 1) % n, y, z),
+                                      IDX(x, (y + n - 1) % n, z), IDX(x, (y + 1) % n, z),
+                                      IDX(x, y, (z + n - 1) % n), IDX(x, y, (z + 1) % n)};
+                double a[7], s[7], d[7], p[7], tt[6], dsr, dsd;
+                for (int k = 0; k < 7; ++k) {
+                    a[k] = (double)pw[id[k]] + (double)pg[id[k]] * ratioD;
+                    s[k] = sr_in[id[k]];
+                    d[k] = sd_in[id[k]];
+                    p[k] = phi_in[id[k]];
+                }
+                slopes_tt(pw[id[0]] > 0.0 || pg[id[0]] > 0.0, a, tt);
+                slopes_rates(tt, s, d, p, (double)Dw, ih2, &dsr, &dsd);
+                /* the rates are stored as Real (:162,:182), the update in double (:221-222) */
+                const float fr = (float)dsr, fd = (float)dsd;
+                sr_out[id[0]] = (float)((double)sr_in[id[0]] + dt * (double)fr);
+                sd_out[id[0]] = (float)((double)sd_in[id[0]] + dt * (double)fd);
+            }
+}
+
 long orc_num_steps(double dt, double tend) {
     double t = 0.0;
     long k = 0;

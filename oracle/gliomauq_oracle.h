@@ -77,6 +77,24 @@ void orc_loglik(int nx, int ny, int nz, const double *model, const double *pet,
                 const orc_lik_params *p, int step_pet, int step_ti, int selective,
                 orc_lik_result *out);
 
+/* One step of the MALA variant (Glioma_HG_UQ_MALA::_reactionDiffusionMALAStep,
+ * source/Glioma/Glioma_HG_UQ_MALA.cpp:575-591): the RD step above plus the
+ * slopes sRho = dphi/drho and sD = dphi/dDw of Glioma_MALAslopesRHS<3> and
+ * UpdateMALAslopes<3> (source/Glioma/Glioma_MALA_SlopesOperator.h:122-187,
+ * 215-223), both right-hand sides from the state before the step. The
+ * slopes' tissue tensor is the non-Case2 one (harmonic means of
+ * p_w + p_g Dg/Dw, Neumann doubling where a face is 0) and their sources are
+ * phi (1 - phi) and div(T grad phi), as the reference writes them. Outputs
+ * must not alias inputs. f64: double storage; f32ref: the default build
+ * (float storage, double fluxes, rates rounded to float). */
+void orc_mala_step_f64(int n, const double *pw, const double *pg, const double *phi_in,
+                       const double *sr_in, const double *sd_in, double *phi_out,
+                       double *sr_out, double *sd_out, double Dw, double Dg, double rho,
+                       double dt, double h);
+void orc_mala_step_f32ref(int n, const float *pw, const float *pg, const float *phi_in,
+                          const float *sr_in, const float *sd_in, float *phi_out, float *sr_out,
+                          float *sd_out, float Dw, float Dg, float rho, double dt, double h);
+
 /* Number of steps the reference's time loop takes: while (t <= tend) t += dt
  * (source/Glioma/Glioma_HG_UQ.cpp:544-552). */
 long orc_num_steps(double dt, double tend);

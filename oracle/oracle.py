@@ -42,6 +42,10 @@ def lib():
         L.orc_blockgrid_destroy.argtypes = [C.c_void_p]
         L.orc_loglik.argtypes = [C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, C.c_long,
                                  C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.orc_mala_step_f64.argtypes = [C.c_int, dp, dp, dp, dp, dp, dp, dp, dp, C.c_double,
+                                        C.c_double, C.c_double, C.c_double, C.c_double]
+        L.orc_mala_step_f32ref.argtypes = [C.c_int, fp, fp, fp, fp, fp, fp, fp, fp, C.c_float,
+                                           C.c_float, C.c_float, C.c_double, C.c_double]
         L.orc_num_steps.restype = C.c_long
         L.orc_num_steps.argtypes = [C.c_double, C.c_double]
         _lib = L
@@ -80,6 +84,29 @@ def rd_solve(pw, pg, phi0, Dw, Dg, rho, dt, nsteps, prec="f64", nthreads=0):
     else:
         raise ValueError(prec)
     return phi
+
+
+def mala_solve(pw, pg, phi0, Dw, Dg, rho, dt, nsteps, prec="f64", sr0=None, sd0=None):
+    """nsteps steps of the MALA variant (phi and the slopes sRho, sD, from
+    zero slopes unless given); returns (phi, sRho, sD)."""
+    n = pw.shape[0]
+    h = 1.0 / n
+    t = np.float64 if prec == "f64" else np.float32
+    ct = C.c_double if prec == "f64" else C.c_float
+    if prec not in ("f64", "f32ref"):
+        raise ValueError(prec)
+    a = [np.ascontiguousarray(x, dtype=t) for x in (pw, pg)]
+    cur = [np.array(phi0, dtype=t, order="C", copy=True),
+           np.zeros_like(a[0]) if sr0 is None else np.array(sr0, dtype=t, order="C", copy=True),
+           np.zeros_like(a[0]) if sd0 is None else np.array(sd0, dtype=t, order="C", copy=True)]
+    nxt = [np.empty_like(x) for x in cur]
+    f = lib().orc_mala_step_f64 if prec == "f64" else lib().orc_mala_step_f32ref
+    par = (Dw, Dg, rho) if prec == "f64" else (np.float32(Dw), np.float32(Dg), np.float32(rho))
+    for _ in range(nsteps):
+        f(n, _p(a[0], ct), _p(a[1], ct), *[_p(x, ct) for x in cur], *[_p(x, ct) for x in nxt],
+          *par, dt, h)
+        cur, nxt = nxt, cur
+    return tuple(cur)
 
 
 class BlockGrid:

@@ -9,6 +9,8 @@
 //   BlockProcessing (TBB pipeline)      source/MRAGmultithreading/MRAGBlockProcessing_TBB.h:314-512
 //   Glioma_ReactionDiffusionOperator<3> source/Glioma/Glioma_ReactionDiffusionOperator.h:12-222
 //   UpdateTumor<3>                      source/Glioma/Glioma_ReactionDiffusionOperator.h:227-266
+//   Glioma_MALAslopesRHS<3>, UpdateMALAslopes<3>
+//                                       source/Glioma/Glioma_MALA_SlopesOperator.h:13-229
 //   Science::AutomaticRefinement/Compression
 //                                       source/MRAGscience/MRAGScienceCore.h:42-177
 // The time loop is Glioma_HG_UQ::run (source/Glioma/Glioma_HG_UQ.cpp:511-588)
@@ -26,7 +28,11 @@
 //                       maxima after the loop, blocks after k more steps,
 //                       blocks after one more regrid
 //   timing <in>         times steps only (no output), prints cell-steps/s
+//   mala   <in> <out>   nsteps steps of Glioma_HG_UQ_MALA::_reactionDiffusionMALAStep
+//                       (source/Glioma/Glioma_HG_UQ_MALA.cpp:575-591) from zero
+//                       slopes; writes phi, sRho and sD on the uniform grid
 #include "Glioma_Types.h"
+#include "Glioma_MALA_SlopesOperator.h"
 
 #include <chrono>
 #include <cstdint>
@@ -134,6 +140,20 @@ struct Sim {
         UpdateTumor<_DIM> updateTumor(dt);
         blockProcessing.pipeline_process(vInfo, coll, *bi, rhs);
         BlockProcessing::process(vInfo, coll, updateTumor, gran);
+    }
+    // Glioma_HG_UQ_MALA::_reactionDiffusionMALAStep (Glioma_HG_UQ_MALA.cpp:575-591):
+    // both right-hand sides from the state before the step, then both updates
+    void malaStep(BoundaryInfo *bi, int gran, Real Dw, Real Dg, Real rho, double dt) {
+        vector<BlockInfo> vInfo = grid->getBlocksInfo();
+        const BlockCollection<B> &coll = grid->getBlockCollection();
+        Glioma_ReactionDiffusionOperator<_DIM> rhs(Dw, Dg, rho);
+        UpdateTumor<_DIM> updateTumor(dt);
+        Glioma_MALAslopesRHS<_DIM> slopesRhs(Dw, Dg);
+        UpdateMALAslopes<_DIM> updateSlopes(dt);
+        blockProcessing.pipeline_process(vInfo, coll, *bi, rhs);
+        blockProcessing.pipeline_process(vInfo, coll, *bi, slopesRhs);
+        BlockProcessing::process(vInfo, coll, updateTumor, gran);
+        BlockProcessing::process(vInfo, coll, updateSlopes, gran);
     }
     void regrid() {
         const int r = Science::AutomaticRefinement<0, 0>(*grid, blockfwt, refinement_tolerance, maxLevel, 1, &profiler);
@@ -244,6 +264,61 @@ static std::vector<double> uniformPhi(Grid<W, B> &grid, int n) {
         grid.getBlockCollection().release(info.blockID);
     }
     return out;
+}
+
+// One cell field of a uniform grid at the finest level (no regridding).
+template <typename F>
+static std::vector<double> uniformField(Grid<W, B> &grid, int n, F get) {
+    std::vector<double> out((size_t)n * n * n, 0.0);
+    std::vector<BlockInfo> vInfo = grid.getBlocksInfo();
+    for (size_t i = 0; i < vInfo.size(); i++) {
+        BlockInfo &info = vInfo[i];
+        B &block = grid.getBlockCollection()[info.blockID];
+        for (int iz = 0; iz < B::sizeZ; iz++)
+            for (int iy = 0; iy < B::sizeY; iy++)
+                for (int ix = 0; ix < B::sizeX; ix++) {
+                    const size_t gx = (size_t)info.index[0] * B::sizeX + ix;
+                    const size_t gy = (size_t)info.index[1] * B::sizeY + iy;
+                    const size_t gz = (size_t)info.index[2] * B::sizeZ + iz;
+                    out[gx + n * (gy + n * gz)] = get(block(ix, iy, iz));
+                }
+        grid.getBlockCollection().release(info.blockID);
+    }
+    return out;
+}
+
+// The MALA variant's loop (Glioma_HG_UQ_MALA::run, Glioma_HG_UQ_MALA.cpp:717-758:
+// the same parameter rescale and step rule as Glioma_HG_UQ::run) for a fixed
+// number of steps on a uniform grid.
+static int cmdMala(const char *inp, const char *outp) {
+    Input in = readInput(inp);
+    if (in.nsteps < 0 || in.adaptive) die("mala: fixed nsteps, uniform grid");
+    Sim s(in.bpd);
+    fillGrid(*s.grid, in);
+    const int gran = (s.grid->getBlocksInfo().size() <= 8 ? 1 : 4);
+    BoundaryInfo *boundaryInfo = &s.grid->getBoundaryInfo();
+    Real Dw = (Real)in.Dw_file, rho = (Real)in.rho, Dg;
+    const double L = in.L;
+    Dw = Dw / (L * L);
+    Dg = 0.1 * Dw;
+    double h = 1. / (blockSize * in.bpd);
+    double dt = 0.99 * h * h / (2. * _DIM * std::max(Dw, Dg));
+    for (long k = 0; k < in.nsteps; ++k) s.malaStep(boundaryInfo, gran, Dw, Dg, rho, dt);
+    FILE *f = fopen(outp, "wb");
+    if (!f) die("cannot open output");
+    fwrite("GBGMAL01", 1, 8, f);
+    int32_t hdr[4] = {in.n, (int32_t)sizeof(Real), (int32_t)in.nsteps, 0};
+    fwrite(hdr, 4, 4, f);
+    double dh[4] = {dt, (double)Dw, (double)Dg, (double)rho};
+    fwrite(dh, 8, 4, f);
+    std::vector<double> u = uniformField(*s.grid, in.n, [](const CCell_extended &c) { return (double)c.phi; });
+    std::vector<double> sr = uniformField(*s.grid, in.n, [](const CCell_extended &c) { return (double)c.sRho; });
+    std::vector<double> sd = uniformField(*s.grid, in.n, [](const CCell_extended &c) { return (double)c.sD; });
+    fwrite(u.data(), 8, u.size(), f);
+    fwrite(sr.data(), 8, sr.size(), f);
+    fwrite(sd.data(), 8, sd.size(), f);
+    fclose(f);
+    return 0;
 }
 
 static int cmdSolve(const char *inp, const char *outp) {
@@ -465,6 +540,7 @@ int main(int argc, const char **argv) {
     if (cmd == "ghosts") return cmdGhosts(argv[2], argv[3]);
     if (cmd == "fwt") return cmdFwt(argv[2], argv[3]);
     if (cmd == "state") return cmdState(argv[2], argv[3], argc > 4 ? atoi(argv[4]) : 10);
+    if (cmd == "mala") return cmdMala(argv[2], argv[3]);
     die("unknown command");
     return 2;
 }

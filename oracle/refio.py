@@ -45,6 +45,19 @@ def read_solve_output(path):
                 rho=rho, phi=u, blocks=blocks)
 
 
+def read_mala_output(path):
+    """Output of `ref_harness mala`: phi, sRho, sD on the uniform grid."""
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"GBGMAL01"
+    n, real_bytes, steps, _ = struct.unpack_from("<4i", raw, 8)
+    dt, dw, dg, rho = struct.unpack_from("<4d", raw, 24)
+    off = 56
+    N = n ** 3
+    f = [np.frombuffer(raw, "<f8", N, off + 8 * N * k).reshape(n, n, n).copy() for k in range(3)]
+    return dict(n=n, real_bytes=real_bytes, steps=steps, dt=dt, Dw=dw, Dg=dg, rho=rho,
+                phi=f[0], sRho=f[1], sD=f[2])
+
+
 def read_ghosts(path):
     raw = open(path, "rb").read()
     assert raw[:8] == b"GBGGHO01"
@@ -99,6 +112,8 @@ def run_harness(cmd, variant, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, adapti
                        stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
         if cmd == "solve":
             return read_solve_output(outp)
+        if cmd == "mala":
+            return read_mala_output(outp)
         if cmd == "ghosts":
             return read_ghosts(outp)
         if cmd == "fwt":

@@ -86,6 +86,26 @@ def rd_fixtures():
         json.dump(meta, f, indent=1)
 
 
+def mala_fixture():
+    # 32^3 (2^3 blocks): the MALA variant's step (phi and the slopes sRho, sD)
+    # after 1 and 40 steps from zero slopes, FP64 and FP32 builds
+    n, bpd = 32, 2
+    pw, pg, phi0 = inputs(n, 3, (14.6, 16.3, 15.2))
+    Dw, rho, L = 0.13 / 100, 0.025, n * 0.1
+    out = dict(p_w=pw.astype(np.float32), p_g=pg.astype(np.float32),
+               phi0=phi0.astype(np.float32), Dw_file=Dw, rho=rho, L=L)
+    for variant in ("f64", "f32"):
+        for k in (1, 40):
+            r = refio.run_harness("mala", variant, n, bpd, pw, pg, phi0, Dw, rho, 0.0, L, nsteps=k)
+            for f in ("phi", "sRho", "sD"):
+                v = r[f]
+                out[f"{f}_{variant}_{k}"] = v if variant == "f64" else v.astype(np.float32)
+            out[f"dt_{variant}"] = r["dt"]
+            out[f"Dw_{variant}"] = r["Dw"]
+            out[f"Dg_{variant}"] = r["Dg"]
+    np.savez_compressed(os.path.join(HERE, "mala32.npz"), **out)
+
+
 def lik_fixture():
     """The reference `likelihood` program on a 32^3 model and seeded observations."""
     d = np.load(os.path.join(HERE, "rd32.npz"))
@@ -263,7 +283,11 @@ def cli_observations(u):
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 1 and sys.argv[1] == "mala":
+        mala_fixture()
+        sys.exit(0)
     rd_fixtures()
+    mala_fixture()
     lik_fixture()
     amr_fixtures()
     cli_fixture()

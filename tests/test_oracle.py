@@ -32,6 +32,24 @@ def test_oracle_f32ref_matches_reference_bitwise(oracle_lib, k):
     assert np.array_equal(out, d[f"phi_f32_{k}"])
 
 
+@pytest.mark.parametrize("k", [1, 40])
+@pytest.mark.parametrize("prec,variant", [("f64", "f64"), ("f32ref", "f32")])
+def test_oracle_mala_matches_reference_bitwise(oracle_lib, prec, variant, k):
+    """The MALA variant's step (phi and the slopes sRho, sD of
+    Glioma_MALA_SlopesOperator.h) against the reference compiled in place."""
+    d = golden_npz("mala32.npz")
+    t = np.float64 if prec == "f64" else np.float32
+    pw, pg, phi0 = (d[x].astype(t) for x in ("p_w", "p_g", "phi0"))
+    phi, sr, sd = oracle_lib.mala_solve(pw, pg, phi0, float(d[f"Dw_{variant}"]),
+                                        float(d[f"Dg_{variant}"]), float(d["rho"]),
+                                        float(d[f"dt_{variant}"]), k, prec=prec)
+    for name, a in (("phi", phi), ("sRho", sr), ("sD", sd)):
+        g = d[f"{name}_{variant}_{k}"]
+        assert np.array_equal(a, g), name
+    # the slopes are not trivially zero
+    assert np.abs(sr).max() > 0 and np.abs(sd).max() > 0
+
+
 @pytest.mark.parametrize("variant", ["f64", "f32"])
 def test_oracle_config1_full_solve(oracle_lib, variant):
     meta = golden_json("c1_64.json")
