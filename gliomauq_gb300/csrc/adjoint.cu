@@ -74,13 +74,21 @@ struct Tabs {
 };
 
 // L(f)_c = sum_f c_f (f_nb - f_c)
+// cell c of an n^3 field (n <= 1024, so every index fits 32 bits) -> x, y, z
+__device__ __forceinline__ void decomp(int c, int n, int &x, int &y, int &z) {
+    const int row = c / n;
+    x = c - row * n;
+    z = row / n;
+    y = row - z * n;
+}
+
 template <typename Real>
 __device__ __forceinline__ Real lap(const Real *f, const Real *cx, const Real *cy, const Real *cz, int n,
-                                    size_t c, int x, int y, int z) {
-    const size_t nn = n, pl = nn * nn;
-    const size_t cW = c - x + wm(x, n), cE = c - x + wp(x, n);
-    const size_t cS = c + ((size_t)wm(y, n) - y) * nn, cN = c + ((size_t)wp(y, n) - y) * nn;
-    const size_t cB = c + ((size_t)wm(z, n) - z) * pl, cF = c + ((size_t)wp(z, n) - z) * pl;
+                                    int c, int x, int y, int z) {
+    const int pl = n * n;
+    const int cW = c - x + wm(x, n), cE = c - x + wp(x, n);
+    const int cS = c + (wm(y, n) - y) * n, cN = c + (wp(y, n) - y) * n;
+    const int cB = c + (wm(z, n) - z) * pl, cF = c + (wp(z, n) - z) * pl;
     const Real f0 = f[c];
     return cx[cW] * (f[cW] - f0) + cx[c] * (f[cE] - f0) + cy[cS] * (f[cS] - f0) + cy[c] * (f[cN] - f0) +
            cz[cB] * (f[cB] - f0) + cz[c] * (f[cF] - f0);
@@ -93,11 +101,11 @@ __device__ __forceinline__ double fma_r(double a, double b, double c) { return f
 // solver's operation order (faces -x, +x, -y, +y, -z, +z)
 template <typename Real>
 __device__ __forceinline__ Real step_value(const Real *f, const Real *cx, const Real *cy, const Real *cz, int n,
-                                           size_t c, int x, int y, int z, Real a, Real b) {
-    const size_t nn = n, pl = nn * nn;
-    const size_t cW = c - x + wm(x, n), cE = c - x + wp(x, n);
-    const size_t cS = c + ((size_t)wm(y, n) - y) * nn, cN = c + ((size_t)wp(y, n) - y) * nn;
-    const size_t cB = c + ((size_t)wm(z, n) - z) * pl, cF = c + ((size_t)wp(z, n) - z) * pl;
+                                           int c, int x, int y, int z, Real a, Real b) {
+    const int pl = n * n;
+    const int cW = c - x + wm(x, n), cE = c - x + wp(x, n);
+    const int cS = c + (wm(y, n) - y) * n, cN = c + (wp(y, n) - y) * n;
+    const int cB = c + (wm(z, n) - z) * pl, cF = c + (wp(z, n) - z) * pl;
     const Real f0 = f[c];
     Real lap = cx[cW] * (f[cW] - f0);
     lap = fma_r(cx[c], f[cE] - f0, lap);
@@ -112,10 +120,12 @@ __device__ __forceinline__ Real step_value(const Real *f, const Real *cx, const 
 template <typename Real>
 __global__ void k_adj_ic(int n, int S, const gbg_sample *__restrict__ smp, double peak, double sigma,
                          const double *__restrict__ pw, const double *__restrict__ pg, Real *__restrict__ phi) {
-    const size_t N = (size_t)n * n * n;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N * S; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t s = i / N, c = i % N;
-        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+    const int N = n * n * n;
+    for (int s = blockIdx.y; s < S; s += gridDim.y)
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+        const size_t i = (size_t)s * N + c;
+        int x, y, z;
+        decomp(c, n, x, y, z);
         double v = 0.0;
         if (pw[c] + pg[c] > 0.0) {
             const double dx = x - smp[s].x0, dy = y - smp[s].y0, dz = z - smp[s].z0;
@@ -130,20 +140,25 @@ __global__ void k_adj_ic(int n, int S, const gbg_sample *__restrict__ smp, doubl
 template <typename Real>
 __global__ void k_adj_fwd(int n, int S, const Real *__restrict__ in, Real *__restrict__ out, Tabs t,
                           const double *__restrict__ a, const double *__restrict__ b) {
-    const size_t N = (size_t)n * n * n;
+    const int N = n * n * n;
     const Real *cx = (const Real *)t.cx, *cy = (const Real *)t.cy, *cz = (const Real *)t.cz,
                *m = (const Real *)t.msk;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N * S; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t s = i / N, c = i % N;
-        const Real *f = in + s * N;
-        if (a[s] < 0) {
-            out[i] = f[c];
-            continue;
+    for (int s = blockIdx.y; s < S; s += gridDim.y) {
+        const Real *f = in + (size_t)s * N;
+        Real *o = out + (size_t)s * N;
+        const bool act = a[s] >= 0;
+        const Real as = (Real)a[s], bs = (Real)b[s];
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            if (!act) {
+                o[c] = f[c];
+                continue;
+            }
+            int x, y, z;
+            decomp(c, n, x, y, z);
+            Real v = step_value(f, cx, cy, cz, n, c, x, y, z, as, bs);
+            v = v < (Real)0 ? (Real)0 : (v > (Real)1 ? (Real)1 : v);
+            o[c] = m[c] != (Real)0 ? v : (Real)0;
         }
-        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
-        Real v = step_value(f, cx, cy, cz, n, c, x, y, z, (Real)a[s], (Real)b[s]);
-        v = v < (Real)0 ? (Real)0 : (v > (Real)1 ? (Real)1 : v);
-        out[i] = m[c] != (Real)0 ? v : (Real)0;
     }
 }
 
@@ -167,20 +182,21 @@ template <typename Real>
 __global__ void k_adj_mu(int n, const Real *__restrict__ phi, const Real *__restrict__ lam, Real *__restrict__ mu,
                          Tabs t, const double *__restrict__ a, const double *__restrict__ b,
                          double *__restrict__ gA, double *__restrict__ gB) {
-    const size_t N = (size_t)n * n * n;
+    const int N = n * n * n;
     const int s = blockIdx.y;
     const Real *cx = (const Real *)t.cx, *cy = (const Real *)t.cy, *cz = (const Real *)t.cz,
                *m = (const Real *)t.msk;
     const Real *f = phi + (size_t)s * N;
     double sa = 0.0, sbb = 0.0;
     const bool act = a[s] >= 0;
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
         const size_t i = (size_t)s * N + c;
         if (!act) {
             mu[i] = lam[i];
             continue;
         }
-        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        int x, y, z;
+        decomp(c, n, x, y, z);
         const Real p = f[c];
         const Real L = lap(f, cx, cy, cz, n, c, x, y, z);
         const Real v = step_value(f, cx, cy, cz, n, c, x, y, z, (Real)a[s], (Real)b[s]);
@@ -201,18 +217,195 @@ __global__ void k_adj_mu(int n, const Real *__restrict__ phi, const Real *__rest
 template <typename Real>
 __global__ void k_adj_lam(int n, int S, const Real *__restrict__ phi, const Real *__restrict__ mu,
                           Real *__restrict__ lam, Tabs t, const double *__restrict__ a, const double *__restrict__ b) {
-    const size_t N = (size_t)n * n * n;
+    const int N = n * n * n;
     const Real *cx = (const Real *)t.cx, *cy = (const Real *)t.cy, *cz = (const Real *)t.cz;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N * S; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t s = i / N, c = i % N;
-        const Real *u = mu + s * N;
+    for (int s = blockIdx.y; s < S; s += gridDim.y) {
+        const Real *u = mu + (size_t)s * N;
+        const Real *ps = phi + (size_t)s * N;
+        Real *ls = lam + (size_t)s * N;
+        const bool act = a[s] >= 0;
+        const Real as = (Real)a[s], bs = (Real)b[s];
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+            if (!act) {
+                ls[c] = u[c];
+                continue;
+            }
+            int x, y, z;
+            decomp(c, n, x, y, z);
+            const Real p = ps[c];
+            ls[c] = u[c] * ((Real)1 + bs * ((Real)1 - (Real)2 * p)) + as * lap(u, cx, cy, cz, n, c, x, y, z);
+        }
+    }
+}
+
+// Fused backward step for the float path at n = 128 (k_adj_mu + k_adj_lam in
+// one pass over the state). A CTA of 10 warps owns a tile of 8 rows x TZ
+// planes of one sample. Warp w handles row y0 - 1 + w: marching z from the
+// tile's first plane - 1 to its last + 1 it forms, from phi_k, the pre-clamp
+// update v (the batched solver's operation sequence) and
+//   mu = [m != 0 and 0 <= v < 1] lambda_{k+1},
+// writes mu to a 3-plane shared ring and keeps its own row's last three planes
+// in registers; after one block barrier per plane, warps 1..8 form
+//   lambda_k = mu (1 + b (1 - 2 phi)) + a L(mu)
+// for the plane behind (rows y +- 1 from the ring) and accumulate
+// sum mu L(phi) and sum mu phi (1 - phi) for the tile's own cells.
+// Per sample and step: phi_k and lambda_{k+1} read once, lambda_k written once.
+namespace fb {
+constexpr int LR = 32, NN = 128, RY = 8, NW = RY + 2, TZ = 16;
+}
+
+__device__ __forceinline__ float4 ld4(const float *p, unsigned o) {
+    return __ldcg(reinterpret_cast<const float4 *>(p + o));
+}
+__device__ __forceinline__ float4 lg4(const float *p, unsigned o) {
+    return __ldg(reinterpret_cast<const float4 *>(p + o));
+}
+
+__global__ void __launch_bounds__(320, 2)
+    k_adj_back128(int S, int k, const int *__restrict__ ns, const float *__restrict__ phi, float *__restrict__ lam0,
+                  float *__restrict__ lam1,
+                  const float *__restrict__ cx, const float *__restrict__ cy, const float *__restrict__ cz,
+                  const float *__restrict__ msk, const double *__restrict__ a, const double *__restrict__ b,
+                  double *__restrict__ gA, double *__restrict__ gB) {
+    using namespace fb;
+    constexpr unsigned plane = NN * NN, N = NN * NN * NN;
+    constexpr int tiles_y = NN / RY, tiles = tiles_y * (NN / TZ);
+    __shared__ __align__(16) float ring[3][NW][NN];
+    __shared__ double red[2][NW];
+    const int w = threadIdx.x / LR, li = threadIdx.x % LR, x0 = 4 * li;
+    const int left_l = (li + LR - 1) % LR, right_l = (li + 1) % LR;
+    for (int it = blockIdx.x; it < S * tiles; it += gridDim.x) {
+        const int s = it % S, t = it / S;
+        const int y0 = (t % tiles_y) * RY, tz0 = (t / tiles_y) * TZ;
+        const float *f = phi + (size_t)s * N;
+        const bool odd = ((ns[s] - 1 - k) & 1) != 0;  // lambda of sample s is in lam1
+        const float *li_ = (odd ? lam1 : lam0) + (size_t)s * N;
+        float *lo = (odd ? lam0 : lam1) + (size_t)s * N;
+        const int y = (y0 - 1 + w + NN) % NN;
+        const int ym = y == 0 ? NN - 1 : y - 1, yp = y == NN - 1 ? 0 : y + 1;
+        const bool inner = w >= 1 && w <= RY;
+        const unsigned oy = (unsigned)(x0 + NN * y), oym = (unsigned)(x0 + NN * ym), oyp = (unsigned)(x0 + NN * yp);
         if (a[s] < 0) {
-            lam[i] = u[c];
+            // finished sample: lambda passes through unchanged
+            if (inner)
+                for (int dz = 0; dz < TZ; ++dz) {
+                    const unsigned o = oy + plane * (unsigned)(tz0 + dz);
+                    __stcg(reinterpret_cast<float4 *>(lo + o), ld4(li_, o));
+                }
             continue;
         }
-        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
-        const Real p = phi[i];
-        lam[i] = u[c] * ((Real)1 + (Real)b[s] * ((Real)1 - (Real)2 * p)) + (Real)a[s] * lap(u, cx, cy, cz, n, c, x, y, z);
+        const float as = (float)a[s], bs = (float)b[s];
+        auto wz = [](int z) { return z < 0 ? z + NN : (z >= NN ? z - NN : z); };
+        const int zstart = tz0 - 1;
+        float4 Pp = ld4(f, oy + plane * (unsigned)wz(zstart - 1));
+        float4 Pc = ld4(f, oy + plane * (unsigned)wz(zstart));
+        float4 CZp = lg4(cz, oy + plane * (unsigned)wz(zstart - 1));
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 U2 = z4, U1 = z4, Pb = z4;  // mu at z-2, z-1; phi at z-1
+        double sa = 0.0, sb = 0.0;
+        for (int st = 0; st < TZ + 2; ++st) {
+            const int zu = zstart + st;
+            const unsigned zo = plane * (unsigned)wz(zu), zno = plane * (unsigned)wz(zu + 1);
+            // ---- mu at (y, zu) ----
+            const float4 Pn = ld4(f, oy + zno);
+            const float4 PS = ld4(f, oym + zo), PN = ld4(f, oyp + zo);
+            const float4 CX = lg4(cx, oy + zo), CY = lg4(cy, oy + zo), CYm = lg4(cy, oym + zo);
+            const float4 CZ = lg4(cz, oy + zo), M = lg4(msk, oy + zo);
+            const float4 LI = ld4(li_, oy + zo);
+            float4 U;
+            {
+                const float left = __shfl_sync(0xffffffffu, Pc.w, left_l);
+                const float right = __shfl_sync(0xffffffffu, Pc.x, right_l);
+                const float cxl = __shfl_sync(0xffffffffu, CX.w, left_l);
+                const float pv[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
+                const float cxa[5] = {cxl, CX.x, CX.y, CX.z, CX.w};
+                const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
+                const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
+                const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
+                const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
+                const float m4[4] = {M.x, M.y, M.z, M.w}, l4[4] = {LI.x, LI.y, LI.z, LI.w};
+                float u[4];
+                const bool own = inner && zu >= tz0 && zu < tz0 + TZ;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float f0 = pv[i + 1];
+                    float lap = cxa[i] * (pv[i] - f0);
+                    lap = fmaf(cxa[i + 1], pv[i + 2] - f0, lap);
+                    lap = fmaf(cym4[i], ps[i] - f0, lap);
+                    lap = fmaf(cy4[i], pn[i] - f0, lap);
+                    lap = fmaf(czp4[i], pp[i] - f0, lap);
+                    lap = fmaf(cz4[i], pq[i] - f0, lap);
+                    float v = fmaf(as, lap, f0);
+                    v = fmaf(bs * f0, 1.0f - f0, v);
+                    const float g = (m4[i] != 0.0f && v >= 0.0f && v < 1.0f) ? 1.0f : 0.0f;
+                    u[i] = g * l4[i];
+                    if (own) {
+                        sa += (double)u[i] * (double)lap;
+                        sb += (double)u[i] * (double)f0 * (1.0 - (double)f0);
+                    }
+                }
+                U = make_float4(u[0], u[1], u[2], u[3]);
+            }
+            *reinterpret_cast<float4 *>(&ring[st % 3][w][x0]) = U;
+            __syncthreads();
+            // ---- lambda_k at (y, zu - 1) ----
+            if (st >= 2 && inner) {
+                const unsigned zc = plane * (unsigned)wz(zu - 1), zb = plane * (unsigned)wz(zu - 2);
+                const float4 S1 = *reinterpret_cast<const float4 *>(&ring[(st - 1) % 3][w - 1][x0]);
+                const float4 N1 = *reinterpret_cast<const float4 *>(&ring[(st - 1) % 3][w + 1][x0]);
+                const float4 AX = lg4(cx, oy + zc), AY = lg4(cy, oy + zc), AYm = lg4(cy, oym + zc);
+                const float4 AZ = lg4(cz, oy + zc), AZp = lg4(cz, oy + zb);
+                const float left = __shfl_sync(0xffffffffu, U1.w, left_l);
+                const float right = __shfl_sync(0xffffffffu, U1.x, right_l);
+                const float cxl = __shfl_sync(0xffffffffu, AX.w, left_l);
+                const float uv[6] = {left, U1.x, U1.y, U1.z, U1.w, right};
+                const float cxa[5] = {cxl, AX.x, AX.y, AX.z, AX.w};
+                const float us[4] = {S1.x, S1.y, S1.z, S1.w}, un[4] = {N1.x, N1.y, N1.z, N1.w};
+                const float up[4] = {U2.x, U2.y, U2.z, U2.w}, uq[4] = {U.x, U.y, U.z, U.w};
+                const float cy4[4] = {AY.x, AY.y, AY.z, AY.w}, cym4[4] = {AYm.x, AYm.y, AYm.z, AYm.w};
+                const float cz4[4] = {AZ.x, AZ.y, AZ.z, AZ.w}, czp4[4] = {AZp.x, AZp.y, AZp.z, AZp.w};
+                const float p4[4] = {Pb.x, Pb.y, Pb.z, Pb.w};
+                float o[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float u0 = uv[i + 1];
+                    float lu = cxa[i] * (uv[i] - u0);
+                    lu = fmaf(cxa[i + 1], uv[i + 2] - u0, lu);
+                    lu = fmaf(cym4[i], us[i] - u0, lu);
+                    lu = fmaf(cy4[i], un[i] - u0, lu);
+                    lu = fmaf(czp4[i], up[i] - u0, lu);
+                    lu = fmaf(cz4[i], uq[i] - u0, lu);
+                    o[i] = fmaf(as, lu, u0 * (1.0f + bs * (1.0f - 2.0f * p4[i])));
+                }
+                __stcg(reinterpret_cast<float4 *>(lo + oy + zc), make_float4(o[0], o[1], o[2], o[3]));
+            }
+            U2 = U1;
+            U1 = U;
+            Pb = Pc;
+            Pp = Pc;
+            Pc = Pn;
+            CZp = CZ;
+        }
+        // per-sample sensitivities of this tile
+        for (int o = 16; o > 0; o >>= 1) {
+            sa += __shfl_down_sync(0xffffffffu, sa, o);
+            sb += __shfl_down_sync(0xffffffffu, sb, o);
+        }
+        if (li == 0) {
+            red[0][w] = sa;
+            red[1][w] = sb;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double ta = 0.0, tb = 0.0;
+            for (int j = 0; j < NW; ++j) {
+                ta += red[0][j];
+                tb += red[1][j];
+            }
+            atomicAdd(gA + s, ta);
+            atomicAdd(gB + s, tb);
+        }
+        __syncthreads();
     }
 }
 
@@ -255,15 +448,20 @@ __global__ void k_adj_seed_ti(int S, size_t N, int nti, const int *__restrict__ 
 
 // dlogL/dx0 = sum_c lambda0_c * phi0_c * (x_c - x0) / sigma^2 (same for y0, z0)
 template <typename Real>
-__global__ void k_adj_ic_grad(int n, const gbg_sample *__restrict__ smp, double sigma, const Real *__restrict__ lam,
-                              const Real *__restrict__ phi0, double *__restrict__ gx) {
+// lam1 non-null: lambda_0 of sample s is in lam1 when ns[s] is odd (the fused
+// backward kernel's ping-pong), else in lam
+__global__ void k_adj_ic_grad(int n, const gbg_sample *__restrict__ smp, double sigma, const Real *__restrict__ lam_,
+                              const Real *__restrict__ lam1, const int *__restrict__ ns, const Real *__restrict__ phi0,
+                              double *__restrict__ gx) {
     const size_t N = (size_t)n * n * n;
     const int s = blockIdx.y;
+    const Real *lam = (lam1 && (ns[s] & 1)) ? lam1 : lam_;
     double acc[3] = {0, 0, 0};
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < (int)N; c += gridDim.x * blockDim.x) {
         const size_t i = (size_t)s * N + c;
         const double w = (double)lam[i] * (double)phi0[i] / (sigma * sigma);
-        const int x = (int)(c % n), y = (int)((c / n) % n), z = (int)(c / ((size_t)n * n));
+        int x, y, z;
+        decomp(c, n, x, y, z);
         acc[0] += w * (x - smp[s].x0);
         acc[1] += w * (y - smp[s].y0);
         acc[2] += w * (z - smp[s].z0);
@@ -272,6 +470,15 @@ __global__ void k_adj_ic_grad(int n, const gbg_sample *__restrict__ smp, double 
         const double t = block_sum<Real>(acc[k]);
         if (threadIdx.x == 0) atomicAdd(gx + 3 * s + k, t);
     }
+}
+
+// x over the cells of a sample, y over samples; about 16 CTAs per SM in all
+dim3 grid_cells(const Handle &h, int S) {
+    const size_t per = (h.N + 255) / 256;
+    size_t gx = (size_t)h.num_sms * 16 / (size_t)std::max(S, 1);
+    if (gx < 1) gx = 1;
+    if (gx > per) gx = per;
+    return dim3((unsigned)gx, (unsigned)std::min(S, 65535));
 }
 
 int grid_of(const Handle &h, size_t work) {
@@ -308,6 +515,30 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
             return rc;
         }
     }
+    // samples ordered by step count, longest first, so that the samples still
+    // running at step k are a prefix [0, A_k): every launch covers that prefix
+    // only (a finished sample's state and adjoint are left where they are)
+    {
+        bool sorted = true;
+        for (int s = 1; s < S; ++s) sorted = sorted && recs[s].nsteps <= recs[s - 1].nsteps;
+        if (!sorted) {
+            std::vector<int> perm(S);
+            for (int s = 0; s < S; ++s) perm[s] = s;
+            std::stable_sort(perm.begin(), perm.end(),
+                             [&](int i, int j) { return recs[i].nsteps > recs[j].nsteps; });
+            std::vector<gbg_sample> sp(S);
+            for (int i = 0; i < S; ++i) sp[i] = samples[perm[i]];
+            std::vector<double> ll(S), gg(grad ? 6 * (size_t)S : 0);
+            const int rc = run_adjoint<Real>(h, sp.data(), S, o, ll.data(), grad ? gg.data() : nullptr);
+            if (rc) return rc;
+            for (int i = 0; i < S; ++i) {
+                if (loglik) loglik[perm[i]] = ll[i];
+                if (grad)
+                    for (int j = 0; j < 6; ++j) grad[6 * (size_t)perm[i] + j] = gg[6 * (size_t)i + j];
+            }
+            return GBG_OK;
+        }
+    }
     std::vector<int> ns(S);
     std::vector<double> dtl(S);
     int nmax = 0;
@@ -319,6 +550,10 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
         dtl[s] = samples[s].tend - (k - 1) * dts[s];
         nmax = std::max(nmax, k);
     }
+    // A[k] = samples still running at step k (ns[s] > k)
+    std::vector<int> A(nmax + 1, 0);
+    for (int k = 0; k <= nmax; ++k)
+        while (A[k] < S && ns[A[k]] > k) ++A[k];
     if (f32) {
         if (int rc = fast_build_tables(h, (double)0.1f)) return rc;
     }
@@ -334,7 +569,8 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
                             segs * SN * sizeof(Real), SN * sizeof(Real), SN * sizeof(Real), SN * sizeof(Real),
                             (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
                             (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
-                            3 * S * sizeof(double), S * sizeof(gbg_sample), S * sizeof(gbg_lik_result)};
+                            3 * S * sizeof(double), S * sizeof(gbg_sample), S * sizeof(gbg_lik_result),
+                            S * sizeof(int)};
     size_t total = 0;
     for (size_t b : sizes) total += bwork_align(b);
     if (h.adj_ws_bytes < total) {
@@ -348,10 +584,10 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
         }
         h.adj_ws_bytes = total;
     }
-    void *parts[13];
+    void *parts[14];
     {
         char *q = (char *)h.adj_ws;
-        for (int i = 0; i < 13; ++i) {
+        for (int i = 0; i < 14; ++i) {
             parts[i] = q;
             q += bwork_align(sizes[i]);
         }
@@ -370,6 +606,7 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     double *gX = (double *)parts[10];
     gbg_sample *dsm = (gbg_sample *)parts[11];
     gbg_lik_result *dlik = (gbg_lik_result *)parts[12];
+    int *dns = (int *)parts[13];
     // per-step coefficients; a < 0 marks a finished sample
     std::vector<double> ha((size_t)nmax * S), hb((size_t)nmax * S);
     for (int k = 0; k < nmax; ++k)
@@ -401,6 +638,7 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     ADJ_TRY(cudaMemcpyAsync(da, ha.data(), ha.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     ADJ_TRY(cudaMemcpyAsync(db, hb.data(), hb.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     ADJ_TRY(cudaMemcpyAsync(dsm, samples, S * sizeof(gbg_sample), cudaMemcpyHostToDevice, st));
+    ADJ_TRY(cudaMemcpyAsync(dns, ns.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     ADJ_TRY(cudaMemsetAsync(gA, 0, (size_t)nmax * S * sizeof(double), st));
     ADJ_TRY(cudaMemsetAsync(gB, 0, (size_t)nmax * S * sizeof(double), st));
     ADJ_TRY(cudaMemsetAsync(gX, 0, 3 * S * sizeof(double), st));
@@ -414,31 +652,32 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
         }
     } else {
         k_adj_tables<Real><<<grid_of(h, N), 256, 0, st>>>(n, h.pw, h.pg, tab, tab + N, tab + 2 * N, tab + 3 * N);
-        k_adj_ic<Real><<<grid_of(h, N * S), 256, 0, st>>>(n, S, dsm, o.ic_peak, o.ic_sigma, h.pw, h.pg, ck);
+        k_adj_ic<Real><<<grid_cells(h, S), 256, 0, st>>>(n, S, dsm, o.ic_peak, o.ic_sigma, h.pw, h.pg, ck);
         h.launches += 2;
     }
-    // forward with checkpoints
-    const int gS = grid_of(h, N * S);
-    if (!grad) {
-        // forward only: ping-pong through two segment slots, last state into fin
+    // forward with checkpoints, each step over the samples still running; a
+    // sample's final state is gathered into fin at the step it finishes
+    auto finish = [&](const Real *from, int lo, int hi) -> cudaError_t {
+        if (hi <= lo || from == fin) return cudaSuccess;
+        return cudaMemcpyAsync(fin + (size_t)lo * N, from + (size_t)lo * N, (size_t)(hi - lo) * N * sizeof(Real),
+                               cudaMemcpyDeviceToDevice, st);
+    };
+    ADJ_TRY(finish(ck, A[0], S));  // samples with no step keep the initial state
+    {
         Real *cur = ck;
         for (int k = 0; k < nmax; ++k) {
-            Real *nxt = (k + 1) == nmax ? fin : seg + (size_t)((k + 1) & 1) * S * N;
-            k_adj_fwd<Real><<<gS, 256, 0, st>>>(n, S, cur, nxt, t, da + (size_t)k * S, db + (size_t)k * S);
+            Real *nxt;
+            if (!grad)  // forward only: ping-pong through two segment slots
+                nxt = (k + 1) == nmax ? fin : seg + (size_t)((k + 1) & 1) * S * N;
+            else
+                nxt = ((k + 1) % K == 0) ? ck + (size_t)((k + 1) / K) * S * N
+                                         : ((k + 1) == nmax ? fin : seg + (size_t)((k + 1) % K) * S * N);
+            k_adj_fwd<Real><<<grid_cells(h, A[k]), 256, 0, st>>>(n, A[k], cur, nxt, t, da + (size_t)k * S,
+                                                                 db + (size_t)k * S);
             h.launches++;
+            ADJ_TRY(finish(nxt, A[k + 1], A[k]));
             cur = nxt;
         }
-    } else {
-        Real *cur = ck;
-        for (int k = 0; k < nmax; ++k) {
-            Real *nxt = ((k + 1) % K == 0) ? ck + (size_t)((k + 1) / K) * S * N
-                                           : ((k + 1) == nmax ? fin : seg + (size_t)((k + 1) % K) * S * N);
-            k_adj_fwd<Real><<<gS, 256, 0, st>>>(n, S, cur, nxt, t, da + (size_t)k * S, db + (size_t)k * S);
-            h.launches++;
-            cur = nxt;
-        }
-        if (nmax % K == 0) ADJ_TRY(cudaMemcpyAsync(fin, ck + (size_t)(nmax / K) * S * N, S * N * sizeof(Real),
-                                                   cudaMemcpyDeviceToDevice, st));
     }
     // log-likelihood and its gradient at the final state
     {
@@ -468,27 +707,48 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
             if (loglik) loglik[s] = hl[s].total;
         return GBG_OK;
     }
-    // backward, segment by segment
-    const dim3 gC((unsigned)std::min<size_t>((N + 255) / 256, (size_t)h.num_sms * 4), (unsigned)S);
+    // backward, segment by segment; the float path at n = 128 runs the fused
+    // kernel with lambda ping-ponging between lam and mu
+    // backward, segment by segment, each step over the samples running at it.
+    // The fused float kernel (n = 128) moves lambda between lam and mu, per
+    // sample: before step k sample s has taken ns[s] - 1 - k backward steps, so
+    // its lambda is in mu when that count is odd.
+    const unsigned gcx = (unsigned)std::min<size_t>((N + 255) / 256, (size_t)h.num_sms * 4);
+    const bool fused = f32 && n == fb::NN;
     for (int sgm = (nmax - 1) / K; sgm >= 0; --sgm) {
         const int k0 = sgm * K, k1 = std::min(nmax, k0 + K);
         // recompute states k0+1 .. k1-1 into seg[1..]
-        ADJ_TRY(cudaMemcpyAsync(seg, ck + (size_t)sgm * S * N, S * N * sizeof(Real), cudaMemcpyDeviceToDevice, st));
+        ADJ_TRY(cudaMemcpyAsync(seg, ck + (size_t)sgm * S * N, (size_t)A[k0] * N * sizeof(Real),
+                                cudaMemcpyDeviceToDevice, st));
         for (int k = k0; k < k1 - 1; ++k) {
-            k_adj_fwd<Real><<<gS, 256, 0, st>>>(n, S, seg + (size_t)(k - k0) * S * N,
-                                                seg + (size_t)(k - k0 + 1) * S * N, t, da + (size_t)k * S,
-                                                db + (size_t)k * S);
+            k_adj_fwd<Real><<<grid_cells(h, A[k]), 256, 0, st>>>(n, A[k], seg + (size_t)(k - k0) * S * N,
+                                                                 seg + (size_t)(k - k0 + 1) * S * N, t,
+                                                                 da + (size_t)k * S, db + (size_t)k * S);
             h.launches++;
         }
         for (int k = k1 - 1; k >= k0; --k) {
             const Real *phik = seg + (size_t)(k - k0) * S * N;
-            k_adj_mu<Real><<<gC, 256, 0, st>>>(n, phik, lam, mu, t, da + (size_t)k * S, db + (size_t)k * S,
-                                               gA + (size_t)k * S, gB + (size_t)k * S);
-            k_adj_lam<Real><<<gS, 256, 0, st>>>(n, S, phik, mu, lam, t, da + (size_t)k * S, db + (size_t)k * S);
-            h.launches += 2;
+            if (fused) {
+                constexpr int tiles = (fb::NN / fb::RY) * (fb::NN / fb::TZ);
+                const long items = (long)A[k] * tiles;
+                const unsigned grid = (unsigned)std::min<long>(items, (long)h.num_sms * 8);
+                k_adj_back128<<<grid, 320, 0, st>>>(A[k], k, dns, (const float *)phik, (float *)lam, (float *)mu,
+                                                    (const float *)t.cx, (const float *)t.cy, (const float *)t.cz,
+                                                    (const float *)t.msk, da + (size_t)k * S, db + (size_t)k * S,
+                                                    gA + (size_t)k * S, gB + (size_t)k * S);
+                h.launches++;
+            } else {
+                const dim3 gC(gcx, (unsigned)A[k]);
+                k_adj_mu<Real><<<gC, 256, 0, st>>>(n, phik, lam, mu, t, da + (size_t)k * S, db + (size_t)k * S,
+                                                   gA + (size_t)k * S, gB + (size_t)k * S);
+                k_adj_lam<Real><<<grid_cells(h, A[k]), 256, 0, st>>>(n, A[k], phik, mu, lam, t,
+                                                                     da + (size_t)k * S, db + (size_t)k * S);
+                h.launches += 2;
+            }
         }
     }
-    k_adj_ic_grad<Real><<<gC, 256, 0, st>>>(n, dsm, o.ic_sigma, lam, ck, gX);
+    k_adj_ic_grad<Real><<<dim3(gcx, (unsigned)S), 256, 0, st>>>(n, dsm, o.ic_sigma, lam, fused ? mu : nullptr, dns,
+                                                                ck, gX);
     h.launches++;
     ADJ_TRY(cudaGetLastError());
     std::vector<double> hA((size_t)nmax * S), hB((size_t)nmax * S), hX(3 * S);
