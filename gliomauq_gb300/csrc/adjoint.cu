@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(320, 2)
                 const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
                 const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
                 const float m4[4] = {M.x, M.y, M.z, M.w}, l4[4] = {LI.x, LI.y, LI.z, LI.w};
-                float u[4];
+                float u[4], pa = 0.0f, pb = 0.0f;
                 const bool own = inner && zu >= tz0 && zu < tz0 + TZ;
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
@@ -339,10 +339,14 @@ __global__ void __launch_bounds__(320, 2)
                     v = fmaf(bs * f0, 1.0f - f0, v);
                     const float g = (m4[i] != 0.0f && v >= 0.0f && v < 1.0f) ? 1.0f : 0.0f;
                     u[i] = g * l4[i];
-                    if (own) {
-                        sa += (double)u[i] * (double)lap;
-                        sb += (double)u[i] * (double)f0 * (1.0 - (double)f0);
-                    }
+                    pa = fmaf(u[i], lap, pa);
+                    pb = fmaf(u[i] * f0, 1.0f - f0, pb);
+                }
+                // a thread's four cells summed in float, the plane partials in
+                // double (the FP64 pipe is narrow on this GPU)
+                if (own) {
+                    sa += (double)pa;
+                    sb += (double)pb;
                 }
                 U = make_float4(u[0], u[1], u[2], u[3]);
             }
