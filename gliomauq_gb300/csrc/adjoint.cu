@@ -187,7 +187,9 @@ __global__ void k_adj_mu(int n, const Real *__restrict__ phi, const Real *__rest
     const Real *cx = (const Real *)t.cx, *cy = (const Real *)t.cy, *cz = (const Real *)t.cz,
                *m = (const Real *)t.msk;
     const Real *f = phi + (size_t)s * N;
-    double sa = 0.0, sbb = 0.0;
+    // a thread's partial sums in Real (float: the FP64 pipe is narrow on this
+    // GPU; a thread adds a few dozen terms), combined in double below
+    Real sa = 0, sbb = 0;
     const bool act = a[s] >= 0;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
         const size_t i = (size_t)s * N + c;
@@ -203,11 +205,11 @@ __global__ void k_adj_mu(int n, const Real *__restrict__ phi, const Real *__rest
         const Real g = (m[c] != (Real)0 && v >= (Real)0 && v < (Real)1) ? (Real)1 : (Real)0;
         const Real u = g * lam[i];
         mu[i] = u;
-        sa += (double)u * (double)L;
-        sbb += (double)u * (double)p * (1.0 - (double)p);
+        sa += u * L;
+        sbb += u * p * ((Real)1 - p);
     }
-    const double ta = block_sum<Real>(sa);
-    const double tb = block_sum<Real>(sbb);
+    const double ta = block_sum<Real>((double)sa);
+    const double tb = block_sum<Real>((double)sbb);
     if (threadIdx.x == 0 && act) {
         atomicAdd(gA + s, ta);
         atomicAdd(gB + s, tb);
