@@ -581,7 +581,8 @@ def main():
                                            f"({NCU_BYTES_PER_CELL_STEP:.3f} B per cell-step), scaled "
                                            "by this launch's cell-steps; the register-family variants "
                                            "the autotuner picks between move the same density stream",
-                         "kernel": f"k_population (autotuned variant {variant})", "kernel_ms": kern_ms,
+                         "kernel": f"{h.population_variant_name(variant)} (autotuned variant {variant})",
+                         "kernel_ms": kern_ms,
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "peak_source": f"{peak_kind} hbm_gbs"},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 48 * S,

@@ -34,6 +34,7 @@ EXPORTS = [
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
     "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_surrogate_set_engine",
     "gbg_set_slopes", "gbg_get_slopes", "gbg_mala_step", "gbg_run_mala",
+    "gbg_population_variant_name",
 ]
 
 
@@ -126,6 +127,7 @@ def load(path: str = LIB_PATH):
         "gbg_last_population_ms": [vp, C.POINTER(C.c_float)],
         "gbg_population_variants": [vp, C.POINTER(C.c_int)],
         "gbg_set_population_variant": [vp, C.c_int],
+        "gbg_population_variant_name": [vp, C.c_int, C.c_char_p, C.c_int],
         "gbg_population_variant_shape": [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)],
         "gbg_autotune": [vp, C.c_int, C.c_char_p, C.POINTER(C.c_int)],
@@ -347,6 +349,11 @@ class Handle:
 
     def sync(self):
         check(self.lib.gbg_sync(self._h))
+
+    def population_variant_name(self, index: int) -> str:
+        buf = C.create_string_buffer(64)
+        check(self.lib.gbg_population_variant_name(self._h, index, buf, 64))
+        return buf.value.decode()
 
     def population_variants(self) -> list[tuple[int, int, int]]:
         """(rows per tile, samples per CTA, threads) of every population-kernel shape."""

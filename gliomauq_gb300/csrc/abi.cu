@@ -290,6 +290,15 @@ int gbg_rd_step(gbg_handle *hh, double Dw, double Dg, double rho, double dt, lon
     return gbg::exact_steps(h, Dw, Dg, rho, dt, nsteps);
 }
 
+int gbg_population_variant_name(gbg_handle *hh, int index, char *buf, int len) {
+    if (int rc = check_handle(hh)) return rc;
+    if (gbg::population_variant_name(hh->h.n, index, buf, len) != GBG_OK) {
+        set_error("variant index out of range or no buffer");
+        return GBG_ERR_ARG;
+    }
+    return GBG_OK;
+}
+
 namespace {
 
 // slopes and the slopes' tissue tensor, allocated on first use (exact modes)

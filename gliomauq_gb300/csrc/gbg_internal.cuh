@@ -181,6 +181,7 @@ int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, doubl
 int fast_steps_single(Handle &h, double Dw, double rho, double dt, long nsteps);
 int population_variant_count(int n);
 int population_variant_shape(int n, int vi, int *ry, int *g, int *threads);
+int population_variant_name(int n, int vi, char *buf, int len);
 // reads and clears the device status word (synchronises the stream)
 int check_device_status(Handle &h);
 int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,

@@ -48,6 +48,7 @@
 // shared-memory ring of first-step planes, density read and written once per
 // two steps). All run the same per-cell operation sequence, so every variant
 // gives the same bits.
+#include <cstdio>
 #include <vector>
 
 #include "gbg_internal.cuh"
@@ -1413,6 +1414,7 @@ struct PopVariant {
     int ry, g, threads, tz;
     size_t smem;
     bool tb = false;  // two steps per round (start buffer per sample, see k_gaussian_ic)
+    char name[64] = {0};  // kernel and template arguments, plus the tile depth
 };
 
 template <int LR, int MINB = 1, int PF = 0, int D = 0>
@@ -1424,6 +1426,7 @@ PopVariant make_register_variant(int tz) {
     v.threads = 256;
     v.tz = tz;
     v.smem = 0;
+    std::snprintf(v.name, sizeof(v.name), "k_population1<%d,%d,%d,%d> TZ %d", LR, MINB, PF, D, tz);
     return v;
 }
 
@@ -1436,6 +1439,7 @@ PopVariant make_signmask_variant(int tz) {
     v.threads = 256;
     v.tz = tz;
     v.smem = 0;
+    std::snprintf(v.name, sizeof(v.name), "k_population8<%d,%d> TZ %d", LR, MINB, tz);
     return v;
 }
 
@@ -1448,6 +1452,7 @@ PopVariant make_pair_variant(int tz) {
     v.threads = 256;
     v.tz = tz;
     v.smem = 0;
+    std::snprintf(v.name, sizeof(v.name), "k_population9<%d,%d> TZ %d", LR, MINB, tz);
     return v;
 }
 
@@ -1461,6 +1466,7 @@ PopVariant make_variant(int tz) {
     v.tz = tz;
     const int n = 4 * LR;
     v.smem = (size_t)(4 * (4 * RY + 1) * n + G * 4 * (RY + 2) * n) * sizeof(float);
+    std::snprintf(v.name, sizeof(v.name), "k_population3<%d,%d,%d> TZ %d", LR, RY, G, tz);
     return v;
 }
 
@@ -1474,6 +1480,7 @@ PopVariant make_tb_variant(int tz) {
     v.tz = tz;
     v.smem = 0;
     v.tb = true;
+    std::snprintf(v.name, sizeof(v.name), "k_population7<%d,%d> TZ %d", MINB, (int)RELOAD, tz);
     return v;
 }
 
@@ -1486,6 +1493,7 @@ PopVariant make_ws_variant(int tz) {
     v.threads = LR * RY + 32;
     v.tz = tz;
     v.smem = TmaRing<LR, RY, D>::smem();
+    std::snprintf(v.name, sizeof(v.name), "k_population6<%d,%d,%d,%d> TZ %d", LR, RY, D, MINB, tz);
     return v;
 }
 
@@ -1498,6 +1506,7 @@ PopVariant make_tma_variant(int tz) {
     v.threads = LR * RY;
     v.tz = tz;
     v.smem = TmaRing<LR, RY, D>::smem();
+    std::snprintf(v.name, sizeof(v.name), "k_population5<%d,%d,%d,%d> TZ %d", LR, RY, D, MINB, tz);
     return v;
 }
 
@@ -1618,6 +1627,14 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
 int population_variant_count(int n) {
     PopVariant vs[32];
     return variants_for(n, vs);
+}
+
+int population_variant_name(int n, int vi, char *buf, int len) {
+    PopVariant vs[32];
+    const int nv = variants_for(n, vs);
+    if (vi < 0 || vi >= nv || !buf || len < 1) return GBG_ERR_ARG;
+    std::snprintf(buf, (size_t)len, "%s", vs[vi].name);
+    return GBG_OK;
 }
 
 int population_variant_shape(int n, int vi, int *ry, int *g, int *threads) {

@@ -365,6 +365,10 @@ int gbg_population_variants(gbg_handle *h, int *count);
 int gbg_set_population_variant(gbg_handle *h, int index);
 int gbg_population_variant_shape(gbg_handle *h, int index, int *rows, int *samples_per_cta,
                                  int *threads);
+/* The kernel a variant launches, with its template arguments and tile depth
+ * (e.g. "k_population8<32,4> TZ 16"), as a NUL-terminated string of at most
+ * len bytes. */
+int gbg_population_variant_name(gbg_handle *h, int index, char *buf, int len);
 int gbg_autotune(gbg_handle *h, int probe_samples, const char *cache_path, int *chosen);
 
 /* ---- log-likelihood without any allocation -----------------------------------

@@ -115,13 +115,17 @@ def test_every_population_shape_gives_identical_results(gbg, n):
         h.set_anatomy(an.p_w, an.p_g)
         shapes = h.population_variants()
         assert len(shapes) >= 2
+        names = [h.population_variant_name(i) for i in range(len(shapes))]
+        assert names[0].startswith("k_population8<") and len(set(names)) == len(names), names
+        with pytest.raises(_lib.GbgError):
+            h.population_variant_name(len(shapes))
         outs = []
         for i in range(len(shapes)):
             h.set_population_variant(i)
             outs.append(h.batch_solve([s.as_tuple() for s in sm], an.L, with_loglik=False,
                                       want_phi=True)["phi"])
     for i, o in enumerate(outs[1:], 1):
-        assert np.array_equal(o, outs[0]), shapes[i]
+        assert np.array_equal(o, outs[0]), names[i]
 
 
 def test_autotune_picks_and_caches(gbg, tmp_path):
