@@ -783,9 +783,9 @@ __global__ void k_up2_bwd(Geom gc, int C, Slice dout, Slice din) {
 
 // sigmoid output and squared-error loss against targets: loss += sum (s - t)^2 / nv,
 // dlogit = 2 (s - t) s (1 - s) / nv (scaled by loss_scale for bf16 range)
-__global__ void k_loss(long nv, const float *__restrict__ logit, const float *__restrict__ target,
-                       float *__restrict__ pred, __nv_bfloat16 *__restrict__ dlogit, float loss_scale,
-                       double *__restrict__ loss) {
+// pred may be logit itself (in-place sigmoid): neither is declared restrict
+__global__ void k_loss(long nv, const float *logit, const float *__restrict__ target, float *pred,
+                       __nv_bfloat16 *__restrict__ dlogit, float loss_scale, double *__restrict__ loss) {
     __shared__ double red[256];
     double s_acc = 0.0;
     for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < nv; v += (long)gridDim.x * blockDim.x) {
