@@ -711,6 +711,27 @@ def refine_cov(post, u_map: np.ndarray, cov: np.ndarray, span: float = 8.0, npts
     return cov_r, ratio
 
 
+def polish_mode(post, v_map: np.ndarray, lp_map: float, cov0: np.ndarray, polish: int = 8,
+                iters: int = 5, gain: float = 1.0):
+    """Mode search continued along the posterior's profiles: the posterior of
+    the tumour model is a narrow curved ridge in (log rho T, log Dw/rho),
+    along which damped Newton can stop short of the mode. While refine_cov's
+    profiles hold a point more than `gain` nats above the current estimate,
+    Newton restarts from that point (at most `polish` times). Returns
+    (v_map, log pi(v_map), Laplace covariance, refined covariance, restarts)."""
+    restarts = 0
+    for _ in range(polish):
+        cov, _, v_best, lp_best = refine_cov(post, v_map, cov0, with_best=True)
+        if not lp_best > lp_map + gain:
+            return v_map, lp_map, cov0, cov, restarts
+        v_new, lp_new, cov_new, _ = find_mode(post, v_best[None], iters=iters)
+        restarts += 1
+        if lp_new > lp_map:
+            v_map, lp_map, cov0 = v_new, lp_new, cov_new
+    cov, _ = refine_cov(post, v_map, cov0)
+    return v_map, lp_map, cov0, cov, restarts
+
+
 def stable_dt0(n: int, L: float, dw_max: float) -> float:
     """Largest explicit step of the smooth time grid for diffusivities up to
     dw_max [cm^2/day]: the reference's CFL rule dt = 0.99 h^2 / (6 Dw / L^2)."""
@@ -862,16 +883,7 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
     ld, _ = post.loglik(dv, False)
     starts = dv[np.argsort(ld)[::-1][:4]]
     v_map, lp_map, cov0, _ = find_mode(post, starts, iters=10)
-    # the posterior is a narrow curved ridge in (log rho T, log Dw/rho), along
-    # which damped Newton can stop short of the mode: while a profile point
-    # lies above the current point, restart Newton from it
-    for _ in range(polish):
-        cov, _, v_best, lp_best = refine_cov(post, v_map, cov0, with_best=True)
-        if not lp_best > lp_map + 1.0:
-            break
-        v_map, lp_map, cov0, _ = find_mode(post, v_best[None], iters=5)
-    else:
-        cov, _ = refine_cov(post, v_map, cov0)
+    v_map, lp_map, cov0, cov, _ = polish_mode(post, v_map, lp_map, cov0, polish=polish)
     sd = np.sqrt(np.diag(cov))
     Lc = np.linalg.cholesky(cov)
     sur = AffineSurrogate(post, v_map, 0.5 * sd, quad_axis=0)

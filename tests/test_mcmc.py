@@ -298,6 +298,52 @@ def test_refine_cov_reports_a_higher_profile_point():
     assert lbm <= lm + 1e-9
 
 
+class BananaStub(GaussianStub):
+    """A narrow curved ridge in coordinates z = (theta - mu) / sd (the prior
+    box is |z| <= 20):
+    log pi = -(z0^2 + ((z1 - k z0^2) / eps)^2 + z2^2 + ... + z5^2) / 2,
+    mode at mu; its conditional width across the ridge is eps."""
+
+    def __init__(self, k=0.1, eps=0.02):
+        super().__init__()
+        self.k, self.eps = k, eps
+
+    def _z(self, th):
+        return (np.atleast_2d(th) - self.mu) / self.sd
+
+    def loglik(self, th, with_grad):
+        th = np.atleast_2d(th)
+        self.solves += th.shape[0]
+        z = self._z(th)
+        r = (z[:, 1] - self.k * z[:, 0] ** 2) / self.eps
+        lp = -0.5 * (z[:, 0] ** 2 + r ** 2 + np.sum(z[:, 2:] ** 2, axis=1))
+        gz = np.zeros_like(z)
+        gz[:, 0] = -z[:, 0] + r / self.eps * 2 * self.k * z[:, 0]
+        gz[:, 1] = -r / self.eps
+        gz[:, 2:] = -z[:, 2:]
+        return lp + self.prior.logp(th), gz / self.sd
+
+
+def test_polish_mode_reaches_the_mode_along_a_curved_ridge():
+    """Newton started far along the ridge (across-ridge width 1/50 of the
+    along-ridge one, as in the tumour model's (log rho T, log Dw/rho)) and cut
+    short stops below the mode; polish_mode restarts it from higher profile
+    points until no profile point is higher, and ends at the mode."""
+    post = BananaStub()
+    w = post.sd
+    z0 = np.zeros(6)
+    z0[0], z0[1] = 5.0, post.k * 25.0  # on the ridge, 12.5 nats below the mode
+    start = post.mu + z0 * w
+    v, lp, cov0, _ = mcmc.find_mode(post, start[None], iters=1)
+    lm = post.loglik(post.mu[None], False)[0][0]
+    assert lp < lm - 1.0  # one Newton step does not get there
+    v2, lp2, _, cov, restarts = mcmc.polish_mode(post, v, lp, cov0, polish=8, gain=0.01)
+    assert restarts >= 1
+    assert lp2 > lm - 0.05
+    assert np.all(np.abs((v2 - post.mu) / w) < 0.2)
+    assert np.all(np.isfinite(cov)) and np.all(np.linalg.eigvalsh(cov) > 0)
+
+
 def test_stranded_chains_and_discrepancy():
     lp = np.array([0.0, -1.0, -2.0, -3.0, -40.0, -np.inf])
     assert mcmc._stranded(lp).tolist() == [False, False, False, False, True, True]
