@@ -98,6 +98,28 @@ def test_delayed_acceptance_targets_the_exact_posterior():
     assert np.all(mcmc.rhat(r.samples[200:]) < 1.05)
 
 
+def test_burn_in_resets_stranded_chains():
+    """A quarter of the chains start 10 sd away (≈ 150 nats below the
+    bulk): at the rebuild points of burn-in they are moved onto copies of
+    chains in the bulk, and the post-burn-in population samples the
+    posterior; reset_stranded=False makes no resets."""
+    rng = np.random.default_rng(5)
+    post = GaussianStub()
+    sur = BiasedSurrogateStub(post)
+    spost = mcmc.SurrogatePosterior(sur, post.prior)
+    th0 = post.mu + post.sd * rng.standard_normal((32, 6))
+    th0[:8] = post.mu + 10.0 * post.sd * np.array([1, -1, 1, -1, 1, -1])
+    kw = dict(inner=6, burn=60, chol=np.diag(post.sd), adapt=True, rebuild_every=10)
+    r = mcmc.da(post, spost, th0, 400, 0.02, rng, **kw)
+    assert r.history["stranded_resets"] >= 8
+    s = r.samples[60:]
+    z = np.abs((s - post.mu) / post.sd).max(axis=(0, 2))  # per chain, after burn-in
+    assert np.all(z < 6.0), z
+    assert np.all(np.abs(s.reshape(-1, 6).mean(axis=0) - post.mu) < 0.3 * post.sd)
+    r0 = mcmc.da(post, spost, th0, 61, 0.02, np.random.default_rng(5), reset_stranded=False, **kw)
+    assert r0.history["stranded_resets"] == 0
+
+
 class InvariantStub(GaussianStub):
     """Likelihood that depends on (log rho T, log Dw/rho, x0, y0, z0) only
     (Gaussian there), prior box on theta: the tumour model's symmetry."""
