@@ -2,6 +2,7 @@
 answers -- ESS of AR(1) chains, and RWM / MALA on a Gaussian posterior
 stub with the solver's call signature."""
 import numpy as np
+import pytest
 
 from gliomauq_gb300 import mcmc
 
@@ -118,6 +119,46 @@ def test_burn_in_resets_stranded_chains():
     assert np.all(np.abs(s.reshape(-1, 6).mean(axis=0) - post.mu) < 0.3 * post.sd)
     r0 = mcmc.da(post, spost, th0, 61, 0.02, np.random.default_rng(5), reset_stranded=False, **kw)
     assert r0.history["stranded_resets"] == 0
+
+
+class TiltedSurrogate:
+    """Exact log pi plus a linear tilt; rebuild() scales the tilt by
+    `factor` (below 1: a better surrogate, above 1: a worse one);
+    state()/restore() as the affine surrogate's."""
+
+    def __init__(self, post, tilt, factor):
+        self.post, self.tilt, self.factor = post, np.asarray(tilt, dtype=float), factor
+        self.evals = 0
+
+    def logpost(self, th):
+        th = np.atleast_2d(th)
+        self.evals += th.shape[0]
+        lp, _ = self.post.loglik(th, False)
+        return lp + ((th - self.post.mu) / self.post.sd) @ self.tilt
+
+    def rebuild(self, centre, steps):
+        self.tilt = self.tilt * self.factor
+
+    def state(self):
+        return self.tilt.copy()
+
+    def restore(self, st):
+        self.tilt = st.copy()
+
+
+@pytest.mark.parametrize("factor,kept", [(0.5, 5), (2.0, 0)])
+def test_surrogate_rebuilds_are_kept_only_when_they_help(factor, kept):
+    rng = np.random.default_rng(9)
+    post = GaussianStub()
+    tilt = np.array([0.3, -0.2, 0.1, 0.0, 0.2, -0.1])
+    sur = TiltedSurrogate(post, tilt, factor)
+    th0 = post.mu + post.sd * rng.standard_normal((32, 6))
+    r = mcmc.da(post, sur, th0, 40, 0.02, rng, inner=4, burn=30, chol=np.diag(post.sd),
+                adapt=True, rebuild_every=5)
+    assert r.history["rebuilds_tried"] == 5
+    assert r.history["rebuilds_kept"] == kept
+    expect = tilt * factor ** kept
+    assert np.allclose(sur.tilt, expect)
 
 
 class InvariantStub(GaussianStub):
