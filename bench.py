@@ -448,9 +448,10 @@ def run_reference_arm(args):
     print(json.dumps(line))
 
 
-# DRAM bytes per cell-step of the population kernel measured by ncu
-# (profiles/k_population8_128_pop64_ncu.md: 268.87 GB read + written for
-# 3.2076e10 cell-steps); traffic grows with the cell-steps of a launch.
+# DRAM bytes per cell-step of k_population8<32,4> measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum on a 64-sample 128^3
+# population: 268.87 GB for 3.2076e10 cell-steps); traffic grows with the
+# cell-steps of a launch.
 NCU_BYTES_PER_CELL_STEP = 268.869814e9 / 32075939840.0
 
 

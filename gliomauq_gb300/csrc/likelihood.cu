@@ -266,27 +266,73 @@ static_assert(GBG_NOALLOC_MAX_ENTRIES == kNoAllocMaxChunks * gbg::kLikChunk,
 
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxChunks * 3];
 
-// Device address of g_noalloc_partials per device ordinal, looked up once per
-// device with that device current (a host-side name of a __device__ array is
-// not a device address).
-constexpr int kMaxDevices = 64;
-double *g_noalloc_ptr[kMaxDevices] = {};
+// Device address of g_noalloc_partials per CUDA context. A host-side name of
+// a __device__ array is not a device address: the address is looked up with
+// cudaGetSymbolAddress once per context, with that context current. Every
+// context that loads the module has its own copy of the array (the primary
+// context of each device, any context a caller created with the driver API,
+// and the new primary context after cudaDeviceReset), so the cache is keyed
+// by the driver's context ID, which the driver never reuses in a process.
+// The two driver calls are resolved through the runtime, so the library keeps
+// no link-time dependency on libcuda.
+using CtxGetCurrentFn = int (*)(void **ctx);
+using CtxGetIdFn = int (*)(void *ctx, unsigned long long *id);
+
+struct NoAllocEntry {
+    unsigned long long ctx_id;
+    double *ptr;
+};
+constexpr int kMaxContexts = 64;
+NoAllocEntry g_noalloc_cache[kMaxContexts];  // a ring: the oldest entry is replaced
+int g_noalloc_count = 0, g_noalloc_next = 0;
 std::mutex g_noalloc_mu;
 
-int noalloc_scratch(double **out) {
-    int dev = -1;
-    GBG_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) {
-        gbg::set_error("device ordinal beyond the no-alloc scratch table");
-        return GBG_ERR_UNSUPPORTED;
+int current_context_id(unsigned long long *id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        GBG_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1));
+        GBG_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+            gbg::set_error("gbg_loglik_noalloc: the driver lacks cuCtxGetCurrent/cuCtxGetId");
+            return GBG_ERR_UNSUPPORTED;
+        }
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        get_id = reinterpret_cast<CtxGetIdFn>(f2);
     }
+    void *ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, id) != 0) {
+        gbg::set_error("gbg_loglik_noalloc: no current CUDA context");
+        return GBG_ERR_CUDA;
+    }
+    return GBG_OK;
+}
+
+int noalloc_scratch(double **out) {
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    unsigned long long id = 0;
+    if (current_context_id(&id) != GBG_OK) {
+        // no context bound to this thread yet: the runtime binds the current
+        // device's primary context on its next call, then ask again
+        int dev = -1;
+        GBG_CUDA_TRY(cudaGetDevice(&dev));
         void *p = nullptr;
         GBG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_partials));
-        g_noalloc_ptr[dev] = static_cast<double *>(p);
+        if (int rc = current_context_id(&id)) return rc;
     }
-    *out = g_noalloc_ptr[dev];
+    for (int i = 0; i < g_noalloc_count; ++i)
+        if (g_noalloc_cache[i].ctx_id == id) {
+            *out = g_noalloc_cache[i].ptr;
+            return GBG_OK;
+        }
+    void *p = nullptr;
+    GBG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_partials));
+    g_noalloc_cache[g_noalloc_next] = {id, static_cast<double *>(p)};
+    g_noalloc_next = (g_noalloc_next + 1) % kMaxContexts;
+    if (g_noalloc_count < kMaxContexts) ++g_noalloc_count;
+    *out = static_cast<double *>(p);
     return GBG_OK;
 }
 

@@ -387,15 +387,20 @@ int gbg_autotune(gbg_handle *h, int probe_samples, const char *cache_path, int *
  *   ti_idx/t1_val/t2_val : cell index and T1/T2 value of every evaluation
  *                      point (n_ti entries)
  * -- the scalar parameters in p (its step/selective fields are not used: the
- * lists already encode them), and out_device, one gbg_lik_result.
+ * lists already encode them), and out_device, one gbg_lik_result. n must be
+ * the field's edge and every index in pet_idx and ti_idx must lie in
+ * [0, n^3): the kernels read phi_device at those indices unchecked.
  * stream is a cudaStream_t (null: the legacy default stream); the call only
  * enqueues work and does not synchronise.
  *
  * Its scratch is a fixed device array inside the library (3 doubles per chunk
  * of 2048 list entries, at most GBG_NOALLOC_MAX_ENTRIES entries, 96 KiB),
  * which every GPU that loads the library keeps until the process exits. The
- * first call on a device looks that array's address up with that device
- * current, so make the first call before any stream capture. Every call
+ * first call in a CUDA context (the primary context of a device, a context
+ * the caller made current with the driver API, or the new primary context
+ * after cudaDeviceReset) looks that array's address up with the context
+ * current, so make the first call in each context before any stream capture
+ * on it. Every call
  * shares the array: calls whose kernels may overlap on the GPU (different
  * streams, or different host threads) race and must be serialised by the
  * caller. Lists longer than the maximum are rejected with GBG_ERR_ARG. */

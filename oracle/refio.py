@@ -11,6 +11,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
+# The reference's source tree (GliomaUQ's source/ folder), read only by the
+# recipes that compile it in place and by the tests that need it; override
+# with GLIOMAUQ_REF. oracle/Makefile takes the same variable.
+REF_SOURCE = os.environ.get("GLIOMAUQ_REF", "/root/reference/source")
 
 
 def write_input(path, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, adaptive=0, nsteps=-1,

@@ -7,7 +7,8 @@ stores inputs and outputs as small .npz/.json files. Inputs are rounded to
 float32 values so that they are exact in both the FP32 and the FP64 build and
 independent of the platform that regenerates them.
 
-Usage (needs /root/reference and `make -C oracle ref`):
+Usage (needs the reference's source tree at $GLIOMAUQ_REF, default
+/root/reference/source, and `make -C oracle ref`):
     python tests/golden/make_golden.py
 """
 from __future__ import annotations

@@ -1,0 +1,150 @@
+"""GPU: parity of the benchmarked configuration -- the batched population at
+128^3 on the bench's own anatomy (make_anatomy(128, seed=0)), prior
+(draw_prior(..., 512, seed=1)) and observations, for every population-kernel
+variant the autotuner can pick at 128^3 (k_population8 and k_population9 at
+each tile depth) and the tissue-and-support-skipping kernel:
+
+  (a) every sample equals the single-solve fast path (gbg_rd_step, FP32)
+      bit for bit;
+  (b) every sample is within 1e-4 relative L2 of the FP64 oracle
+      (oracle.rd_solve, the reference's Case2 step restated; the error is
+      printed: this is the stated FP32 error of the configuration);
+  (c) every sample's log-likelihood is within 1e-11 (relative) of the oracle's
+      likelihood of the same float field.
+
+Six samples span the prior's step counts: the shortest, four quantiles and
+the longest of the 512. Also the discrete adjoint at 128^3 against central
+finite differences on two of them."""
+import numpy as np
+import pytest
+
+from gliomauq_gb300 import _lib, synthetic as S
+from helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+N = 128
+F32_VS_F64_TOL = 1e-4  # the per-solve density bound of the sampler's accuracy target
+LIK_REL_TOL = 1e-11
+LIK = (0.0025, 1.0, 0.7, 0.25, 0.09)
+QUANTILES = (0.0, 0.2, 0.4, 0.6, 0.8, 1.0)
+
+
+@pytest.fixture(scope="module")
+def bench_case(oracle_lib):
+    """The bench workload's anatomy, six of its prior draws, its observations,
+    and for each draw the single-solve GPU result and the FP64 oracle."""
+    an = S.make_anatomy(N, seed=0)
+    prior = S.draw_prior(an, 512, seed=1)
+    steps = np.array([S.num_steps(S.reference_dt(N, p.Dw, an.L, f32=True)[0], p.T)
+                      for p in prior])
+    order = np.argsort(steps, kind="stable")
+    picks = [int(order[min(len(order) - 1, int(q * (len(order) - 1)))]) for q in QUANTILES]
+    samples = [prior[i] for i in picks]
+    truth = S.draw_prior(an, 1, seed=10_000)[0]
+    with _lib.Handle(N, "f32", max_samples=len(samples)) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        u = h.batch_solve([truth.as_tuple()], an.L, with_loglik=False, want_phi=True)["phi"][0]
+        ic = h.batch_solve([s.as_tuple()[:5] + (-1.0,) for s in samples], an.L,
+                           with_loglik=False, want_phi=True)["phi"]
+    obs = S.make_observations(u.astype(np.float64), an, seed=3,
+                              centre_xyz=(truth.x0, truth.y0, truth.z0), radius_vox=27.0)
+    single, fp64, nsteps = [], [], []
+    for i, s in enumerate(samples):
+        dt32, dw32, dg32 = S.reference_dt(N, s.Dw, an.L, f32=True)
+        k = S.num_steps(dt32, s.T)
+        nsteps.append(k)
+        with _lib.Handle(N, "f32") as h1:
+            h1.set_anatomy(an.p_w, an.p_g)
+            h1.set_phi(ic[i].astype(np.float64))
+            # the batch schedule rounds Dw, Dg and rho to float (the default
+            # build's Real), then forms a = dt Dw / h^2 and b = dt rho
+            h1.rd_step(dw32, dg32, float(np.float32(s.rho)), dt32, k)
+            single.append(h1.get_phi())
+        dt, dw, dg = S.reference_dt(N, s.Dw, an.L)
+        phi0 = S.gaussian_ic(an, s.x0, s.y0, s.z0).astype(np.float32).astype(np.float64)
+        k64 = S.num_steps(dt, s.T)
+        if k64 != k:
+            print(f"sample {i}: {k} steps with float Dw, {k64} with double Dw")
+        fp64.append(oracle_lib.rd_solve(an.p_w, an.p_g, phi0, dw, dg, s.rho, dt, k64))
+    return dict(an=an, samples=samples, obs=obs, single=single, fp64=fp64, nsteps=nsteps)
+
+
+def _variants_at_128():
+    """Indices and names of the population variants the autotuner chooses
+    from at 128^3 (names are read from the library on the GPU)."""
+    with _lib.Handle(N, "f32", max_samples=1) as h:
+        names = [h.population_variant_name(i) for i in range(len(h.population_variants()))]
+    return [(i, nm) for i, nm in enumerate(names)
+            if nm.startswith(("k_population8<", "k_population9<", "k_population10<"))]
+
+
+def test_bench_variants_cover_default_and_pair_kernels(gbg):
+    names = [nm for _, nm in _variants_at_128()]
+    assert names[0].startswith("k_population8<32,4>"), names
+    assert any(nm.startswith("k_population9<") for nm in names), names
+
+
+@pytest.mark.parametrize("which", ["default", "pair", "sparse"])
+def test_bench_population_matches_single_solve_oracle_and_loglik(gbg, oracle_lib, bench_case,
+                                                                  which):
+    c = bench_case
+    an, samples, obs = c["an"], c["samples"], c["obs"]
+    pick = {"default": "k_population8<", "pair": "k_population9<", "sparse": "k_population10<"}
+    chosen = [(i, nm) for i, nm in _variants_at_128() if nm.startswith(pick[which])]
+    if not chosen:
+        pytest.skip(f"no {pick[which]} variant at 128^3")
+    for idx, name in chosen:
+        with _lib.Handle(N, "f32", max_samples=len(samples)) as h:
+            h.set_anatomy(an.p_w, an.p_g)
+            h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2,
+                               selective=True)
+            h.set_population_variant(idx)
+            res = h.batch_solve([s.as_tuple() for s in samples], an.L, with_loglik=True,
+                                want_phi=True)
+        for i, s in enumerate(samples):
+            assert int(res["nsteps"][i]) == c["nsteps"][i]
+            got = res["phi"][i].astype(np.float64)
+            # (a) bitwise against the single solve
+            assert np.array_equal(got, c["single"][i]), (name, i)
+            # (b) the FP32 path against the FP64 oracle
+            err = rel_l2(got, c["fp64"][i])
+            print(f"{name}: sample {i} ({c['nsteps'][i]} steps) rel L2 vs FP64 = {err:.3e}")
+            assert err <= F32_VS_F64_TOL, (name, i, err)
+            # (c) the log-likelihood against the oracle's on the same field
+            o = oracle_lib.loglik(got, obs.pet, obs.t1, obs.t2, obs.points, LIK, 3, 2, True)
+            g = res["loglik"][i]
+            assert g["n_pet"] == o["n_pet"]
+            for k in ("l_pet", "l_t1", "l_t2", "total"):
+                assert abs(g[k] - o[k]) <= LIK_REL_TOL * max(1.0, abs(o[k])), (name, i, k)
+
+
+def test_adjoint_gradient_at_128_matches_central_differences(gbg, bench_case):
+    """Two bench samples (the 0.2 and 0.4 step-count quantiles), scaled time
+    grid, float states: relative sensitivities theta_i dlogL/dtheta_i within
+    1e-3 of central differences (h = 1e-4 relative) of the FP64-state model."""
+    c = bench_case
+    an, obs = c["an"], c["obs"]
+    samples = [c["samples"][1].as_tuple(), c["samples"][2].as_tuple()]
+    dt0 = -1.0
+    with _lib.Handle(N, "f32", max_samples=2) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2,
+                           selective=True)
+        _, ga = h.adjoint_grad(samples, dt0, an.L, state="f32")
+        gf = np.zeros((2, 6))
+        for s, base in enumerate(samples):
+            for i in range(6):
+                step = 1e-4 * abs(base[i])
+                p, m = list(base), list(base)
+                p[i] += step
+                m[i] -= step
+                lp, _ = h.adjoint_grad([tuple(p)], dt0, an.L, state="f64", want_grad=False)
+                lm, _ = h.adjoint_grad([tuple(m)], dt0, an.L, state="f64", want_grad=False)
+                gf[s, i] = (lp[0] - lm[0]) / (2 * step)
+    th = np.abs(np.array(samples))
+    a, f = ga * th, gf * th
+    err = np.linalg.norm(a - f, axis=1) / np.linalg.norm(f, axis=1)
+    for s in range(2):
+        print(f"128^3 adjoint sample {s}: rel err {err[s]:.2e}")
+    assert np.all(err <= 1e-3), (a, f)

@@ -8,6 +8,7 @@ import pytest
 
 from gliomauq_gb300 import matrix_io, synthetic as S
 from helpers import boundary_layer, golden_json, golden_npz
+from oracle import refio
 
 
 def _sha(a):
@@ -128,7 +129,7 @@ def test_matrix_io_roundtrip_and_errors(tmp_path):
 
 def test_reference_sphere_file_format_reads():
     """The reference's own Sphere.dat (D2D<double> 80160 x 3) parses, when present."""
-    path = "/root/reference/source/Likelihood/makefile/Sphere.dat"
+    path = os.path.join(refio.REF_SOURCE, "Likelihood", "makefile", "Sphere.dat")
     if not os.path.exists(path):
         pytest.skip("reference tree not present")
     m = matrix_io.read_d2d(path)
@@ -153,14 +154,14 @@ def test_oracle_live_vs_reference_random_case(oracle_lib):
     assert np.array_equal(out, r["phi"])
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/source"), reason="reference tree not present")
+@pytest.mark.skipif(not os.path.isdir(refio.REF_SOURCE), reason="reference tree not present")
 def test_dropin_backend_compiles_against_reference_types():
     """include/gbglioma_blockprocessing.hpp instantiated at the reference's own
     call-site types (Grid, BlockCollection, BoundaryInfo, Glioma operators, the
     TBB pipeline as CPU back-end): a compile-only check."""
     import subprocess
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    ref = "/root/reference/source"
+    ref = refio.REF_SOURCE
     r = subprocess.run(["g++", "-fsyntax-only", "-std=gnu++11", "-fpermissive", "-w",
                         "-I" + os.path.join(root, "oracle", "shim"),
                         "-I" + os.path.join(root, "oracle", "shim", "vtk"), "-I" + ref,

@@ -2,7 +2,9 @@
 nothing (for callers that cannot call cudaMalloc: code running during CUDA
 graph capture, hosts whose device memory belongs to another allocator, fixed
 real-time budgets). Called through the C ABI twice in a row, each result must
-match the handle-based gbg_loglik on the same field and observations.
+match the handle-based gbg_loglik on the same field and observations, and the
+CPU oracle (pinned to the reference's likelihood program), which shares no
+code with the two GPU entry points.
 
 This file is named to be collected last, so a run that stops at the first
 failure has already run every other test."""
@@ -33,7 +35,7 @@ def compact_lists(n, pet, t1, t2, points, step_pet, step_ti):
             t2.ravel()[ti_idx].astype(np.float64))
 
 
-def test_loglik_noalloc_matches_handle_entry_twice(gbg):
+def test_loglik_noalloc_matches_handle_entry_twice(gbg, oracle_lib):
     torch = pytest.importorskip("torch")
     d = golden_npz("lik32.npz")
     ref = golden_json("lik32.json")
@@ -66,8 +68,12 @@ def test_loglik_noalloc_matches_handle_entry_twice(gbg):
         got = dict(l_pet=raw[0], l_t1=raw[1], l_t2=raw[2], total=raw[3],
                    n_pet=int(raw[4:5].view(np.int64)[0]))
         assert got["n_pet"] == exp["n_pet"]
+        o = oracle_lib.loglik(field.astype(np.float64), pet, t1, t2, d["points"], ref["params"],
+                              step_pet=sp, step_ti=st, selective=True)
+        assert got["n_pet"] == o["n_pet"]
         for k in ("l_pet", "l_t1", "l_t2", "total"):
             assert abs(got[k] - exp[k]) <= REL_TOL * max(1.0, abs(exp[k])), (k, got[k], exp[k])
+            assert abs(got[k] - o[k]) <= REL_TOL * max(1.0, abs(o[k])), (k, got[k], o[k])
 
 
 def test_loglik_noalloc_rejects_oversize_and_bad_args(gbg):
