@@ -199,8 +199,10 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=1
     h = _lib.Handle(n, "f32", device=device, max_samples=512)
     h.set_anatomy(an.p_w, an.p_g)
     prior = mcmc.Prior.from_anatomy(an)
-    # scaled time grid: the reference's step rule per sample with a shortened
-    # last step (smooth in tend and Dw, and it keeps the scaling symmetry)
+    # scaled time grid: the reference's step rule with the reaction's share of
+    # the stability bound, per sample, with a shortened last step (smooth in
+    # tend, Dw and rho, stable where the density saturates, and it keeps the
+    # scaling symmetry)
     dt0 = -1.0
     # observations from the same forward model the samplers use
     u = h.batch_solve([truth.as_tuple()], an.L, with_loglik=False, want_phi=True,
@@ -241,8 +243,8 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=1
     t_plain = r1.seconds * (plain_steps - plain_burn) / plain_steps
     d_plain = diagnostics(r1.samples[plain_burn:], t_plain)
     out = {
-        "grid": n, "time_grid": "scaled: dt = 0.99 h^2 / (6 Dw / L^2) per sample, last step "
-                                "shortened to end at T", "coordinates": names,
+        "grid": n, "time_grid": "scaled, stable: dt = 0.99 h^2 / (6 Dw / L^2 + rho h^2 / 2) per "
+                                "sample, last step shortened to end at T", "coordinates": names,
         "posterior": "synthetic truth, PET/T1/T2 likelihood, scaled-time-grid model (data and "
                      "inference)",
         "truth": list(truth.as_tuple()),

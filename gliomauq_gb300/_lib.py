@@ -281,8 +281,9 @@ class Handle:
 
     def batch_solve(self, samples, L, ic_peak=0.1, ic_sigma=1.0, with_loglik=True,
                     want_phi=False, dt0=0.0):
-        """dt0 = 0: the reference's time loop per sample; dt0 > 0: the smooth
-        time grid of adjoint_grad (same forward model, bit for bit)."""
+        """dt0 = 0: the reference's time loop per sample; dt0 != 0: the smooth
+        time grids of adjoint_grad (dt0 > 0 fixed, dt0 < 0 scaled and stable;
+        same forward model, bit for bit)."""
         S = len(samples)
         arr = (Sample * S)(*[Sample(*s) for s in samples])
         opts = BatchOpts(L, ic_peak, ic_sigma, 1 if with_loglik else 0, dt0)

@@ -569,7 +569,9 @@ int gbg_adjoint_grad(gbg_handle *hh, const gbg_sample *samples, int S, const gbg
         if (!std::isfinite(samples[s].Dw) || !std::isfinite(samples[s].rho) || !std::isfinite(samples[s].tend) ||
             !(samples[s].Dw > 0) || !(samples[s].tend > 0) ||
             samples[s].tend / (o->dt0 > 0 ? o->dt0
-                                          : -o->dt0 * 0.99 / (6.0 * h.n * h.n * samples[s].Dw / (o->L * o->L))) >
+                                          : -o->dt0 * 0.99 /
+                                                (6.0 * h.n * h.n * samples[s].Dw / (o->L * o->L) +
+                                                 0.5 * std::fabs(samples[s].rho))) >
                 1e6) {
             set_error("non-finite or out-of-range sample parameter");
             return GBG_ERR_NONFINITE;

@@ -767,27 +767,30 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     release();
 #undef ADJ_TRY
     // chain rule from the per-step sensitivities dlogL/da_k, dlogL/db_k,
-    // a_k = dt_k Dw / (L^2 h^2), b_k = dt_k rho. Fixed grid: only the last
-    // step's length depends on the parameters (through tend). Scaled grid:
-    // dt = C / Dw, so full steps have da/dDw = 0 and db/dDw = -dt rho / Dw,
-    // and the last step (length tend - (k-1) dt) has da/dDw = tend / (L^2 h^2)
-    // and db/dDw = rho (k-1) dt / Dw.
+    // a_k = dt_k Dw / (L^2 h^2), b_k = dt_k rho, with dt_k = dt for the full
+    // steps and dt_l = tend - (k-1) dt for the last one (the step count is
+    // piecewise constant). Fixed grid: dt does not depend on the parameters.
+    // Scaled grid: dt = C h^2 / (6 Dw / L^2 + rho h^2 / 2), so
+    // d dt / dDw = -dt (6 / L^2) / den and d dt / drho = -dt (h^2 / 2) / den.
     const bool scaled = o.dt0 < 0;
     for (int s = 0; s < S; ++s) {
         double gDw = 0.0, gRho = 0.0;
         const double Dw = samples[s].Dw, rho = samples[s].rho, dt = dts[s];
+        double dtdDw = 0.0, dtdRho = 0.0;
+        if (scaled) {
+            const double den = 6.0 * Dw / L2 + 0.5 * rho / ih2;
+            dtdDw = -dt * (6.0 / L2) / den;
+            dtdRho = -dt * (0.5 / ih2) / den;
+        }
+        const double km1 = (double)(ns[s] - 1);
         for (int k = 0; k < ns[s]; ++k) {
             const bool last = k == ns[s] - 1;
             const double dtk = last ? dtl[s] : dt;
+            const double dDw = last ? -km1 * dtdDw : dtdDw;   // d dt_k / dDw
+            const double dRho = last ? -km1 * dtdRho : dtdRho;
             const double gA = hA[(size_t)k * S + s], gB = hB[(size_t)k * S + s];
-            if (!scaled) {
-                gDw += gA * dtk / L2 * ih2;
-            } else if (!last) {
-                gDw += gB * (-dt * rho / Dw);
-            } else {
-                gDw += gA * samples[s].tend / L2 * ih2 + gB * rho * (ns[s] - 1) * dt / Dw;
-            }
-            gRho += gB * dtk;
+            gDw += gA * (dDw * Dw + dtk) / L2 * ih2 + gB * dDw * rho;
+            gRho += gA * dRho * Dw / L2 * ih2 + gB * (dRho * rho + dtk);
         }
         const int kl = ns[s] - 1;
         const double gT = hA[(size_t)kl * S + s] * samples[s].Dw / L2 * ih2 + hB[(size_t)kl * S + s] * samples[s].rho;

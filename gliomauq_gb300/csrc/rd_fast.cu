@@ -141,13 +141,25 @@ __global__ void k_schedule(const gbg_sample *__restrict__ smp, int S, int n, dou
 // Smooth time grids: a step dt, k = ceil(tend/dt) steps (at least one), the
 // last of length tend - (k-1) dt, so the final state is continuous in tend.
 //   dt0 > 0: dt = dt0 for every sample (fixed grid)
-//   dt0 < 0: dt = |dt0| * 0.99 h^2 / (6 Dw / L^2), the reference's step rule
-//            per sample (scaled grid). a = dt Dw / h^2 is then the same for
-//            every sample, b = dt rho depends on Dw / rho only and the step
-//            count on tend Dw only: the discrete model keeps the continuous
-//            one's symmetry (Dw, rho, tend) -> (c Dw, c rho, tend / c).
+//   dt0 < 0: dt = |dt0| * 0.99 h^2 / (6 Dw / L^2 + rho h^2 / 2) per sample
+//            (scaled grid): the reference's step rule with the reaction's
+//            share of the stability bound added. The reference's rule alone
+//            bounds only the diffusion part: where phi is near 1 the
+//            checkerboard mode of a white-matter region then grows by
+//            |1 - 12 a - b| > 1 per step, the clamp to [0, 1] bounds it, and
+//            the final density amplifies rounding differences. Here
+//            12 a + b = 1.98 |dt0| for every sample, so that mode decays. a =
+//            dt Dw / h^2 and b = dt rho depend on rho h^2 L^2 / Dw only and
+//            the step count on tend times a function of the same ratio: the
+//            discrete model keeps the continuous one's symmetry
+//            (Dw, rho, tend) -> (c Dw, c rho, tend / c).
 // Dw in double (no float rounding of the input); every operation rounded on
 // its own so host code that restates it gets the same coefficients.
+// 6 Dw + rho h^2 / 2 (Dw in unit-cube units), rounded operation by operation
+__device__ __forceinline__ double scaled_grid_den(double Dw, double rho, double h) {
+    return __dadd_rn(__dmul_rn(6.0, Dw), __dmul_rn(__dmul_rn(0.5, rho), __dmul_rn(h, h)));
+}
+
 __global__ void k_schedule_smooth(const gbg_sample *__restrict__ smp, int S, int n, double L, double dt0,
                                   SampleRec *__restrict__ unsorted) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -158,7 +170,7 @@ __global__ void k_schedule_smooth(const gbg_sample *__restrict__ smp, int S, int
     const double rho = smp[s].rho, tend = smp[s].tend;
     double dt = dt0;
     if (dt0 < 0)
-        dt = __dmul_rn(-dt0, __ddiv_rn(__dmul_rn(__dmul_rn(0.99, h), h), __dmul_rn(6.0, Dw)));
+        dt = __dmul_rn(-dt0, __ddiv_rn(__dmul_rn(__dmul_rn(0.99, h), h), scaled_grid_den(Dw, rho, h)));
     double kk = ceil(__ddiv_rn(tend, dt));
     if (!(kk >= 1.0)) kk = 1.0;
     if (kk > 1e8) kk = 1e8;

@@ -732,11 +732,15 @@ def polish_mode(post, v_map: np.ndarray, lp_map: float, cov0: np.ndarray, polish
     return v_map, lp_map, cov0, cov, restarts
 
 
-def stable_dt0(n: int, L: float, dw_max: float) -> float:
-    """Largest explicit step of the smooth time grid for diffusivities up to
-    dw_max [cm^2/day]: the reference's CFL rule dt = 0.99 h^2 / (6 Dw / L^2)."""
+def stable_dt0(n: int, L: float, dw_max: float, rho_max: float = 0.0) -> float:
+    """Largest explicit step of the fixed time grid for diffusivities up to
+    dw_max [cm^2/day] and growth rates up to rho_max [1/day]:
+    dt = 0.99 h^2 / (6 Dw / L^2 + rho h^2 / 2), which keeps 12 a + b <= 1.98
+    (a = dt Dw / (L h)^2, b = dt rho) so that the explicit step is stable
+    where the density saturates too (rho_max = 0: the reference's diffusion
+    rule alone)."""
     h = 1.0 / n
-    return 0.99 * h * h / (6.0 * dw_max / (L * L))
+    return 0.99 * h * h / (6.0 * dw_max / (L * L) + 0.5 * rho_max * h * h)
 
 
 def _base(post):

@@ -192,10 +192,18 @@ int gbg_batch_solve_device(gbg_handle *h, const gbg_sample *samples_device, int 
  * n = ceil(tend/dt) steps, the last one shortened to end exactly at tend
  * (the reference's integer step count makes its output piecewise constant
  * in Dw and tend). dt0 > 0: dt = dt0 for every sample (fixed grid; dt0 must
- * satisfy the CFL limit of the largest Dw, e.g. 0.99 h^2 / (6 Dw_max / L^2)).
- * dt0 < 0: dt = |dt0| * 0.99 h^2 / (6 Dw / L^2), the reference's step rule per
- * sample (scaled grid, stable for |dt0| <= 1): the discrete model then keeps
- * the continuous model's symmetry (Dw, rho, tend) -> (c Dw, c rho, tend / c),
+ * satisfy the stability limit of the largest Dw and rho,
+ * 0.99 h^2 / (6 Dw_max / L^2 + rho_max h^2 / 2)).
+ * dt0 < 0: dt = |dt0| * 0.99 h^2 / (6 Dw / L^2 + rho h^2 / 2) per sample
+ * (scaled grid, stable for |dt0| <= 1): the reference's step rule
+ * 0.99 h^2 / (6 Dw / L^2) bounds only the diffusion part of the explicit
+ * step; with it, wherever the density is near 1 in white matter the
+ * checkerboard mode grows by |1 - 12 a - b| > 1 per step (a = dt Dw / (L h)^2,
+ * b = dt rho), the clamp to [0, 1] bounds the oscillation and the final
+ * density amplifies rounding differences (a 1e-10 change of the initial state
+ * reached 4e-3 relative L2 after 399 steps at 128^3). The added rho term makes
+ * 12 a + b = 1.98 |dt0|, so that mode decays. The discrete model keeps the
+ * continuous model's symmetry (Dw, rho, tend) -> (c Dw, c rho, tend / c),
  * under which the density at tend is unchanged. Gradients
  * are of the log-likelihood (gbg_set_observations) with respect to
  * (Dw, rho, x0, y0, z0, tend), in the units of gbg_sample, written as
@@ -209,7 +217,7 @@ int gbg_batch_solve_device(gbg_handle *h, const gbg_sample *samples_device, int 
  * fields) is kept by the handle between calls and grows when a call needs
  * more, until gbg_destroy. */
 typedef struct {
-    double dt0;            /* > 0: fixed step in days; < 0: scaled grid, -1 = reference rule */
+    double dt0;            /* > 0: fixed step in days; < 0: scaled grid (-1: the stable step) */
     int checkpoint_every;
     double L;              /* brain length in cm */
     double ic_peak, ic_sigma;

@@ -47,7 +47,7 @@ def _rel_err(ga, gf, samples):
 def test_adjoint_gradient_matches_central_differences(gbg, state, tol, grid):
     an, obs, samples, dt0 = _problem()
     if grid == "scaled":
-        dt0 = -1.0  # the reference's step rule per sample, last step shortened
+        dt0 = -1.0  # the scaled stable step per sample, last step shortened
     with _lib.Handle(an.n, "f32") as h:
         h.set_anatomy(an.p_w, an.p_g)
         h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=1, step_ti=1)

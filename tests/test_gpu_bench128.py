@@ -2,19 +2,33 @@
 128^3 on the bench's own anatomy (make_anatomy(128, seed=0)), prior
 (draw_prior(..., 512, seed=1)) and observations, for every population-kernel
 variant the autotuner can pick at 128^3 (k_population8 and k_population9 at
-each tile depth) and the tissue-and-support-skipping kernel:
+each tile depth) and the tissue-and-support-skipping kernel. Six samples span
+the prior's step counts: the shortest, four quantiles and the longest of the
+512.
 
-  (a) every sample equals the single-solve fast path (gbg_rd_step, FP32)
-      bit for bit;
-  (b) every sample is within 1e-4 relative L2 of the FP64 oracle
-      (oracle.rd_solve, the reference's Case2 step restated; the error is
-      printed: this is the stated FP32 error of the configuration);
+On the reference's time grid (the bench's workload, dt0 = 0):
+  (a) every sample equals the single-solve fast path (gbg_rd_step) bit for bit;
+  (b) every sample's relative L2 error against the FP64 oracle (the
+      reference's Case2 step restated) is at most 1e-4 or, where the
+      reference's own default FP32 build is further off, three times that
+      build's error (its restatement in the oracle is pinned bit for bit to
+      the reference's FP32 binary). The reference's step rule bounds only the
+      diffusion part of the explicit step: where the density saturates in
+      white matter the checkerboard mode grows by |1 - 12 a - b| > 1 per step
+      (b = dt rho > 0.02 for nearly every prior draw), the clamp bounds it,
+      and the final field amplifies rounding differences to 1e-3..1e-2 --
+      FP64 codes that differ only in rounding order disagree by that much;
   (c) every sample's log-likelihood is within 1e-11 (relative) of the oracle's
       likelihood of the same float field.
+On the scaled stable grid (dt0 = -1: dt = 0.99 h^2 / (6 Dw / L^2 + rho h^2 / 2),
+last step shortened): (a), (c), and every sample within 1e-4 relative L2 of
+the FP64 oracle on the same grid. The errors are printed: they are the stated
+FP32 errors of the configuration.
 
-Six samples span the prior's step counts: the shortest, four quantiles and
-the longest of the 512. Also the discrete adjoint at 128^3 against central
-finite differences on two of them."""
+Also the discrete adjoint at 128^3 against central finite differences on two
+of the samples."""
+import math
+
 import numpy as np
 import pytest
 
@@ -30,14 +44,25 @@ LIK = (0.0025, 1.0, 0.7, 0.25, 0.09)
 QUANTILES = (0.0, 0.2, 0.4, 0.6, 0.8, 1.0)
 
 
+def scaled_grid(Dw_cm2, rho, T, L, n=N):
+    """dt, step count and last step of the scaled stable grid, rounded as the
+    library's schedule kernel rounds them."""
+    h = 1.0 / n
+    dw = Dw_cm2 / (L * L)
+    dt = ((0.99 * h) * h) / (6.0 * dw + (0.5 * rho) * (h * h))
+    k = max(1, math.ceil(T / dt))
+    return dt, k, T - (k - 1) * dt, dw
+
+
 @pytest.fixture(scope="module")
 def bench_case(oracle_lib):
     """The bench workload's anatomy, six of its prior draws, its observations,
-    and for each draw the single-solve GPU result and the FP64 oracle."""
+    and for each draw on both time grids the single-solve GPU result and the
+    FP64 oracle, and on the reference grid the error of the reference's FP32
+    build."""
     an = S.make_anatomy(N, seed=0)
     prior = S.draw_prior(an, 512, seed=1)
-    steps = np.array([S.num_steps(S.reference_dt(N, p.Dw, an.L, f32=True)[0], p.T)
-                      for p in prior])
+    steps = np.array([S.num_steps(S.reference_dt(N, p.Dw, an.L)[0], p.T) for p in prior])
     order = np.argsort(steps, kind="stable")
     picks = [int(order[min(len(order) - 1, int(q * (len(order) - 1)))]) for q in QUANTILES]
     samples = [prior[i] for i in picks]
@@ -49,25 +74,41 @@ def bench_case(oracle_lib):
                            with_loglik=False, want_phi=True)["phi"]
     obs = S.make_observations(u.astype(np.float64), an, seed=3,
                               centre_xyz=(truth.x0, truth.y0, truth.z0), radius_vox=27.0)
-    single, fp64, nsteps = [], [], []
+    out = {g: dict(single=[], fp64=[], nsteps=[]) for g in ("ref", "scaled")}
+    f32ref_err = []
     for i, s in enumerate(samples):
-        dt32, dw32, dg32 = S.reference_dt(N, s.Dw, an.L, f32=True)
-        k = S.num_steps(dt32, s.T)
-        nsteps.append(k)
+        phi0 = S.gaussian_ic(an, s.x0, s.y0, s.z0).astype(np.float32).astype(np.float64)
+        # reference grid, the fast path's schedule: Dw / L^2, dt and the step
+        # count in double (the reference's loop), then a = dt Dw / h^2 and
+        # b = dt rho rounded to float once
+        dt, dw, dg = S.reference_dt(N, s.Dw, an.L)
+        k = S.num_steps(dt, s.T)
+        # scaled stable grid
+        dts, ks, dtl, dws = scaled_grid(s.Dw, s.rho, s.T, an.L)
         with _lib.Handle(N, "f32") as h1:
             h1.set_anatomy(an.p_w, an.p_g)
             h1.set_phi(ic[i].astype(np.float64))
-            # the batch schedule rounds Dw, Dg and rho to float (the default
-            # build's Real), then forms a = dt Dw / h^2 and b = dt rho
-            h1.rd_step(dw32, dg32, float(np.float32(s.rho)), dt32, k)
-            single.append(h1.get_phi())
-        dt, dw, dg = S.reference_dt(N, s.Dw, an.L)
-        phi0 = S.gaussian_ic(an, s.x0, s.y0, s.z0).astype(np.float32).astype(np.float64)
-        k64 = S.num_steps(dt, s.T)
-        if k64 != k:
-            print(f"sample {i}: {k} steps with float Dw, {k64} with double Dw")
-        fp64.append(oracle_lib.rd_solve(an.p_w, an.p_g, phi0, dw, dg, s.rho, dt, k64))
-    return dict(an=an, samples=samples, obs=obs, single=single, fp64=fp64, nsteps=nsteps)
+            h1.rd_step(dw, dg, s.rho, dt, k)
+            out["ref"]["single"].append(h1.get_phi())
+            h1.set_phi(ic[i].astype(np.float64))
+            if ks > 1:
+                h1.rd_step(dws, 0.1 * dws, s.rho, dts, ks - 1)
+            h1.rd_step(dws, 0.1 * dws, s.rho, dtl, 1)
+            out["scaled"]["single"].append(h1.get_phi())
+        out["ref"]["nsteps"].append(k)
+        out["scaled"]["nsteps"].append(ks)
+        f64 = oracle_lib.rd_solve(an.p_w, an.p_g, phi0, dw, dg, s.rho, dt, k)
+        out["ref"]["fp64"].append(f64)
+        # the reference's default build: Real = float (Dw, Dg, rho and the
+        # fields in float, its dt from the float Dw)
+        dt32, dw32, dg32 = S.reference_dt(N, s.Dw, an.L, f32=True)
+        f32 = oracle_lib.rd_solve(an.p_w, an.p_g, phi0, dw32, dg32, s.rho, dt32,
+                                  S.num_steps(dt32, s.T), prec="f32ref")
+        f32ref_err.append(rel_l2(f32, f64))
+        g = oracle_lib.rd_solve(an.p_w, an.p_g, phi0, dws, 0.1 * dws, s.rho, dts, ks - 1)
+        out["scaled"]["fp64"].append(oracle_lib.rd_solve(an.p_w, an.p_g, g, dws, 0.1 * dws, s.rho,
+                                                         dtl, 1))
+    return dict(an=an, samples=samples, obs=obs, grids=out, f32ref_err=f32ref_err)
 
 
 def _variants_at_128():
@@ -85,15 +126,17 @@ def test_bench_variants_cover_default_and_pair_kernels(gbg):
     assert any(nm.startswith("k_population9<") for nm in names), names
 
 
+@pytest.mark.parametrize("grid", ["ref", "scaled"])
 @pytest.mark.parametrize("which", ["default", "pair", "sparse"])
 def test_bench_population_matches_single_solve_oracle_and_loglik(gbg, oracle_lib, bench_case,
-                                                                  which):
+                                                                  which, grid):
     c = bench_case
-    an, samples, obs = c["an"], c["samples"], c["obs"]
+    an, samples, obs, g = c["an"], c["samples"], c["obs"], c["grids"][grid]
     pick = {"default": "k_population8<", "pair": "k_population9<", "sparse": "k_population10<"}
     chosen = [(i, nm) for i, nm in _variants_at_128() if nm.startswith(pick[which])]
     if not chosen:
         pytest.skip(f"no {pick[which]} variant at 128^3")
+    dt0 = 0.0 if grid == "ref" else -1.0
     for idx, name in chosen:
         with _lib.Handle(N, "f32", max_samples=len(samples)) as h:
             h.set_anatomy(an.p_w, an.p_g)
@@ -101,22 +144,29 @@ def test_bench_population_matches_single_solve_oracle_and_loglik(gbg, oracle_lib
                                selective=True)
             h.set_population_variant(idx)
             res = h.batch_solve([s.as_tuple() for s in samples], an.L, with_loglik=True,
-                                want_phi=True)
+                                want_phi=True, dt0=dt0)
         for i, s in enumerate(samples):
-            assert int(res["nsteps"][i]) == c["nsteps"][i]
+            assert int(res["nsteps"][i]) == g["nsteps"][i]
             got = res["phi"][i].astype(np.float64)
             # (a) bitwise against the single solve
-            assert np.array_equal(got, c["single"][i]), (name, i)
+            assert np.array_equal(got, g["single"][i]), (name, grid, i)
             # (b) the FP32 path against the FP64 oracle
-            err = rel_l2(got, c["fp64"][i])
-            print(f"{name}: sample {i} ({c['nsteps'][i]} steps) rel L2 vs FP64 = {err:.3e}")
-            assert err <= F32_VS_F64_TOL, (name, i, err)
+            err = rel_l2(got, g["fp64"][i])
+            if grid == "ref":
+                bound = max(F32_VS_F64_TOL, 3.0 * c["f32ref_err"][i])
+                print(f"{name} reference grid: sample {i} ({g['nsteps'][i]} steps) rel L2 vs "
+                      f"FP64 = {err:.3e} (the reference's FP32 build: {c['f32ref_err'][i]:.3e})")
+            else:
+                bound = F32_VS_F64_TOL
+                print(f"{name} stable grid: sample {i} ({g['nsteps'][i]} steps) rel L2 vs "
+                      f"FP64 = {err:.3e}")
+            assert err <= bound, (name, grid, i, err)
             # (c) the log-likelihood against the oracle's on the same field
             o = oracle_lib.loglik(got, obs.pet, obs.t1, obs.t2, obs.points, LIK, 3, 2, True)
-            g = res["loglik"][i]
-            assert g["n_pet"] == o["n_pet"]
+            lk = res["loglik"][i]
+            assert lk["n_pet"] == o["n_pet"]
             for k in ("l_pet", "l_t1", "l_t2", "total"):
-                assert abs(g[k] - o[k]) <= LIK_REL_TOL * max(1.0, abs(o[k])), (name, i, k)
+                assert abs(lk[k] - o[k]) <= LIK_REL_TOL * max(1.0, abs(o[k])), (name, i, k)
 
 
 def test_adjoint_gradient_at_128_matches_central_differences(gbg, bench_case):
