@@ -12,9 +12,11 @@ log-likelihood accumulated in FP64.
            (gbg_batch_solve_device), CUDA events on the library's stream
   e2e    : solves/s through the host C-ABI entry gbg_batch_solve (parameters
            copied in, log-likelihoods and step counts copied out each step)
-  roofline: the population kernel's algorithmic bytes (8 B per cell-step of
-           state plus 8/S B of shared anatomy) over its event-timed duration,
-           against the measured HBM copy bandwidth
+  roofline: the population kernel's algorithmic bytes (8 B per cell-step it
+           computes, plus 8/S B of shared anatomy) over its event-timed
+           duration, against the measured HBM copy bandwidth; the skipping
+           kernel computes only cells whose value can be nonzero, and the
+           dense-equivalent figure (every cell of every step) is given beside
   cpu_baseline: the oracle's block-lab restatement of the reference's CPU
            step (FP32, all host cores) on a bounded sample, scaled to solves/s
 
@@ -450,11 +452,22 @@ def run_reference_arm(args):
     print(json.dumps(line))
 
 
-# DRAM bytes per cell-step of k_population8<32,4> measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum on a 64-sample 128^3
-# population: 268.87 GB for 3.2076e10 cell-steps); traffic grows with the
-# cell-steps of a launch.
-NCU_BYTES_PER_CELL_STEP = 268.869814e9 / 32075939840.0
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture
+# of the kernel on a 64-sample 128^3 population of the bench's prior) per
+# cell-step the kernel computed; traffic grows with the computed cell-steps.
+NCU_BYTES_PER_CELL_STEP = {
+    "k_population8<": 268.869814e9 / 32075939840.0,
+}
+
+
+def computed_cells(h):
+    """Cell-steps the latest population launch computed, or None for kernel
+    families that do not count them."""
+    from gliomauq_gb300 import _lib
+    try:
+        return h.last_population_cells()
+    except _lib.GbgError:
+        return None
 
 
 def main():
@@ -475,6 +488,8 @@ def main():
                     help="print the surrogate-network measurement alone (profiling runs)")
     ap.add_argument("--samples", type=int, default=S,
                     help="population size (profiling runs use a smaller one)")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="population-kernel variant to run (default: the autotuner's choice)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -499,7 +514,11 @@ def main():
     h.set_anatomy(an.p_w, an.p_g)
     tune_cache = os.path.join(ROOT, "gliomauq_gb300", "_build", "tune.json")
     os.makedirs(os.path.dirname(tune_cache), exist_ok=True)
-    variant = h.autotune(probe_samples=min(S, 64), cache_path=tune_cache)
+    if args.variant >= 0:
+        variant = args.variant
+        h.set_population_variant(variant)
+    else:
+        variant = h.autotune(probe_samples=min(S, 64), cache_path=tune_cache)
     shape = h.population_variants()[variant]
     obs = observations(h, an, truth)
     h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2,
@@ -530,12 +549,13 @@ def main():
     launches0 = h.launch_count()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    pop_ms = []
+    pop_ms, pop_cells = [], []
     with torch.cuda.stream(stream):
         ev0.record(stream)
         for _ in range(args.steps):
             device_step()
             pop_ms.append(h.last_population_ms())
+            pop_cells.append(computed_cells(h))
         ev1.record(stream)
     barrier()
     launches = h.launch_count() - launches0
@@ -559,9 +579,17 @@ def main():
     if rank == 0:
         peak, peak_kind = measured_peaks()
         cell_steps = per_solve * S
-        alg_bytes = cell_steps * (8.0 + 8.0 / S)
+        dense_bytes = cell_steps * (8.0 + 8.0 / S)
+        computed = (float(np.mean(pop_cells)) if all(c is not None for c in pop_cells)
+                    else cell_steps)
+        # bytes the kernel has to move: the density of every cell-step it
+        # computes read and written once, the shared anatomy once per sample
+        alg_bytes = computed * (8.0 + 8.0 / S)
         kern_ms = float(np.mean(pop_ms))
         achieved = alg_bytes / (kern_ms / 1000.0) / 1e9
+        kname = h.population_variant_name(variant)
+        ncu_key = next((k for k in NCU_BYTES_PER_CELL_STEP if kname.startswith(k)), None)
+        traffic = NCU_BYTES_PER_CELL_STEP[ncu_key] * computed if ncu_key else None
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
@@ -575,18 +603,26 @@ def main():
                        "population_kernel_shape": {"rows_per_tile": shape[0],
                                                    "samples_per_cta": shape[1],
                                                    "threads": shape[2],
-                                                   "chosen_by": "gbg_autotune"}},
+                                                   "chosen_by": "gbg_autotune" if args.variant < 0 else "--variant"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
-                         "traffic": NCU_BYTES_PER_CELL_STEP * cell_steps,
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
-                                           "k_population8<32, 4> (TZ 16) on the 64-sample population "
-                                           f"({NCU_BYTES_PER_CELL_STEP:.3f} B per cell-step), scaled "
-                                           "by this launch's cell-steps; the register-family variants "
-                                           "the autotuner picks between move the same density stream",
-                         "kernel": f"{h.population_variant_name(variant)} (autotuned variant {variant})",
+                         "traffic": traffic,
+                         "traffic_source": (
+                             f"ncu dram__bytes_read.sum + dram__bytes_write.sum of {ncu_key}...> on a "
+                             f"64-sample population of this prior "
+                             f"({NCU_BYTES_PER_CELL_STEP[ncu_key]:.3f} B per computed cell-step), "
+                             f"scaled by this launch's computed cell-steps" if ncu_key else
+                             "no ncu capture of this kernel family"),
+                         "kernel": f"{kname} (autotuned variant {variant})",
                          "kernel_ms": kern_ms,
+                         "cell_steps_computed": computed,
                          "algorithmic_bytes_per_launch": alg_bytes,
+                         "dense_equivalent": {
+                             "cell_steps": cell_steps, "bytes": dense_bytes,
+                             "achieved": dense_bytes / (kern_ms / 1000.0) / 1e9,
+                             "frac": dense_bytes / (kern_ms / 1000.0) / 1e9 / peak,
+                             "note": "every cell of every step, as the dense kernels compute it; the "
+                                     "skipping kernel leaves out cells that are provably 0"},
                          "peak_source": f"{peak_kind} hbm_gbs"},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 48 * S,
                     "d2h_bytes_per_step": 64 * S + 4},

@@ -25,7 +25,8 @@ EXPORTS = [
     "gbg_create", "gbg_destroy", "gbg_last_error", "gbg_version", "gbg_set_anatomy",
     "gbg_set_phi", "gbg_get_phi", "gbg_rd_step", "gbg_run", "gbg_set_observations",
     "gbg_loglik", "gbg_batch_solve", "gbg_batch_solve_device", "gbg_launch_count",
-    "gbg_stream", "gbg_sync", "gbg_last_population_ms", "gbg_loglik_noalloc",
+    "gbg_stream", "gbg_sync", "gbg_last_population_ms", "gbg_last_population_cells",
+    "gbg_loglik_noalloc",
     "gbg_population_variants", "gbg_set_population_variant", "gbg_population_variant_shape",
     "gbg_autotune", "gbg_amr_create", "gbg_amr_set_grid", "gbg_amr_set_ghosts", "gbg_amr_step",
     "gbg_amr_get_phi", "gbg_amr_fwt_detail", "gbg_adjoint_grad", "gbg_amr_remap",
@@ -125,6 +126,7 @@ def load(path: str = LIB_PATH):
         "gbg_stream": [vp, C.POINTER(vp)],
         "gbg_sync": [vp],
         "gbg_last_population_ms": [vp, C.POINTER(C.c_float)],
+        "gbg_last_population_cells": [vp, C.POINTER(C.c_longlong)],
         "gbg_population_variants": [vp, C.POINTER(C.c_int)],
         "gbg_set_population_variant": [vp, C.c_int],
         "gbg_population_variant_name": [vp, C.c_int, C.c_char_p, C.c_int],
@@ -381,6 +383,13 @@ class Handle:
         ms = C.c_float()
         check(self.lib.gbg_last_population_ms(self._h, C.byref(ms)))
         return ms.value
+
+    def last_population_cells(self) -> int:
+        """Cell-steps the latest population-kernel launch computed (tiles
+        visited times cells per tile)."""
+        c = C.c_longlong()
+        check(self.lib.gbg_last_population_cells(self._h, C.byref(c)))
+        return c.value
 
 
 class AmrHandle:

@@ -78,7 +78,8 @@ void free_handle(Handle &h) {
     void *ptrs[] = {h.pw, h.pg, h.phi[0], h.phi[1], h.b0, h.dfx, h.dfy, h.dfz, h.cx, h.cy, h.cz,
                     h.msk, h.cxs, h.sr[0], h.sr[1], h.sd[0], h.sd[1], h.mala_tt, h.bphi[0], h.bphi[1], h.bwork, h.dev_status, h.barrier,
                     h.obs.pet_idx, h.obs.pet_val, h.obs.ti_idx, h.obs.t1_val, h.obs.t2_val,
-                    h.lik_partials, h.lik_out, h.adj_ws, h.aff_phi0, h.aff_J, h.aff_out, h.aff_delta};
+                    h.lik_partials, h.lik_out, h.adj_ws, h.aff_phi0, h.aff_J, h.aff_out, h.aff_delta,
+                    h.tile_live, h.live_list, h.live_count};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (cudaEvent_t e : h.ev_pop)
@@ -177,10 +178,10 @@ int gbg_create(const gbg_config *cfg, gbg_handle **out) {
     h.bwork_bytes = gbg::bwork_total(h);
     TRY_ALLOC(h.bwork, h.bwork_bytes);
     TRY_ALLOC(h.dev_status, sizeof(int));
-    TRY_ALLOC(h.barrier, 2 * sizeof(unsigned));
+    TRY_ALLOC(h.barrier, 4 * sizeof(unsigned));
 #undef TRY_ALLOC
     if (cudaMemset(h.dev_status, 0, sizeof(int)) != cudaSuccess ||
-        cudaMemset(h.barrier, 0, 2 * sizeof(unsigned)) != cudaSuccess) {
+        cudaMemset(h.barrier, 0, 4 * sizeof(unsigned)) != cudaSuccess) {
         set_error("memset failed");
         return fail(GBG_ERR_CUDA);
     }
@@ -215,6 +216,7 @@ int gbg_set_anatomy(gbg_handle *hh, const double *p_w, const double *p_g) {
     h.anatomy_set = true;
     h.tables_valid = false;
     h.fast_valid = false;
+    h.live_valid = false;
     h.mala_valid = false;
     return GBG_OK;
 }
@@ -985,6 +987,29 @@ int gbg_last_population_ms(gbg_handle *hh, float *ms) {
     return GBG_OK;
 }
 
+int gbg_last_population_cells(gbg_handle *hh, long long *cell_steps) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!cell_steps) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    if (!h.ev_pop_recorded) {
+        set_error("no population kernel launched yet");
+        return GBG_ERR_STATE;
+    }
+    if (!h.pop_tile_cells) {
+        set_error("the latest population kernel does not count the tiles it computes");
+        return GBG_ERR_UNSUPPORTED;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    GBG_CUDA_TRY(cudaEventSynchronize(h.ev_pop[1]));
+    unsigned long long tiles = 0;
+    GBG_CUDA_TRY(cudaMemcpy(&tiles, h.barrier + 2, sizeof(tiles), cudaMemcpyDeviceToHost));
+    *cell_steps = (long long)tiles * h.pop_tile_cells;
+    return GBG_OK;
+}
+
 int gbg_population_variants(gbg_handle *hh, int *count) {
     if (int rc = check_handle(hh)) return rc;
     if (!count) {
@@ -1091,7 +1116,10 @@ int gbg_autotune(gbg_handle *hh, int probe_samples, const char *cache_path, int 
             return GBG_OK;
         }
     }
-    // probe: samples near the centre, about 24 steps each
+    // probe: samples near the centre, about 24 steps each, from an initial
+    // Gaussian wide enough (sigma = n / 4) to be nonzero on every tissue cell,
+    // so that the skipping kernel visits every live tile of every round, as it
+    // does once a population's tumours have spread
     std::vector<gbg_sample> probe(probe_samples);
     const double L = h.n * 0.1, c = 0.5 * (h.n - 1);
     for (int i = 0; i < probe_samples; ++i) {
@@ -1100,7 +1128,7 @@ int gbg_autotune(gbg_handle *hh, int probe_samples, const char *cache_path, int 
         gbg::reference_dt(h.n, Dw, L, false, &dt, &Dwu, &Dgu, &r);
         probe[i] = gbg_sample{Dw, 0.05, c + (i % 3) - 1.0, c, c + (i % 5) - 2.0, 23.5 * dt};
     }
-    gbg_batch_opts o{L, 0.1, 1.0, 0, 0.0};
+    gbg_batch_opts o{L, 0.1, 0.25 * h.n, 0, 0.0};
     int best = 0;
     float best_ms = 1e30f;
     const int saved = h.pop_variant;

@@ -22,7 +22,15 @@ void set_error(const std::string &msg);
     } while (0)
 
 // Device-side error codes written to the handle's status word.
-enum DeviceStatus : int { DEV_OK = 0, DEV_BARRIER_TIMEOUT = 1, DEV_COPY_TIMEOUT = 2, DEV_MMA_TIMEOUT = 3 };
+// DEV_DRAIN_TIMEOUT: after a copy timeout, waiting for the copies still in
+// flight timed out as well (they may have landed after the CTA left).
+enum DeviceStatus : int {
+    DEV_OK = 0,
+    DEV_BARRIER_TIMEOUT = 1,
+    DEV_COPY_TIMEOUT = 2,
+    DEV_MMA_TIMEOUT = 3,
+    DEV_DRAIN_TIMEOUT = 4
+};
 
 // Compact observation lists for the likelihood (see likelihood.cu).
 struct ObsDevice {
@@ -101,10 +109,22 @@ struct Handle {
     void *bwork = nullptr;                // per-sample schedule records
     size_t bwork_bytes = 0;
     int *dev_status = nullptr;            // device status word
-    unsigned *barrier = nullptr;          // grid barrier {count, generation}
+    unsigned *barrier = nullptr;          // grid barrier {count, generation}, then a
+                                          // 64-bit visited-tile counter
+    long long pop_tile_cells = 0;         // cells per tile of the latest launch (0: not counted)
 
     // population-kernel shape (index into the candidates for this n; 0 = default)
     int pop_variant = 0;
+
+    // tiles of the skipping population kernel (k_population10): a tile (RY
+    // rows of full x-rows by TZ planes) is live when one of its cells has a
+    // mask of 1; live_list holds the live tile indices (count in *live_count,
+    // device); built for tile depth live_tz from the fast tables' mask
+    unsigned char *tile_live = nullptr;
+    int *live_list = nullptr;
+    int *live_count = nullptr;
+    int live_tz = 0, live_ry = 0;
+    bool live_valid = false;
 
     // events bracketing the latest population-kernel launch
     cudaEvent_t ev_pop[2] = {nullptr, nullptr};
@@ -151,7 +171,8 @@ struct SampleRec {
     float a2, b2; // coefficients of the last step (== a, b on the reference schedule)
 };
 // Layout of Handle::bwork, each region 256-byte aligned, cap = max(1, max_samples):
-// unsorted records | sorted records | rank_of ints | staged gbg_sample inputs.
+// unsorted records | sorted records | rank_of ints | staged gbg_sample inputs |
+// initial-support boxes (4 ints per sample, unsorted order; see k_gaussian_ic).
 inline size_t bwork_align(size_t b) { return (b + 255) & ~(size_t)255; }
 inline int bwork_cap(const Handle &h) { return h.max_samples > 1 ? h.max_samples : 1; }
 inline size_t bwork_off_sorted(const Handle &h) { return bwork_align(bwork_cap(h) * sizeof(SampleRec)); }
@@ -159,9 +180,10 @@ inline size_t bwork_off_rank(const Handle &h) { return 2 * bwork_off_sorted(h); 
 inline size_t bwork_off_samples(const Handle &h) {
     return bwork_off_rank(h) + bwork_align(bwork_cap(h) * sizeof(int));
 }
-inline size_t bwork_total(const Handle &h) {
+inline size_t bwork_off_boxes(const Handle &h) {
     return bwork_off_samples(h) + bwork_align(bwork_cap(h) * sizeof(gbg_sample));
 }
+inline size_t bwork_total(const Handle &h) { return bwork_off_boxes(h) + bwork_align(bwork_cap(h) * 4 * sizeof(int)); }
 inline SampleRec *batch_unsorted(Handle &h) { return reinterpret_cast<SampleRec *>(h.bwork); }
 inline SampleRec *batch_sorted(Handle &h) {
     return reinterpret_cast<SampleRec *>((char *)h.bwork + bwork_off_sorted(h));
@@ -170,6 +192,7 @@ inline int *batch_rank_of(Handle &h) { return reinterpret_cast<int *>((char *)h.
 inline gbg_sample *batch_samples(Handle &h) {
     return reinterpret_cast<gbg_sample *>((char *)h.bwork + bwork_off_samples(h));
 }
+inline int *batch_boxes(Handle &h) { return reinterpret_cast<int *>((char *)h.bwork + bwork_off_boxes(h)); }
 int fast_build_tables(Handle &h, double ratio);
 // smooth time grid (fixed dt0, last step shortened): per-sample records into
 // dev_out (S entries, unsorted order)

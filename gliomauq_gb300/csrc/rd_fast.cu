@@ -35,19 +35,18 @@
 // Samples are ordered by step count, longest first, so the active samples of
 // round k are a prefix of that order.
 //
-// Kernel families (the autotuner times them per grid size): registers
-// (k_population8, the default: planes carried in registers, the mask in the
-// sign bit of the x-face table, 32-bit offsets; k_population9: the same with
-// two samples of one tile per warp sharing the anatomy loads; k_population1:
-// a separate mask table, optional one-plane-ahead loads or L2 prefetches),
-// cp.async rings (k_population3), and bulk-copy
-// rings fed by the TMA unit with mbarrier completion (k_population5: one
-// elected thread issues, a block barrier per plane; k_population6: a
-// producer warp and full/empty barriers per slot, no block barriers), and
-// temporal blocking (k_population7: two steps per round through a
-// shared-memory ring of first-step planes, density read and written once per
-// two steps). All run the same per-cell operation sequence, so every variant
-// gives the same bits.
+// Kernel families (the autotuner times them per grid size): the skipping
+// kernel (k_population10, the batched solver's default: k_population8's tile
+// march over only the tiles whose output can be nonzero -- tiles with a live
+// cell, inside each sample's initial support grown by a cell per step);
+// registers (k_population8: planes carried in registers, the mask in the sign
+// bit of the x-face table, 32-bit offsets; k_population9: the same with two
+// samples of one tile per warp sharing the anatomy loads); a bulk-copy ring
+// fed by the TMA unit with mbarrier completion and a producer warp
+// (k_population6); and temporal blocking (k_population7: two steps per round
+// through a shared-memory ring of first-step planes, density read and written
+// once per two steps). All run the same per-cell operation sequence, so every
+// variant gives the same bits.
 #include <cstdio>
 #include <vector>
 
@@ -230,10 +229,21 @@ __device__ __forceinline__ float gaussian_ic_value(int x, int y, int z, double x
 // Grid: y over samples, x over groups of four consecutive cells of one
 // sample (float4 stores when n is a multiple of 4, cell by cell otherwise).
 // 32-bit index arithmetic inside a sample (n <= 1024, n^3 < 2^32).
+// box non-null (the skipping population kernel): the y and z extent of the
+// cells given a nonzero value is recorded per sample as four ints
+// {n - ymin, ymax + 1, n - zmin, zmax + 1} (all 0: no nonzero cell) with
+// atomicMax, from zero-filled entries.
+__device__ __forceinline__ void record_support(int *box, int n, int y, int z) {
+    atomicMax(box + 0, n - y);
+    atomicMax(box + 1, y + 1);
+    atomicMax(box + 2, n - z);
+    atomicMax(box + 3, z + 1);
+}
+
 __global__ void k_gaussian_ic(int n, const gbg_sample *__restrict__ smp, int S, double peak,
                               double sigma, const double *__restrict__ pw, const double *__restrict__ pg,
                               float *__restrict__ phi, float *__restrict__ phi1 = nullptr,
-                              const SampleRec *__restrict__ recs = nullptr) {
+                              const SampleRec *__restrict__ recs = nullptr, int *__restrict__ box = nullptr) {
     const unsigned un = (unsigned)n, N = un * un * un, groups = (N + 3) / 4;
     const double two_s2 = __dmul_rn(__dmul_rn(2.0, sigma), sigma);
     const float screen = (float)(two_s2 * 120.0) + 1.0f;
@@ -250,11 +260,15 @@ __global__ void k_gaussian_ic(int n, const gbg_sample *__restrict__ smp, int S, 
                 for (int j = 0; j < 4; ++j)
                     v[j] = gaussian_ic_value(x + j, y, z, x0, y0, z0, peak, two_s2, screen, pw, pg, c + j);
                 *reinterpret_cast<float4 *>(dst + c) = make_float4(v[0], v[1], v[2], v[3]);
+                if (box && (v[0] != 0.0f || v[1] != 0.0f || v[2] != 0.0f || v[3] != 0.0f))
+                    record_support(box + 4 * s, n, y, z);
             } else {
                 for (unsigned cj = c; cj < c + 4 && cj < N; ++cj) {
                     const unsigned row = cj / un;
-                    dst[cj] = gaussian_ic_value((int)(cj - row * un), (int)(row % un), (int)(row / un), x0, y0, z0,
-                                                peak, two_s2, screen, pw, pg, cj);
+                    const float v = gaussian_ic_value((int)(cj - row * un), (int)(row % un), (int)(row / un), x0,
+                                                      y0, z0, peak, two_s2, screen, pw, pg, cj);
+                    dst[cj] = v;
+                    if (box && v != 0.0f) record_support(box + 4 * s, n, (int)(row % un), (int)(row / un));
                 }
             }
         }
@@ -319,136 +333,18 @@ struct PopArgs {
     const SampleRec *rec;          // sorted by nsteps descending
     unsigned *barrier;
     int *status;
+    // skipping kernel only: live tiles, per-tile liveness, initial-support
+    // boxes (unsorted sample order, see k_gaussian_ic)
+    const int *live_list, *live_count;
+    const unsigned char *tile_live;
+    const int *box;
+    unsigned long long *visited;  // tiles computed by this launch (k_population8/10)
 };
-
-__device__ __forceinline__ void cp_async16(float *smem_dst, const float *gmem_src) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem_src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// Population kernel, register variant: a thread marches TZ planes keeping
-// the z-1, z, z+1 planes of its four cells in registers; the y-neighbour
-// rows and the anatomy come through L2 (density, __ldcg) and L1 (anatomy,
-// __ldg).
-// PF = 1: the z+2 density plane (the DRAM stream) is loaded one plane ahead,
-// so two planes of each thread's new data are in flight at once.
-// D > 0: every lane asks for its own 16 bytes of density D planes ahead to be
-// brought into L2 (prefetch.global.L2; no registers held), so the z+1 load
-// the march waits on is an L2 hit.
-__device__ __forceinline__ void l2_prefetch_lane(const float *p) {
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));
-}
-
-template <int LR, int PF = 0, int D = 0>  // lanes per x-row = n/4
-__device__ __forceinline__ void march_tile(int n, int TZ, int ty0, int tz0,
-                                           const float *__restrict__ in, float *__restrict__ out,
-                                           const float *__restrict__ cx, const float *__restrict__ cy,
-                                           const float *__restrict__ cz, const float *__restrict__ msk,
-                                           float a, float b) {
-    const int lane = threadIdx.x & 31;
-    const int li = lane % LR;
-    const int y = ty0 + (int)(threadIdx.x / LR);
-    const int x0 = 4 * li;
-    const int ym = wrapm(y, n), yp = wrapp(y, n);
-    const size_t nn = n, plane = nn * nn;
-    auto at = [&](int yy, int zz) -> size_t { return (size_t)x0 + nn * (size_t)yy + plane * (size_t)zz; };
-    const int zs = wrapm(tz0, n);
-    float4 Pp = __ldcg(reinterpret_cast<const float4 *>(in + at(y, zs)));
-    float4 Pc = __ldcg(reinterpret_cast<const float4 *>(in + at(y, tz0)));
-    float4 CZp = __ldg(reinterpret_cast<const float4 *>(cz + at(y, zs)));
-    float4 Pahead;
-    if (PF) Pahead = __ldcg(reinterpret_cast<const float4 *>(in + at(y, wrapp(tz0, n))));
-    // planes tz0 + 1 .. tz0 + TZ are this tile's DRAM stream (tz0 - 1 and tz0
-    // were just loaded); rows start at x = 0, 16-byte aligned, n * 4 bytes
-    auto prefetch = [&](int zu) {
-        if (zu <= tz0 + TZ) l2_prefetch_lane(in + at(y, zu % n));
-    };
-    if (D > 1)
-        for (int d = 1; d < D; ++d) prefetch(tz0 + d);
-    for (int dz = 0; dz < TZ; ++dz) {
-        const int z = tz0 + dz;
-        const int zn = wrapp(z, n);
-        if (D > 0) prefetch(z + D);
-        float4 Pn;
-        if (PF) {
-            Pn = Pahead;
-            if (dz + 1 < TZ) Pahead = __ldcg(reinterpret_cast<const float4 *>(in + at(y, wrapp(zn, n))));
-        } else {
-            Pn = __ldcg(reinterpret_cast<const float4 *>(in + at(y, zn)));
-        }
-        const float4 PS = __ldcg(reinterpret_cast<const float4 *>(in + at(ym, z)));
-        const float4 PN = __ldcg(reinterpret_cast<const float4 *>(in + at(yp, z)));
-        const float4 CX = __ldg(reinterpret_cast<const float4 *>(cx + at(y, z)));
-        const float4 CY = __ldg(reinterpret_cast<const float4 *>(cy + at(y, z)));
-        const float4 CYm = __ldg(reinterpret_cast<const float4 *>(cy + at(ym, z)));
-        const float4 CZ = __ldg(reinterpret_cast<const float4 *>(cz + at(y, z)));
-        const float4 M = __ldg(reinterpret_cast<const float4 *>(msk + at(y, z)));
-        const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
-        const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
-        const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
-        const float p[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
-        const float cxa[5] = {cxl, CX.x, CX.y, CX.z, CX.w};
-        const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
-        const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
-        const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
-        const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
-        const float m4[4] = {M.x, M.y, M.z, M.w};
-        float o[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const float f0 = p[i + 1];
-            float lap = cxa[i] * (p[i] - f0);
-            lap = fmaf(cxa[i + 1], p[i + 2] - f0, lap);
-            lap = fmaf(cym4[i], ps[i] - f0, lap);
-            lap = fmaf(cy4[i], pn[i] - f0, lap);
-            lap = fmaf(czp4[i], pp[i] - f0, lap);
-            lap = fmaf(cz4[i], pq[i] - f0, lap);
-            float v = fmaf(a, lap, f0);
-            v = fmaf(b * f0, 1.0f - f0, v);
-            v = fminf(fmaxf(v, 0.0f), 1.0f);
-            o[i] = m4[i] != 0.0f ? v : 0.0f;
-        }
-        *reinterpret_cast<float4 *>(out + at(y, z)) = make_float4(o[0], o[1], o[2], o[3]);
-        Pp = Pc;
-        Pc = Pn;
-        CZp = CZ;
-    }
-}
-
-// Items of a round are ordered tile-major (item = tile * active + sample):
-// CTAs running at the same time work on the same tile of different samples,
-// so each tile's anatomy comes from DRAM once per round and is then shared
-// through L2.
-template <int LR, int MINB, int PF = 0, int D = 0>
-__global__ void __launch_bounds__(256, MINB) k_population1(PopArgs p) {
-    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
-    int active = p.S;
-    const int rows = 256 / LR;
-    for (int k = 0; k < maxsteps; ++k) {
-        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
-        const float *in = (k & 1) ? p.buf1 : p.buf0;
-        float *out = (k & 1) ? p.buf0 : p.buf1;
-        const long items = (long)active * p.tiles;
-        for (long it = blockIdx.x; it < items; it += gridDim.x) {
-            const int r = (int)(it % active), t = (int)(it / active);
-            const int ty = t % p.tiles_y, tz = t / p.tiles_y;
-            const size_t off = (size_t)p.rec[r].order * p.stride;
-            const bool last = k == p.rec[r].nsteps - 1;
-            march_tile<LR, PF, D>(p.n, p.TZ, ty * rows, tz * p.TZ, in + off, out + off, p.cx, p.cy, p.cz,
-                           p.msk, last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
-        }
-        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
-    }
-}
-
 
 // Register variant with fewer loads and cheaper addressing: the mask comes
 // from the sign bit of the x-face table (one float4 load less per plane), and
 // offsets inside a sample are 32-bit, formed once per tile and advanced by a
-// plane per step. Same operation sequence as march_tile on |cxs| = cx.
+// plane per step. The mask is applied as the sign bit of cxs (|cxs| = cx).
 template <int LR>
 __device__ __forceinline__ void march_tile_s(int n, int TZ, int ty0, int tz0,
                                              const float *__restrict__ in, float *__restrict__ out,
@@ -516,6 +412,7 @@ __global__ void __launch_bounds__(256, MINB) k_population8(PopArgs p) {
     const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
     int active = p.S;
     const int rows = 256 / LR;
+    unsigned long long visited = 0;
     for (int k = 0; k < maxsteps; ++k) {
         while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
         const float *in = (k & 1) ? p.buf1 : p.buf0;
@@ -528,16 +425,109 @@ __global__ void __launch_bounds__(256, MINB) k_population8(PopArgs p) {
             const bool last = k == p.rec[r].nsteps - 1;
             march_tile_s<LR>(p.n, p.TZ, ty * rows, tz * p.TZ, in + off, out + off, p.cxs, p.cy, p.cz,
                              last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
+            ++visited;
         }
-        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
+        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) break;
     }
+    if (threadIdx.x == 0 && visited) atomicAdd(p.visited, visited);
+}
+
+// Skipping variant of k_population8: a round visits only the tiles whose
+// output can be nonzero, with the same per-cell operation sequence, so the
+// results are bitwise those of the dense kernels.
+//   * A tile none of whose cells has mask 1 writes only zeros (masked cells
+//     get 0 whatever their inputs).
+//   * The output of round k can be nonzero only within one cell of the input's
+//     support, so inside the initial support's y/z box grown by k + 1 cells (a
+//     grown range reaching past a face covers the whole periodic axis); a
+//     tile outside it writes only zeros too (with inputs that are all +0 the
+//     step gives +0).
+// A skipped tile therefore has to hold zeros in the output buffer already:
+// the second buffer is zero-filled before the launch, the first holds the
+// initial state, which is zero outside the initial support. Round 0 reads the
+// initial state, which can be nonzero on masked tissue cells next to the
+// non-tissue region; round 1 writes that buffer, so it also rewrites (with
+// zeros) every tile without a live cell that meets the initial support. A
+// live tile, once visited, is visited in every later round of its sample (the
+// boxes only grow), so from round 2 on both buffers hold zeros in every tile a
+// round skips.
+__device__ __forceinline__ bool span_hits(int lo, int hi, int grow, int a, int b, int n) {
+    lo -= grow;
+    hi += grow;
+    if (lo < 0 || hi > n - 1) return true;
+    return lo <= b && a <= hi;
+}
+
+template <int LR, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_population10(PopArgs p) {
+    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
+    int active = p.S;
+    const int rows = 256 / LR;
+    const int n = p.n;
+    const int nlive = *p.live_count;
+    unsigned long long visited = 0;
+    for (int k = 0; k < maxsteps; ++k) {
+        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
+        const float *in = (k & 1) ? p.buf1 : p.buf0;
+        float *out = (k & 1) ? p.buf0 : p.buf1;
+        const int ntiles = k == 1 ? p.tiles : nlive;
+        const long items = (long)active * ntiles;
+        for (long it = blockIdx.x; it < items; it += gridDim.x) {
+            const int r = (int)(it % active), ti = (int)(it / active);
+            const int t = k == 1 ? ti : p.live_list[ti];
+            const int order = p.rec[r].order;
+            const int4 bx = reinterpret_cast<const int4 *>(p.box)[order];
+            if (bx.y == 0) continue;  // no nonzero initial cell: the sample stays 0
+            const int ylo = n - bx.x, yhi = bx.y - 1, zlo = n - bx.z, zhi = bx.w - 1;
+            const int y0 = (t % p.tiles_y) * rows, z0 = (t / p.tiles_y) * p.TZ;
+            const int y1 = y0 + rows - 1, z1 = z0 + p.TZ - 1;
+            bool go = span_hits(ylo, yhi, k + 1, y0, y1, n) && span_hits(zlo, zhi, k + 1, z0, z1, n);
+            if (go && k == 1 && !p.tile_live[t])
+                go = span_hits(ylo, yhi, 0, y0, y1, n) && span_hits(zlo, zhi, 0, z0, z1, n);
+            if (!go) continue;
+            const size_t off = (size_t)order * p.stride;
+            const bool last = k == p.rec[r].nsteps - 1;
+            march_tile_s<LR>(n, p.TZ, y0, z0, in + off, out + off, p.cxs, p.cy, p.cz,
+                             last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
+            ++visited;
+        }
+        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) break;
+    }
+    if (threadIdx.x == 0 && visited) atomicAdd(p.visited, visited);
+}
+
+// Liveness of the tiles of rows x tz cells (full x-rows): one CTA per tile,
+// a tile is live when a cell has the mask (sign bit of cxs clear).
+__global__ void k_tile_live(int n, int rows, int tz, const float *__restrict__ cxs, unsigned char *__restrict__ live) {
+    const int tiles_y = n / rows;
+    const int t = blockIdx.x;
+    const int y0 = (t % tiles_y) * rows, z0 = (t / tiles_y) * tz;
+    const unsigned cells = (unsigned)rows * (unsigned)tz * (unsigned)n;
+    int any = 0;
+    for (unsigned i = threadIdx.x; i < cells; i += blockDim.x) {
+        const unsigned x = i % (unsigned)n, yz = i / (unsigned)n;
+        const unsigned y = (unsigned)y0 + yz % (unsigned)rows, z = (unsigned)z0 + yz / (unsigned)rows;
+        any |= !signbit(cxs[x + (size_t)n * (y + (size_t)n * z)]);
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) live[t] = (unsigned char)(any != 0);
+}
+
+// Live tile indices in increasing order (one thread: at most a few thousand tiles).
+__global__ void k_compact_live(int tiles, const unsigned char *__restrict__ live, int *__restrict__ list,
+                               int *__restrict__ count) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int c = 0;
+    for (int t = 0; t < tiles; ++t)
+        if (live[t]) list[c++] = t;
+    *count = c;
 }
 
 // Two samples on one tile per warp: the anatomy (cxs, cy, cz) is loaded once
 // for both, so a plane costs 6 density + 4 anatomy loads for two samples
 // (5 per sample in place of 7), and each round trip of loads feeds twice the
 // arithmetic. The second slot is idle (two = false) for the odd sample of a
-// round. Per-sample operation sequence as march_tile.
+// round. Per-sample operation sequence as march_tile_s.
 template <int LR>
 __device__ __forceinline__ void stencil4(const float4 &Pc, const float4 &Pp, const float4 &Pn, const float4 &PS,
                                          const float4 &PN, const float4 &CX, const float4 &CY,
@@ -624,7 +614,7 @@ __device__ __forceinline__ void march_tile_pair(int n, int TZ, int ty0, int tz0,
 }
 
 // Items of a round: item = tile * pairs + pair, pair q = sorted samples 2q and
-// 2q + 1 (tile-major, as k_population1).
+// 2q + 1 (tile-major, as k_population8).
 template <int LR, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_population9(PopArgs p) {
     const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
@@ -661,156 +651,10 @@ __global__ void __launch_bounds__(256, MINB) k_population9(PopArgs p) {
     }
 }
 
-// Population kernel.
-//   LR lanes per x-row (n = 4 LR), RY rows per sample slot, G sample slots per
-//   CTA (CTA = LR*RY*G threads). An item is one (y-tile, z-chunk of TZ planes)
-//   of up to G samples: the G slots run the same tile of G different samples.
-//   Everything the stencil reads is staged in shared memory by cp.async.cg two
-//   planes ahead of the plane being computed, in rings of 4 planes:
-//     density, per slot: rows y0-1 .. y0+RY (periodic), RY+2 rows
-//     anatomy, shared by the slots: cy rows y0-1 .. y0+RY-1, then cx, cz and
-//     the mask rows y0 .. y0+RY-1 (4 RY + 1 rows)
-//   cp.async.cg reads L2, which is coherent with the previous round's stores;
-//   the z-1 and z planes of a thread's own row are carried in registers.
-template <int LR, int RY, int G>
-__global__ void __launch_bounds__(LR *RY *G, (LR * RY * G >= 1024) ? 1 : 1024 / (LR * RY * G))
-    k_population3(PopArgs p) {
-    constexpr int n = 4 * LR;
-    constexpr int SLOT_T = LR * RY;       // threads per slot
-    constexpr int NT = SLOT_T * G;
-    constexpr int PROWS = RY + 2;
-    constexpr int PPLANE = PROWS * n;     // floats per staged density plane
-    constexpr int AROWS = 4 * RY + 1;
-    constexpr int APLANE = AROWS * n;     // floats per staged anatomy plane
-    constexpr int plane_sz = n * n;       // cell indices within a field fit in int (n <= 128)
-    extern __shared__ __align__(16) float smem[];
-    float *aring = smem;                                // [4][AROWS][n]
-    const int g = threadIdx.x / SLOT_T;
-    const int t = threadIdx.x % SLOT_T;
-    const int r = t / LR;
-    const int li = t % LR;
-    const int x0 = 4 * li;
-    float *pring = smem + 4 * APLANE + g * 4 * PPLANE;  // this slot's [4][PROWS][n]
-    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
-    int active = p.S;
-    for (int k = 0; k < maxsteps; ++k) {
-        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
-        const float *in = (k & 1) ? p.buf1 : p.buf0;
-        float *out = (k & 1) ? p.buf0 : p.buf1;
-        const int groups = (active + G - 1) / G;
-        const long items = (long)groups * p.tiles;
-        for (long it = blockIdx.x; it < items; it += gridDim.x) {
-            const int grp = (int)(it / p.tiles), tile = (int)(it % p.tiles);
-            const int y0 = (tile % p.tiles_y) * RY, z0 = (tile / p.tiles_y) * p.TZ;
-            const int rank = grp * G + g;
-            const bool valid = rank < active;
-            float a = 0.f, b = 0.f;
-            size_t off = 0;
-            if (valid) {
-                const bool last = k == p.rec[rank].nsteps - 1;
-                a = last ? p.rec[rank].a2 : p.rec[rank].a;
-                b = last ? p.rec[rank].b2 : p.rec[rank].b;
-                off = (size_t)p.rec[rank].order * p.stride;
-            }
-            const float *src = in + off;
-            auto stage = [&](int zz, int q) {
-                const int zw = (zz + n) % n;
-                float *ad = aring + q * APLANE;
-                for (int c = threadIdx.x; c < AROWS * LR; c += NT) {
-                    const int ar = c / LR, col = 4 * (c % LR);
-                    const float *base;
-                    int yy;
-                    if (ar < RY + 1) { base = p.cy; yy = y0 - 1 + ar; }
-                    else if (ar < 2 * RY + 1) { base = p.cx; yy = y0 + ar - (RY + 1); }
-                    else if (ar < 3 * RY + 1) { base = p.cz; yy = y0 + ar - (2 * RY + 1); }
-                    else { base = p.msk; yy = y0 + ar - (3 * RY + 1); }
-                    yy = (yy + n) % n;
-                    cp_async16(ad + ar * n + col, base + (yy * n + col + plane_sz * zw));
-                }
-                if (valid) {
-                    float *pd = pring + q * PPLANE;
-                    for (int c = t; c < PROWS * LR; c += SLOT_T) {
-                        const int row = c / LR, col = 4 * (c % LR);
-                        const int yw = (y0 - 1 + row + n) % n;
-                        cp_async16(pd + row * n + col, src + (yw * n + col + plane_sz * zw));
-                    }
-                }
-                cp_async_commit();
-            };
-            stage(z0 - 1, 0);
-            stage(z0, 1);
-            stage(z0 + 1, 2);
-            const int y = y0 + r;
-            float4 Pp, Pc, CZp;
-            for (int dz = 0; dz < p.TZ; ++dz) {
-                const int z = z0 + dz;
-                if (dz + 2 <= p.TZ) stage(z + 2, (dz + 3) & 3);
-                else cp_async_commit();
-                cp_async_wait<1>();
-                __syncthreads();
-                const float *A0 = aring + ((dz + 1) & 3) * APLANE;
-                if (dz == 0) {
-                    const float *Am = aring + (dz & 3) * APLANE;
-                    CZp = *reinterpret_cast<const float4 *>(Am + (2 * RY + 1 + r) * n + x0);
-                }
-                if (valid) {
-                    const float *Lp = pring + ((dz + 2) & 3) * PPLANE;   // z+1
-                    const float *L0 = pring + ((dz + 1) & 3) * PPLANE;   // z
-                    if (dz == 0) {
-                        Pp = *reinterpret_cast<const float4 *>(pring + (dz & 3) * PPLANE + (r + 1) * n + x0);
-                        Pc = *reinterpret_cast<const float4 *>(L0 + (r + 1) * n + x0);
-                    }
-                    const float4 Pn = *reinterpret_cast<const float4 *>(Lp + (r + 1) * n + x0);
-                    const float4 PS = *reinterpret_cast<const float4 *>(L0 + r * n + x0);
-                    const float4 PN = *reinterpret_cast<const float4 *>(L0 + (r + 2) * n + x0);
-                    const float4 CYm = *reinterpret_cast<const float4 *>(A0 + r * n + x0);
-                    const float4 CY = *reinterpret_cast<const float4 *>(A0 + (r + 1) * n + x0);
-                    const float4 CX = *reinterpret_cast<const float4 *>(A0 + (RY + 1 + r) * n + x0);
-                    const float4 CZ = *reinterpret_cast<const float4 *>(A0 + (2 * RY + 1 + r) * n + x0);
-                    const float4 M = *reinterpret_cast<const float4 *>(A0 + (3 * RY + 1 + r) * n + x0);
-                    const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
-                    const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
-                    const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
-                    const float pv[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
-                    const float cxa[5] = {cxl, CX.x, CX.y, CX.z, CX.w};
-                    const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
-                    const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
-                    const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
-                    const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
-                    const float m4[4] = {M.x, M.y, M.z, M.w};
-                    float o[4];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const float f0 = pv[i + 1];
-                        float lap = cxa[i] * (pv[i] - f0);
-                        lap = fmaf(cxa[i + 1], pv[i + 2] - f0, lap);
-                        lap = fmaf(cym4[i], ps[i] - f0, lap);
-                        lap = fmaf(cy4[i], pn[i] - f0, lap);
-                        lap = fmaf(czp4[i], pp[i] - f0, lap);
-                        lap = fmaf(cz4[i], pq[i] - f0, lap);
-                        float v = fmaf(a, lap, f0);
-                        v = fmaf(b * f0, 1.0f - f0, v);
-                        v = fminf(fmaxf(v, 0.0f), 1.0f);
-                        o[i] = m4[i] != 0.0f ? v : 0.0f;
-                    }
-                    const int ci = x0 + n * y + plane_sz * z;
-                    __stcg(reinterpret_cast<float4 *>(out + off + ci), make_float4(o[0], o[1], o[2], o[3]));
-                    Pp = Pc;
-                    Pc = Pn;
-                    CZp = CZ;
-                }
-                __syncthreads();  // ring slot dz&3 is refilled next iteration
-            }
-            cp_async_wait<0>();
-        }
-        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
-    }
-}
-
-// ---- population kernel, bulk-copy (TMA) staged family --------------------------
-// Same arithmetic and operation order as march_tile. One elected thread
+// ---- population kernel, bulk-copy (TMA) staged ---------------------------------
+// Same arithmetic and operation order as march_tile_s. A producer warp
 // copies each z-plane of a tile into a ring of D shared-memory slots with
-// cp.async.bulk (the TMA unit; one mbarrier per slot, completion by byte
+// cp.async.bulk (the TMA unit; mbarriers per slot, completion by byte
 // count), up to D planes ahead of the plane being computed, so a CTA keeps
 // D planes of loads in flight without holding registers for them. A slot
 // holds, for one plane: density rows y0-1 .. y0+RY (periodic), cy rows
@@ -862,206 +706,6 @@ struct TmaRing {
     static constexpr unsigned BYTES = SLOT * 4;
     static constexpr size_t smem() { return (size_t)D * BYTES + 64 * D; }
 };
-
-template <int LR, int RY, int D, int MINB>
-__global__ void __launch_bounds__(LR *RY, MINB) k_population5(PopArgs p) {
-    using R = TmaRing<LR, RY, D>;
-    constexpr int n = R::n;
-    constexpr int plane = n * n;
-    extern __shared__ __align__(128) float smem5[];
-    float *ring = smem5;
-    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem5 + (size_t)D * R::SLOT);
-    const int r = threadIdx.x / LR, li = threadIdx.x % LR, x0 = 4 * li;
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < D; ++i) mbar_init(bar + i, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    __syncthreads();
-    // Planes form one sequence per CTA: plane q goes to slot q % D and
-    // completes phase (q / D) & 1 of that slot's barrier. Within a round the
-    // CTA's items (blockIdx.x, + gridDim.x, ...) are known in advance, so the
-    // producer (thread 0) runs ahead across item boundaries: plane q is
-    // issued once plane q - D is no longer read. Producer and consumers walk
-    // the sequence with incremental cursors (no divisions per plane).
-    struct Cursor {
-        int slot;
-        unsigned phase;
-        __device__ void step() {
-            if (++slot == D) {
-                slot = 0;
-                phase ^= 1u;
-            }
-        }
-    };
-    Cursor prod{0, 0u}, cons{0, 0u};  // next plane to issue / to wait for
-    int n_issued = 0;                 // within the round
-    unsigned used = 0, last_phase = 0;  // per slot (bit s): ever issued, phase of its latest copy
-    bool okw = true;                  // this thread's last copy wait succeeded
-    bool ok = true;                   // CTA-uniform
-    const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
-    const int nplanes = p.TZ + 2;     // planes tz0-1 .. tz0+TZ of an item
-    int active = p.S;
-    for (int k = 0; k < maxsteps && ok; ++k) {
-        while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
-        const float *in = (k & 1) ? p.buf1 : p.buf0;
-        float *out = (k & 1) ? p.buf0 : p.buf1;
-        const int items = active * p.tiles;
-        const int my_items = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-        const int round_planes = my_items * nplanes;
-        auto item_of = [&](int m, int &y0, int &tz0, size_t &off, int &smp) {
-            const int it = (int)blockIdx.x + m * (int)gridDim.x;
-            smp = it % active;
-            const int t = it / active;
-            y0 = (t % p.tiles_y) * RY;
-            tz0 = (t / p.tiles_y) * p.TZ;
-            off = (size_t)p.rec[smp].order * p.stride;
-        };
-        // producer cursor within the round
-        int pm = 0, pj = 0, py0 = 0, ptz0 = 0, psmp = 0;
-        size_t poff = 0;
-        if (threadIdx.x == 0 && my_items > 0) item_of(0, py0, ptz0, poff, psmp);
-        n_issued = 0;
-        // issue planes up to (not including) round-local index lim
-        auto issue_upto = [&](int lim) {
-            if (lim > round_planes) lim = round_planes;
-            if (threadIdx.x == 0) {
-                while (n_issued < lim) {
-                    unsigned long long *mb = bar + prod.slot;
-                    float *slot = ring + (size_t)prod.slot * R::SLOT;
-                    int zz = ptz0 - 1 + pj;
-                    zz = zz < 0 ? zz + n : (zz >= n ? zz - n : zz);
-                    const int ym = py0 == 0 ? n - 1 : py0 - 1, yp = py0 + RY == n ? 0 : py0 + RY;
-                    const float *pl = in + poff + (size_t)zz * plane;
-                    const size_t ao = (size_t)zz * plane;
-                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                    mbar_expect_tx(mb, R::BYTES);
-                    bulk_g2s(slot, pl + (size_t)ym * n, R::ROW, mb);
-                    bulk_g2s(slot + n, pl + (size_t)py0 * n, RY * R::ROW, mb);
-                    bulk_g2s(slot + (RY + 1) * n, pl + (size_t)yp * n, R::ROW, mb);
-                    float *cyb = slot + R::DEN;
-                    bulk_g2s(cyb, p.cy + ao + (size_t)ym * n, R::ROW, mb);
-                    bulk_g2s(cyb + n, p.cy + ao + (size_t)py0 * n, RY * R::ROW, mb);
-                    float *cxb = cyb + R::CYR, *czb = cxb + R::BLK, *mkb = czb + R::BLK;
-                    bulk_g2s(cxb, p.cx + ao + (size_t)py0 * n, RY * R::ROW, mb);
-                    bulk_g2s(czb, p.cz + ao + (size_t)py0 * n, RY * R::ROW, mb);
-                    bulk_g2s(mkb, p.msk + ao + (size_t)py0 * n, RY * R::ROW, mb);
-                    used |= 1u << prod.slot;
-                    last_phase = (last_phase & ~(1u << prod.slot)) | (prod.phase << prod.slot);
-                    prod.step();
-                    ++n_issued;
-                    if (++pj == nplanes) {
-                        pj = 0;
-                        if (++pm < my_items) item_of(pm, py0, ptz0, poff, psmp);
-                    }
-                }
-            } else if (lim > n_issued) {
-                n_issued = lim;
-            }
-        };
-        for (int m = 0; m < my_items; ++m) {
-            const int base = m * nplanes;  // round-local index of plane j = 0
-            int y0, tz0, smp;
-            size_t off;
-            item_of(m, y0, tz0, off, smp);
-            const bool last = k == p.rec[smp].nsteps - 1;
-            const float a = last ? p.rec[smp].a2 : p.rec[smp].a;
-            const float b = last ? p.rec[smp].b2 : p.rec[smp].b;
-            // the previous item is fully read: planes < base are free; a failed
-            // wait anywhere in the CTA ends the launch (a CTA-uniform decision)
-            if (__syncthreads_or(!okw)) {
-                ok = false;
-                break;
-            }
-            issue_upto(base + D);
-            const float *s0 = ring + (size_t)cons.slot * R::SLOT;
-            okw = mbar_wait(bar + cons.slot, cons.phase);
-            cons.step();
-            const float *sc = ring + (size_t)cons.slot * R::SLOT;  // plane tz0 (j = 1)
-            okw = mbar_wait(bar + cons.slot, cons.phase) && okw;
-            cons.step();
-            if (__syncthreads_or(!okw)) {
-                ok = false;
-                break;
-            }
-            const int y = y0 + r;
-            float4 Pp = *reinterpret_cast<const float4 *>(s0 + (r + 1) * n + x0);
-            float4 Pc = *reinterpret_cast<const float4 *>(sc + (r + 1) * n + x0);
-            float4 CZp = *reinterpret_cast<const float4 *>(s0 + R::DEN + R::CYR + R::BLK + r * n + x0);
-            for (int dz = 0; dz < p.TZ; ++dz) {
-                const int z = tz0 + dz;
-                // iteration dz - 1 (or the reads above) is done: planes j <= dz
-                // of this item are free, so planes up to j = dz + D may go out
-                if (__syncthreads_or(!okw)) {
-                    ok = false;
-                    break;
-                }
-                issue_upto(base + dz + 1 + D);
-                // plane z + 1 (j = dz + 2). After a failed wait the values read
-                // below are stale; the launch ends at the next barrier.
-                const float *sn = ring + (size_t)cons.slot * R::SLOT;
-                okw = mbar_wait(bar + cons.slot, cons.phase);
-                cons.step();
-                const float4 Pn = *reinterpret_cast<const float4 *>(sn + (r + 1) * n + x0);
-                const float4 PS = *reinterpret_cast<const float4 *>(sc + r * n + x0);
-                const float4 PN = *reinterpret_cast<const float4 *>(sc + (r + 2) * n + x0);
-                const float *cyb = sc + R::DEN, *cxb = cyb + R::CYR, *czb = cxb + R::BLK, *mkb = czb + R::BLK;
-                const float4 CYm = *reinterpret_cast<const float4 *>(cyb + r * n + x0);
-                const float4 CY = *reinterpret_cast<const float4 *>(cyb + (r + 1) * n + x0);
-                const float4 CX = *reinterpret_cast<const float4 *>(cxb + r * n + x0);
-                const float4 CZ = *reinterpret_cast<const float4 *>(czb + r * n + x0);
-                const float4 M = *reinterpret_cast<const float4 *>(mkb + r * n + x0);
-                const float left = __shfl_sync(0xffffffffu, Pc.w, (li + LR - 1) % LR, LR);
-                const float right = __shfl_sync(0xffffffffu, Pc.x, (li + 1) % LR, LR);
-                const float cxl = __shfl_sync(0xffffffffu, CX.w, (li + LR - 1) % LR, LR);
-                const float pv[6] = {left, Pc.x, Pc.y, Pc.z, Pc.w, right};
-                const float cxa[5] = {cxl, CX.x, CX.y, CX.z, CX.w};
-                const float ps[4] = {PS.x, PS.y, PS.z, PS.w}, pn[4] = {PN.x, PN.y, PN.z, PN.w};
-                const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
-                const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
-                const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
-                const float m4[4] = {M.x, M.y, M.z, M.w};
-                float o[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const float f0 = pv[i + 1];
-                    float lap = cxa[i] * (pv[i] - f0);
-                    lap = fmaf(cxa[i + 1], pv[i + 2] - f0, lap);
-                    lap = fmaf(cym4[i], ps[i] - f0, lap);
-                    lap = fmaf(cy4[i], pn[i] - f0, lap);
-                    lap = fmaf(czp4[i], pp[i] - f0, lap);
-                    lap = fmaf(cz4[i], pq[i] - f0, lap);
-                    float v = fmaf(a, lap, f0);
-                    v = fmaf(b * f0, 1.0f - f0, v);
-                    v = fminf(fmaxf(v, 0.0f), 1.0f);
-                    o[i] = m4[i] != 0.0f ? v : 0.0f;
-                }
-                __stcg(reinterpret_cast<float4 *>(out + off + (size_t)x0 + (size_t)n * y + (size_t)plane * z),
-                       make_float4(o[0], o[1], o[2], o[3]));
-                Pp = Pc;
-                Pc = Pn;
-                CZp = CZ;
-                sc = sn;
-            }
-            if (!ok) break;
-        }
-        // this round's stores (generic proxy) before the next round's bulk
-        // copies (async proxy) read them, across the grid barrier
-        asm volatile("fence.proxy.async.global;\n" ::: "memory");
-        if (ok && __syncthreads_or(!okw)) ok = false;
-        if (!ok) break;
-        if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) return;
-        asm volatile("fence.proxy.async.global;\n" ::: "memory");
-    }
-    if (!ok && threadIdx.x == 0) {
-        // a copy never completed: record it and let the copies this CTA has in
-        // flight land (bounded) before its shared memory is released; the other
-        // CTAs see the status word at their next grid barrier and leave
-        atomicExch(p.status, (int)DEV_COPY_TIMEOUT);
-        // the latest copy of a slot completes after all earlier ones of that slot
-        for (int sl = 0; sl < D; ++sl)
-            if (used >> sl & 1u) mbar_wait(bar + sl, last_phase >> sl & 1u);
-    }
-}
 
 // Warp-specialised variant of the bulk-copy family: warp NC (after the NC
 // consumer warps) produces, the consumer warps compute. Each slot has a
@@ -1241,9 +885,13 @@ __global__ void __launch_bounds__(LR *RY + 32, MINB) k_population6(PopArgs p) {
         asm volatile("fence.proxy.async.global;\n" ::: "memory");
     }
     if (abort_flag && producer && lane == 0) {
-        // let this CTA's copies in flight land (bounded) before leaving
+        // let this CTA's copies in flight land (bounded) before leaving; if one
+        // of these waits gives up too, copies may still be writing this CTA's
+        // shared memory when it exits, and the host is told so apart from the
+        // ordinary timeout
         for (int sl = 0; sl < D; ++sl)
-            if (used >> sl & 1u) mbar_wait(full + sl, last_phase >> sl & 1u);
+            if ((used >> sl & 1u) && !mbar_wait(full + sl, last_phase >> sl & 1u))
+                atomicExch(p.status, (int)DEV_DRAIN_TIMEOUT);
     }
 }
 
@@ -1251,7 +899,7 @@ __global__ void __launch_bounds__(LR *RY + 32, MINB) k_population6(PopArgs p) {
 // A CTA of 10 warps owns a tile of 8 rows (y0 .. y0+7) x TZ planes. Warp w
 // computes the first step for row y0-1+w (the tile's rows and one halo row
 // on each side) while marching z from tz0-1 to tz0+TZ, with the same
-// per-cell operation sequence as march_tile; the first-step rows go through a
+// per-cell operation sequence as march_tile_s; the first-step rows go through a
 // 3-plane ring in shared memory, from which warps 1..8 compute the second
 // step of plane z-1 (own row's z-2, z-1, z in registers, rows y-1 and y+1
 // from the ring, x-neighbours by shuffle). Each round advances every active
@@ -1426,21 +1074,10 @@ struct PopVariant {
     int ry, g, threads, tz;
     size_t smem;
     bool tb = false;  // two steps per round (start buffer per sample, see k_gaussian_ic)
+    bool skip = false;  // visits only tiles that can be nonzero (needs the batched solver's set-up)
+    bool counts = false;  // counts the tiles it computes (gbg_last_population_cells)
     char name[64] = {0};  // kernel and template arguments, plus the tile depth
 };
-
-template <int LR, int MINB = 1, int PF = 0, int D = 0>
-PopVariant make_register_variant(int tz) {
-    PopVariant v;
-    v.fn = (const void *)k_population1<LR, MINB, PF, D>;
-    v.ry = 256 / LR;
-    v.g = 1;
-    v.threads = 256;
-    v.tz = tz;
-    v.smem = 0;
-    std::snprintf(v.name, sizeof(v.name), "k_population1<%d,%d,%d,%d> TZ %d", LR, MINB, PF, D, tz);
-    return v;
-}
 
 template <int LR, int MINB>
 PopVariant make_signmask_variant(int tz) {
@@ -1451,7 +1088,23 @@ PopVariant make_signmask_variant(int tz) {
     v.threads = 256;
     v.tz = tz;
     v.smem = 0;
+    v.counts = true;
     std::snprintf(v.name, sizeof(v.name), "k_population8<%d,%d> TZ %d", LR, MINB, tz);
+    return v;
+}
+
+template <int LR, int MINB>
+PopVariant make_skip_variant(int tz) {
+    PopVariant v;
+    v.fn = (const void *)k_population10<LR, MINB>;
+    v.ry = 256 / LR;
+    v.g = 1;
+    v.threads = 256;
+    v.tz = tz;
+    v.smem = 0;
+    v.skip = true;
+    v.counts = true;
+    std::snprintf(v.name, sizeof(v.name), "k_population10<%d,%d> TZ %d", LR, MINB, tz);
     return v;
 }
 
@@ -1465,20 +1118,6 @@ PopVariant make_pair_variant(int tz) {
     v.tz = tz;
     v.smem = 0;
     std::snprintf(v.name, sizeof(v.name), "k_population9<%d,%d> TZ %d", LR, MINB, tz);
-    return v;
-}
-
-template <int LR, int RY, int G>
-PopVariant make_variant(int tz) {
-    PopVariant v;
-    v.fn = (const void *)k_population3<LR, RY, G>;
-    v.ry = RY;
-    v.g = G;
-    v.threads = LR * RY * G;
-    v.tz = tz;
-    const int n = 4 * LR;
-    v.smem = (size_t)(4 * (4 * RY + 1) * n + G * 4 * (RY + 2) * n) * sizeof(float);
-    std::snprintf(v.name, sizeof(v.name), "k_population3<%d,%d,%d> TZ %d", LR, RY, G, tz);
     return v;
 }
 
@@ -1509,65 +1148,41 @@ PopVariant make_ws_variant(int tz) {
     return v;
 }
 
-template <int LR, int RY, int D, int MINB>
-PopVariant make_tma_variant(int tz) {
-    PopVariant v;
-    v.fn = (const void *)k_population5<LR, RY, D, MINB>;
-    v.ry = RY;
-    v.g = 1;
-    v.threads = LR * RY;
-    v.tz = tz;
-    v.smem = TmaRing<LR, RY, D>::smem();
-    std::snprintf(v.name, sizeof(v.name), "k_population5<%d,%d,%d,%d> TZ %d", LR, RY, D, MINB, tz);
-    return v;
-}
-
-// Candidate shapes per grid size; index 0 is the default.
+// Candidate shapes per grid size; index 0 is the default. The batched solver
+// runs the skipping kernel by default; paths without its set-up (the single
+// solve) run the first dense register variant instead (dense_default).
 int variants_for(int n, PopVariant *out) {
     int k = 0;
     switch (n) {
         case 128:
+            out[k++] = make_skip_variant<32, 4>(8);
+            out[k++] = make_skip_variant<32, 4>(16);
             out[k++] = make_signmask_variant<32, 4>(16);
             out[k++] = make_signmask_variant<32, 4>(32);
-            out[k++] = make_signmask_variant<32, 3>(16);
             out[k++] = make_signmask_variant<32, 5>(16);
             out[k++] = make_pair_variant<32, 3>(16);
             out[k++] = make_pair_variant<32, 3>(32);
-            out[k++] = make_register_variant<32, 4>(16);
-            out[k++] = make_register_variant<32, 5>(16);
-            out[k++] = make_register_variant<32>(16);
-            out[k++] = make_register_variant<32, 4, 1>(16);
-            out[k++] = make_register_variant<32, 4, 0, 2>(16);
-            out[k++] = make_tb_variant<2, true>(16);
             out[k++] = make_tb_variant<2, true>(32);
-            out[k++] = make_tma_variant<32, 8, 3, 3>(32);
-            out[k++] = make_ws_variant<32, 8, 3, 3>(16);
             out[k++] = make_ws_variant<32, 8, 3, 3>(32);
-            out[k++] = make_variant<32, 8, 2>(32);
-            out[k++] = make_variant<32, 8, 1>(32);
-            out[k++] = make_variant<32, 4, 4>(32);
             break;
         case 64:
+            out[k++] = make_skip_variant<16, 4>(8);
             out[k++] = make_signmask_variant<16, 4>(16);
             out[k++] = make_signmask_variant<16, 5>(16);
-            out[k++] = make_register_variant<16>(16);
-            out[k++] = make_register_variant<16, 6>(16);
-            out[k++] = make_register_variant<16, 5, 1>(16);
-            out[k++] = make_tma_variant<16, 16, 3, 3>(16);
-            out[k++] = make_variant<16, 16, 2>(16);
-            out[k++] = make_variant<16, 16, 1>(16);
-            out[k++] = make_variant<16, 8, 2>(16);
-            out[k++] = make_variant<16, 8, 4>(32);
             break;
         case 32:
+            out[k++] = make_skip_variant<8, 4>(8);
             out[k++] = make_signmask_variant<8, 4>(8);
-            out[k++] = make_register_variant<8>(8);
-            out[k++] = make_variant<8, 32, 1>(8);
-            out[k++] = make_variant<8, 32, 2>(8);
-            out[k++] = make_variant<8, 16, 2>(16);
             break;
     }
     return k;
+}
+
+// index of the first variant that is neither temporally blocked nor skipping
+int dense_default(const PopVariant *vs, int nv) {
+    for (int i = 0; i < nv; ++i)
+        if (!vs[i].tb && !vs[i].skip) return i;
+    return 0;
 }
 
 int launch_population_v(Handle &h, PopArgs &a, const PopVariant &v) {
@@ -1582,7 +1197,9 @@ int launch_population_v(Handle &h, PopArgs &a, const PopVariant &v) {
     long grid = (long)bps * h.num_sms;
     if (grid > maxitems) grid = maxitems;
     if (grid < 1) grid = 1;
-    GBG_CUDA_TRY(cudaMemsetAsync(a.barrier, 0, sizeof(unsigned), h.stream));
+    // barrier count and generation, and the visited-tile counter after them
+    GBG_CUDA_TRY(cudaMemsetAsync(a.barrier, 0, 4 * sizeof(unsigned), h.stream));
+    h.pop_tile_cells = v.counts ? (long long)v.ry * v.tz * a.n : 0;
     void *args[] = {&a};
     GBG_CUDA_TRY(cudaEventRecord(h.ev_pop[0], h.stream));
     GBG_CUDA_TRY(cudaLaunchCooperativeKernel(v.fn, dim3((unsigned)grid), dim3(v.threads), args, v.smem,
@@ -1600,10 +1217,43 @@ bool variant_is_tb(const Handle &h) {
     return vi >= 0 && vi < nv && vs[vi].tb;
 }
 
+bool variant_is_skip(const Handle &h) {
+    PopVariant vs[32];
+    const int nv = variants_for(h.n, vs);
+    const int vi = h.pop_variant;
+    return vi >= 0 && vi < nv && vs[vi].skip;
+}
+
+// Live-tile list of the skipping kernel for tiles of rows x tz cells, built
+// from the fast tables' mask (sign bit of cxs) and kept until the anatomy
+// changes or another tile shape is asked for.
+int ensure_live_tiles(Handle &h, int rows, int tz) {
+    if (h.live_valid && h.live_ry == rows && h.live_tz == tz) return GBG_OK;
+    const int tiles = (h.n / rows) * (h.n / tz);
+    if (!h.tile_live) {
+        // sized for the smallest tiles any variant uses (rows >= 8, tz >= 8)
+        const size_t cap = (size_t)(h.n / 8 + 1) * (size_t)(h.n / 8 + 1);
+        GBG_CUDA_TRY(cudaMalloc((void **)&h.tile_live, cap));
+        GBG_CUDA_TRY(cudaMalloc((void **)&h.live_list, cap * sizeof(int)));
+        GBG_CUDA_TRY(cudaMalloc((void **)&h.live_count, sizeof(int)));
+    }
+    k_tile_live<<<tiles, 256, 0, h.stream>>>(h.n, rows, tz, h.cxs, h.tile_live);
+    k_compact_live<<<1, 32, 0, h.stream>>>(tiles, h.tile_live, h.live_list, h.live_count);
+    h.launches += 2;
+    GBG_CUDA_TRY(cudaGetLastError());
+    h.live_valid = true;
+    h.live_ry = rows;
+    h.live_tz = tz;
+    return GBG_OK;
+}
+
 // allow_tb = false (the single-solve path, whose state must start in buf0)
-// runs the default variant in place of a temporally blocked one
+// runs the default variant in place of a temporally blocked one; allow_skip =
+// false (any path but the batched solver, which sets up the initial-support
+// boxes and the zero-filled second buffer) runs it in place of the skipping
+// kernel
 int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_sorted, int S,
-                      bool allow_tb = true) {
+                      bool allow_tb = true, bool allow_skip = false) {
     const int LR = lanes_per_row(h.n);
     if (!LR) {
         set_error("fast path supports n = 32, 64 or 128");
@@ -1612,7 +1262,8 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
     PopVariant vs[32];
     const int nv = variants_for(h.n, vs);
     int vi = h.pop_variant;
-    if (vi < 0 || vi >= nv || (vs[vi].tb && !allow_tb)) vi = 0;
+    if (vi < 0 || vi >= nv || (vs[vi].tb && !allow_tb) || (vs[vi].skip && !allow_skip))
+        vi = dense_default(vs, nv);
     const PopVariant &v = vs[vi];
     PopArgs a;
     a.n = h.n;
@@ -1631,6 +1282,22 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
     a.rec = rec_sorted;
     a.barrier = h.barrier;
     a.status = h.dev_status;
+    a.live_list = nullptr;
+    a.live_count = nullptr;
+    a.tile_live = nullptr;
+    a.box = nullptr;
+    a.visited = reinterpret_cast<unsigned long long *>(h.barrier + 2);
+    if (v.skip) {
+        if (h.n % v.tz || h.n % v.ry) {
+            set_error("tile shape does not divide the grid");
+            return GBG_ERR_UNSUPPORTED;
+        }
+        if (int rc = ensure_live_tiles(h, v.ry, v.tz)) return rc;
+        a.live_list = h.live_list;
+        a.live_count = h.live_count;
+        a.tile_live = h.tile_live;
+        a.box = batch_boxes(h);
+    }
     return launch_population_v(h, a, v);
 }
 
@@ -1666,9 +1333,11 @@ int check_device_status(Handle &h) {
     if (st != DEV_OK) {
         const int zero = 0;
         cudaMemcpy(h.dev_status, &zero, sizeof(int), cudaMemcpyHostToDevice);
-        set_error(st == DEV_COPY_TIMEOUT  ? "device-side bulk copy did not complete"
-                  : st == DEV_MMA_TIMEOUT ? "device-side tensor-core MMA did not complete"
-                                          : "device-side grid barrier timed out");
+        set_error(st == DEV_COPY_TIMEOUT    ? "device-side bulk copy did not complete"
+                  : st == DEV_DRAIN_TIMEOUT ? "device-side bulk copy did not complete, and copies still in "
+                                              "flight did not land before the kernel left"
+                  : st == DEV_MMA_TIMEOUT   ? "device-side tensor-core MMA did not complete"
+                                            : "device-side grid barrier timed out");
         return GBG_ERR_TIMEOUT;
     }
     return GBG_OK;
@@ -1744,9 +1413,16 @@ int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
                                                           unsorted);
     k_sort_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(unsorted, S, sorted, rank_of);
     const bool tb = variant_is_tb(h);
+    // the skipping kernel: initial-support boxes recorded by the IC kernel and
+    // a zero-filled second buffer (it holds zeros wherever a round skips)
+    const bool skip = !f32ref && variant_is_skip(h);
+    if (skip) {
+        GBG_CUDA_TRY(cudaMemsetAsync(batch_boxes(h), 0, (size_t)S * 4 * sizeof(int), h.stream));
+        GBG_CUDA_TRY(cudaMemsetAsync(h.bphi[1], 0, (size_t)S * h.N * sizeof(float), h.stream));
+    }
     k_gaussian_ic<<<ic_grid(h, S), 256, 0, h.stream>>>(h.n, samples_device, S, o.ic_peak, o.ic_sigma, h.pw,
                                                         h.pg, h.bphi[0], tb ? h.bphi[1] : nullptr,
-                                                        tb ? unsorted : nullptr);
+                                                        tb ? unsorted : nullptr, skip ? batch_boxes(h) : nullptr);
     h.launches += 3;
     GBG_CUDA_TRY(cudaGetLastError());
     if (f32ref) {
@@ -1755,7 +1431,7 @@ int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
     }
     int rc = fast_build_tables(h, (double)0.1f);
     if (rc) return rc;
-    rc = launch_population(h, h.bphi[0], h.bphi[1], sorted, S);
+    rc = launch_population(h, h.bphi[0], h.bphi[1], sorted, S, true, skip);
     if (rc) return rc;
     if (o.with_loglik && loglik_device) {
         // final field of sample s sits in buffer (nsteps_s & 1); the likelihood

@@ -358,6 +358,14 @@ int gbg_sync(gbg_handle *h);
  * single solve), measured with CUDA events around that launch on the handle's
  * stream; waits for it to finish. */
 int gbg_last_population_ms(gbg_handle *h, float *ms);
+/* No reference counterpart. Cell-steps the most recent population-kernel
+ * launch computed: the tiles it visited times the cells of a tile. The
+ * skipping kernel (the batched solver's default) visits only the tiles whose
+ * output can be nonzero, so this is at most the population's step count times
+ * n^3; the dense register kernel visits every tile of every active sample.
+ * Waits for the launch to finish; GBG_ERR_UNSUPPORTED for the other kernel
+ * families, which do not count. */
+int gbg_last_population_cells(gbg_handle *h, long long *cell_steps);
 
 /* ---- population-kernel shape and autotuner --------------------------------
  * No counterpart in the reference (its TBB pipeline has a compile-time

@@ -116,7 +116,8 @@ def test_every_population_shape_gives_identical_results(gbg, n):
         shapes = h.population_variants()
         assert len(shapes) >= 2
         names = [h.population_variant_name(i) for i in range(len(shapes))]
-        assert names[0].startswith("k_population8<") and len(set(names)) == len(names), names
+        assert names[0].startswith(("k_population8<", "k_population10<")), names
+        assert len(set(names)) == len(names), names
         with pytest.raises(_lib.GbgError):
             h.population_variant_name(len(shapes))
         outs = []
@@ -142,3 +143,48 @@ def test_autotune_picks_and_caches(gbg, tmp_path):
     with open(cache) as f:
         d = json.load(f)
     assert list(d.values()) == [c1]
+
+
+@pytest.mark.parametrize("n", [32, 64])
+def test_skipping_kernel_equals_dense_on_edge_cases(gbg, n):
+    """k_population10 visits only tiles that can be nonzero; its results
+    equal the dense default's bit for bit on the cases its bookkeeping has to
+    get right: a seed on the brain's boundary layer (masked tissue cells hold
+    initial values in round 0 and must be cleared in round 1), a seed outside
+    the tissue (empty support), samples of 0, 1 and 2 steps, a wide Gaussian
+    whose support box reaches past the faces (periodic wrap), and ordinary
+    samples."""
+    from helpers import boundary_layer
+    an = S.make_anatomy(n, seed=9)
+    bl = np.argwhere(boundary_layer(an.brain))  # (z, y, x)
+    bz, by, bx = (float(v) for v in bl[len(bl) // 3])
+    c = (n - 1) / 2.0
+    dt = S.reference_dt(n, 0.0013, an.L)[0]
+    smp = [(0.0013, 0.05, bx, by, bz, 30 * dt),          # seed on the boundary layer
+           (0.0020, 0.10, -500.0, -500.0, -500.0, 12 * dt),  # far from any tissue: stays 0
+           (0.0013, 0.05, c + 0.3, c - 0.2, c, 0.0),      # one step
+           (0.0013, 0.05, c - 1.1, c + 0.4, c, 1.5 * dt),  # two steps
+           (0.0013, 0.05, c, c, c, -1.0),                 # no step
+           (0.0009, 0.12, c + 2.2, c - 3.1, c + 1.7, 40 * dt),
+           (0.0024, 0.02, c - 4.0, c + 2.0, c - 1.0, 25 * dt)]
+    with _lib.Handle(n, "f32", max_samples=len(smp)) as h:
+        h.set_anatomy(an.p_w, an.p_g)
+        names = [h.population_variant_name(i) for i in range(len(h.population_variants()))]
+        skip = [i for i, nm in enumerate(names) if nm.startswith("k_population10<")]
+        dense = [i for i, nm in enumerate(names) if nm.startswith("k_population8<")][0]
+        assert skip, names
+        for sigma in (1.0, 2.0 * n):
+            h.set_population_variant(dense)
+            ref = h.batch_solve(smp, an.L, ic_sigma=sigma, with_loglik=False, want_phi=True)
+            dense_cells = h.last_population_cells()
+            assert dense_cells == int(np.sum(ref["nsteps"])) * n ** 3
+            if sigma == 1.0:  # the far seed gives an empty support
+                assert not ref["phi"][1].any()
+            for i in skip:
+                h.set_population_variant(i)
+                got = h.batch_solve(smp, an.L, ic_sigma=sigma, with_loglik=False, want_phi=True)
+                assert 0 < h.last_population_cells() <= dense_cells
+                assert np.array_equal(got["nsteps"], ref["nsteps"])
+                for j in range(len(smp)):
+                    assert np.array_equal(got["phi"][j], ref["phi"][j]), (names[i], sigma, j)
+        assert list(ref["nsteps"][2:5]) == [1, 2, 0]

@@ -122,7 +122,7 @@ def _variants_at_128():
 
 def test_bench_variants_cover_default_and_pair_kernels(gbg):
     names = [nm for _, nm in _variants_at_128()]
-    assert names[0].startswith("k_population8<32,4>"), names
+    assert names[0].startswith(("k_population8<32,4>", "k_population10<32,4>")), names
     assert any(nm.startswith("k_population9<") for nm in names), names
 
 
