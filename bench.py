@@ -456,6 +456,7 @@ def run_reference_arm(args):
 # of the kernel on a 64-sample 128^3 population of the bench's prior) per
 # cell-step the kernel computed; traffic grows with the computed cell-steps.
 NCU_BYTES_PER_CELL_STEP = {
+    "k_population10<": (68.581464e9 + 61.917909e9) / 16350494720.0,
     "k_population8<": 268.869814e9 / 32075939840.0,
 }
 
