@@ -241,9 +241,11 @@ def dump_uniform(blocks, phi, gpd, reference_rules=True):
             continue
         ratio = gpd // cells
         r = ratio if not reference_rules else (ratio if ratio in (1, 2, 3) else 4)
-        for z in range(BS):
-            for y in range(BS):
-                for x in range(BS):
-                    mz, my, mx = ((bz * BS + z) * ratio, (by * BS + y) * ratio, (bx * BS + x) * ratio)
-                    out[mz:mz + r, my:my + r, mx:mx + r] = f[i, z, y, x]
+        # cell (z, y, x) of the block writes the r^3 cells starting at
+        # ((b * BS + z) * ratio, ...); viewed as (BS, ratio)^3 the block's
+        # region takes the first r of every ratio
+        span = BS * ratio
+        reg = out[bz * span:(bz + 1) * span, by * span:(by + 1) * span, bx * span:(bx + 1) * span]
+        reg = reg.reshape(BS, ratio, BS, ratio, BS, ratio)
+        reg[:, :r, :, :r, :, :r] = f[i][:, None, :, None, :, None]
     return out

@@ -31,8 +31,33 @@
 //   mala   <in> <out>   nsteps steps of Glioma_HG_UQ_MALA::_reactionDiffusionMALAStep
 //                       (source/Glioma/Glioma_HG_UQ_MALA.cpp:575-591) from zero
 //                       slopes; writes phi, sRho and sD on the uniform grid
+//   dump   <in> <out> [regrid]   (builds with GBG_HARNESS_DUMP only) the time
+//                       loop as `state` runs it, optionally one more regrid,
+//                       then the blocks and the reference's own
+//                       Glioma_HG_UQ::_dumpUQoutput of that grid
+//                       (source/Glioma/Glioma_HG_UQ.cpp:309-372), which
+//                       resamples to (blocksPerDimension * blockSize)^3 with
+//                       its h / 2h / 3h / else-4h replication rules
+//   dumpgrid <out> <r1> [r2 ...]  (GBG_HARNESS_DUMP builds) a grid of
+//                       blocksPerDimension^3 blocks at the maximum level
+//                       compressed once per radius by Grid::compress (blocks
+//                       whose centre lies farther than r1, then r2, ... from
+//                       the point (0.3, 0.35, 0.4) of the unit cube), its cells set to
+//                       phi = ((7 gx + 13 gy + 29 gz + 101 level) mod 1009) / 1009
+//                       (gx, gy, gz: the cell's index on its level), then the
+//                       blocks and _dumpUQoutput of that grid
 #include "Glioma_Types.h"
 #include "Glioma_MALA_SlopesOperator.h"
+#ifdef GBG_HARNESS_DUMP
+// _dumpUQoutput is a private member of Glioma_HG_UQ; this test-only
+// translation unit lifts the access specifier for the class declaration so
+// that the reference's own member function can be called on a grid of the
+// harness's choosing (the definitions are compiled unmodified from
+// Glioma_HG_UQ.cpp).
+#define private public
+#include "Glioma_HG_UQ.h"
+#undef private
+#endif
 
 #include <chrono>
 #include <cstdint>
@@ -516,6 +541,87 @@ static int cmdState(const char *inp, const char *outp, int extra) {
     return 0;
 }
 
+#ifdef GBG_HARNESS_DUMP
+// Glioma_HG_UQ's constructor reads the patient files; _dumpUQoutput reads no
+// member of the object but bVerbose, so it runs on zeroed storage of the
+// class's size and alignment (bVerbose = false) instead of a constructed
+// object. It writes HGG_data.dat (MatrixD3D<double>) into the working
+// directory.
+static int cmdDump(const char *inp, const char *outp, int regrid) {
+    Input in = readInput(inp);
+    Sim s(in.bpd);
+    fillGrid(*s.grid, in);
+    RunInfo ri = runLoop(s, in, true, nullptr, false);
+    if (regrid) {
+        s.regrid();
+        ri.regrids++;
+    }
+    alignas(Glioma_HG_UQ) static unsigned char storage[sizeof(Glioma_HG_UQ)];
+    memset(storage, 0, sizeof storage);
+    reinterpret_cast<Glioma_HG_UQ *>(storage)->_dumpUQoutput(*s.grid);
+    FILE *f = fopen(outp, "wb");
+    if (!f) die("cannot open output");
+    fwrite("GBGDMP01", 1, 8, f);
+    int32_t hdr[4] = {in.n, (int32_t)sizeof(Real), (int32_t)ri.steps, ri.regrids};
+    fwrite(hdr, 4, 4, f);
+    int32_t gpd = blocksPerDimension * blockSize;
+    fwrite(&gpd, 4, 1, f);
+    writeBlocks(f, *s.grid);
+    fclose(f);
+    return 0;
+}
+#endif
+
+#ifdef GBG_HARNESS_DUMP
+static int cmdDumpGrid(const char *outp, const std::vector<double> &radii) {
+    Sim s(blocksPerDimension);
+    const double c[3] = {0.3, 0.35, 0.4};
+    for (double r : radii) {
+        std::vector<BlockInfo> v = s.grid->getBlocksInfo();
+        std::set<int> toCompress;
+        for (const BlockInfo &b : v) {
+            const double w = 1.0 / (1 << b.level);
+            double d2 = 0;
+            for (int k = 0; k < 3; k++) {
+                const double x = (b.index[k] + 0.5) * w - c[k];
+                d2 += x * x;
+            }
+            if (d2 > r * r) toCompress.insert(b.blockID);
+        }
+        int nc = 0;
+        s.grid->compress(toCompress, nc);
+    }
+    std::vector<BlockInfo> vInfo = s.grid->getBlocksInfo();
+    for (size_t i = 0; i < vInfo.size(); i++) {
+        BlockInfo &info = vInfo[i];
+        B &block = s.grid->getBlockCollection()[info.blockID];
+        for (int iz = 0; iz < B::sizeZ; iz++)
+            for (int iy = 0; iy < B::sizeY; iy++)
+                for (int ix = 0; ix < B::sizeX; ix++) {
+                    const long gx = (long)info.index[0] * B::sizeX + ix;
+                    const long gy = (long)info.index[1] * B::sizeY + iy;
+                    const long gz = (long)info.index[2] * B::sizeZ + iz;
+                    block(ix, iy, iz).phi = (Real)((double)((7 * gx + 13 * gy + 29 * gz + 101 * info.level) % 1009) / 1009.0);
+                }
+        s.grid->getBlockCollection().release(info.blockID);
+    }
+    alignas(Glioma_HG_UQ) static unsigned char storage[sizeof(Glioma_HG_UQ)];
+    memset(storage, 0, sizeof storage);
+    reinterpret_cast<Glioma_HG_UQ *>(storage)->_dumpUQoutput(*s.grid);
+    FILE *f = fopen(outp, "wb");
+    if (!f) die("cannot open output");
+    fwrite("GBGDMP02", 1, 8, f);
+    int32_t hdr[2] = {blocksPerDimension * blockSize, (int32_t)vInfo.size()};
+    fwrite(hdr, 4, 2, f);
+    for (const BlockInfo &b : vInfo) {
+        int32_t bh[4] = {b.level, b.index[0], b.index[1], b.index[2]};
+        fwrite(bh, 4, 4, f);
+    }
+    fclose(f);
+    return 0;
+}
+#endif
+
 static int cmdTiming(const char *inp, int nthreads) {
     Environment::setup(nthreads);
     Input in = readInput(inp);
@@ -531,7 +637,7 @@ static int cmdTiming(const char *inp, int nthreads) {
 }
 
 int main(int argc, const char **argv) {
-    if (argc < 3) die("usage: ref_harness solve|ghosts|fwt|timing <in> [out|nthreads]");
+    if (argc < 3) die("usage: ref_harness solve|ghosts|fwt|state|mala|dump|dumpgrid|timing <in> [out|nthreads]");
     std::string cmd = argv[1];
     if (cmd == "timing") return cmdTiming(argv[2], argc > 3 ? atoi(argv[3]) : 1);
     Environment::setup(1);
@@ -541,6 +647,15 @@ int main(int argc, const char **argv) {
     if (cmd == "fwt") return cmdFwt(argv[2], argv[3]);
     if (cmd == "state") return cmdState(argv[2], argv[3], argc > 4 ? atoi(argv[4]) : 10);
     if (cmd == "mala") return cmdMala(argv[2], argv[3]);
+#ifdef GBG_HARNESS_DUMP
+    if (cmd == "dump") return cmdDump(argv[2], argv[3], argc > 4 ? atoi(argv[4]) : 0);
+    if (cmd == "dumpgrid") {
+        if (argc < 4) die("dumpgrid <out> <r1> [r2 ...]");
+        std::vector<double> radii;
+        for (int i = 3; i < argc; i++) radii.push_back(atof(argv[i]));
+        return cmdDumpGrid(argv[2], radii);
+    }
+#endif
     die("unknown command");
     return 2;
 }

@@ -191,3 +191,64 @@ def run_state(variant, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, dumpfreq, ext
         subprocess.run([exe, "state", inp, outp, str(extra)], check=True, timeout=timeout,
                        stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
         return read_state(outp)
+
+
+def run_dump(exe_name, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, adaptive=1, nsteps=-1,
+             dumpfreq=1e30, regrid=0, timeout=3600):
+    """`ref_dump_* dump`: the time loop as `state` runs it (optionally one
+    more regrid), the blocks of the resulting grid, and the reference's own
+    Glioma_HG_UQ::_dumpUQoutput of that grid (HGG_data.dat, read back as a
+    (gpd, gpd, gpd) array indexed [z, y, x])."""
+    exe = os.path.join(REF_DIR, exe_name)
+    with tempfile.TemporaryDirectory() as td:
+        inp = os.path.join(td, "in.bin")
+        outp = os.path.join(td, "out.bin")
+        write_input(inp, n, bpd, pw, pg, phi, Dw_file, rho, tend, L, adaptive, nsteps, dumpfreq)
+        subprocess.run([exe, "dump", inp, outp, str(int(regrid))], check=True, timeout=timeout,
+                       cwd=td, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+        raw = open(outp, "rb").read()
+        assert raw[:8] == b"GBGDMP01"
+        n_, real_bytes, steps, regrids = struct.unpack_from("<4i", raw, 8)
+        (gpd,) = struct.unpack_from("<i", raw, 24)
+        blocks, _ = _read_blocks(raw, 28)
+        d = open(os.path.join(td, "HGG_data.dat"), "rb").read()
+    # Matrix::D3D (Glioma/Matrix.h): ints {1234, 3, nx, ny, nz, type 0 = double},
+    # then the values, x fastest
+    magic, dim, sx, sy, sz, tid = struct.unpack_from("<6i", d, 0)
+    assert magic == 1234 and dim == 3 and tid == 0, (magic, dim, tid)
+    dump = np.frombuffer(d, "<f8", sx * sy * sz, 24).reshape(sz, sy, sx).copy()
+    return dict(steps=steps, regrids=regrids, gpd=gpd, blocks=blocks, dump=dump)
+
+
+def run_dumpgrid(exe_name, radii, timeout=3600):
+    """`ref_dump_* dumpgrid`: the blocks (level, ix, iy, iz) of the forced
+    multi-level grid and the reference's _dumpUQoutput of it (cells set by
+    dumpgrid_phi)."""
+    exe = os.path.join(REF_DIR, exe_name)
+    with tempfile.TemporaryDirectory() as td:
+        outp = os.path.join(td, "out.bin")
+        subprocess.run([exe, "dumpgrid", outp, *[repr(float(r)) for r in radii]], cwd=td,
+                       check=True, timeout=timeout, stdout=subprocess.DEVNULL,
+                       stderr=subprocess.PIPE)
+        raw = open(outp, "rb").read()
+        assert raw[:8] == b"GBGDMP02"
+        gpd, nb = struct.unpack_from("<2i", raw, 8)
+        blocks = np.frombuffer(raw, "<i4", 4 * nb, 16).reshape(nb, 4).copy()
+        d = open(os.path.join(td, "HGG_data.dat"), "rb").read()
+    magic, dim, sx, sy, sz, tid = struct.unpack_from("<6i", d, 0)
+    assert magic == 1234 and dim == 3 and tid == 0, (magic, dim, tid)
+    dump = np.frombuffer(d, "<f8", sx * sy * sz, 24).reshape(sz, sy, sx).copy()
+    return dict(gpd=gpd, blocks=blocks, dump=dump)
+
+
+def dumpgrid_phi(blocks):
+    """The cell values `dumpgrid` sets: ((7 gx + 13 gy + 29 gz + 101 level) mod
+    1009) / 1009 with (gx, gy, gz) the cell's index on its level; (nb, 16, 16,
+    16) indexed [block, z, y, x]."""
+    b = np.asarray(blocks, dtype=np.int64)
+    z, y, x = np.meshgrid(np.arange(16), np.arange(16), np.arange(16), indexing="ij")
+    out = np.empty((b.shape[0], 16, 16, 16))
+    for i, (lv, ix, iy, iz) in enumerate(b.tolist()):
+        out[i] = ((7 * (ix * 16 + x) + 13 * (iy * 16 + y) + 29 * (iz * 16 + z) + 101 * lv)
+                  % 1009) / 1009.0
+    return out

@@ -200,6 +200,44 @@ def amr_fixtures():
             s2_p_g=np.stack([b["p_g"] for b in st["s2"]]))
 
 
+def dump_fixtures():
+    """The reference's own Glioma_HG_UQ::_dumpUQoutput (Glioma_HG_UQ.cpp:309-372)
+    on multi-level grids, as SHA-256 of its HGG_data.dat:
+      dump64 : the adaptive 64^3 grid of amr64_f64.npz (levels 1, 2; h = hf,
+               2 hf), by ref_dump_b4 running the same loop;
+      grid3  : a 256^3 grid of levels 2, 3, 4 (h = 4 hf, 2 hf, hf) made by
+               ref_dump_b16 dumpgrid (two forced compressions), cell values
+               refio.dumpgrid_phi;
+      grid12 : a 256^3 grid of levels 1 and 2 (h = 8 hf, 4 hf): the dump
+               replicates a level-1 cell 4^3 times where it covers 8^3 cells,
+               and leaves the rest of the MatrixD3D it allocated with new[]
+               uninitialised -- the hash covers the cells it writes."""
+    a = np.load(os.path.join(HERE, "anatomy64.npz"))
+    pw, pg = a["p_w"].astype(np.float64), a["p_g"].astype(np.float64)
+    an = S.Anatomy(n=64, p_w=pw, p_g=pg, psi=None)
+    phi0 = f32(S.gaussian_ic(an, 20.3, 24.6, 22.1, peak=0.5, sigma=1.5))
+    r = refio.run_dump("ref_dump_b4", 64, 4, pw, pg, phi0, 0.0013, 0.1, 60.0, 6.4, dumpfreq=25.0)
+    d = np.load(os.path.join(HERE, "amr64_f64.npz"))
+    bl = np.array([[b["level"], *b["index"]] for b in r["blocks"]], dtype=np.int32)
+    assert np.array_equal(bl, d["blocks"]), "the dump run's grid differs from amr64_f64"
+    assert np.array_equal(np.stack([b["phi"] for b in r["blocks"]]), d["phi"])
+    out = {"dump64": dict(gpd=64, sha256=sha(r["dump"]), nonzero=int(np.count_nonzero(r["dump"])))}
+    for name, radii in (("grid3", [0.2, 0.45]), ("grid12", [0.0, 0.0, 0.4])):
+        g = refio.run_dumpgrid("ref_dump_b16", radii)
+        blocks = g["blocks"]
+        from oracle import amr_oracle as A
+        written = A.dump_uniform(blocks, np.ones((len(blocks), 16, 16, 16)), g["gpd"]) != 0
+        out[name] = dict(gpd=g["gpd"], radii=radii, blocks=blocks.tolist(),
+                         levels=sorted(set(blocks[:, 0].tolist())),
+                         written=int(written.sum()),
+                         sha256_written=hashlib.sha256(
+                             np.ascontiguousarray(g["dump"][written], dtype="<f8").tobytes()).hexdigest())
+        if written.all():
+            out[name]["sha256"] = sha(g["dump"])
+    with open(os.path.join(HERE, "dump_ref.json"), "w") as f:
+        json.dump(out, f)
+
+
 def patient_files(d, pat):
     """Write a synthetic patient the way the reference's `brain` reads it:
     <d>/Anatmoy/Patient01/P01_{GM,WM,CSF,T1,T2}.dat; returns the work folder
@@ -287,10 +325,14 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "mala":
         mala_fixture()
         sys.exit(0)
+    if len(sys.argv) > 1 and sys.argv[1] == "dump":
+        dump_fixtures()
+        sys.exit(0)
     rd_fixtures()
     mala_fixture()
     lik_fixture()
     amr_fixtures()
+    dump_fixtures()
     cli_fixture()
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))

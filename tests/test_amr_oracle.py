@@ -4,7 +4,7 @@ outputs (tests/golden/amr64_*.npz, made from oracle/_ref): ghost layout,
 import numpy as np
 import pytest
 
-from helpers import golden_npz
+from helpers import golden_json, golden_npz
 from oracle import amr_oracle as A
 
 REAL = {"f64": np.float64, "f32": np.float32}
@@ -56,18 +56,35 @@ def test_amr_remap_oracle_matches_reference(variant):
         assert np.array_equal(out.astype(np.float64), d[key]), name
 
 
-def test_amr_dump_rules():
+def _sha(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def test_amr_dump_oracle_matches_reference_dump():
+    """oracle.amr_oracle.dump_uniform against the reference's own
+    Glioma_HG_UQ::_dumpUQoutput (tests/golden/dump_ref.json, made by
+    oracle/_ref/ref_dump_*): the adaptive 64^3 grid of amr64_f64.npz (levels
+    1, 2), a 256^3 grid of levels 2, 3, 4, and a 256^3 grid of levels 1, 2
+    whose level-1 cells the reference replicates 4^3 times where they cover
+    8^3 (it leaves the rest of its output uninitialised; the hash covers the
+    cells it writes)."""
+    from oracle import refio
+    ref = golden_json("dump_ref.json")
     d = golden_npz("amr64_f64.npz")
     u = A.dump_uniform(d["blocks"], d["phi"], 64)
-    # level-2 blocks are copied, level-1 blocks replicated 2^3
-    b = [i for i, x in enumerate(d["blocks"].tolist()) if x[0] == 1][0]
-    l, bx, by, bz = d["blocks"][b]
-    assert u[bz * 32, by * 32, bx * 32] == d["phi"][b, 0, 0, 0]
-    assert u[bz * 32 + 1, by * 32 + 1, bx * 32 + 1] == d["phi"][b, 0, 0, 0]
-    assert np.count_nonzero(u) == np.count_nonzero(
-        np.concatenate([np.repeat(np.repeat(np.repeat(d["phi"][i], 2 ** (2 - d["blocks"][i][0]), 0),
-                                            2 ** (2 - d["blocks"][i][0]), 1),
-                                  2 ** (2 - d["blocks"][i][0]), 2).ravel() for i in range(len(d["blocks"]))]))
+    assert _sha(u) == ref["dump64"]["sha256"]
+    assert np.count_nonzero(u) == ref["dump64"]["nonzero"]
+    for name in ("grid3", "grid12"):
+        g = ref[name]
+        bl = np.array(g["blocks"], dtype=np.int32)
+        assert sorted(set(bl[:, 0].tolist())) == g["levels"]
+        ph = refio.dumpgrid_phi(bl)
+        u = A.dump_uniform(bl, ph, g["gpd"])
+        written = A.dump_uniform(bl, np.ones_like(ph), g["gpd"]) != 0
+        assert int(written.sum()) == g["written"]
+        assert _sha(u[written]) == g["sha256_written"], name
+    assert ref["grid12"]["written"] < 256 ** 3 == ref["grid3"]["written"]
 
 
 def test_same_level_ghost_tables_are_periodic_copies():

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from gliomauq_gb300 import _lib
-from helpers import golden_npz
+from helpers import golden_json, golden_npz
 from oracle import amr_oracle as A
 
 pytestmark = pytest.mark.gpu
@@ -99,6 +99,40 @@ def test_amr_dump_matches_oracle(gbg):
         u2 = h.dump_uniform(32, reference_rules=False)
     assert np.array_equal(u, A.dump_uniform(d["blocks"], d["phi"], 64))
     assert np.array_equal(u2, A.dump_uniform(d["blocks"], d["phi"], 32, reference_rules=False))
+
+
+def _sha(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", ["dump64", "grid3", "grid12"])
+def test_amr_dump_matches_reference_dump(gbg, name):
+    """gbg_amr_dump_uniform(reference_rules = 1) against the reference's own
+    Glioma_HG_UQ::_dumpUQoutput (hashes in tests/golden/dump_ref.json): the
+    adaptive 64^3 grid (levels 1, 2), a 256^3 grid of levels 2, 3, 4 and a
+    256^3 grid of levels 1, 2, where the reference replicates a level-1 cell
+    4^3 times over the 8^3 it covers. The reference leaves the cells it does
+    not write uninitialised; the library writes 0 there."""
+    from oracle import refio
+    ref = golden_json("dump_ref.json")[name]
+    if name == "dump64":
+        d = golden_npz("amr64_f64.npz")
+        bl, ph = d["blocks"], d["phi"]
+    else:
+        bl = np.array(ref["blocks"], dtype=np.int32)
+        ph = refio.dumpgrid_phi(bl)
+    zeros = np.zeros(ph.size)
+    with _lib.AmrHandle(len(bl), "f64") as h:
+        h.set_grid(bl, zeros, zeros, ph)
+        u = h.dump_uniform(ref["gpd"])
+    if "sha256" in ref:
+        assert _sha(u) == ref["sha256"]
+    if name != "dump64":
+        written = A.dump_uniform(bl, np.ones_like(ph), ref["gpd"]) != 0
+        assert int(written.sum()) == ref["written"]
+        assert _sha(u[written]) == ref["sha256_written"]
+        assert not u[~written].any()
 
 
 @pytest.mark.parametrize("variant", ["f64", "f32"])
