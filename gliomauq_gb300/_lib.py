@@ -30,7 +30,9 @@ EXPORTS = [
     "gbg_population_variants", "gbg_set_population_variant", "gbg_population_variant_shape",
     "gbg_autotune", "gbg_amr_create", "gbg_amr_set_grid", "gbg_amr_set_ghosts", "gbg_amr_step",
     "gbg_amr_get_phi", "gbg_amr_fwt_detail", "gbg_adjoint_grad", "gbg_amr_remap",
-    "gbg_amr_dump_uniform", "gbg_surrogate_create", "gbg_surrogate_destroy",
+    "gbg_amr_dump_uniform", "gbg_amr_ghost_tables", "gbg_amr_plan_refine", "gbg_amr_plan_compress",
+    "gbg_amr_build_ghosts", "gbg_amr_auto_refine", "gbg_amr_auto_compress", "gbg_amr_get_blocks",
+    "gbg_amr_run", "gbg_surrogate_create", "gbg_surrogate_destroy",
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
     "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_surrogate_set_engine",
@@ -73,6 +75,13 @@ class Sample(C.Structure):
 class AdjointOpts(C.Structure):
     _fields_ = [("dt0", C.c_double), ("checkpoint_every", C.c_int), ("L", C.c_double),
                 ("ic_peak", C.c_double), ("ic_sigma", C.c_double), ("state_precision", C.c_int)]
+
+
+class AmrRunOpts(C.Structure):
+    _fields_ = [("Dw_file", C.c_double), ("rho", C.c_double), ("tend", C.c_double),
+                ("L", C.c_double), ("dumpfreq", C.c_double), ("bpd", C.c_int),
+                ("adaptive", C.c_int), ("max_level", C.c_int), ("final_refine", C.c_int),
+                ("refine_tol", C.c_double), ("compress_tol", C.c_double)]
 
 
 class AmrConfig(C.Structure):
@@ -142,6 +151,16 @@ def load(path: str = LIB_PATH):
         "gbg_amr_fwt_detail": [vp, dp],
         "gbg_amr_remap": [vp, C.c_int, vp, vp, vp],
         "gbg_amr_dump_uniform": [vp, C.c_int, C.c_int, dp],
+        "gbg_amr_ghost_tables": [C.c_int, vp, vp, vp, vp, dp, C.c_long, lp],
+        "gbg_amr_plan_refine": [C.c_int, vp, vp, C.c_int, C.c_int, vp, vp, vp,
+                                C.POINTER(C.c_int), C.POINTER(C.c_int)],
+        "gbg_amr_plan_compress": [C.c_int, vp, vp, C.c_int, vp, vp, vp, C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int)],
+        "gbg_amr_build_ghosts": [vp],
+        "gbg_amr_auto_refine": [vp, C.c_double, C.c_int, C.POINTER(C.c_int)],
+        "gbg_amr_auto_compress": [vp, C.c_double, C.POINTER(C.c_int)],
+        "gbg_amr_get_blocks": [vp, vp, C.c_int, C.POINTER(C.c_int)],
+        "gbg_amr_run": [vp, C.POINTER(AmrRunOpts), lp, C.POINTER(C.c_int)],
         "gbg_surrogate_create": [vp, C.POINTER(SurrogateConfig), C.POINTER(vp)],
         "gbg_surrogate_destroy": [vp],
         "gbg_surrogate_nparams": [vp, lp],
@@ -464,6 +483,84 @@ class AmrHandle:
         out = np.empty((gpd, gpd, gpd), dtype=np.float64)
         check(self.lib.gbg_amr_dump_uniform(self._h, gpd, 1 if reference_rules else 0, dptr(out)))
         return out
+
+    def build_ghosts(self):
+        """Compile and install the ghost tables of the current blocks."""
+        check(self.lib.gbg_amr_build_ghosts(self._h))
+
+    def blocks(self) -> np.ndarray:
+        """(nb, 4) ints (level, ix, iy, iz) of the current grid, device order."""
+        n = C.c_int()
+        check(self.lib.gbg_amr_get_blocks(self._h, None, 0, C.byref(n)))
+        out = np.empty((n.value, 4), dtype=np.int32)
+        check(self.lib.gbg_amr_get_blocks(self._h, out.ctypes.data, n.value, C.byref(n)))
+        self.nb = n.value
+        return out
+
+    def auto_refine(self, tol=1e-4, max_level=-1) -> int:
+        r = C.c_int()
+        check(self.lib.gbg_amr_auto_refine(self._h, tol, max_level, C.byref(r)))
+        self.blocks()
+        return r.value
+
+    def auto_compress(self, tol=1e-5) -> int:
+        c = C.c_int()
+        check(self.lib.gbg_amr_auto_compress(self._h, tol, C.byref(c)))
+        self.blocks()
+        return c.value
+
+    def run(self, Dw_file, rho, tend, L, bpd, dumpfreq=1e30, adaptive=False, max_level=-1,
+            final_refine=True, refine_tol=1e-4, compress_tol=1e-5):
+        """Glioma_HG_UQ::run on this grid (gbg_amr_run); returns (steps, regrids)."""
+        o = AmrRunOpts(Dw_file, rho, tend, L, dumpfreq, bpd, 1 if adaptive else 0, max_level,
+                       1 if final_refine else 0, refine_tol, compress_tol)
+        steps, regrids = C.c_long(), C.c_int()
+        check(self.lib.gbg_amr_run(self._h, C.byref(o), C.byref(steps), C.byref(regrids)))
+        self.blocks()
+        return steps.value, regrids.value
+
+
+def amr_ghost_tables(blocks):
+    """Host-only: (start, src_block, src_cell, w) of a periodic block tree
+    (gbg_amr_ghost_tables)."""
+    lib = load()
+    b = np.ascontiguousarray(blocks, dtype=np.int32)
+    nb = b.shape[0]
+    start = np.empty(nb * AmrHandle.GHOSTS_PER_BLOCK + 1, dtype=np.int64)
+    n = C.c_long()
+    check(lib.gbg_amr_ghost_tables(nb, b.ctypes.data, start.ctypes.data, None, None, None, 0,
+                                   C.byref(n)))
+    sb = np.empty(n.value, dtype=np.int32)
+    sc = np.empty(n.value, dtype=np.int32)
+    w = np.empty(n.value, dtype=np.float64)
+    check(lib.gbg_amr_ghost_tables(nb, b.ctypes.data, start.ctypes.data, sb.ctypes.data,
+                                   sc.ctypes.data, dptr(w), n.value, C.byref(n)))
+    return start, sb, sc, w
+
+
+def _plan(fn, blocks, flagged, *extra):
+    lib = load()
+    b = np.ascontiguousarray(blocks, dtype=np.int32)
+    nb = b.shape[0]
+    f = np.ascontiguousarray(flagged, dtype=np.uint8)
+    cap = 8 * nb
+    nbk = np.empty((cap, 4), dtype=np.int32)
+    kind = np.empty(cap, dtype=np.int32)
+    src = np.empty((cap, 8), dtype=np.int32)
+    nn, cnt = C.c_int(), C.c_int()
+    check(getattr(lib, fn)(nb, b.ctypes.data, f.ctypes.data, *extra, cap, nbk.ctypes.data,
+                           kind.ctypes.data, src.ctypes.data, C.byref(nn), C.byref(cnt)))
+    return nbk[:nn.value], kind[:nn.value], src[:nn.value], cnt.value
+
+
+def amr_plan_refine(blocks, flagged, max_level=-1):
+    """Host-only: (new blocks, kind, src, refined) of Grid::refine's plan."""
+    return _plan("gbg_amr_plan_refine", blocks, flagged, max_level)
+
+
+def amr_plan_compress(blocks, flagged):
+    """Host-only: (new blocks, kind, src, collapses) of Grid::compress's plan."""
+    return _plan("gbg_amr_plan_compress", blocks, flagged)
 
 
 def _samples(samples):

@@ -736,6 +736,75 @@ int gbg_amr_remap(gbg_handle *hh, int nbn, const gbg_block *blocks, const int *k
     return gbg::amr_remap(h, nbn, blocks, kind, src);
 }
 
+int gbg_amr_build_ghosts(gbg_handle *hh) {
+    if (int rc = check_amr(hh)) return rc;
+    if (hh->h.amr.nb < 1) {
+        set_error("set the grid first");
+        return GBG_ERR_STATE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
+    return gbg::amr_build_ghosts(hh->h);
+}
+
+int gbg_amr_auto_refine(gbg_handle *hh, double tol, int max_level, int *nrefined) {
+    if (int rc = check_amr(hh)) return rc;
+    if (!nrefined || !(tol >= 0) || hh->h.amr.nb < 1) {
+        set_error("bad refinement arguments (set the grid first)");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
+    if (!hh->h.amr.ghosts_valid)
+        if (int rc = gbg::amr_build_ghosts(hh->h)) return rc;
+    return gbg::amr_auto_refine(hh->h, tol, max_level, nrefined);
+}
+
+int gbg_amr_auto_compress(gbg_handle *hh, double tol, int *ncollapsed) {
+    if (int rc = check_amr(hh)) return rc;
+    if (!ncollapsed || !(tol >= 0) || hh->h.amr.nb < 1) {
+        set_error("bad compression arguments (set the grid first)");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
+    if (!hh->h.amr.ghosts_valid)
+        if (int rc = gbg::amr_build_ghosts(hh->h)) return rc;
+    return gbg::amr_auto_compress(hh->h, tol, ncollapsed);
+}
+
+int gbg_amr_get_blocks(gbg_handle *hh, gbg_block *blocks, int capacity, int *nblocks) {
+    if (int rc = check_amr(hh)) return rc;
+    if (!nblocks) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    const std::vector<gbg_block> &b = hh->h.amr.hblocks;
+    *nblocks = (int)b.size();
+    if (!blocks) return GBG_OK;
+    if (capacity < (int)b.size()) {
+        set_error("capacity below the block count (see *nblocks)");
+        return GBG_ERR_ARG;
+    }
+    std::copy(b.begin(), b.end(), blocks);
+    return GBG_OK;
+}
+
+int gbg_amr_run(gbg_handle *hh, const gbg_amr_run_opts *o, long *steps, int *regrids) {
+    if (int rc = check_amr(hh)) return rc;
+    if (!o || !steps || !regrids || hh->h.amr.nb < 1 || !std::isfinite(o->Dw_file) || !(o->Dw_file > 0) ||
+        !std::isfinite(o->rho) || !std::isfinite(o->tend) || !(o->L > 0) || o->bpd < 1 ||
+        (o->adaptive && (!(o->dumpfreq > 0) || !(o->refine_tol >= 0) || !(o->compress_tol >= 0)))) {
+        set_error("bad adaptive-run arguments (set the grid first)");
+        return GBG_ERR_ARG;
+    }
+    double dt, Dw, Dg, rho = o->rho;
+    gbg::reference_dt(16 * o->bpd, o->Dw_file, o->L, false, &dt, &Dw, &Dg, &rho);
+    if (o->tend / dt > 1e8) {
+        set_error("too many steps (tend / dt > 1e8)");
+        return GBG_ERR_ARG;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(hh->h.device));
+    return gbg::amr_run(hh->h, *o, steps, regrids);
+}
+
 int gbg_amr_dump_uniform(gbg_handle *hh, int gpd, int reference_rules, double *out) {
     if (int rc = check_amr(hh)) return rc;
     if (gpd < 1 || gpd > 2048 || (gpd & (gpd - 1)) || !out || hh->h.amr.nb < 1) {

@@ -442,6 +442,7 @@ int amr_set_grid(Handle &h, int nb, const gbg_block *blocks, const double *pw, c
     }
     h.amr.nb = nb;
     h.amr.cur = 0;
+    h.amr.hblocks.assign(blocks, blocks + nb);
     h.amr.ghosts_valid = false;
     h.amr.tables_valid = false;
     return GBG_OK;
@@ -663,6 +664,7 @@ int amr_remap(Handle &h, int nbn, const gbg_block *blocks, const int *kind, cons
     std::swap(h.amr.pg, h.amr.pg2);
     h.amr.cur ^= 1;
     h.amr.nb = nbn;
+    h.amr.hblocks.assign(blocks, blocks + nbn);
     h.amr.ghosts_valid = false;
     h.amr.tables_valid = false;
     return GBG_OK;

@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/gbglioma.h"
 
@@ -62,6 +63,7 @@ struct AmrState {
     int *rkind = nullptr, *rsrc = nullptr;  // remap plan
     bool ghosts_valid = false, tables_valid = false;
     double tab_Dw = -1, tab_Dg = -1;
+    std::vector<gbg_block> hblocks;  // host copy of the blocks, in the device order
 };
 
 struct Handle {
@@ -223,6 +225,13 @@ int amr_get_phi(Handle &h, double *phi);
 int amr_fwt_detail(Handle &h, double *detail);
 int amr_remap(Handle &h, int nbn, const gbg_block *blocks, const int *kind, const int *src);
 int amr_dump_uniform(Handle &h, int gpd, int reference_rules, double *out);
+// ---- amr_plan.cu ----
+// ghost tables of the handle's blocks, compiled on the host and installed
+int amr_build_ghosts(Handle &h);
+// Science::AutomaticRefinement with one pass / AutomaticCompression to a fixpoint
+int amr_auto_refine(Handle &h, double tol, int max_level, int *refined);
+int amr_auto_compress(Handle &h, double tol, int *collapsed);
+int amr_run(Handle &h, const gbg_amr_run_opts &o, long *steps, int *regrids);
 
 // ---- adjoint.cu ----
 int adjoint_grad(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_opts &o, double *loglik,

@@ -346,6 +346,70 @@ int gbg_amr_remap(gbg_handle *h, int nblocks_new, const gbg_block *blocks_new, c
  * the dump grid's points. */
 int gbg_amr_dump_uniform(gbg_handle *h, int gpd, int reference_rules, double *out);
 
+/* ---- adaptive grid: ghost tables, regrid plans, the adaptive time loop -------
+ * Host-only (no GPU, no handle): the ghost instruction tables of a periodic
+ * block tree, as MRAG_BBInfoCreator::createBoundaryInfoBlock and
+ * Grid::getBoundaryInfo build them (source/MRAGcore/MRAG_BBInfoCreator.inl:902-1316,
+ * MRAGrid.inl:514-700) for Interpolating 2nd-order wavelets and the stencil
+ * [-1, 2), in the layout gbg_amr_set_ghosts takes: start[nb*1736 + 1]
+ * offsets and nentries (source block, source cell, weight) entries. With
+ * src_block, src_cell or w null only start and *nentries are written (a size
+ * query); otherwise capacity must be at least *nentries. The blocks must tile
+ * the unit cube as the leaves of a block tree. */
+int gbg_amr_ghost_tables(int nblocks, const gbg_block *blocks, long *start, int *src_block, int *src_cell,
+                         double *w, long capacity, long *nentries);
+/* Host-only. Grid::refine's plan for the flagged blocks (flagged[i] != 0):
+ * Refiner_SpaceExtension::createPlan + Refiner::createPlan
+ * (source/MRAGscience/MRAGRefiner_SpaceExtension.h:25-67, MRAGcore/MRAGRefiner.h:45-195,
+ * level jump 1, periodic): also every block with a finer neighbour that is
+ * not a periodic image, never a block on max_level (< 0: no limit), and
+ * every block the level-jump rule then requires. Writes the new blocks with
+ * the gbg_amr_remap kind/src arrays (8 src entries per block) for them,
+ * *nb_new and the number of refined blocks. */
+int gbg_amr_plan_refine(int nblocks, const gbg_block *blocks, const unsigned char *flagged, int max_level,
+                        int capacity, gbg_block *blocks_new, int *kind, int *src, int *nb_new, int *nrefined);
+/* Host-only. Grid::compress's plan (Compressor::createPlan,
+ * source/MRAGcore/MRAGCompressor.h:68-144, level jump 1, periodic): eight
+ * siblings collapse when all are flagged and all their neighbours are within
+ * one level of the parent. Output as gbg_amr_plan_refine. */
+int gbg_amr_plan_compress(int nblocks, const gbg_block *blocks, const unsigned char *flagged, int capacity,
+                          gbg_block *blocks_new, int *kind, int *src, int *nb_new, int *ncollapsed);
+/* Compiles and installs the ghost tables of the handle's current blocks
+ * (replaces gbg_amr_set_ghosts for grids the library manages). */
+int gbg_amr_build_ghosts(gbg_handle *h);
+/* Science::AutomaticRefinement with one pass (source/MRAGscience/MRAGScienceCore.h:42-108):
+ * the blocks below max_level whose FWT detail is >= tol are refined by the
+ * plan above, the data moved on the device and the new tables installed. */
+int gbg_amr_auto_refine(gbg_handle *h, double tol, int max_level, int *nrefined);
+/* Science::AutomaticCompression (MRAGScienceCore.h:117-177): passes of FWT,
+ * flag (detail < tol), collapse, new tables, until a pass collapses nothing; a
+ * block not flagged in a pass is not examined again in the call. */
+int gbg_amr_auto_compress(gbg_handle *h, double tol, int *ncollapsed);
+/* The current blocks, in the device order (capacity >= the block count;
+ * blocks null: only *nblocks). */
+int gbg_amr_get_blocks(gbg_handle *h, gbg_block *blocks, int capacity, int *nblocks);
+
+typedef struct {
+    double Dw_file;      /* cm^2/day, as HGG_InputParameters.txt gives it */
+    double rho;          /* 1/day */
+    double tend;         /* days */
+    double L;            /* brain length in cm */
+    double dumpfreq;     /* a regrid whenever t passes the next multiple (-dumpfreq) */
+    int bpd;             /* blocks per dimension of the initial grid: dt from h = 1/(16 bpd) */
+    int adaptive;        /* regrid at the dump times (-adaptive 1) */
+    int max_level;       /* finest level a refinement may create (_MAXLEVEL_) */
+    int final_refine;    /* the refinement after the loop (Glioma_HG_UQ.cpp:574-575) */
+    double refine_tol;   /* 1e-4 in the reference (Glioma_Types.h:462) */
+    double compress_tol; /* 1e-5 (Glioma_Types.h:463) */
+} gbg_amr_run_opts;
+/* Glioma_HG_UQ::run (source/Glioma/Glioma_HG_UQ.cpp:511-582) on the handle's
+ * grid: Dw /= L^2, Dg = 0.1 Dw (rounded to float in GBG_PREC_F32REF, as the
+ * default build's Real), dt = 0.99 h^2 / (6 max(Dw, Dg)), steps while
+ * t <= tend, the automatic regrids at the dump times and after the loop when
+ * adaptive. Ghost tables are compiled by the library. Writes the step and
+ * regrid counts. */
+int gbg_amr_run(gbg_handle *h, const gbg_amr_run_opts *opts, long *steps, int *regrids);
+
 /* ---- introspection ---------------------------------------------------------- */
 /* number of kernels this handle has launched since creation */
 int gbg_launch_count(gbg_handle *h, long long *count);

@@ -45,7 +45,8 @@
 //                       the point (0.3, 0.35, 0.4) of the unit cube), its cells set to
 //                       phi = ((7 gx + 13 gy + 29 gz + 101 level) mod 1009) / 1009
 //                       (gx, gy, gz: the cell's index on its level), then the
-//                       blocks and _dumpUQoutput of that grid
+//                       blocks, the grid's ghost tables (as `state` writes
+//                       them) and _dumpUQoutput of that grid
 #include "Glioma_Types.h"
 #include "Glioma_MALA_SlopesOperator.h"
 #ifdef GBG_HARNESS_DUMP
@@ -610,13 +611,14 @@ static int cmdDumpGrid(const char *outp, const std::vector<double> &radii) {
     reinterpret_cast<Glioma_HG_UQ *>(storage)->_dumpUQoutput(*s.grid);
     FILE *f = fopen(outp, "wb");
     if (!f) die("cannot open output");
-    fwrite("GBGDMP02", 1, 8, f);
+    fwrite("GBGDMP03", 1, 8, f);
     int32_t hdr[2] = {blocksPerDimension * blockSize, (int32_t)vInfo.size()};
     fwrite(hdr, 4, 2, f);
     for (const BlockInfo &b : vInfo) {
-        int32_t bh[4] = {b.level, b.index[0], b.index[1], b.index[2]};
-        fwrite(bh, 4, 4, f);
+        int32_t bh[5] = {b.blockID, b.level, b.index[0], b.index[1], b.index[2]};
+        fwrite(bh, 4, 5, f);
     }
+    writeGhostTables(f, *s.grid);
     fclose(f);
     return 0;
 }

@@ -138,6 +138,49 @@ def _read_blocks(raw, off):
     return blocks, off
 
 
+def _read_ghost_tables(raw, off):
+    """writeGhostTables output: per block its blockID, 27 region headers and
+    per ghost the (source blockID, source cell, weight product) entries."""
+    (nb,) = struct.unpack_from("<i", raw, off)
+    off += 4
+    rec = np.dtype([("b", "<i4"), ("c", "<i4"), ("w", "<f8")])
+    ghosts = []
+    for _ in range(nb):
+        bid, ng = struct.unpack_from("<2i", raw, off)
+        off += 8
+        regions = np.frombuffer(raw, "<i4", 54, off).reshape(27, 2).copy()
+        off += 4 * 54
+        counts = np.empty(ng, dtype=np.int32)
+        parts = []
+        for g in range(ng):
+            (cnt,) = struct.unpack_from("<i", raw, off)
+            off += 4
+            counts[g] = cnt
+            if cnt:
+                parts.append(np.frombuffer(raw, rec, cnt, off))
+                off += 16 * cnt
+        e = np.concatenate(parts) if parts else np.empty(0, dtype=rec)
+        ghosts.append(dict(id=bid, regions=regions, counts=counts,
+                           src_block=e["b"].astype(np.int32), src_cell=e["c"].astype(np.int32),
+                           w=e["w"].astype(np.float64)))
+    return ghosts, off
+
+
+def flatten_tables(ghosts, ids):
+    """The tables as gbg_amr_set_ghosts takes them, blocks in the order of
+    `ids` (source blockIDs mapped to positions in that order)."""
+    slot = {int(b): i for i, b in enumerate(ids)}
+    by_id = {g["id"]: g for g in ghosts}
+    counts = np.concatenate([by_id[int(b)]["counts"] for b in ids])
+    start = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    lut = np.vectorize(lambda x: slot[int(x)], otypes=[np.int32])
+    sb = np.concatenate([lut(by_id[int(b)]["src_block"]) if by_id[int(b)]["src_block"].size
+                         else np.empty(0, np.int32) for b in ids]).astype(np.int32)
+    sc = np.concatenate([by_id[int(b)]["src_cell"] for b in ids]).astype(np.int32)
+    w = np.concatenate([by_id[int(b)]["w"] for b in ids])
+    return start, sb, sc, w
+
+
 def read_state(path):
     """Output of `ref_harness state`: S0 blocks + ghost tables + FWT maxima,
     S1 blocks (after k more steps), S2 blocks (after one more regrid)."""
@@ -231,14 +274,16 @@ def run_dumpgrid(exe_name, radii, timeout=3600):
                        check=True, timeout=timeout, stdout=subprocess.DEVNULL,
                        stderr=subprocess.PIPE)
         raw = open(outp, "rb").read()
-        assert raw[:8] == b"GBGDMP02"
+        assert raw[:8] == b"GBGDMP03"
         gpd, nb = struct.unpack_from("<2i", raw, 8)
-        blocks = np.frombuffer(raw, "<i4", 4 * nb, 16).reshape(nb, 4).copy()
+        hdr = np.frombuffer(raw, "<i4", 5 * nb, 16).reshape(nb, 5).copy()
+        ids, blocks = hdr[:, 0], hdr[:, 1:]
+        ghosts, _ = _read_ghost_tables(raw, 16 + 20 * nb)
         d = open(os.path.join(td, "HGG_data.dat"), "rb").read()
     magic, dim, sx, sy, sz, tid = struct.unpack_from("<6i", d, 0)
     assert magic == 1234 and dim == 3 and tid == 0, (magic, dim, tid)
     dump = np.frombuffer(d, "<f8", sx * sy * sz, 24).reshape(sz, sy, sx).copy()
-    return dict(gpd=gpd, blocks=blocks, dump=dump)
+    return dict(gpd=gpd, blocks=blocks, dump=dump, tables=flatten_tables(ghosts, ids))
 
 
 def dumpgrid_phi(blocks):
