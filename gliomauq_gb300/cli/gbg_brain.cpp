@@ -4,15 +4,20 @@
 //           HGG_TumorIC.bin          (tumour centre, float32, unit coordinates)
 //           ../../Anatmoy/PatientNN/PNN_{GM,WM,CSF,T1,T2}.dat (Matrix::D3D)
 //   writes  HGG_data.dat             (Matrix::D3D<double>, (bpd*16)^3)
-// Command line: -anatomy HGG_UQ -pID N -adaptive 0 [-dumpfreq d -vtk 0 -verbose 0
-// -nthreads k] plus -bpd (blocks per dimension, the reference's compile-time
-// _BPD_, default 4) and -precision f32ref|f64|f32 (default f32ref, the
-// reference's default Real = float build).
+// Command line: -anatomy HGG_UQ -pID N -adaptive 0|1 [-dumpfreq d -vtk 0
+// -verbose 0 -nthreads k] plus -bpd (blocks per dimension, the reference's
+// compile-time _BPD_, default 4), -maxlevel (its _MAXLEVEL_; default the
+// initial grid's level log2(bpd), as the reference's makefile pairs them) and
+// -precision f32ref|f64|f32 (default f32ref, the reference's default
+// Real = float build).
 //
 // The initial state restates Glioma_HG_UQ::_ic_PatientCase (:67-225) in the
-// chosen Real type; the time loop is gbg_run (Glioma_HG_UQ::run, :511-552);
-// the dump is _dumpUQoutput (:309-372) on the uniform finest grid.
-// -adaptive 1 needs MRAG's grid and is rejected.
+// chosen Real type. -adaptive 0: the time loop is gbg_run
+// (Glioma_HG_UQ::run, :511-552) on the uniform grid. -adaptive 1: the same
+// loop on the library's block grid (gbg_amr_run): regrids at every dump time
+// and the refinement after the loop, tolerances 1e-4 / 1e-5
+// (Glioma_Types.h:462-463). The dump is _dumpUQoutput (:309-372), with its
+// replication rules for coarse blocks, on the (bpd * 16)^3 grid.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -39,9 +44,16 @@ int fail(const std::string &m, int code = 1) {
 int main(int argc, char **argv) {
     Args args{argc, argv};
     if (args.as_string("-anatomy", "") != "HGG_UQ") return fail("only -anatomy HGG_UQ is supported");
-    if (args.as_int("-adaptive", 0) != 0) return fail("-adaptive 1 needs MRAG's grid; use -adaptive 0");
+    const bool adaptive = args.as_int("-adaptive", 0) != 0;
     const int pID = args.as_int("-pID", 0);
     const int bpd = args.as_int("-bpd", 4);
+    int level0 = 0;
+    while ((1 << level0) < bpd) ++level0;
+    if ((1 << level0) != bpd) return fail("-bpd must be a power of two");
+    const int max_level = args.as_int("-maxlevel", level0);
+    if (max_level < level0 || max_level > 6) return fail("-maxlevel must lie in [log2(bpd), 6]");
+    const double dumpfreq = args.as_double("-dumpfreq", 1000.0);
+    if (adaptive && !(dumpfreq > 0)) return fail("-dumpfreq must be positive");
     const std::string prec = args.as_string("-precision", "f32ref");
     const int precision = prec == "f64" ? GBG_PREC_F64 : prec == "f32" ? GBG_PREC_F32 : GBG_PREC_F32REF;
     const bool verbose = args.as_int("-verbose", 0) != 0;
@@ -87,6 +99,49 @@ int main(int argc, char **argv) {
         gbgcli::initial_state<float>(bpd, GM, WM, CSF, T1, T2, t, pw, pg, phi, L);
     }
     const int n = bpd * 16;
+    if (adaptive) {
+        // the uniform initial state as the blocks of the initial grid (level
+        // log2(bpd), ix fastest), block-major with x fastest inside a block
+        const int nb = bpd * bpd * bpd;
+        std::vector<gbg_block> blocks(nb);
+        std::vector<double> bw((size_t)nb * 4096), bg(bw.size()), bp(bw.size());
+        for (int bz = 0, b = 0; bz < bpd; ++bz)
+            for (int by = 0; by < bpd; ++by)
+                for (int bx = 0; bx < bpd; ++bx, ++b) {
+                    blocks[b] = {level0, bx, by, bz};
+                    for (int z = 0; z < 16; ++z)
+                        for (int y = 0; y < 16; ++y)
+                            for (int x = 0; x < 16; ++x) {
+                                const size_t g = (size_t)(bx * 16 + x) +
+                                                 (size_t)n * ((size_t)(by * 16 + y) + (size_t)n * (bz * 16 + z));
+                                const size_t c = (size_t)b * 4096 + x + 16 * (y + 16 * z);
+                                bw[c] = pw[g];
+                                bg[c] = pg[g];
+                                bp[c] = phi[g];
+                            }
+                }
+        const int cap = 1 << (3 * max_level);
+        gbg_amr_config acfg = {cap, precision, 0};
+        gbg_handle *a = nullptr;
+        if (gbg_amr_create(&acfg, &a) != GBG_OK) return fail(gbg_last_error(), 4);
+        gbg_amr_run_opts o = {Dw, rho, tend, L, dumpfreq, bpd, 1, max_level, 1, 1e-4, 1e-5};
+        long nsteps = 0;
+        int regrids = 0;
+        std::vector<double> out((size_t)n * n * n);
+        if (gbg_amr_set_grid(a, nb, blocks.data(), bw.data(), bg.data(), bp.data()) != GBG_OK ||
+            gbg_amr_run(a, &o, &nsteps, &regrids) != GBG_OK ||
+            gbg_amr_dump_uniform(a, n, 1, out.data()) != GBG_OK) {
+            const std::string m = gbg_last_error();
+            gbg_destroy(a);
+            return fail(m, 4);
+        }
+        int nbf = 0;
+        gbg_amr_get_blocks(a, nullptr, 0, &nbf);
+        gbg_destroy(a);
+        if (verbose) std::printf("steps=%ld regrids=%d blocks=%d L=%f\n", nsteps, regrids, nbf, L);
+        gbgcli::write_d3d("HGG_data.dat", n, n, n, out);
+        return 0;
+    }
     gbg_config cfg = {n, precision, 0, 0};
     gbg_handle *h = nullptr;
     if (gbg_create(&cfg, &h) != GBG_OK) return fail(gbg_last_error(), 4);

@@ -211,7 +211,10 @@ def dump_fixtures():
       grid12 : a 256^3 grid of levels 1 and 2 (h = 8 hf, 4 hf): the dump
                replicates a level-1 cell 4^3 times where it covers 8^3 cells,
                and leaves the rest of the MatrixD3D it allocated with new[]
-               uninitialised -- the hash covers the cells it writes."""
+               uninitialised -- the hash covers the cells it writes;
+      grid34 : a 256^3 grid of levels 3 and 4.
+    For the 256^3 grids also the hash of the grid's ghost instruction tables
+    (Grid::getBoundaryInfo, flattened in the grid's block order)."""
     a = np.load(os.path.join(HERE, "anatomy64.npz"))
     pw, pg = a["p_w"].astype(np.float64), a["p_g"].astype(np.float64)
     an = S.Anatomy(n=64, p_w=pw, p_g=pg, psi=None)
@@ -222,19 +225,58 @@ def dump_fixtures():
     assert np.array_equal(bl, d["blocks"]), "the dump run's grid differs from amr64_f64"
     assert np.array_equal(np.stack([b["phi"] for b in r["blocks"]]), d["phi"])
     out = {"dump64": dict(gpd=64, sha256=sha(r["dump"]), nonzero=int(np.count_nonzero(r["dump"])))}
-    for name, radii in (("grid3", [0.2, 0.45]), ("grid12", [0.0, 0.0, 0.4])):
+    for name, radii in (("grid3", [0.2, 0.45]), ("grid12", [0.0, 0.0, 0.4]), ("grid34", [0.35])):
         g = refio.run_dumpgrid("ref_dump_b16", radii)
         blocks = g["blocks"]
+        th = hashlib.sha256()
+        for arr, t in zip(g["tables"], ("<i8", "<i4", "<i4", "<f8")):
+            th.update(np.ascontiguousarray(arr, dtype=t).tobytes())
         from oracle import amr_oracle as A
         written = A.dump_uniform(blocks, np.ones((len(blocks), 16, 16, 16)), g["gpd"]) != 0
         out[name] = dict(gpd=g["gpd"], radii=radii, blocks=blocks.tolist(),
                          levels=sorted(set(blocks[:, 0].tolist())),
                          written=int(written.sum()),
+                         table_entries=int(len(g["tables"][1])), tables_sha256=th.hexdigest(),
                          sha256_written=hashlib.sha256(
                              np.ascontiguousarray(g["dump"][written], dtype="<f8").tobytes()).hexdigest())
         if written.all():
             out[name]["sha256"] = sha(g["dump"])
     with open(os.path.join(HERE, "dump_ref.json"), "w") as f:
+        json.dump(out, f)
+
+
+ADAPTIVE64 = dict(Dw=0.0013, rho=0.15, tend=110.0, L=6.4, dumpfreq=10.0, bpd=4, max_level=2,
+                  seed_xyz=(20.3, 24.6, 22.1), peak=0.5, sigma=1.5)
+
+
+def adaptive_phi_sha(blocks, phi):
+    """SHA-256 of the block densities in (level, ix, iy, iz) order."""
+    order = sorted(range(len(blocks)), key=lambda i: tuple(blocks[i]))
+    h = hashlib.sha256()
+    for i in order:
+        h.update(np.ascontiguousarray(phi[i], dtype="<f8").tobytes())
+    return h.hexdigest()
+
+
+def adaptive_fixture():
+    """The reference's adaptive run (ref_harness solve, -adaptive 1, the
+    Glioma_HG_UQ::run loop with its final refinement) on the 64^3 anatomy:
+    regrids every 10 days to 110 days, refinements and compressions both
+    happen; step and regrid counts, final blocks and a hash of their
+    densities, FP64 and the default FP32 build."""
+    a = np.load(os.path.join(HERE, "anatomy64.npz"))
+    pw, pg = a["p_w"].astype(np.float64), a["p_g"].astype(np.float64)
+    an = S.Anatomy(n=64, p_w=pw, p_g=pg, psi=None)
+    c = ADAPTIVE64
+    phi0 = f32(S.gaussian_ic(an, *c["seed_xyz"], peak=c["peak"], sigma=c["sigma"]))
+    out = {"params": c}
+    for variant in ("f64", "f32"):
+        r = refio.run_harness("solve", f"{variant}_l2", 64, c["bpd"], pw, pg, phi0, c["Dw"], c["rho"],
+                              c["tend"], c["L"], adaptive=1, dumpfreq=c["dumpfreq"])
+        blocks = [[b["level"], *b["index"]] for b in r["blocks"]]
+        out[variant] = dict(steps=r["steps"], regrids=r["regrids"], blocks=sorted(blocks),
+                            phi_sha256=adaptive_phi_sha(blocks, [b["phi"] for b in r["blocks"]]))
+    with open(os.path.join(HERE, "adaptive64.json"), "w") as f:
         json.dump(out, f)
 
 
@@ -310,6 +352,26 @@ def cli_fixture():
         json.dump(out, f, indent=1)
 
 
+def cli_adaptive_fixture():
+    """The reference's `brain` built with _MAXLEVEL_ = 2 (its 4 blocks per
+    dimension) run with -adaptive 1 -dumpfreq 10 on the synthetic patient:
+    the hash of its HGG_data.dat, added to patient32.json."""
+    pat = synthetic_patient()
+    with tempfile.TemporaryDirectory() as td:
+        work = patient_files(td, pat)
+        subprocess.run([os.path.join(refio.REF_DIR, "brain_l2"), "-anatomy", "HGG_UQ", "-pID", "1",
+                        "-adaptive", "1", "-dumpfreq", "10", "-vtk", "0", "-verbose", "0",
+                        "-nthreads", "1"], cwd=work, check=True, capture_output=True)
+        u = matrix_io.read_d3d(os.path.join(work, "HGG_data.dat"))
+    path = os.path.join(HERE, "patient32.json")
+    with open(path) as f:
+        out = json.load(f)
+    out["brain_adaptive"] = dict(sha256=sha(u), sum=float(u.sum()), max=float(u.max()), dumpfreq=10.0,
+                                 max_level=2)
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+
+
 def cli_observations(u):
     """Observations of a model field, deterministic from a seed (numpy only)."""
     rng = np.random.default_rng(21)
@@ -328,11 +390,17 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "dump":
         dump_fixtures()
         sys.exit(0)
+    if len(sys.argv) > 1 and sys.argv[1] == "adaptive":
+        adaptive_fixture()
+        cli_adaptive_fixture()
+        sys.exit(0)
     rd_fixtures()
     mala_fixture()
     lik_fixture()
     amr_fixtures()
     dump_fixtures()
+    adaptive_fixture()
     cli_fixture()
+    cli_adaptive_fixture()
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))

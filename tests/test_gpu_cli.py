@@ -66,11 +66,28 @@ def test_brain_and_likelihood_match_reference(cli, tmp_path):
     assert abs(got - ref["likelihood"]) <= 2e-6
 
 
-def test_brain_rejects_adaptive_and_missing_files(cli, tmp_path):
+def test_adaptive_brain_matches_reference(cli, tmp_path):
+    """gbg_brain -adaptive 1 (the library's block grid with its regrids)
+    against the reference's brain built with _MAXLEVEL_ = 2, -adaptive 1
+    -dumpfreq 10: HGG_data.dat bit for bit."""
+    ref = golden_json("patient32.json")["brain_adaptive"]
+    d = golden_npz("patient32.npz")
+    work = _patient(tmp_path, [float(x) for x in d["params"]])
+    subprocess.run([cli["gbg_brain"], "-anatomy", "HGG_UQ", "-pID", "1", "-adaptive", "1",
+                    "-dumpfreq", "10", "-maxlevel", "2", "-vtk", "0", "-verbose", "0"],
+                   cwd=work, check=True, capture_output=True)
+    u = matrix_io.read_d3d(os.path.join(work, "HGG_data.dat"))
+    assert _sha(u) == ref["sha256"]
+
+
+def test_brain_rejects_bad_options_and_missing_files(cli, tmp_path):
     work = _patient(tmp_path, [0.0013, 0.2, 10.0])
-    r = subprocess.run([cli["gbg_brain"], "-anatomy", "HGG_UQ", "-pID", "1", "-adaptive", "1"],
+    r = subprocess.run([cli["gbg_brain"], "-anatomy", "HGG_UQ", "-pID", "1", "-adaptive", "1",
+                        "-maxlevel", "1"], cwd=work, capture_output=True, text=True)
+    assert r.returncode != 0 and "maxlevel" in r.stderr
+    r = subprocess.run([cli["gbg_brain"], "-anatomy", "HGG_UQ", "-pID", "1", "-bpd", "3"],
                        cwd=work, capture_output=True, text=True)
-    assert r.returncode != 0 and "adaptive" in r.stderr
+    assert r.returncode != 0 and "power of two" in r.stderr
     os.remove(os.path.join(work, "HGG_TumorIC.bin"))
     r = subprocess.run([cli["gbg_brain"], "-anatomy", "HGG_UQ", "-pID", "1"], cwd=work,
                        capture_output=True, text=True)
