@@ -378,6 +378,49 @@ def amr_measurement(device, level=4, steps=20, err_steps=60):
     return out
 
 
+def amr_adaptive_measurement(device, level=4, seed=7, steps_per_regrid=20):
+    """The adaptive configuration: the seeded anatomy at effective 256^3
+    (16^3 blocks at level 4, the maximum level), one prior draw (Dw, rho,
+    seed point, T), the Glioma_HG_UQ::run loop on the library's block grid
+    with a regrid (one refinement pass at 1e-4, compression at 1e-5 until it
+    stops) every `steps_per_regrid` steps and the refinement after the loop
+    (gbg_amr_run), in FP64 (exact) and the fast FP32 mode. Reports each
+    mode's wall time, cell-steps/s over the steps, regrid seconds per call,
+    the range of block counts, and the FP32 run's relative L2 error against
+    FP64 on the uniform 256^3 resample."""
+    from gliomauq_gb300 import _lib, amr, synthetic as Syn
+    n = 16 << level
+    an = Syn.make_anatomy(n, seed=0)
+    p = Syn.draw_prior(an, 1, seed=seed)[0]
+    dt = Syn.reference_dt(n, p.Dw, an.L)[0]
+    phi0 = Syn.gaussian_ic(an, p.x0, p.y0, p.z0).astype(np.float32).astype(np.float64)
+    blocks = amr.uniform_blocks(level)
+    fields = [amr.to_block_major(x, level) for x in (an.p_w, an.p_g, phi0)]
+    out = {"config": f"effective {n}^3, 16^3 blocks, levels <= {level}, refine 1e-4, compress "
+                     f"1e-5, regrid every {steps_per_regrid} steps",
+           "sample": list(p.as_tuple())}
+    dumps = {}
+    for mode in ("f64", "f32"):
+        with _lib.AmrHandle(len(blocks), mode, device=device) as h:
+            h.set_grid(blocks, *fields)
+            t0 = time.perf_counter()
+            steps, regrids = h.run(p.Dw, p.rho, p.T, an.L, bpd=1 << level,
+                                   dumpfreq=steps_per_regrid * dt, adaptive=True, max_level=level)
+            wall = time.perf_counter() - t0
+            st = h.last_run_stats()
+            dumps[mode] = h.dump_uniform(n, reference_rules=False)
+            lv = h.blocks()[:, 0]
+        out[mode] = {"steps": steps, "regrids": regrids, "seconds": wall,
+                     "cell_steps_per_s": st["cell_steps"] / st["step_seconds"],
+                     "step_seconds": st["step_seconds"],
+                     "regrid_ms_per_call": 1e3 * st["regrid_seconds"] / max(1, st["regrid_calls"]),
+                     "blocks_min_max": [st["min_blocks"], st["max_blocks"]],
+                     "final_levels": {int(k): int(v) for k, v in zip(*np.unique(lv, return_counts=True))}}
+    b = dumps["f64"]
+    out["f32_vs_f64_rel_l2"] = float(np.linalg.norm(dumps["f32"] - b) / np.linalg.norm(b))
+    return out
+
+
 def surrogate_measurement(device, n=128, batch=32, reps=5):
     """Forward throughput of the bf16 U-Net surrogate at n^3 (its grid is
     (n/2)^3): milliseconds per sample of gbg_surrogate_loglik (features,
@@ -636,6 +679,7 @@ def main():
             line["mcmc"] = mcmc_comparison(local_rank)
         if not args.no_amr:
             line["amr"] = amr_measurement(local_rank)
+            line["amr"]["adaptive"] = amr_adaptive_measurement(local_rank)
         if not args.no_surrogate:
             line["surrogate"] = surrogate_measurement(local_rank)
         print(json.dumps(line))

@@ -32,7 +32,7 @@ EXPORTS = [
     "gbg_amr_get_phi", "gbg_amr_fwt_detail", "gbg_adjoint_grad", "gbg_amr_remap",
     "gbg_amr_dump_uniform", "gbg_amr_ghost_tables", "gbg_amr_plan_refine", "gbg_amr_plan_compress",
     "gbg_amr_build_ghosts", "gbg_amr_auto_refine", "gbg_amr_auto_compress", "gbg_amr_get_blocks",
-    "gbg_amr_run", "gbg_surrogate_create", "gbg_surrogate_destroy",
+    "gbg_amr_run", "gbg_amr_last_run_stats", "gbg_surrogate_create", "gbg_surrogate_destroy",
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
     "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_surrogate_set_engine",
@@ -82,6 +82,12 @@ class AmrRunOpts(C.Structure):
                 ("L", C.c_double), ("dumpfreq", C.c_double), ("bpd", C.c_int),
                 ("adaptive", C.c_int), ("max_level", C.c_int), ("final_refine", C.c_int),
                 ("refine_tol", C.c_double), ("compress_tol", C.c_double)]
+
+
+class AmrRunStats(C.Structure):
+    _fields_ = [("cell_steps", C.c_longlong), ("step_seconds", C.c_double),
+                ("regrid_seconds", C.c_double), ("regrid_calls", C.c_int),
+                ("min_blocks", C.c_int), ("max_blocks", C.c_int)]
 
 
 class AmrConfig(C.Structure):
@@ -161,6 +167,7 @@ def load(path: str = LIB_PATH):
         "gbg_amr_auto_compress": [vp, C.c_double, C.POINTER(C.c_int)],
         "gbg_amr_get_blocks": [vp, vp, C.c_int, C.POINTER(C.c_int)],
         "gbg_amr_run": [vp, C.POINTER(AmrRunOpts), lp, C.POINTER(C.c_int)],
+        "gbg_amr_last_run_stats": [vp, C.POINTER(AmrRunStats)],
         "gbg_surrogate_create": [vp, C.POINTER(SurrogateConfig), C.POINTER(vp)],
         "gbg_surrogate_destroy": [vp],
         "gbg_surrogate_nparams": [vp, lp],
@@ -518,6 +525,11 @@ class AmrHandle:
         check(self.lib.gbg_amr_run(self._h, C.byref(o), C.byref(steps), C.byref(regrids)))
         self.blocks()
         return steps.value, regrids.value
+
+    def last_run_stats(self) -> dict:
+        s = AmrRunStats()
+        check(self.lib.gbg_amr_last_run_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in AmrRunStats._fields_}
 
 
 def amr_ghost_tables(blocks):

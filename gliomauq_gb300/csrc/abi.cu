@@ -805,6 +805,16 @@ int gbg_amr_run(gbg_handle *hh, const gbg_amr_run_opts *o, long *steps, int *reg
     return gbg::amr_run(hh->h, *o, steps, regrids);
 }
 
+int gbg_amr_last_run_stats(gbg_handle *hh, gbg_amr_run_stats *stats) {
+    if (int rc = check_amr(hh)) return rc;
+    if (!stats) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    *stats = hh->h.amr.last_run;
+    return GBG_OK;
+}
+
 int gbg_amr_dump_uniform(gbg_handle *hh, int gpd, int reference_rules, double *out) {
     if (int rc = check_amr(hh)) return rc;
     if (gpd < 1 || gpd > 2048 || (gpd & (gpd - 1)) || !out || hh->h.amr.nb < 1) {

@@ -45,6 +45,7 @@
 // the same call is not examined again.
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <set>
@@ -479,34 +480,50 @@ int amr_auto_compress(Handle &h, double tol, int *collapsed) {
 // pass, then compression until it stops) whenever t reaches the next dump
 // time, and the refinement after the loop.
 int amr_run(Handle &h, const gbg_amr_run_opts &o, long *steps, int *regrids) {
+    using clock = std::chrono::steady_clock;
     *steps = 0;
     *regrids = 0;
+    gbg_amr_run_stats st{};
+    st.min_blocks = st.max_blocks = h.amr.nb;
     double dt, Dw, Dg, rho = o.rho;
     reference_dt(BS * o.bpd, o.Dw_file, o.L, h.prec == GBG_PREC_F32REF, &dt, &Dw, &Dg, &rho);
     if (!h.amr.ghosts_valid)
         if (int rc = install_tables(h)) return rc;
+    // a regrid, timed from the end of the steps before it
+    auto regrid = [&](bool compress) -> int {
+        GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        const auto r0 = clock::now();
+        int r = 0, c = 0;
+        if (int rc = amr_auto_refine(h, o.refine_tol, o.max_level, &r)) return rc;
+        if (compress)
+            if (int rc = amr_auto_compress(h, o.compress_tol, &c)) return rc;
+        st.regrid_seconds += std::chrono::duration<double>(clock::now() - r0).count();
+        ++st.regrid_calls;
+        ++*regrids;
+        st.min_blocks = std::min(st.min_blocks, h.amr.nb);
+        st.max_blocks = std::max(st.max_blocks, h.amr.nb);
+        return GBG_OK;
+    };
+    const auto t0 = clock::now();
     double t = 0.0, when = o.dumpfreq;
     long k = 0;
     while (t <= o.tend && k < 100000000L) {
         if (int rc = amr_steps(h, Dw, Dg, rho, dt, 1)) return rc;
+        st.cell_steps += (long long)h.amr.nb * BS * BS * BS;
         t += dt;
         ++k;
         if (t >= when) {
-            if (o.adaptive) {
-                int r = 0, c = 0;
-                if (int rc = amr_auto_refine(h, o.refine_tol, o.max_level, &r)) return rc;
-                if (int rc = amr_auto_compress(h, o.compress_tol, &c)) return rc;
-                ++*regrids;
-            }
+            if (o.adaptive)
+                if (int rc = regrid(true)) return rc;
             when = when + o.dumpfreq;
         }
     }
     *steps = k;
-    if (o.adaptive && o.final_refine) {
-        int r = 0;
-        if (int rc = amr_auto_refine(h, o.refine_tol, o.max_level, &r)) return rc;
-        ++*regrids;
-    }
+    if (o.adaptive && o.final_refine)
+        if (int rc = regrid(false)) return rc;
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    st.step_seconds = std::chrono::duration<double>(clock::now() - t0).count() - st.regrid_seconds;
+    h.amr.last_run = st;
     return GBG_OK;
 }
 

@@ -64,6 +64,7 @@ struct AmrState {
     bool ghosts_valid = false, tables_valid = false;
     double tab_Dw = -1, tab_Dg = -1;
     std::vector<gbg_block> hblocks;  // host copy of the blocks, in the device order
+    gbg_amr_run_stats last_run{};    // statistics of the latest gbg_amr_run
 };
 
 struct Handle {

@@ -409,6 +409,18 @@ typedef struct {
  * adaptive. Ghost tables are compiled by the library. Writes the step and
  * regrid counts. */
 int gbg_amr_run(gbg_handle *h, const gbg_amr_run_opts *opts, long *steps, int *regrids);
+/* No reference counterpart. Statistics of the handle's latest gbg_amr_run:
+ * cell-steps computed (blocks x 4096 summed over the steps), the wall time
+ * of the steps and of the regrids (each regrid waits for the steps before
+ * it, then FWT on the device, plans and ghost tables on the host, data
+ * movement on the device), the number of regrid calls, and the fewest and
+ * most blocks the grid had. */
+typedef struct {
+    long long cell_steps;
+    double step_seconds, regrid_seconds;
+    int regrid_calls, min_blocks, max_blocks;
+} gbg_amr_run_stats;
+int gbg_amr_last_run_stats(gbg_handle *h, gbg_amr_run_stats *stats);
 
 /* ---- introspection ---------------------------------------------------------- */
 /* number of kernels this handle has launched since creation */
