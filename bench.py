@@ -150,9 +150,18 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def cpu_baseline(an, prior, seconds=12.0):
+# The block-lab port against the reference's own TBB pipeline (compiled in place
+# with _MRAG_TBB_NTHREADS_HINT = cores on a project-written thread-backed TBB
+# stand-in; oracle/Makefile target ref_harness_f32_tbb), same 128^3 bench sample
+# and steps, on the 8-core x86 build machine: port / reference cell-steps/s.
+PORT_OVER_REFERENCE = {"threads_1": 10.285e6 / 10.229e6, "threads_8": 77.37e6 / 56.28e6}
+
+
+def cpu_baseline(an, prior, seconds=12.0, obs=None):
     """The oracle's block-lab restatement of the reference CPU step, all cores,
-    on one sample of the workload for about `seconds`; scaled to solves/s."""
+    on one sample of the workload for about `seconds`, plus the reference's
+    likelihood (HGG_Likelihood restated) on the final field when `obs` is
+    given; extrapolated to solves/s with the population's mean step count."""
     from gliomauq_gb300 import synthetic as Syn
     from oracle import oracle
     p = prior[0]
@@ -170,11 +179,23 @@ def cpu_baseline(an, prior, seconds=12.0):
             break
     cs = steps * N ** 3 / el
     per_solve, _ = mean_cell_steps(an, prior)
-    return dict(value=cs / per_solve, unit="solves/s", cores=cores, kind="port",
-                sample=f"{steps} steps of one 128^3 sample ({el:.1f} s), block-lab restatement "
-                       f"of the reference CPU step (FP32 Real, {cores} threads); "
-                       f"{cs / 1e6:.1f} Mcell-steps/s scaled by the population's mean "
-                       f"{per_solve / N ** 3:.1f} steps per solve")
+    lik_s = 0.0
+    if obs is not None:
+        u = g.phi().astype(np.float64)
+        t1 = time.perf_counter()
+        oracle.loglik(u, obs.pet, obs.t1, obs.t2, obs.points, LIK, 3, 2, True)
+        lik_s = time.perf_counter() - t1
+    solve_s = per_solve / cs + lik_s
+    return dict(value=1.0 / solve_s, unit="solves/s", cores=cores, kind="port",
+                extrapolated=True, measured_cell_steps=steps * N ** 3, measured_seconds=el,
+                mean_cell_steps_per_solve=per_solve, loglik_seconds_per_solve=lik_s,
+                port_over_reference_x86=PORT_OVER_REFERENCE,
+                sample=f"{steps} steps of one 128^3 sample ({el:.1f} s) through the block-lab "
+                       f"restatement of the reference CPU step (FP32 Real, {cores} threads): "
+                       f"{cs / 1e6:.1f} Mcell-steps/s, extrapolated to the population's mean "
+                       f"{per_solve / N ** 3:.1f} steps per solve"
+                       + (f", plus the likelihood ({1e3 * lik_s:.1f} ms per solve)" if obs is not None
+                          else ""))
 
 
 def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=16,
@@ -472,20 +493,36 @@ def surrogate_measurement(device, n=128, batch=32, reps=5):
     return out
 
 
+def reference_arm_observations(an, truth):
+    """Observations for the reference arm's likelihood without a GPU: the
+    hidden truth solved by the oracle's block-lab port (the reference's FP32
+    step) on the host."""
+    from gliomauq_gb300 import synthetic as Syn
+    from oracle import oracle
+    dt, dw, dg = Syn.reference_dt(N, truth.Dw, an.L, f32=True)
+    g = oracle.BlockGrid(an.p_w, an.p_g, Syn.gaussian_ic(an, truth.x0, truth.y0, truth.z0))
+    g.steps(dw, dg, truth.rho, dt, Syn.num_steps(dt, truth.T), 0)
+    u = g.phi().astype(np.float64)
+    return Syn.make_observations(u, an, seed=3, centre_xyz=(truth.x0, truth.y0, truth.z0),
+                                 radius_vox=27.0)
+
+
 def run_reference_arm(args):
     rank, _, world = rank_info()
     if rank != 0:
         return
-    an, prior, _ = make_workload()
+    an, prior, truth = make_workload()
+    obs = reference_arm_observations(an, truth)
     vals = []
     for i in range(args.warmup + args.steps):
-        b = cpu_baseline(an, prior, seconds=max(2.0, args.ref_seconds))
+        b = cpu_baseline(an, prior, seconds=max(2.0, args.ref_seconds), obs=obs)
         if i >= args.warmup:
             vals.append(b["value"])
     v = float(np.mean(vals))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * S / v, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": 1000.0 * S / v, "ms_per_step_extrapolated": True,
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batched population: 512 forward solves at 128^3 "
                                    "+ per-sample log-likelihood", "n": N, "samples": S},
@@ -674,7 +711,7 @@ def main():
             "gpu_launches": int(launches),
         }
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(an, prior)
+            line["cpu_baseline"] = cpu_baseline(an, prior, obs=obs)
         if not args.no_mcmc:
             line["mcmc"] = mcmc_comparison(local_rank)
         if not args.no_amr:
