@@ -32,7 +32,8 @@ EXPORTS = [
     "gbg_amr_get_phi", "gbg_amr_fwt_detail", "gbg_adjoint_grad", "gbg_amr_remap",
     "gbg_amr_dump_uniform", "gbg_amr_ghost_tables", "gbg_amr_plan_refine", "gbg_amr_plan_compress",
     "gbg_amr_build_ghosts", "gbg_amr_auto_refine", "gbg_amr_auto_compress", "gbg_amr_get_blocks",
-    "gbg_amr_run", "gbg_amr_last_run_stats", "gbg_surrogate_create", "gbg_surrogate_destroy",
+    "gbg_amr_run", "gbg_amr_last_run_stats", "gbg_field_statistics", "gbg_batch_statistics",
+    "gbg_surrogate_create", "gbg_surrogate_destroy",
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
     "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_surrogate_set_engine",
@@ -168,6 +169,8 @@ def load(path: str = LIB_PATH):
         "gbg_amr_get_blocks": [vp, vp, C.c_int, C.POINTER(C.c_int)],
         "gbg_amr_run": [vp, C.POINTER(AmrRunOpts), lp, C.POINTER(C.c_int)],
         "gbg_amr_last_run_stats": [vp, C.POINTER(AmrRunStats)],
+        "gbg_field_statistics": [C.c_int, vp, C.c_int, C.c_int, vp, vp, vp],
+        "gbg_batch_statistics": [vp, C.POINTER(Sample), C.c_int, C.POINTER(BatchOpts), C.c_int, dp, dp],
         "gbg_surrogate_create": [vp, C.POINTER(SurrogateConfig), C.POINTER(vp)],
         "gbg_surrogate_destroy": [vp],
         "gbg_surrogate_nparams": [vp, lp],
@@ -328,6 +331,19 @@ class Handle:
         if want_phi:
             out["phi"] = phi
         return out
+
+    def batch_statistics(self, samples, L, ic_peak=0.1, ic_sigma=1.0, dt0=0.0,
+                         reference_rules=True):
+        """Batched solve of the samples, then the per-cell mean and variance of
+        their final densities (gbg_batch_statistics): two [z, y, x] arrays."""
+        S = len(samples)
+        arr = (Sample * S)(*[Sample(*s) for s in samples])
+        opts = BatchOpts(L, ic_peak, ic_sigma, 0, dt0)
+        mean = np.empty((self.n,) * 3)
+        var = np.empty((self.n,) * 3)
+        check(self.lib.gbg_batch_statistics(self._h, arr, S, C.byref(opts),
+                                            1 if reference_rules else 0, dptr(mean), dptr(var)))
+        return mean, var
 
     def batch_solve_device(self, samples_dev_ptr: int, S: int, L, lik_dev_ptr: int | None,
                            ic_peak=0.1, ic_sigma=1.0, dt0=0.0):

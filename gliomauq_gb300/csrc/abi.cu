@@ -553,6 +553,49 @@ int gbg_batch_solve(gbg_handle *hh, const gbg_sample *samples, int S, const gbg_
     return GBG_OK;
 }
 
+int gbg_batch_statistics(gbg_handle *hh, const gbg_sample *samples, int S, const gbg_batch_opts *o,
+                         int reference_rules, double *mean, double *var) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (int rc = validate_batch(h, S, o)) return rc;
+    if (!samples || !mean || !var) {
+        set_error("null samples or outputs");
+        return GBG_ERR_ARG;
+    }
+    for (int s = 0; s < S; ++s) {
+        const gbg_sample &q = samples[s];
+        if (!std::isfinite(q.Dw) || !(q.Dw > 0) || !std::isfinite(q.rho) || !std::isfinite(q.x0) ||
+            !std::isfinite(q.y0) || !std::isfinite(q.z0) || !std::isfinite(q.tend)) {
+            set_error("non-finite or non-positive sample parameter");
+            return GBG_ERR_NONFINITE;
+        }
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    gbg_sample *d_samples = gbg::batch_samples(h);
+    GBG_CUDA_TRY(cudaMemcpyAsync(d_samples, samples, sizeof(gbg_sample) * S, cudaMemcpyHostToDevice, h.stream));
+    float *d = nullptr;
+    GBG_CUDA_TRY(cudaMalloc((void **)&d, 2 * h.N * sizeof(float)));
+    gbg_batch_opts oo = *o;
+    oo.with_loglik = 0;
+    int rc = gbg::batch_statistics(h, d_samples, S, oo, reference_rules, d, d + h.N);
+    if (!rc) rc = gbg::check_device_status(h);
+    std::vector<float> tmp(2 * h.N);
+    if (!rc && cudaMemcpyAsync(tmp.data(), d, 2 * h.N * sizeof(float), cudaMemcpyDeviceToHost, h.stream) !=
+                   cudaSuccess)
+        rc = GBG_ERR_CUDA;
+    if (!rc && cudaStreamSynchronize(h.stream) != cudaSuccess) rc = GBG_ERR_CUDA;
+    cudaFree(d);
+    if (rc) {
+        if (rc == GBG_ERR_CUDA) set_error("gbg_batch_statistics: CUDA error");
+        return rc;
+    }
+    for (size_t c = 0; c < h.N; ++c) {
+        mean[c] = tmp[c];
+        var[c] = tmp[h.N + c];
+    }
+    return GBG_OK;
+}
+
 int gbg_adjoint_grad(gbg_handle *hh, const gbg_sample *samples, int S, const gbg_adjoint_opts *o,
                      double *loglik, double *grad) {
     if (int rc = check_handle(hh)) return rc;

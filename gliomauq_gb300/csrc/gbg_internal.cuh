@@ -213,6 +213,12 @@ int check_device_status(Handle &h);
 int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
                        const gbg_batch_opts &o, gbg_lik_result *loglik_device, long *nsteps_host);
 
+// ---- propagation.cu ----
+// batched solve of S samples, then per-cell mean and variance of their final
+// densities into mean_device / var_device (n^3 floats each)
+int batch_statistics(Handle &h, const gbg_sample *samples_device, int S, const gbg_batch_opts &o,
+                     int reference_rules, float *mean_device, float *var_device);
+
 // ---- amr.cu ----
 int amr_region_start(int code);
 int amr_alloc(Handle &h);

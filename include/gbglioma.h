@@ -186,6 +186,26 @@ int gbg_batch_solve(gbg_handle *h, const gbg_sample *samples, int S, const gbg_b
 int gbg_batch_solve_device(gbg_handle *h, const gbg_sample *samples_device, int S,
                            const gbg_batch_opts *o, gbg_lik_result *loglik_device);
 
+/* ---- posterior propagation statistics -------------------------------------------
+ * Per-cell mean and variance of S density fields as the reference's
+ * propagation tool computes them over the posterior samples' HGG_data.dat
+ * files (Glioma_HG_Propagation::_ic_PatientCasePropagation,
+ * source/Glioma/Glioma_HG_Propagation.cpp:346-440, PropagationStatistics,
+ * Glioma_PropagationStatisticsOperator.h:24-50) in its default Real = float:
+ * the sum in sample order, the squared deviations from (1/S) * sum, both
+ * scaled by 1/S. reference_rules != 0 keeps the tool's index rule: cells with
+ * a zero x, y or z index get mean = var = 0 (it accumulates mapped indices in
+ * (0, size] only). Device pointers; fields_device holds S fields of n^3 floats
+ * (x fastest) one after another; the call enqueues on stream (a
+ * cudaStream_t, null = legacy default) and allocates nothing. */
+int gbg_field_statistics(int n, const float *fields_device, int S, int reference_rules, float *mean_device,
+                         float *var_device, void *stream);
+/* The batched solve of the S samples (as gbg_batch_solve; S <= max_samples),
+ * then the statistics above over their final densities, written to the host
+ * arrays mean and var (n^3 each). */
+int gbg_batch_statistics(gbg_handle *h, const gbg_sample *samples, int S, const gbg_batch_opts *o,
+                         int reference_rules, double *mean, double *var);
+
 /* ---- gradients for MALA: discrete adjoint ----------------------------------------
  * No reference counterpart for the adjoint itself; the forward model it
  * differentiates is the fast-path step on a smooth time grid: a step dt,

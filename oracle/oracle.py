@@ -146,3 +146,33 @@ def loglik(model, pet, t1, t2, points, params, step_pet=3, step_ti=2, selective=
                      _p(pts, C.c_double) if npts else None, npts, C.byref(lp), step_pet, step_ti,
                      1 if selective else 0, C.byref(res))
     return dict(l_pet=res.l_pet, l_t1=res.l_t1, l_t2=res.l_t2, total=res.total, n_pet=res.n_pet)
+
+
+def propagation_stats(fields, reference_rules=True):
+    """Per-cell mean and variance of S density fields [S, z, y, x] as the
+    reference's propagation tool forms them in Real = float
+    (source/Glioma/Glioma_HG_Propagation.cpp:346-440: the sum over samples,
+    then the squared deviations from inSamples * sum; then
+    Glioma_PropagationStatisticsOperator.h:34-47 scales both by inSamples).
+    A field value enters as the double it was stored as, so each sum step is a
+    double addition rounded to float. With reference_rules, cells with a zero
+    x, y or z index stay 0 (the tool's mapped-index test `> 0 && <= size`,
+    :380-381 and :430). Returns two float32 [z, y, x] arrays."""
+    F = np.asarray(fields, dtype=np.float32)
+    S, n = F.shape[0], F.shape[1]
+    inv = np.float32(1.0 / S)
+    m = np.zeros(F.shape[1:], np.float32)
+    for s in range(S):
+        m = (m.astype(np.float64) + F[s].astype(np.float64)).astype(np.float32)
+    p = (inv * m).astype(np.float32)
+    v = np.zeros_like(m)
+    for s in range(S):
+        t = (F[s].astype(np.float64) - p.astype(np.float64)).astype(np.float32)
+        v = (v + (t * t).astype(np.float32)).astype(np.float32)
+    mean, var = (m * inv).astype(np.float32), (v * inv).astype(np.float32)
+    if reference_rules:
+        for a in (mean, var):
+            a[0, :, :] = 0
+            a[:, 0, :] = 0
+            a[:, :, 0] = 0
+    return mean, var

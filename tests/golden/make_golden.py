@@ -372,6 +372,52 @@ def cli_adaptive_fixture():
         json.dump(out, f, indent=1)
 
 
+PROPAGATION = [dict(n=64, S=12, seed=31), dict(n=32, S=3, seed=32), dict(n=32, S=1, seed=33)]
+
+
+def propagation_fields(n, S, seed):
+    """S seeded density-like fields [S, z, y, x] (float32): zero on a random
+    30% of the cells, elsewhere a scaled, noisy copy of one base field in
+    [0, 1]."""
+    rng = np.random.default_rng(seed)
+    base = rng.random((n, n, n))
+    out = [np.where(base > 0.3, np.clip(base * rng.uniform(0.5, 1.5) + rng.normal(0, 0.05, (n, n, n)), 0, 1),
+                    0.0).astype(np.float32) for _ in range(S)]
+    return np.stack(out)
+
+
+def propagation_fixture():
+    """The reference's own `propagation` program (Glioma_HG_Propagation.cpp
+    built unmodified, FP32) on seeded fields written as the S samples'
+    HGG_data.dat: hashes of its PropagationMean_S.dat / PropagationVar_S.dat.
+    The 32^3 cases use the tool built for 2 blocks per dimension."""
+    pat = synthetic_patient()
+    out = []
+    for case in PROPAGATION:
+        n, nS = case["n"], case["S"]
+        fields = propagation_fields(n, nS, case["seed"])
+        with tempfile.TemporaryDirectory() as td:
+            work = patient_files(td, pat)
+            folder = os.path.join(td, "Anatmoy", "Patient01", "Patient01_All_4K_Ti_step_3_mpp1")
+            for s in range(nS):
+                d = os.path.join(folder, f"tmpdir.0.0.0.{s}")
+                os.makedirs(d)
+                matrix_io.write_d3d(os.path.join(d, "HGG_data.dat"), fields[s].astype(np.float64))
+            np.array([nS], dtype="<f4").tofile(os.path.join(work, "HGG_Nsamples.bin"))
+            prog = "propagation" if n == 64 else "propagation_b2"
+            subprocess.run([os.path.join(refio.REF_DIR, prog), "-anatomy", "HGG_Propagation", "-IC", "1",
+                            "-pID", "1", "-vtk", "0", "-verbose", "0", "-nthreads", "1"],
+                           cwd=work, check=True, capture_output=True)
+            mean = matrix_io.read_d3d(os.path.join(work, f"PropagationMean_{nS}.dat"))
+            var = matrix_io.read_d3d(os.path.join(work, f"PropagationVar_{nS}.dat"))
+        assert mean.shape == (n, n, n)
+        out.append(dict(case, mean_sha256=sha(mean), var_sha256=sha(var), mean_sum=float(mean.sum()),
+                        var_sum=float(var.sum()), mean_center=float(mean[n // 2, n // 3, n // 4]),
+                        var_center=float(var[n // 2, n // 3, n // 4])))
+    with open(os.path.join(HERE, "propagation.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
 def cli_observations(u):
     """Observations of a model field, deterministic from a seed (numpy only)."""
     rng = np.random.default_rng(21)
@@ -390,6 +436,9 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "dump":
         dump_fixtures()
         sys.exit(0)
+    if len(sys.argv) > 1 and sys.argv[1] == "propagation":
+        propagation_fixture()
+        sys.exit(0)
     if len(sys.argv) > 1 and sys.argv[1] == "adaptive":
         adaptive_fixture()
         cli_adaptive_fixture()
@@ -402,5 +451,6 @@ if __name__ == "__main__":
     adaptive_fixture()
     cli_fixture()
     cli_adaptive_fixture()
+    propagation_fixture()
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
