@@ -199,22 +199,29 @@ def cpu_baseline(an, prior, seconds=12.0, obs=None):
 
 
 def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=16,
-                    plain_steps=3000, plain_burn=500, unet=True):
+                    plain_chains=4, plain_steps=1500, plain_burn=300, ref_generations=500,
+                    plain_cap_s=120.0, unet=True):
     """Posterior effective samples per second at n^3 on one synthetic
-    patient: plain single-solve MCMC (one random-walk chain in theta, one
-    forward solve per step, the proposal scaled by the prior box and its
-    step adapted during burn-in) against the batched + adjoint + surrogate
-    pipeline (gliomauq_gb300.mcmc.sample_posterior: batched prior screen,
-    adjoint Newton mode and Hessian, profile-refined Gaussian, then delayed
-    acceptance with the affine tangent surrogate over `chains` lock-step
-    chains in the scaling symmetry's coordinates). Both target the same
-    posterior (smooth-time-grid forward model, dt0 from the prior's largest
-    Dw); the observations come from the same model. Diagnostics (multi-chain
-    and within-chain ESS, split R-hat) are taken in the invariant
-    coordinates (log c, log rho T, log Dw/rho, x0, y0, z0) for both samplers;
-    times exclude burn-in (setup and burn-in are reported separately). The
-    learned U-Net surrogate is measured as a stage-1 screen in the same
-    delayed-acceptance sampler."""
+    patient, plain single-solve MCMC against the batched + adjoint +
+    surrogate pipeline, both in the scaling symmetry's coordinates
+    (log rho, log rho T, log Dw/rho, x0, y0, z0) with the same Laplace
+    preconditioning:
+      * plain (gliomauq_gb300.mcmc.plain_chains): `plain_chains` chains run
+        one after another, one forward solve per step; random walk on the
+        identified coordinates with the pipeline's refined Laplace
+        covariance, the symmetry axis redrawn from its prior conditional
+        every step; more steps are added until split R-hat <= 1.05;
+      * pipeline (gliomauq_gb300.mcmc.sample_posterior): batched prior
+        screen, adjoint Newton mode and Hessian, profile-refined Gaussian,
+        then delayed acceptance with the affine tangent surrogate over
+        `chains` lock-step chains.
+    Both target the same posterior (scaled time grid); the observations come
+    from the same model. The setup (screen, mode, covariance) is shared and
+    reported separately; ESS/s counts the post-burn-in sampling time of
+    each. A second, longer pipeline run from fresh chains gives the
+    reference posterior mean that both samplers' means are checked against
+    (2 % per theta coordinate). The learned U-Net surrogate is measured as a
+    stage-1 screen in the same delayed-acceptance sampler."""
     from gliomauq_gb300 import _lib, mcmc, synthetic as Syn
     an = Syn.make_anatomy(n, seed=0)
     truth = Syn.draw_prior(an, 1, seed=10_000)[0]
@@ -253,18 +260,60 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=1
                 "mean_v": v.reshape(-1, 6).mean(axis=0).tolist(),
                 "sd_v": v.reshape(-1, 6).std(axis=0).tolist()}
 
+    def start_points(k, scale=2.0):
+        """Dispersed starts: the refined Gaussian widened by `scale`, the
+        symmetry axis from its prior conditional, inside the prior."""
+        Lc = np.linalg.cholesky(res.cov)
+        v = np.empty((0, 6))
+        while len(v) < k:
+            d = res.v_map + scale * rng.standard_normal((4 * k, 6)) @ Lc.T
+            d = lc.prior.redraw_axis(d, 0, rng)
+            v = np.concatenate([v, d[np.isfinite(lc.prior.logp(d))]])
+        return v[:k]
+
     th = res.theta
     d_pipe = diagnostics(th, res.sample_seconds)
     half = chains // 2
     va = lc.to_u(th[:, :half]).reshape(-1, 6).mean(axis=0)
     vb = lc.to_u(th[:, half:]).reshape(-1, 6).mean(axis=0)
     d_pipe["halves_mean_diff_in_sd"] = (np.abs(va - vb) / np.array(d_pipe["sd_v"])).tolist()
-    # plain single-solve chain, started at the same point as the pipeline's mode
+
+    # plain single-solve chains, same coordinates and preconditioning
     post1 = mcmc.Posterior(h, an.L, dt0, prior)
-    start = lc.to_theta(res.v_map[None])
-    r1 = mcmc.rwm(post1, start, plain_steps, 1e-3, rng, burn=plain_burn)
-    t_plain = r1.seconds * (plain_steps - plain_burn) / plain_steps
-    d_plain = diagnostics(r1.samples[plain_burn:], t_plain)
+    lc1 = mcmc.LogCoords(post1, A=mcmc.INVARIANT_MAP)
+    r1 = mcmc.plain_chains(lc1, start_points(plain_chains), plain_burn + plain_steps, res.cov, rng,
+                           burn=plain_burn)
+    draws = r1.samples[plain_burn:]
+    t_plain = r1.seconds - r1.history["burn_seconds"]
+    acc_n, acc_sum = plain_steps * plain_chains, r1.accept * plain_steps * plain_chains
+    t_round = r1.seconds
+    spent = r1.seconds
+    while np.max(mcmc.rhat(draws)) > 1.05 and spent + t_round < plain_cap_s:
+        more = mcmc.plain_chains(lc1, draws[-1], plain_steps, res.cov, rng, burn=0, step=r1.step)
+        draws = np.concatenate([draws, more.samples])
+        t_plain += more.seconds
+        spent += more.seconds
+        t_round = more.seconds
+        acc_n += plain_steps * plain_chains
+        acc_sum += more.accept * plain_steps * plain_chains
+    th_plain = lc.to_theta(draws)
+    d_plain = diagnostics(th_plain, t_plain)
+    # reference posterior mean: a longer pipeline run from fresh chains with
+    # the same setup (its surrogate as adapted above; stage 2 keeps it exact)
+    post_r = mcmc.LogCoords(mcmc.Posterior(h, an.L, dt0, prior), A=mcmc.INVARIANT_MAP)
+    rr = mcmc.da(post_r, res.surrogate, start_points(chains, 1.0), ref_generations + burn,
+                 2.38 / np.sqrt(6), np.random.default_rng(12345), inner=inner, burn=burn,
+                 chol=np.linalg.cholesky(res.cov), adapt=True, axis=0)
+    th_ref = lc.to_theta(rr.samples[burn:]).reshape(-1, 6)
+    ref_mean = th_ref.mean(axis=0)
+    ref_sd = th_ref.std(axis=0)
+
+    def mean_check(theta):
+        m = theta.reshape(-1, 6).mean(axis=0)
+        rel = np.abs(m - ref_mean) / np.abs(ref_mean)
+        return {"rel_err": rel.tolist(), "err_in_sd": (np.abs(m - ref_mean) / ref_sd).tolist(),
+                "within_2pct": bool(np.all(rel <= 0.02))}
+
     out = {
         "grid": n, "time_grid": "scaled, stable: dt = 0.99 h^2 / (6 Dw / L^2 + rho h^2 / 2) per "
                                 "sample, last step shortened to end at T", "coordinates": names,
@@ -273,12 +322,18 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=1
         "truth": list(truth.as_tuple()),
         "note": "the model depends on (Dw/rho, rho T) only (the scaled grid keeps this "
                 "symmetry of the continuous model): along (c Dw, c rho, T/c) the posterior is the "
-                "prior's, and the pipeline draws that coordinate exactly from its prior "
+                "prior's, and both samplers draw that coordinate exactly from its prior "
                 "conditional; ESS/s is reported for the identified coordinates and for the "
                 "symmetry axis separately",
-        "plain": dict(sampler="RWM, 1 chain in theta, 1 forward solve per step, "
-                              "prior-box-scaled proposal, step adapted in burn-in",
-                      steps=plain_steps - plain_burn, accept=float(r1.accept), **d_plain),
+        "setup_seconds": res.setup_seconds,
+        "plain": dict(sampler=f"{plain_chains} chains one after another, 1 forward solve per step, "
+                              f"random walk on the identified coordinates with the refined "
+                              f"Laplace covariance, symmetry axis redrawn from its prior "
+                              f"conditional, step adapted in burn-in",
+                      chains=plain_chains, steps_per_chain=int(draws.shape[0]),
+                      burn_per_chain=plain_burn, accept=float(acc_sum / acc_n),
+                      burn_seconds=r1.history["burn_seconds"],
+                      ms_per_solve=1e3 * post1.seconds / max(post1.solves, 1), **d_plain),
         "pipeline": dict(sampler=f"delayed acceptance, tangent surrogate (affine + second order "
                                  f"along the symmetry axis), {chains} chains x {inner} surrogate "
                                  f"steps per solve, invariant coordinates",
@@ -287,7 +342,14 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=1
                          stage1_accept=float(res.result.history["stage1_accept"]),
                          stage2_accept=float(res.result.history["stage2_accept"]),
                          setup_seconds=res.setup_seconds, burn_seconds=res.burn_seconds,
+                         solver_seconds_all_generations=res.solver_seconds,
+                         surrogate_seconds_all_generations=res.surrogate_seconds,
                          **d_pipe),
+        "reference_posterior": dict(sampler="the pipeline's delayed acceptance, fresh chains, "
+                                            f"{chains} chains x {ref_generations} generations",
+                                    mean_theta=ref_mean.tolist(), sd_theta=ref_sd.tolist(),
+                                    rhat=mcmc.rhat(lc.to_u(lc.to_theta(rr.samples[burn:]))).tolist()),
+        "mean_check": {"pipeline": mean_check(th), "plain": mean_check(th_plain)},
     }
     for k in ("identified", "symmetry_axis", "all"):
         a, b = d_pipe[f"ess_per_s_{k}"], d_plain[f"ess_per_s_{k}"]
@@ -567,6 +629,8 @@ def main():
                     help="skip the surrogate-network measurement")
     ap.add_argument("--only-surrogate", action="store_true",
                     help="print the surrogate-network measurement alone (profiling runs)")
+    ap.add_argument("--only-mcmc", action="store_true",
+                    help="print the ESS/s comparison alone")
     ap.add_argument("--samples", type=int, default=S,
                     help="population size (profiling runs use a smaller one)")
     ap.add_argument("--variant", type=int, default=-1,
@@ -576,6 +640,9 @@ def main():
         return run_reference_arm(args)
     if args.only_surrogate:
         print(json.dumps({"surrogate": surrogate_measurement(int(os.environ.get("LOCAL_RANK", "0")))}))
+        return
+    if args.only_mcmc:
+        print(json.dumps({"mcmc": mcmc_comparison(int(os.environ.get("LOCAL_RANK", "0")))}))
         return
     set_population(args.samples)
 

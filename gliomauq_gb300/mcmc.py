@@ -197,6 +197,64 @@ def mala(post: Posterior, theta0: np.ndarray, steps: int, eps: float, rng, burn:
     return ChainResult(out, acc / n_acc, eps, time.perf_counter() - t0, post.solves)
 
 
+def plain_chains(post, v0: np.ndarray, steps: int, cov: np.ndarray, rng, burn: int = 0,
+                 axis: int = 0, step: float = None, target: float = 0.25) -> ChainResult:
+    """Plain single-solve MCMC: every chain (row of v0, coordinates of a
+    LogCoords posterior) runs on its own, one forward solve per step, the
+    chains one after another. The proposal is the random walk
+    v' = v + step * C xi on the coordinates other than `axis` (C C^T = cov
+    with `axis` decoupled: the Laplace-preconditioned proposal), with v'_axis
+    drawn from the prior conditional given the others (prior.redraw_axis);
+    accepted with min(1, L(v') m(v') / (L(v) m(v))), m the prior marginal
+    of the other coordinates (prior.axis_log_marginal), which is the
+    Metropolis-Hastings ratio of this proposal for pi = L * prior. The step
+    is adapted toward `target` during the first `burn` steps of each chain
+    and fixed after them."""
+    v0 = np.atleast_2d(np.asarray(v0, dtype=np.float64))
+    m, d = v0.shape
+    Lc = np.linalg.cholesky(_decoupled(np.asarray(cov, dtype=np.float64), axis))
+    step0 = 2.38 / np.sqrt(d - 1) if step is None else step
+    pr = post.prior
+    out = np.empty((steps, m, d))
+    acc = 0
+    steps_used = []
+    t0 = time.perf_counter()
+    t_burn = 0.0
+    for c in range(m):
+        v = v0[c:c + 1].copy()
+        lp, _ = post.loglik(v, False)
+        ll = lp - pr.logp(v) + pr.axis_log_marginal(v, axis)
+        st = step0
+        tb = time.perf_counter()
+        for k in range(steps):
+            if k == burn:
+                t_burn += time.perf_counter() - tb
+            prop = v + st * rng.standard_normal((1, d)) @ Lc.T
+            prop[:, axis] = v[:, axis]
+            prop = pr.redraw_axis(prop, axis, rng)
+            lm = pr.axis_log_marginal(prop, axis)
+            if np.isfinite(lm[0]):
+                lq, _ = post.loglik(prop, False)
+                lq = lq - pr.logp(prop) + lm
+            else:
+                lq = lm
+            with np.errstate(invalid="ignore"):
+                a = bool(np.isfinite(lq[0]) and np.log(rng.random()) < lq[0] - ll[0])
+            if a:
+                v, ll = prop, lq
+            if k < burn:
+                st *= np.exp((float(a) - target) / np.sqrt(k + 1.0))
+            else:
+                acc += int(a)
+            out[k, c] = v[0]
+        if burn >= steps:
+            t_burn += time.perf_counter() - tb
+        steps_used.append(st)
+    n_acc = max(1, (steps - burn) * m)
+    return ChainResult(out, acc / n_acc, float(np.mean(steps_used)), time.perf_counter() - t0,
+                       post.solves, history=dict(burn_seconds=t_burn, steps=steps_used))
+
+
 @dataclass
 class SurrogatePosterior:
     """log pi*(theta) = the surrogate's predicted log L + log prior, in
@@ -546,18 +604,17 @@ class LogPrior:
     def hi(self):
         return self.lo + self.width
 
-    def redraw_axis(self, v: np.ndarray, a: int, rng) -> np.ndarray:
-        """Exact draw of coordinate a from the prior conditional given the
-        others (rows of v): along the line v + t e_a every log coordinate is
-        linear in t, the box gives an interval for t and the density (the
-        log-Jacobian) is exp(alpha t) there, alpha = sum over log coordinates
-        of (A^{-1})_{i,a}. Rows whose line moves a non-log coordinate (the
-        seed, whose prior is a voxel mask) are returned unchanged."""
-        v = np.array(np.atleast_2d(v), dtype=np.float64, copy=True)
+    def _axis_line(self, v: np.ndarray, a: int):
+        """The line v + t e_a through each row of v: the interval [t_lo, t_hi]
+        of t inside the prior box (ok = non-empty) and the rate alpha of the
+        prior density exp(alpha t) along it (every log coordinate is linear in
+        t; alpha = sum over log coordinates of (A^{-1})_{i,a}). None when the
+        line moves a non-log coordinate (the seed, whose prior is a voxel
+        mask)."""
         col = self.Ai[:, a]
         logs = list(self.log_idx)
         if np.any(np.abs(np.delete(col, logs)) > 0):
-            return v
+            return None
         lo_u, hi_u = self._ubox()
         u = self.to_logu(v)
         t_lo = np.full(v.shape[0], -np.inf)
@@ -570,7 +627,18 @@ class LogPrior:
             t_lo = np.maximum(t_lo, np.minimum(b1, b2))
             t_hi = np.minimum(t_hi, np.maximum(b1, b2))
         ok = np.isfinite(t_lo) & np.isfinite(t_hi) & (t_hi > t_lo)
-        alpha = float(col[logs].sum())
+        return t_lo, t_hi, ok, float(col[logs].sum())
+
+    def redraw_axis(self, v: np.ndarray, a: int, rng) -> np.ndarray:
+        """Exact draw of coordinate a from the prior conditional given the
+        others (rows of v): on the line v + t e_a the prior density is
+        exp(alpha t) on [t_lo, t_hi] (_axis_line). Rows whose line moves a
+        non-log coordinate, or misses the box, are returned unchanged."""
+        v = np.array(np.atleast_2d(v), dtype=np.float64, copy=True)
+        line = self._axis_line(v, a)
+        if line is None:
+            return v
+        t_lo, t_hi, ok, alpha = line
         q = rng.random(v.shape[0])
         t = np.zeros(v.shape[0])
         if abs(alpha) < 1e-12:
@@ -581,6 +649,31 @@ class LogPrior:
             t[ok] = t_lo[ok] + np.log1p(q[ok] * np.expm1(span)) / alpha
         v[ok, a] += t[ok]
         return v
+
+    def axis_log_marginal(self, v: np.ndarray, a: int) -> np.ndarray:
+        """log of the prior density integrated over coordinate a through each
+        row of v: the marginal prior of the other coordinates, the normaliser
+        of redraw_axis's conditional (-inf where the line misses the prior's
+        support)."""
+        v = np.atleast_2d(np.asarray(v, dtype=np.float64))
+        line = self._axis_line(v, a)
+        if line is None:
+            raise ValueError("coordinate a moves a non-log coordinate")
+        t_lo, t_hi, ok, alpha = line
+        out = np.full(v.shape[0], -np.inf)
+        if not ok.any():
+            return out
+        mid = v[ok].copy()
+        mid[:, a] += 0.5 * (t_lo[ok] + t_hi[ok])
+        base = self.logp(mid)  # the seed-mask test, and the density at t = mid
+        span = t_hi[ok] - t_lo[ok]
+        if abs(alpha) < 1e-12:
+            w = np.log(span)
+        else:
+            # integral of exp(alpha (t - mid)) over the interval
+            w = np.log(2.0 * np.sinh(0.5 * alpha * span) / alpha)
+        out[ok] = base + w
+        return out
 
     def logp(self, v):
         """Uniform prior on theta as a density in v: the log-Jacobian sum of
@@ -854,6 +947,9 @@ class PipelineResult:
     setup_seconds: float     # prior screen + mode + profiles + surrogate
     sample_seconds: float    # the post-burn-in generations
     burn_seconds: float
+    surrogate: object = None   # the stage-1 surrogate as adapted in burn-in
+    solver_seconds: float = 0.0     # inside the batched solver calls (whole DA run)
+    surrogate_seconds: float = 0.0  # inside the surrogate calls (whole DA run)
 
 
 def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: int = 64,
@@ -910,7 +1006,8 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
            adapt_pool=adapt_pool, reset_stranded=reset_stranded)
     burn_s = r.history["burn_seconds"]
     return PipelineResult(r, post.to_theta(r.samples[burn:]), v_map, cov, setup, r.seconds - burn_s,
-                          burn_s)
+                          burn_s, surrogate=sur, solver_seconds=run.seconds,
+                          surrogate_seconds=sur.seconds)
 
 
 def rhat(samples: np.ndarray) -> np.ndarray:

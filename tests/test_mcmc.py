@@ -515,3 +515,68 @@ def test_redraw_axis_samples_the_prior_conditional():
     emp = np.arange(1, x.size + 1) / x.size
     assert x[0] >= lo - 1e-12 and x[-1] <= hi + 1e-12
     assert np.abs(cdf - emp).max() < 0.015
+
+
+def _invariant_moments(base):
+    """Posterior moments of (v1, v2) for InvariantStub: the Gaussian times the
+    prior volume along the symmetry axis, on a grid."""
+    g1 = base.c[0] + base.s[0] * np.linspace(-6, 6, 241)
+    g2 = base.c[1] + base.s[1] * np.linspace(-6, 6, 241)
+    V1, V2 = np.meshgrid(g1, g2, indexing="ij")
+    lo = np.maximum.reduce([np.full_like(V1, np.log(0.01)), np.log(2e-4) - V2, V1 - np.log(500.0)])
+    hi = np.minimum.reduce([np.full_like(V1, np.log(0.2)), np.log(2.5e-3) - V2, V1 - np.log(100.0)])
+    w = np.exp(-0.5 * (((V1 - base.c[0]) / base.s[0]) ** 2 + ((V2 - base.c[1]) / base.s[1]) ** 2))
+    w *= np.clip(np.exp(hi) - np.exp(lo), 0, None)
+    w /= w.sum()
+    m1, m2 = (w * V1).sum(), (w * V2).sum()
+    return m1, m2, np.sqrt((w * (V1 - m1) ** 2).sum()), np.sqrt((w * (V2 - m2) ** 2).sum())
+
+
+def test_axis_log_marginal_integrates_the_prior_along_the_axis():
+    base = InvariantStub()
+    lc = mcmc.LogCoords(base, A=mcmc.INVARIANT_MAP)
+    rng = np.random.default_rng(4)
+    th = np.column_stack([rng.uniform(3e-4, 2e-3, 6), rng.uniform(0.02, 0.18, 6),
+                          rng.uniform(22, 42, (6, 3)), rng.uniform(120, 480, 6)])
+    v = lc.to_u(th)
+    got = lc.prior.axis_log_marginal(v, 0)
+    ts = np.linspace(-8, 8, 400001)
+    for r in range(len(v)):
+        pts = np.repeat(v[r:r + 1], ts.size, axis=0)
+        pts[:, 0] += ts
+        lp = lc.prior.logp(pts)
+        mx = lp[np.isfinite(lp)].max()
+        ref = np.log(np.trapezoid(np.exp(lp - mx), ts)) + mx
+        assert abs(got[r] - ref) < 1e-4, (r, got[r], ref)
+    far = v[:1].copy()
+    far[0, 2] = 10.0  # log Dw/rho far outside what the box allows
+    assert np.isneginf(lc.prior.axis_log_marginal(far, 0)[0])
+
+
+def test_plain_chains_sample_the_invariant_posterior():
+    """The plain single-solve sampler (Laplace-preconditioned random walk on
+    the identified coordinates, the symmetry axis redrawn from its prior
+    conditional and the prior marginal in the ratio): one solve per step and
+    the exact posterior's moments."""
+    rng = np.random.default_rng(9)
+    base = InvariantStub()
+    lc = mcmc.LogCoords(base, A=mcmc.INVARIANT_MAP)
+    v_c = np.concatenate([[np.log(0.15)], base.c])
+    v0 = v_c + np.concatenate([[0.0], 2 * base.s]) * rng.standard_normal((4, 6))
+    v0 = lc.prior.redraw_axis(v0, 0, rng)
+    cov = np.diag(np.concatenate([[0.3], base.s]) ** 2)
+    steps, burn = 6000, 500
+    s0 = base.solves
+    r = mcmc.plain_chains(lc, v0, steps, cov, rng, burn=burn)
+    assert base.solves - s0 <= 4 * (steps + 1)
+    v = r.samples[burn:]
+    flat = v.reshape(-1, 6)
+    assert np.all(np.abs(flat[:, 3:].mean(axis=0) - base.c[2:]) < 0.1 * base.s[2:])
+    assert np.all(np.abs(flat[:, 3:].std(axis=0) / base.s[2:] - 1) < 0.1)
+    m1, m2, s1, s2 = _invariant_moments(base)
+    assert abs(flat[:, 1].mean() - m1) < 0.1 * s1 and abs(flat[:, 2].mean() - m2) < 0.1 * s2
+    assert abs(flat[:, 1].std() / s1 - 1) < 0.1 and abs(flat[:, 2].std() / s2 - 1) < 0.1
+    ref = lc.prior.redraw_axis(flat[::7], 0, rng)[:, 0]
+    assert abs(flat[:, 0].mean() - ref.mean()) < 0.05 * flat[:, 0].std() + 0.01
+    assert np.all(mcmc.rhat(v) < 1.05)
+    assert 0.15 < r.accept < 0.4
