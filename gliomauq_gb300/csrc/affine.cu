@@ -3,9 +3,12 @@
 // phi0 is the final density at a reference sample, J_p basis fields (the
 // derivatives along the sampler's coordinates, and optionally second-order
 // terms whose coefficients the caller forms, such as delta_0^2 / 2), m the
-// fast path's tissue mask. B such fields are formed in one pass over phi0
-// and J (a thread owns one cell and writes it for every model; phi0 and J
-// are read once per launch) and go through the handle's likelihood kernel.
+// fast path's tissue mask. The likelihood reads the density only at its
+// observation lists' cells, so phi0, J and m are gathered once at those cells
+// (k_affine_gather, when the model or the observations change) and each
+// evaluation forms the B models' densities there inside the likelihood
+// reduction: per model (P + 2) floats per observation instead of a whole
+// n^3 field written and read back.
 #include "gbg_internal.cuh"
 
 namespace gbg {
@@ -13,24 +16,44 @@ namespace {
 
 constexpr int kAffineMaxP = 16;
 
-__global__ void k_affine_fields(size_t N, int B, int P, const float *__restrict__ phi0,
-                                const float *__restrict__ J, const double *__restrict__ delta,
-                                const float *__restrict__ msk, float *__restrict__ out) {
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N; c += (size_t)gridDim.x * blockDim.x) {
-        const float base = phi0[c];
-        float jc[kAffineMaxP];
-#pragma unroll
-        for (int p = 0; p < kAffineMaxP; ++p) jc[p] = p < P ? J[(size_t)p * N + c] : 0.f;
-        const bool tissue = msk[c] != 0.f;
-        for (int s = 0; s < B; ++s) {
-            float v = base;
-#pragma unroll
-            for (int p = 0; p < kAffineMaxP; ++p)
-                if (p < P) v = fmaf((float)delta[(size_t)s * P + p], jc[p], v);
-            v = fminf(fmaxf(v, 0.f), 1.f);
-            out[(size_t)s * N + c] = tissue ? v : 0.f;
-        }
+// cols block of one list: row 0 phi0, rows 1..P the basis fields, row P+1 the
+// mask, each `len` floats, at the list's cells idx[0..len)
+__global__ void k_affine_gather(int len, const int *__restrict__ idx, size_t N, int P,
+                                const float *__restrict__ phi0, const float *__restrict__ J,
+                                const float *__restrict__ msk, float *__restrict__ cols) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+        const size_t c = (size_t)idx[i];
+        cols[i] = phi0[c];
+        for (int p = 0; p < P; ++p) cols[(size_t)(1 + p) * len + i] = J[(size_t)p * N + c];
+        cols[(size_t)(P + 1) * len + i] = msk[c];
     }
+}
+
+int gather_columns(Handle &h) {
+    const int P = h.aff_P;
+    const size_t need = (size_t)(P + 2) * ((size_t)h.obs.n_pet + (size_t)h.obs.n_ti);
+    if (need > h.aff_cols_cap) {
+        if (h.aff_cols) cudaFree(h.aff_cols);
+        h.aff_cols = nullptr;
+        h.aff_cols_cap = 0;
+        GBG_CUDA_TRY(cudaMalloc((void **)&h.aff_cols, need * sizeof(float)));
+        h.aff_cols_cap = need;
+    }
+    const int lens[2] = {h.obs.n_pet, h.obs.n_ti};
+    const int *idx[2] = {h.obs.pet_idx, h.obs.ti_idx};
+    float *dst = h.aff_cols;
+    for (int l = 0; l < 2; ++l) {
+        if (lens[l] > 0) {
+            const int blocks = (lens[l] + 255) / 256;
+            k_affine_gather<<<blocks < h.num_sms * 8 ? blocks : h.num_sms * 8, 256, 0, h.stream>>>(
+                lens[l], idx[l], h.N, P, h.aff_phi0, h.aff_J, h.msk, dst);
+            h.launches++;
+        }
+        dst += (size_t)(P + 2) * lens[l];
+    }
+    GBG_CUDA_TRY(cudaGetLastError());
+    h.aff_cols_stale = false;
+    return GBG_OK;
 }
 
 }  // namespace
@@ -52,6 +75,7 @@ int affine_set(Handle &h, int P, const float *phi0, const float *J) {
     GBG_CUDA_TRY(cudaMemcpyAsync(h.aff_phi0, phi0, h.N * sizeof(float), cudaMemcpyHostToDevice, h.stream));
     GBG_CUDA_TRY(cudaMemcpyAsync(h.aff_J, J, (size_t)P * h.N * sizeof(float), cudaMemcpyHostToDevice, h.stream));
     GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+    h.aff_cols_stale = true;
     return GBG_OK;
 }
 
@@ -60,14 +84,11 @@ int affine_loglik(Handle &h, int B, const double *delta_host, gbg_lik_result *li
         set_error("affine model not set");
         return GBG_ERR_STATE;
     }
-    const int P = h.aff_P;
-    if ((size_t)B > h.aff_out_cap) {
-        if (h.aff_out) cudaFree(h.aff_out);
-        h.aff_out = nullptr;
-        h.aff_out_cap = 0;
-        GBG_CUDA_TRY(cudaMalloc((void **)&h.aff_out, (size_t)B * h.N * sizeof(float)));
-        h.aff_out_cap = B;
+    if (!h.obs.valid) {
+        set_error("observations not set");
+        return GBG_ERR_STATE;
     }
+    const int P = h.aff_P;
     if ((size_t)B * P > h.aff_delta_cap) {
         if (h.aff_delta) cudaFree(h.aff_delta);
         h.aff_delta = nullptr;
@@ -75,14 +96,11 @@ int affine_loglik(Handle &h, int B, const double *delta_host, gbg_lik_result *li
         GBG_CUDA_TRY(cudaMalloc((void **)&h.aff_delta, (size_t)B * P * sizeof(double)));
         h.aff_delta_cap = (size_t)B * P;
     }
+    if (h.aff_cols_stale)
+        if (int rc = gather_columns(h)) return rc;
     GBG_CUDA_TRY(cudaMemcpyAsync(h.aff_delta, delta_host, (size_t)B * P * sizeof(double), cudaMemcpyHostToDevice,
                                  h.stream));
-    const size_t blocks = (h.N + 255) / 256, cap = (size_t)h.num_sms * 8;
-    k_affine_fields<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, h.stream>>>(h.N, B, P, h.aff_phi0, h.aff_J,
-                                                                                   h.aff_delta, h.msk, h.aff_out);
-    h.launches++;
-    GBG_CUDA_TRY(cudaGetLastError());
-    return lik_evaluate(h, h.aff_out, nullptr, B, lik_device);
+    return lik_evaluate_affine(h, h.aff_cols, P, h.aff_delta, B, lik_device);
 }
 
 }  // namespace gbg

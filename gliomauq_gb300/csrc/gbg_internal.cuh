@@ -148,10 +148,14 @@ struct Handle {
     void *adj_ws = nullptr;
     size_t adj_ws_bytes = 0;
 
-    // affine density model phi0 + sum_p delta_p J_p (gbg_affine_*)
-    float *aff_phi0 = nullptr, *aff_J = nullptr, *aff_out = nullptr;
+    // affine density model phi0 + sum_p delta_p J_p (gbg_affine_*); aff_cols
+    // holds phi0, the P basis fields and the tissue mask gathered at the
+    // observation lists' cells (rebuilt when the model or the observations
+    // change)
+    float *aff_phi0 = nullptr, *aff_J = nullptr, *aff_cols = nullptr;
     int aff_P = 0;
-    size_t aff_out_cap = 0;  // fields
+    size_t aff_cols_cap = 0;  // floats
+    bool aff_cols_stale = true;
     double *aff_delta = nullptr;
     size_t aff_delta_cap = 0;  // doubles
 };
@@ -268,6 +272,10 @@ int lik_set_observations(Handle &h, const double *pet, const double *t1, const d
 int lik_evaluate(Handle &h, const float *phi_f32, const double *phi_f64, int S,
                  gbg_lik_result *out_device);
 // population: sample s's final field is in buf[recs[s].nsteps & 1] + s*N.
+// log L of B affine models evaluated at the observation cells only
+// (delta_device: B x P; cols: likelihood.cu's AffineSource layout)
+int lik_evaluate_affine(Handle &h, const float *cols, int P, const double *delta_device, int B,
+                        gbg_lik_result *out_device);
 int lik_evaluate_population(Handle &h, const float *buf0, const float *buf1,
                             const SampleRec *recs_unsorted, int S, gbg_lik_result *out_device);
 

@@ -65,9 +65,40 @@ struct PhiSource {
         const float *b = (recs && (recs[s].nsteps & 1)) ? f1 : f0;
         return (double)b[(size_t)s * stride + c];
     }
+    __device__ __forceinline__ double pet(const LikArgs &a, int s, int i) const {
+        return at(s, a.stride, a.pet_idx[i]);
+    }
+    __device__ __forceinline__ double ti(const LikArgs &a, int s, int i) const {
+        return at(s, a.stride, a.ti_idx[i]);
+    }
 };
 
-__global__ void __launch_bounds__(kLikThreads) k_lik_partial(LikArgs a, PhiSource src) {
+// phi of affine model s at the i-th entry of an observation list, from the
+// model gathered at the list's cells: cols = [pet block | ti block], each
+// block (P + 2) rows of its list's length: phi0, J_0 .. J_{P-1}, tissue mask.
+// The same float operations as forming the whole field would do:
+// v = phi0; v = fma(delta_p, J_p, v) for p = 0..P-1; clamp to [0, 1]; 0
+// outside the mask.
+struct AffineSource {
+    const float *pet_cols, *ti_cols;
+    const double *delta;
+    int P;
+    __device__ __forceinline__ double eval(const float *cols, int len, int s, int i) const {
+        float v = cols[i];
+        for (int p = 0; p < P; ++p) v = fmaf((float)delta[(size_t)s * P + p], cols[(size_t)(1 + p) * len + i], v);
+        v = fminf(fmaxf(v, 0.f), 1.f);
+        return cols[(size_t)(P + 1) * len + i] != 0.f ? (double)v : 0.0;
+    }
+    __device__ __forceinline__ double pet(const LikArgs &a, int s, int i) const {
+        return eval(pet_cols, a.n_pet, s, i);
+    }
+    __device__ __forceinline__ double ti(const LikArgs &a, int s, int i) const {
+        return eval(ti_cols, a.n_ti, s, i);
+    }
+};
+
+template <class Src>
+__global__ void __launch_bounds__(kLikThreads) k_lik_partial(LikArgs a, Src src) {
     const int s = blockIdx.y;
     const int chunk = blockIdx.x;
     double sp = 0.0, s1 = 0.0, s2 = 0.0;
@@ -75,13 +106,13 @@ __global__ void __launch_bounds__(kLikThreads) k_lik_partial(LikArgs a, PhiSourc
     for (int k = 0; k < kLikPerThread; ++k) {
         const int i = base + k * kLikThreads + threadIdx.x;
         if (i < a.n_pet) {
-            const double u = src.at(s, a.stride, a.pet_idx[i]);
+            const double u = src.pet(a, s, i);
             const double pv = a.pet_val[i];
             const double r = u - a.pet_scale * pv;
             sp += r * r;
         }
         if (i < a.n_ti) {
-            const double u = src.at(s, a.stride, a.ti_idx[i]);
+            const double u = src.ti(a, s, i);
             s1 += log_bernoulli(u, a.t1_val[i], a.t1_uc, a.is2);
             s2 += log_bernoulli(u, a.t2_val[i], a.t2_uc, a.is2);
         }
@@ -139,7 +170,8 @@ int upload(T **dst, const std::vector<T> &v) {
     return GBG_OK;
 }
 
-int run_lik(Handle &h, const PhiSource &src, int S, gbg_lik_result *out_device) {
+template <class Src>
+int run_lik(Handle &h, const Src &src, int S, gbg_lik_result *out_device) {
     if (!h.obs.valid) {
         set_error("observations not set");
         return GBG_ERR_STATE;
@@ -234,6 +266,7 @@ int lik_set_observations(Handle &h, const double *pet, const double *t1, const d
     o.t2_uc = p.t2_uc;
     o.slope = p.slope;
     o.valid = true;
+    h.aff_cols_stale = true;
     return GBG_OK;
 }
 
@@ -241,6 +274,12 @@ int lik_evaluate(Handle &h, const float *phi_f32, const double *phi_f64, int S,
                  gbg_lik_result *out_device) {
     PhiSource src{phi_f32, phi_f32, phi_f64, nullptr};
     return run_lik(h, src, S, out_device);
+}
+
+int lik_evaluate_affine(Handle &h, const float *cols, int P, const double *delta_device, int B,
+                        gbg_lik_result *out_device) {
+    AffineSource src{cols, cols + (size_t)(P + 2) * h.obs.n_pet, delta_device, P};
+    return run_lik(h, src, B, out_device);
 }
 
 int lik_evaluate_population(Handle &h, const float *buf0, const float *buf1,

@@ -12,6 +12,10 @@ uniform prior on a box for Dw, rho, T and on the interior seed region for
 
   * rwm  : random-walk Metropolis, Gaussian proposal
   * mala : Metropolis-adjusted Langevin, gradients from gbg_adjoint_grad
+  * tmcmc: transitional MCMC (Ching & Chen 2007), the population sampler
+           of the reference's workflow, every Metropolis step of the
+           population one batched solve
+  * plain_chains: single-solve chains, the plain method
   * da   : delayed acceptance (Christen & Fox 2005) in its surrogate-
            transition form (Liu 2001, sec. 9.4): stage 1 runs `inner`
            random-walk Metropolis steps on the learned surrogate's
@@ -1008,6 +1012,160 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
     return PipelineResult(r, post.to_theta(r.samples[burn:]), v_map, cov, setup, r.seconds - burn_s,
                           burn_s, surrogate=sur, solver_seconds=run.seconds,
                           surrogate_seconds=sur.seconds)
+
+
+@dataclass
+class TmcmcResult:
+    theta: np.ndarray        # final population (N, d), posterior draws
+    loglik: np.ndarray       # their log L (N,)
+    p: list                  # tempering exponents, 0 = p_0 < ... < p_m = 1
+    log_evidence: float      # log of the estimated marginal likelihood
+    accept: list             # Metropolis acceptance per stage
+    solves: int
+    seconds: float
+
+
+def _tempering_step(ll: np.ndarray, room: float, cov_tol: float) -> float:
+    """The increment q in (0, room] of the tempering exponent whose weights
+    exp(q (ll - max ll)) have coefficient of variation cov_tol (room when
+    even q = room stays below it); bisection, the CoV growing with q."""
+    d = ll - ll.max()
+
+    def cov(q):
+        w = np.exp(q * d)
+        return w.std() / w.mean()
+
+    if cov(room) <= cov_tol:
+        return room
+    lo, hi = 0.0, room
+    for _ in range(100):
+        mid = 0.5 * (lo + hi)
+        if cov(mid) > cov_tol:
+            hi = mid
+        else:
+            lo = mid
+        if hi - lo <= 1e-12 * room:
+            break
+    return max(lo, 1e-12 * room)
+
+
+def tmcmc(post, theta0: np.ndarray, rng, cov_tol: float = 1.0, beta2: float = 0.04,
+          max_chain: int = 1, max_stages: int = 200, steps_per_state: int = 3,
+          target_accept: float = 0.3) -> TmcmcResult:
+    """Transitional MCMC (Ching & Chen 2007; the sampler the reference's
+    workflow runs outside its code: one brain + likelihood process pair per
+    sample) on the batched solver. theta0: N draws from the prior (rows, in
+    post's coordinates); post.loglik gives log L + log prior and
+    post.prior.logp the log prior. Stage j targets prior * L^p_j:
+      1. the increment of p is the one whose plausibility weights
+         w_i = L_i^(p_j+1 - p_j) have coefficient of variation cov_tol;
+         log S_j = log mean(w) adds to the log evidence;
+      2. proposal covariance beta2 * the weighted covariance of the
+         population;
+      3. N leaders are drawn with probabilities w / sum(w); a leader drawn c
+         times starts a Metropolis chain whose c states are population
+         members (max_chain > 0 splits it into chains of at most max_chain
+         states, each from the leader);
+      4. all chains step in lock-step: every step is one batched solve of
+         the active chains' proposals; a chain records its state after every
+         `steps_per_state` steps (1: Ching & Chen's chains).
+    With target_accept, beta2 is rescaled after every stage by
+    exp(2 (acceptance - target_accept)) (the proposal scale adaptation of
+    Betz, Papaioannou & Straub 2016). max_chain = 0, steps_per_state = 1,
+    target_accept = None is Ching & Chen's original. The defaults (every
+    resampled state its own chain of 3 steps, adapted scale) keep all N
+    chains in every batched solve, and they remove the bias of the
+    original's log evidence: chains of correlated states from one leader make
+    the next stage's weights and tempering step depend on few distinct points
+    (on a 1-D Gaussian inside a box the original is low by 0.04 +- 0.006 at
+    N = 2000, single-state chains within 0.01). Ends when p reaches 1 (or
+    after max_stages)."""
+    th = np.array(np.atleast_2d(theta0), dtype=np.float64)
+    N, d = th.shape
+    t0 = time.perf_counter()
+    solves0 = getattr(post, "solves", 0)
+    lpost, _ = post.loglik(th, False)
+    lpr = post.prior.logp(th)
+    ll = np.where(np.isfinite(lpr), lpost - lpr, -np.inf)
+    if not np.isfinite(ll).any():
+        raise ValueError("no prior draw has a finite likelihood")
+    p = 0.0
+    ps, acc, log_ev = [0.0], [], 0.0
+    for _ in range(max_stages):
+        if p >= 1.0:
+            break
+        fin = np.isfinite(ll)
+        q = _tempering_step(ll[fin], 1.0 - p, cov_tol)
+        if p + q >= 1.0 - 1e-12:
+            q = 1.0 - p
+        llmax = ll[fin].max()
+        w = np.where(fin, np.exp(q * (ll - llmax)), 0.0)
+        log_ev += np.log(w.sum() / N) + q * llmax
+        wn = w / w.sum()
+        p += q
+        mu = wn @ th
+        dev = th - mu
+        cov = beta2 * (dev * wn[:, None]).T @ dev
+        Lc = np.linalg.cholesky(cov + 1e-12 * np.diag(np.diag(cov)) + 1e-300 * np.eye(d))
+        counts = rng.multinomial(N, wn)
+        starts, lens = [], []
+        for i in np.flatnonzero(counts):
+            c = int(counts[i])
+            while c > 0:
+                k = c if max_chain <= 0 else min(c, max_chain)
+                starts.append(i)
+                lens.append(k)
+                c -= k
+        lens = np.array(lens)
+        cur = th[starts].copy()
+        cur_ll = ll[starts].copy()
+        cur_lpr = lpr[starts].copy()
+        new_th, new_ll, new_lpr = [], [], []
+        n_acc = n_try = 0
+        for k in range(int(lens.max()) * steps_per_state):
+            act = np.flatnonzero(lens > k // steps_per_state)
+            prop = cur[act] + rng.standard_normal((act.size, d)) @ Lc.T
+            pl = post.prior.logp(prop)
+            ok = np.isfinite(pl)
+            pll = np.full(act.size, -np.inf)
+            if ok.any():
+                lq, _ = post.loglik(prop[ok], False)
+                pll[ok] = lq - pl[ok]
+            with np.errstate(invalid="ignore"):
+                logr = (pl + p * pll) - (cur_lpr[act] + p * cur_ll[act])
+            a = ok & np.isfinite(pll) & (np.log(rng.random(act.size)) < logr)
+            sel = act[a]
+            cur[sel], cur_ll[sel], cur_lpr[sel] = prop[a], pll[a], pl[a]
+            n_acc += int(a.sum())
+            n_try += act.size
+            if (k + 1) % steps_per_state == 0:
+                new_th.append(cur[act].copy())
+                new_ll.append(cur_ll[act].copy())
+                new_lpr.append(cur_lpr[act].copy())
+        th = np.concatenate(new_th)
+        ll = np.concatenate(new_ll)
+        lpr = np.concatenate(new_lpr)
+        ps.append(p)
+        acc.append(n_acc / max(n_try, 1))
+        if target_accept is not None:
+            beta2 *= np.exp(2.0 * (acc[-1] - target_accept))
+    return TmcmcResult(th, ll, ps, float(log_ev), acc, getattr(post, "solves", 0) - solves0,
+                       time.perf_counter() - t0)
+
+
+def propagate(handle, L: float, theta: np.ndarray, dt0: float = 0.0, ic_peak: float = 0.1,
+              ic_sigma: float = 1.0, reference_rules: bool = False):
+    """Posterior propagation: the per-cell mean and variance of the final
+    densities of the samples theta (rows), in one batched solve + statistics
+    call (gbg_batch_statistics; the reference's propagation tool over the
+    samples' HGG_data.dat files, Glioma_HG_Propagation.cpp:346-440).
+    len(theta) <= the handle's max_samples. reference_rules keeps the tool's
+    zero planes at index 0."""
+    th = np.atleast_2d(np.asarray(theta, dtype=np.float64))
+    if th.shape[0] > handle.max_samples:
+        raise ValueError("more samples than the handle's max_samples")
+    return handle.batch_statistics([tuple(x) for x in th], L, ic_peak=ic_peak, ic_sigma=ic_sigma,
+                                   dt0=dt0, reference_rules=reference_rules)
 
 
 def rhat(samples: np.ndarray) -> np.ndarray:

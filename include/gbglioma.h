@@ -256,7 +256,10 @@ int gbg_adjoint_grad(gbg_handle *h, const gbg_sample *samples, int S, const gbg_
  * (the handle's observations) of B models given by their coefficients delta
  * (B x P doubles; e.g. u - u_ref and products of its components). The cheap first stage
  * of delayed-acceptance MCMC around a posterior mode. GBG_PREC_F32 handles;
- * the handle keeps the fields until gbg_destroy. */
+ * the handle keeps the fields until gbg_destroy. The models are evaluated at
+ * the observation lists' cells only (phi0, J and m gathered there once per
+ * model and observation set), with the same float operations as forming the
+ * whole field, so log L equals that of the formed field bit for bit. */
 int gbg_affine_set(gbg_handle *h, int P, const float *phi0, const float *J);
 int gbg_affine_loglik(gbg_handle *h, int B, const double *delta, gbg_lik_result *out);
 

@@ -580,3 +580,47 @@ def test_plain_chains_sample_the_invariant_posterior():
     assert abs(flat[:, 0].mean() - ref.mean()) < 0.05 * flat[:, 0].std() + 0.01
     assert np.all(mcmc.rhat(v) < 1.05)
     assert 0.15 < r.accept < 0.4
+
+
+def test_tmcmc_recovers_a_gaussian_and_its_evidence():
+    """TMCMC from prior draws on the Gaussian stub inside its prior box:
+    the final population's moments and the log evidence
+    log( integral of exp(-z^2/2) / box volume ) = sum log(sqrt(2 pi) sd / width)."""
+    rng = np.random.default_rng(3)
+    post = GaussianStub()
+    th0 = post.prior.lo + post.prior.width * rng.random((4000, 6))
+    r = mcmc.tmcmc(post, th0, rng)
+    assert r.p[0] == 0.0 and r.p[-1] == 1.0 and np.all(np.diff(r.p) > 0)
+    assert len(r.p) > 3
+    s = r.theta
+    assert s.shape == (4000, 6)
+    assert np.all(np.abs(s.mean(axis=0) - post.mu) < 0.1 * post.sd)
+    assert np.all(np.abs(s.std(axis=0) / post.sd - 1) < 0.15)
+    exact = float(np.sum(np.log(np.sqrt(2 * np.pi) * post.sd / post.prior.width)))
+    assert abs(r.log_evidence - exact) < 0.25, (r.log_evidence, exact)
+    assert r.solves >= 4000 * len(r.p)
+    assert all(0.1 < a < 0.6 for a in r.accept[2:])
+    # Ching & Chen's original: chains as long as a leader's multiplicity,
+    # fixed beta^2 = 0.04 (its moments only: its evidence is biased low)
+    r0 = mcmc.tmcmc(post, th0, rng, max_chain=0, steps_per_state=1, target_accept=None)
+    assert r0.p[-1] == 1.0
+    assert np.all(np.abs(r0.theta.mean(axis=0) - post.mu) < 0.5 * post.sd)
+    assert np.all(np.abs(r0.theta.std(axis=0) / post.sd - 1) < 0.2)
+
+
+def test_tmcmc_on_the_invariant_posterior_in_log_coordinates():
+    """TMCMC in the scaling symmetry's coordinates (prior density with its
+    Jacobian; the likelihood flat along v0) from prior draws: the identified
+    coordinates' moments."""
+    rng = np.random.default_rng(5)
+    base = InvariantStub()
+    lc = mcmc.LogCoords(base, A=mcmc.INVARIANT_MAP)
+    lo, hi = base.prior.lo, base.prior.hi
+    v0 = lc.to_u(lo + (hi - lo) * rng.random((3000, 6)))
+    r = mcmc.tmcmc(lc, v0, rng)
+    assert r.p[-1] == 1.0 and len(r.p) > 5
+    m1, m2, s1, s2 = _invariant_moments(base)
+    f = r.theta
+    assert abs(f[:, 1].mean() - m1) < 0.15 * s1 and abs(f[:, 2].mean() - m2) < 0.15 * s2
+    assert abs(f[:, 1].std() / s1 - 1) < 0.2 and abs(f[:, 2].std() / s2 - 1) < 0.2
+    assert np.all(np.abs(f[:, 3:].mean(axis=0) - base.c[2:]) < 0.15 * base.s[2:])
