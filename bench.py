@@ -631,6 +631,10 @@ def main():
                     help="print the surrogate-network measurement alone (profiling runs)")
     ap.add_argument("--only-mcmc", action="store_true",
                     help="print the ESS/s comparison alone")
+    ap.add_argument("--mcmc-chains", type=int, default=64, help="pipeline chains")
+    ap.add_argument("--mcmc-inner", type=int, default=16, help="surrogate steps per solve")
+    ap.add_argument("--mcmc-generations", type=int, default=300,
+                    help="pipeline generations (the first 100 are burn-in)")
     ap.add_argument("--samples", type=int, default=S,
                     help="population size (profiling runs use a smaller one)")
     ap.add_argument("--variant", type=int, default=-1,
@@ -642,7 +646,10 @@ def main():
         print(json.dumps({"surrogate": surrogate_measurement(int(os.environ.get("LOCAL_RANK", "0")))}))
         return
     if args.only_mcmc:
-        print(json.dumps({"mcmc": mcmc_comparison(int(os.environ.get("LOCAL_RANK", "0")))}))
+        print(json.dumps({"mcmc": mcmc_comparison(int(os.environ.get("LOCAL_RANK", "0")),
+                                                  chains=args.mcmc_chains, inner=args.mcmc_inner,
+                                                  generations=args.mcmc_generations,
+                                                  unet=not args.no_surrogate)}))
         return
     set_population(args.samples)
 
@@ -780,7 +787,9 @@ def main():
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(an, prior, obs=obs)
         if not args.no_mcmc:
-            line["mcmc"] = mcmc_comparison(local_rank)
+            line["mcmc"] = mcmc_comparison(local_rank, chains=args.mcmc_chains,
+                                           inner=args.mcmc_inner,
+                                           generations=args.mcmc_generations)
         if not args.no_amr:
             line["amr"] = amr_measurement(local_rank)
             line["amr"]["adaptive"] = amr_adaptive_measurement(local_rank)

@@ -13,24 +13,37 @@
 // process(vInfo, collection, functor, granularity).
 //
 // What runs where:
-//  * pipeline_process with Glioma_ReactionDiffusionOperator<3> on a uniform
-//    grid (every block at one level) records Dw, Dg and rho; the following
-//    process with UpdateTumor<3> runs both as one fused step on the GPU
-//    (gbg_rd_step) in the precision of Real: GBG_PREC_F64 for double,
-//    GBG_PREC_F32REF for float, bit-identical to the CPU back-end either way.
-//  * Any other functor, or a grid with more than one level, runs on the CPU
-//    back-end given as the second template argument, after the GPU state has
-//    been copied back into the blocks -- results never silently change.
-//  * After every fused step the new phi is copied back into the blocks
-//    (HostSync::every_step, the default), so code that reads the grid
-//    (regridding, dumps) sees current values. With HostSync::on_demand the
-//    blocks are updated only by sync_to_host(), which the caller must call
-//    before reading them; the device then keeps the state between steps.
+//  * pipeline_process with Glioma_ReactionDiffusionOperator<3> records Dw,
+//    Dg and rho; the following process with UpdateTumor<3> runs both as one
+//    step of the library's block grid (gbg_amr_step) in the precision of
+//    Real: GBG_PREC_F64 for double, GBG_PREC_F32REF for float, bit-identical
+//    to the CPU back-end either way, on a uniform grid or one with blocks at
+//    several levels (the ghost cells of resolution jumps come from the
+//    library's own ghost-table compiler, gbg_amr_build_ghosts).
+//  * Any other functor runs on the CPU back-end given as the second template
+//    argument, after the GPU state has been copied back into the blocks --
+//    results never silently change.
+//  * The fields live on the device block-major, the layout of the blocks
+//    themselves: an upload or a read-back is one pass over each block's
+//    cells, no reordering into a global array.
+//  * When the host blocks get the device's phi (HostSync):
+//      every_step  after every fused step (the default: correct for any
+//                  caller, which may read the grid at any time);
+//      at_times    only where the run loop reads the grid: after the step at
+//                  which the loop's time reaches its next output time (where
+//                  Glioma_HG_UQ::run regrids and dumps) and after the step
+//                  that ends the loop (the final refinement and
+//                  _dumpUQoutput). sync_at(whenToWrite, whenToWriteOffset,
+//                  tend) mirrors the loop's own bookkeeping in the same
+//                  double arithmetic (Glioma_HG_UQ.cpp:541-566);
+//      on_demand   only by sync_to_host(), which the caller must call
+//                  before reading the blocks.
 //  * dphidt is not written back: the fused step keeps the rates on the GPU.
 //  * The anatomy (p_w, p_g) and phi are uploaded at the first fused step and
-//    again whenever the set of blocks changes or a CPU-run functor may have
-//    modified them; between fused steps the GPU copy is authoritative, so code
-//    that writes the blocks directly calls invalidate() afterwards.
+//    again whenever the blocks change (their IDs, levels or positions) or a
+//    CPU-run functor may have modified them; between fused steps the GPU copy
+//    is authoritative, so code that writes the blocks directly calls
+//    invalidate() afterwards.
 //
 // Requires gbglioma.h and linking libgbglioma. The operator templates are
 // matched by name; they are declared (not defined) here so this header can be
@@ -52,7 +65,7 @@ template <int nDim> struct UpdateTumor;
 
 namespace gbglioma {
 
-enum class HostSync { every_step, on_demand };
+enum class HostSync { every_step, at_times, on_demand };
 
 template <typename P> struct is_rd_rhs { static const bool value = false; };
 template <> struct is_rd_rhs<Glioma_ReactionDiffusionOperator<3> > { static const bool value = true; };
@@ -71,6 +84,8 @@ public:
 template <typename BlockType, typename CPUBackend>
 class BlockProcessing_GPU {
 public:
+    static const int kCells = BlockType::sizeX * BlockType::sizeY * BlockType::sizeZ;
+
     explicit BlockProcessing_GPU(HostSync sync = HostSync::every_step, int device = 0)
         : sync_(sync), device_(device) {}
     ~BlockProcessing_GPU() {
@@ -80,10 +95,21 @@ public:
     BlockProcessing_GPU(const BlockProcessing_GPU &) = delete;
     BlockProcessing_GPU &operator=(const BlockProcessing_GPU &) = delete;
 
+    // HostSync::at_times with the run loop's schedule: its first output time
+    // (whenToWrite), the interval (whenToWriteOffset) and its end time (tend);
+    // the loop's time starts at 0 here.
+    void sync_at(double first, double every, double tend) {
+        sync_ = HostSync::at_times;
+        t_ = 0.0;
+        next_ = first;
+        every_ = every;
+        tend_ = tend;
+    }
+
     template <typename Processing, typename Collection, typename Info, typename Boundary>
     void pipeline_process(std::vector<Info> &vInfo, Collection &c, Boundary &b, Processing &p) {
         current() = this;
-        if (is_rd_rhs<Processing>::value && uniform(vInfo)) {
+        if (is_rd_rhs<Processing>::value && !vInfo.empty()) {
             ensure_device(vInfo, c);
             pending_ = true;
             Dw_ = (double)rhs_Dw(p);
@@ -118,9 +144,10 @@ public:
     template <typename Collection, typename Info>
     void sync_to_host(std::vector<Info> &vInfo, Collection &c) {
         if (!host_stale_ || !device_valid_ || !matches(vInfo)) return;
-        check(gbg_get_phi(h_, phi_.data()), "gbg_get_phi");
+        check(gbg_amr_get_phi(h_, phi_.data()), "gbg_amr_get_phi");
         scatter(vInfo, c);
         host_stale_ = false;
+        ++syncs_;
     }
 
     // Call after changing the blocks' phi, p_w or p_g directly: the next fused
@@ -128,6 +155,8 @@ public:
     void invalidate() { device_valid_ = false; host_stale_ = false; }
 
     long long gpu_steps() const { return steps_; }
+    long long host_syncs() const { return syncs_; }
+    long long uploads() const { return uploads_; }
 
 private:
     // Member access kept in one place: Glioma_ReactionDiffusionOperator has
@@ -150,43 +179,38 @@ private:
         if (rc != GBG_OK) throw GpuError(rc, what);
     }
 
-    template <typename Info>
-    static bool uniform(const std::vector<Info> &vInfo) {
-        if (vInfo.empty()) return false;
-        const int l = vInfo[0].level;
-        for (size_t i = 1; i < vInfo.size(); ++i)
-            if (vInfo[i].level != l) return false;
-        const size_t side = (size_t)1 << l;
-        return vInfo.size() == side * side * side;
-    }
-
+    // the blocks the device holds, in the order of vInfo: IDs, levels and
+    // positions must all agree (a regrid can reuse an ID elsewhere)
     template <typename Info>
     bool matches(const std::vector<Info> &vInfo) const {
         if (ids_.size() != vInfo.size()) return false;
-        for (size_t i = 0; i < vInfo.size(); ++i)
-            if (ids_[i] != vInfo[i].blockID) return false;
+        for (size_t i = 0; i < vInfo.size(); ++i) {
+            const gbg_block &g = grid_[i];
+            const Info &info = vInfo[i];
+            if (ids_[i] != info.blockID || g.level != info.level || g.ix != info.index[0] ||
+                g.iy != info.index[1] || g.iz != info.index[2])
+                return false;
+        }
         return true;
     }
 
-    template <typename Info>
-    size_t cell(const Info &info, int ix, int iy, int iz) const {
-        const size_t gx = (size_t)info.index[0] * BlockType::sizeX + ix;
-        const size_t gy = (size_t)info.index[1] * BlockType::sizeY + iy;
-        const size_t gz = (size_t)info.index[2] * BlockType::sizeZ + iz;
-        return gx + (size_t)n_ * (gy + (size_t)n_ * gz);
+    static size_t local(int ix, int iy, int iz) {
+        return (size_t)ix + (size_t)BlockType::sizeX * ((size_t)iy + (size_t)BlockType::sizeY * iz);
     }
 
     template <typename Info, typename Collection>
     void gather(std::vector<Info> &vInfo, Collection &c) {
-        for (const Info &info : vInfo) {
-            BlockType &b = c[info.blockID];
+        for (size_t i = 0; i < vInfo.size(); ++i) {
+            BlockType &b = c[vInfo[i].blockID];
+            double *pw = pw_.data() + i * kCells, *pg = pg_.data() + i * kCells,
+                   *phi = phi_.data() + i * kCells;
             for (int iz = 0; iz < BlockType::sizeZ; iz++)
                 for (int iy = 0; iy < BlockType::sizeY; iy++)
                     for (int ix = 0; ix < BlockType::sizeX; ix++) {
-                        const size_t g = cell(info, ix, iy, iz);
-                        pw_[g] = (double)b(ix, iy, iz).p_w;
-                        pg_[g] = (double)b(ix, iy, iz).p_g;
-                        phi_[g] = (double)b(ix, iy, iz).phi;
+                        const size_t k = local(ix, iy, iz);
+                        pw[k] = (double)b(ix, iy, iz).p_w;
+                        pg[k] = (double)b(ix, iy, iz).p_g;
+                        phi[k] = (double)b(ix, iy, iz).phi;
                     }
         }
     }
@@ -194,64 +218,85 @@ private:
     template <typename Info, typename Collection>
     void scatter(std::vector<Info> &vInfo, Collection &c) {
         typedef typename std::remove_reference<decltype(c[0](0, 0, 0).phi)>::type RealT;
-        for (const Info &info : vInfo) {
-            BlockType &b = c[info.blockID];
+        for (size_t i = 0; i < vInfo.size(); ++i) {
+            BlockType &b = c[vInfo[i].blockID];
+            const double *phi = phi_.data() + i * kCells;
             for (int iz = 0; iz < BlockType::sizeZ; iz++)
                 for (int iy = 0; iy < BlockType::sizeY; iy++)
                     for (int ix = 0; ix < BlockType::sizeX; ix++)
-                        b(ix, iy, iz).phi = (RealT)phi_[cell(info, ix, iy, iz)];
+                        b(ix, iy, iz).phi = (RealT)phi[local(ix, iy, iz)];
         }
     }
 
     template <typename Info, typename Collection>
     void ensure_device(std::vector<Info> &vInfo, Collection &c) {
         if (device_valid_ && matches(vInfo)) return;
-        const int l = vInfo[0].level;
-        const int n = (1 << l) * BlockType::sizeX;
-        if (BlockType::sizeX != BlockType::sizeY || BlockType::sizeX != BlockType::sizeZ)
-            throw std::invalid_argument("BlockProcessing_GPU needs cubic blocks");
+        if (BlockType::sizeX != 16 || BlockType::sizeY != 16 || BlockType::sizeZ != 16)
+            throw std::invalid_argument("BlockProcessing_GPU needs 16^3 blocks");
         typedef typename std::remove_reference<decltype(c[0](0, 0, 0).phi)>::type RealT;
         const int prec = sizeof(RealT) == sizeof(double) ? GBG_PREC_F64 : GBG_PREC_F32REF;
-        if (!h_ || n != n_ || prec != prec_) {
+        const int nb = (int)vInfo.size();
+        if (!h_ || nb > capacity_ || prec != prec_) {
             if (h_) gbg_destroy(h_);
             h_ = nullptr;
-            gbg_config cfg = {n, prec, device_, 0};
-            check(gbg_create(&cfg, &h_), "gbg_create");
-            n_ = n;
+            const int cap = nb > 2 * capacity_ ? nb : 2 * capacity_;
+            gbg_amr_config cfg = {cap, prec, device_};
+            check(gbg_amr_create(&cfg, &h_), "gbg_amr_create");
+            capacity_ = cap;
             prec_ = prec;
         }
-        const size_t N = (size_t)n * n * n;
-        pw_.assign(N, 0.0);
-        pg_.assign(N, 0.0);
-        phi_.assign(N, 0.0);
+        grid_.resize(nb);
+        ids_.resize(nb);
+        for (int i = 0; i < nb; ++i) {
+            const Info &info = vInfo[i];
+            grid_[i] = {(int)info.level, (int)info.index[0], (int)info.index[1], (int)info.index[2]};
+            ids_[i] = info.blockID;
+        }
+        const size_t cells = (size_t)nb * kCells;
+        pw_.resize(cells);
+        pg_.resize(cells);
+        phi_.resize(cells);
         gather(vInfo, c);
-        check(gbg_set_anatomy(h_, pw_.data(), pg_.data()), "gbg_set_anatomy");
-        check(gbg_set_phi(h_, phi_.data()), "gbg_set_phi");
-        ids_.clear();
-        for (const Info &info : vInfo) ids_.push_back(info.blockID);
+        check(gbg_amr_set_grid(h_, nb, grid_.data(), pw_.data(), pg_.data(), phi_.data()),
+              "gbg_amr_set_grid");
+        check(gbg_amr_build_ghosts(h_), "gbg_amr_build_ghosts");
         device_valid_ = true;
         host_stale_ = false;
+        ++uploads_;
     }
 
     template <typename Info, typename Collection>
     void fused_step(std::vector<Info> &vInfo, Collection &c, double dt) {
-        check(gbg_rd_step(h_, Dw_, Dg_, rho_, dt, 1), "gbg_rd_step");
+        check(gbg_amr_step(h_, Dw_, Dg_, rho_, dt, 1), "gbg_amr_step");
         pending_ = false;
         host_stale_ = true;
         ++steps_;
-        if (sync_ == HostSync::every_step) sync_to_host(vInfo, c);
+        if (sync_ == HostSync::every_step) {
+            sync_to_host(vInfo, c);
+        } else if (sync_ == HostSync::at_times) {
+            t_ += dt;  // the run loop's t += dt
+            bool now = false;
+            if (t_ >= next_) {
+                now = true;
+                next_ = next_ + every_;
+            }
+            if (!(t_ <= tend_)) now = true;  // the loop ends after this step
+            if (now) sync_to_host(vInfo, c);
+        }
     }
 
     CPUBackend cpu_;
     HostSync sync_;
     int device_;
     gbg_handle *h_ = nullptr;
-    int n_ = 0, prec_ = -1;
+    int capacity_ = 0, prec_ = -1;
     std::vector<int> ids_;
+    std::vector<gbg_block> grid_;
     std::vector<double> pw_, pg_, phi_;
     bool device_valid_ = false, host_stale_ = false, pending_ = false;
     double Dw_ = 0, Dg_ = 0, rho_ = 0;
-    long long steps_ = 0;
+    double t_ = 0, next_ = 0, every_ = 0, tend_ = 0;
+    long long steps_ = 0, syncs_ = 0, uploads_ = 0;
 };
 
 }  // namespace gbglioma
