@@ -36,7 +36,8 @@ EXPORTS = [
     "gbg_surrogate_create", "gbg_surrogate_destroy",
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
-    "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_surrogate_set_engine",
+    "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_affine_set_prior_mask",
+    "gbg_affine_chain", "gbg_surrogate_set_engine",
     "gbg_set_slopes", "gbg_get_slopes", "gbg_mala_step", "gbg_run_mala",
     "gbg_population_variant_name",
 ]
@@ -100,6 +101,13 @@ class SurrogateConfig(C.Structure):
                 ("dw_lo", C.c_double), ("dw_hi", C.c_double), ("rho_lo", C.c_double),
                 ("rho_hi", C.c_double), ("t_lo", C.c_double), ("t_hi", C.c_double),
                 ("seed", C.c_ulonglong)]
+
+
+class AffineChainOpts(C.Structure):
+    _fields_ = [("axis", C.c_int), ("axis_prob", C.c_double), ("step", C.c_double),
+                ("chol", C.c_double * 36), ("u_ref", C.c_double * 6), ("quad_axis", C.c_int),
+                ("Ai", C.c_double * 36), ("log_mask", C.c_int), ("lo", C.c_double * 6),
+                ("hi", C.c_double * 6)]
 
 
 class BatchOpts(C.Structure):
@@ -184,6 +192,8 @@ def load(path: str = LIB_PATH):
         "gbg_surrogate_set_engine": [vp, C.c_int],
         "gbg_affine_set": [vp, C.c_int, fp, fp],
         "gbg_affine_loglik": [vp, C.c_int, dp, C.POINTER(LikResult)],
+        "gbg_affine_set_prior_mask": [vp, vp],
+        "gbg_affine_chain": [vp, C.POINTER(AffineChainOpts), C.c_int, C.c_int, C.c_ulonglong, dp, dp, dp, vp],
         "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
                                C.POINTER(LikParams), vp, vp],
     }
@@ -381,6 +391,41 @@ class Handle:
         lik = (LikResult * B)()
         check(self.lib.gbg_affine_loglik(self._h, B, dptr(d), lik))
         return np.array([lik[i].total for i in range(B)])
+
+    def affine_set_prior_mask(self, mask):
+        """The prior's seed-voxel mask ([z, y, x] bool) for affine_chain."""
+        m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
+        if m.size != self.N:
+            raise ValueError("mask must have n^3 values")
+        check(self.lib.gbg_affine_set_prior_mask(self._h, m.ctypes.data))
+
+    def affine_chain(self, v, steps: int, seed: int, *, step: float, chol, axis: int = -1,
+                     axis_prob: float = 0.0, u_ref, quad_axis: int = -1, Ai=None, log_mask: int = 0,
+                     lo, hi):
+        """`steps` screening-chain steps for every row of v (B x 6) on the GPU
+        (gbg_affine_chain): (v after, log pi* at the start, at the end,
+        counts B x 4: random-walk accepts and steps, redraw accepts and
+        redraws)."""
+        vv = np.array(np.atleast_2d(v), dtype=np.float64, order="C", copy=True)
+        B = vv.shape[0]
+        o = AffineChainOpts()
+        o.axis = -1 if axis is None else int(axis)
+        o.axis_prob = float(axis_prob)
+        o.step = float(step)
+        o.chol[:] = np.ascontiguousarray(chol, dtype=np.float64).reshape(36).tolist()
+        o.u_ref[:] = np.asarray(u_ref, dtype=np.float64).reshape(6).tolist()
+        o.quad_axis = -1 if quad_axis is None else int(quad_axis)
+        o.Ai[:] = np.asarray(np.eye(6) if Ai is None else Ai, dtype=np.float64).reshape(36).tolist()
+        o.log_mask = int(log_mask)
+        o.lo[:] = np.asarray(lo, dtype=np.float64).reshape(6).tolist()
+        o.hi[:] = np.asarray(hi, dtype=np.float64).reshape(6).tolist()
+        l0 = np.empty(B)
+        l1 = np.empty(B)
+        cnt = np.zeros((B, 4), dtype=np.int32)
+        check(self.lib.gbg_affine_chain(self._h, C.byref(o), B, int(steps),
+                                        int(seed) & 0xFFFFFFFFFFFFFFFF, dptr(vv), dptr(l0), dptr(l1),
+                                        cnt.ctypes.data))
+        return vv, l0, l1, cnt
 
     def launch_count(self) -> int:
         c = C.c_longlong()

@@ -78,7 +78,7 @@ void free_handle(Handle &h) {
     void *ptrs[] = {h.pw, h.pg, h.phi[0], h.phi[1], h.b0, h.dfx, h.dfy, h.dfz, h.cx, h.cy, h.cz,
                     h.msk, h.cxs, h.sr[0], h.sr[1], h.sd[0], h.sd[1], h.mala_tt, h.bphi[0], h.bphi[1], h.bwork, h.dev_status, h.barrier,
                     h.obs.pet_idx, h.obs.pet_val, h.obs.ti_idx, h.obs.t1_val, h.obs.t2_val,
-                    h.lik_partials, h.lik_out, h.adj_ws, h.aff_phi0, h.aff_J, h.aff_cols, h.aff_delta,
+                    h.lik_partials, h.lik_out, h.adj_ws, h.aff_phi0, h.aff_J, h.aff_cols, h.aff_delta, h.aff_mask, h.aff_chain,
                     h.tile_live, h.live_list, h.live_count};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -920,6 +920,61 @@ int gbg_affine_loglik(gbg_handle *hh, int B, const double *delta, gbg_lik_result
     GBG_CUDA_TRY(cudaMemcpyAsync(out, h.lik_out, B * sizeof(gbg_lik_result), cudaMemcpyDeviceToHost, h.stream));
     GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
     return GBG_OK;
+}
+
+int gbg_affine_set_prior_mask(gbg_handle *hh, const unsigned char *mask) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!mask) {
+        set_error("null mask");
+        return GBG_ERR_ARG;
+    }
+    if (h.is_amr) {
+        set_error("affine chain needs a uniform-grid handle");
+        return GBG_ERR_STATE;
+    }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    return gbg::affine_set_prior_mask(h, mask);
+}
+
+int gbg_affine_chain(gbg_handle *hh, const gbg_affine_chain_opts *o, int B, int steps, unsigned long long seed,
+                     double *v, double *lp_start, double *lp_end, int *counts) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    if (!o || !v || !lp_start || !lp_end || B < 1 || B > 65535 || steps < 0) {
+        set_error("bad affine chain arguments");
+        return GBG_ERR_ARG;
+    }
+    if (o->axis < -1 || o->axis > 5 || o->quad_axis < -1 || o->quad_axis > 5 || !(o->axis_prob >= 0) ||
+        !(o->axis_prob <= 1) || !std::isfinite(o->step) || o->log_mask < 0 || o->log_mask > 63) {
+        set_error("affine chain options out of range");
+        return GBG_ERR_ARG;
+    }
+    for (int i = 0; i < 36; ++i)
+        if (!std::isfinite(o->chol[i]) || !std::isfinite(o->Ai[i])) {
+            set_error("non-finite affine chain matrix");
+            return GBG_ERR_NONFINITE;
+        }
+    for (int i = 0; i < 6; ++i) {
+        const bool lg = (o->log_mask >> i) & 1;
+        if (!std::isfinite(o->u_ref[i]) || !std::isfinite(o->lo[i]) || !std::isfinite(o->hi[i]) ||
+            !(o->hi[i] > o->lo[i]) || (lg && !(o->lo[i] > 0))) {
+            set_error("bad affine chain prior box or centre");
+            return GBG_ERR_ARG;
+        }
+        // the redrawn coordinate may move log coordinates only
+        if (o->axis >= 0 && !lg && o->Ai[i * 6 + o->axis] != 0) {
+            set_error("the redrawn coordinate moves a non-log coordinate");
+            return GBG_ERR_ARG;
+        }
+    }
+    for (size_t i = 0; i < (size_t)B * 6; ++i)
+        if (!std::isfinite(v[i])) {
+            set_error("non-finite chain state");
+            return GBG_ERR_NONFINITE;
+        }
+    GBG_CUDA_TRY(cudaSetDevice(h.device));
+    return gbg::affine_chain(h, *o, B, steps, seed, v, lp_start, lp_end, counts);
 }
 
 }  // extern "C"

@@ -29,7 +29,9 @@ __global__ void k_affine_gather(int len, const int *__restrict__ idx, size_t N, 
     }
 }
 
-int gather_columns(Handle &h) {
+}  // namespace
+
+int affine_gather_columns(Handle &h) {
     const int P = h.aff_P;
     const size_t need = (size_t)(P + 2) * ((size_t)h.obs.n_pet + (size_t)h.obs.n_ti);
     if (need > h.aff_cols_cap) {
@@ -55,8 +57,6 @@ int gather_columns(Handle &h) {
     h.aff_cols_stale = false;
     return GBG_OK;
 }
-
-}  // namespace
 
 int affine_set(Handle &h, int P, const float *phi0, const float *J) {
     if (P < 1 || P > kAffineMaxP) {
@@ -97,7 +97,7 @@ int affine_loglik(Handle &h, int B, const double *delta_host, gbg_lik_result *li
         h.aff_delta_cap = (size_t)B * P;
     }
     if (h.aff_cols_stale)
-        if (int rc = gather_columns(h)) return rc;
+        if (int rc = affine_gather_columns(h)) return rc;
     GBG_CUDA_TRY(cudaMemcpyAsync(h.aff_delta, delta_host, (size_t)B * P * sizeof(double), cudaMemcpyHostToDevice,
                                  h.stream));
     return lik_evaluate_affine(h, h.aff_cols, P, h.aff_delta, B, lik_device);

@@ -158,6 +158,9 @@ struct Handle {
     bool aff_cols_stale = true;
     double *aff_delta = nullptr;
     size_t aff_delta_cap = 0;  // doubles
+    unsigned char *aff_mask = nullptr;  // the prior's seed-voxel mask (n^3, affine chain)
+    void *aff_chain = nullptr;          // affine chain scratch, grow-only
+    size_t aff_chain_bytes = 0;
 };
 
 // ---- rd_exact.cu ----
@@ -288,6 +291,12 @@ long reference_num_steps(double dt, double tend);
 // ---- affine.cu ----
 int affine_set(Handle &h, int P, const float *phi0, const float *J);
 int affine_loglik(Handle &h, int B, const double *delta_host, gbg_lik_result *lik_device);
+// phi0, J and the mask gathered at the observation lists' cells (aff_cols)
+int affine_gather_columns(Handle &h);
+// ---- affine_chain.cu ----
+int affine_set_prior_mask(Handle &h, const unsigned char *mask);
+int affine_chain(Handle &h, const gbg_affine_chain_opts &o, int B, int steps, unsigned long long seed,
+                 double *v, double *lp_start, double *lp_end, int *counts);
 
 }  // namespace gbg
 

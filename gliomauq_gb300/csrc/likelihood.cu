@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "gbg_internal.cuh"
+#include "lik_terms.cuh"
 
 namespace gbg {
 namespace {
@@ -25,23 +26,6 @@ namespace {
 constexpr int kLikThreads = 256;
 constexpr int kLikPerThread = 8;
 constexpr int kLikChunk = kLikThreads * kLikPerThread;
-
-__device__ __forceinline__ int sgn_d(double d) {  // HGG_Likelihood::sgn, eps = 0
-    if (d < -0.0) return -1;
-    return d > 0.0;
-}
-
-__device__ __forceinline__ double log_bernoulli(double u, double y, double uc, double is2) {
-    const double diff = u - uc;
-    const double alpha = 0.5 + 0.5 * sgn_d(diff) * (1. - exp(-diff * diff * is2));
-    return (y == 1) ? log(alpha) : log(1. - alpha);
-}
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
 
 struct LikArgs {
     int n_pet, n_ti, chunks;

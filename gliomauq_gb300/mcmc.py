@@ -339,7 +339,7 @@ def _discrepancy(lp: np.ndarray, ls: np.ndarray) -> float:
 def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: int, step: float,
        rng, inner: int = 8, burn: int = 0, target: float = 0.3, chol=None, adapt: bool = False,
        rebuild_every: int = 0, axis=None, axis_prob: float = 0.5,
-       adapt_pool: bool = True, reset_stranded: bool = True) -> ChainResult:
+       adapt_pool: bool = True, reset_stranded: bool = True, gpu_chain: bool = True) -> ChainResult:
     """Delayed-acceptance MCMC, chains in lock-step: per generation `inner`
     batched surrogate calls and one batched solver call for the chains whose
     inner chain moved. The inner random-walk proposal is y + step * C xi:
@@ -367,7 +367,10 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
     proposal's). Both moves keep the inner chain reversible with respect to
     the surrogate posterior. All of it is frozen after burn-in, so the
     sampled chain is a fixed reversible kernel whose invariant law is the
-    exact posterior."""
+    exact posterior. With gpu_chain and a surrogate that has chain() (the
+    affine screen), each generation's inner chains run on the GPU in one
+    launch (the same moves, device random numbers), which also returns the
+    screen's log density at the chains' current points for stage 2."""
     w = post.prior.width
     th = np.array(theta0, dtype=np.float64)
     m, d = th.shape
@@ -421,10 +424,16 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
                     Lc = _chol_cov(pts if len(pts) > 2 * d else th, axis)
                 else:
                     Lc = _chol_cov(th, axis)
-        y, ly = th.copy(), ls.copy()
-        a1 = 0.0   # random-walk acceptances (the step adapts to these)
-        n1 = 0
-        for _ in range(inner):
+        use_gpu = gpu_chain and getattr(spost, "gpu_chain_ready", False)
+        if use_gpu:
+            y, ls, ly, a1 = spost.chain(th, inner, step, Lc, axis, axis_prob,
+                                        int(rng.integers(0, 2 ** 63)))
+            n1 = 1
+        else:
+            y, ly = th.copy(), ls.copy()
+            a1 = 0.0   # random-walk acceptances (the step adapts to these)
+            n1 = 0
+        for _ in range(0 if use_gpu else inner):
             prop = y + step * rng.standard_normal((m, d)) @ Lc.T
             corr = np.zeros(m)
             jump = np.zeros(m, dtype=bool)
@@ -454,7 +463,8 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
             th[a], lp[a], ls[a] = y[a], lpy[a], ly[a]
         else:
             a = np.zeros(m, dtype=bool)
-        a1 /= max(n1, 1)
+        if not use_gpu:
+            a1 /= max(n1, 1)
         if k < burn:
             step *= np.exp((a1 - target) / np.sqrt(k + 1.0))
         else:
@@ -870,6 +880,36 @@ class AffineSurrogate:
         self.calls = 0
         self.seconds = 0.0
         self.rebuild(u_ref, steps)
+        h = self.base.handle
+        self.gpu_chain_ready = hasattr(h, "affine_chain")
+        if self.gpu_chain_ready:
+            base_prior = self.prior.base if isinstance(self.prior, LogPrior) else self.prior
+            h.affine_set_prior_mask(base_prior.seed_mask)
+
+    def chain(self, v: np.ndarray, steps: int, step: float, chol: np.ndarray, axis, axis_prob: float,
+              seed: int):
+        """The inner chain of da on the GPU (gbg_affine_chain): `steps` steps
+        for every row of v on this screen's posterior, the same moves as da's
+        host loop (random walk step * chol xi on the coordinates other than
+        `axis`, or with probability axis_prob a redraw of `axis` from its
+        prior conditional). Returns (end points, log pi* at the start points,
+        log pi* at the end points, random-walk acceptance fraction)."""
+        pr = self.prior
+        if isinstance(pr, LogPrior):
+            Ai, log_mask, lo, hi = pr.Ai, sum(1 << i for i in pr.log_idx), pr.base.lo, pr.base.hi
+        else:
+            Ai, log_mask, lo, hi = np.eye(6), 0, pr.lo, pr.hi
+        t0 = time.perf_counter()
+        y, l0, l1, cnt = self.base.handle.affine_chain(
+            v, steps, seed, step=step, chol=chol, axis=-1 if axis is None else axis,
+            axis_prob=axis_prob if axis is not None else 0.0, u_ref=self.u_ref,
+            quad_axis=-1 if self.quad_axis is None else self.quad_axis, Ai=Ai, log_mask=log_mask,
+            lo=lo, hi=hi)
+        self.seconds += time.perf_counter() - t0
+        self.calls += 1
+        self.evals += int(np.atleast_2d(v).shape[0]) * (steps + 1)
+        rw = cnt[:, 1].sum()
+        return y, l0, l1, float(cnt[:, 0].sum() / rw) if rw else 0.0
 
     def _coeffs(self, delta: np.ndarray) -> np.ndarray:
         if self.quad_axis is None:

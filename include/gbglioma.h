@@ -263,6 +263,37 @@ int gbg_adjoint_grad(gbg_handle *h, const gbg_sample *samples, int S, const gbg_
 int gbg_affine_set(gbg_handle *h, int P, const float *phi0, const float *J);
 int gbg_affine_loglik(gbg_handle *h, int B, const double *delta, gbg_lik_result *out);
 
+/* The screening chain on the GPU: `steps` Metropolis steps on
+ *   log pi*(v) = log L(affine model at c(v - u_ref)) + log prior(v)
+ * for B chains in one launch (the first stage of delayed-acceptance MCMC).
+ * v are the sampler's coordinates; u = Ai v, theta_i = exp(u_i) where bit i of
+ * log_mask is set (else u_i); the prior is uniform on lo <= theta <= hi with
+ * the seed voxel rint(theta_2..4) inside the mask set by
+ * gbg_affine_set_prior_mask (n^3 bytes, x fastest), as a density in v (log
+ * prior = sum of the log coordinates' u_i). c(d) = d, or with quad_axis = a
+ * (d, d_a^2 / 2, d_a d_i for i != a) -- the model needs 6 or 12 fields. A step
+ * is, with probability axis_prob, a redraw of coordinate `axis` from its
+ * prior conditional (accepted with the likelihood ratio), otherwise
+ * v + step * chol xi on the other coordinates (chol row-major 6 x 6).
+ * v (B x 6) is updated in place; lp_start / lp_end get log pi* at the chains'
+ * start and end points (-inf outside the prior); counts (B x 4, may be null)
+ * random-walk accepts, random-walk steps, redraw accepts, redraws. seed fixes
+ * the random numbers (counter-based). No reference counterpart. */
+typedef struct {
+    int axis;          /* coordinate redrawn from its prior conditional, -1: none */
+    double axis_prob;  /* probability of a redraw per step */
+    double step;       /* random-walk scale */
+    double chol[36];   /* random-walk factor */
+    double u_ref[6];   /* the affine model's centre */
+    int quad_axis;     /* second-order terms along this coordinate, -1: none */
+    double Ai[36];     /* u = Ai v */
+    int log_mask;      /* bit i: theta_i = exp(u_i) */
+    double lo[6], hi[6];
+} gbg_affine_chain_opts;
+int gbg_affine_set_prior_mask(gbg_handle *h, const unsigned char *mask);
+int gbg_affine_chain(gbg_handle *h, const gbg_affine_chain_opts *o, int B, int steps, unsigned long long seed,
+                     double *v, double *lp_start, double *lp_end, int *counts);
+
 /* ---- learned surrogate (delayed-acceptance screening) ----------------------------
  * No reference counterpart. A small 3D convolutional U-Net maps a sample's
  * parameters (as input channels: the anatomy, a blob at the seed, the
