@@ -626,7 +626,10 @@ int gbg_adjoint_grad(gbg_handle *hh, const gbg_sample *samples, int S, const gbg
         return GBG_ERR_STATE;
     }
     GBG_CUDA_TRY(cudaSetDevice(h.device));
-    return gbg::adjoint_grad(h, samples, S, *o, loglik, grad);
+    int rc = gbg::adjoint_grad(h, samples, S, *o, loglik, grad);
+    // the forward sweep's population kernel reports a barrier timeout here
+    if (!rc) rc = gbg::check_device_status(h);
+    return rc;
 }
 
 int gbg_amr_create(const gbg_amr_config *cfg, gbg_handle **out) {

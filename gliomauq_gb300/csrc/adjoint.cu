@@ -39,6 +39,10 @@
 namespace gbg {
 namespace {
 
+// device memory the default checkpoint interval may take (checkpoints plus
+// one segment's recomputed states)
+constexpr double kAdjointBudget = 96e9;
+
 __device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
 __device__ __forceinline__ int wp(int i, int n) { return i == n - 1 ? 0 : i + 1; }
 
@@ -563,12 +567,22 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     if (f32) {
         if (int rc = fast_build_tables(h, (double)0.1f)) return rc;
     }
+    // checkpoint interval: 50 steps by default (the MALA configuration's),
+    // fewer when the checkpoints and a segment's states would pass
+    // kAdjointBudget bytes, sqrt(steps) at the least memory
     int K = o.checkpoint_every;
-    if (K <= 0) K = std::max(1, (int)std::ceil(std::sqrt((double)nmax)));
+    if (K <= 0) {
+        K = 50;
+        const double per = (double)S * N * sizeof(Real);
+        if ((K + nmax / K + 1) * per > kAdjointBudget) K = std::max(1, (int)std::ceil(std::sqrt((double)nmax)));
+    }
     // without a gradient only the forward pass runs: no checkpoints kept
     if (!grad) K = nmax + 1;
     const int nck = nmax / K + 1;
-    const size_t segs = grad ? (size_t)K : 2;
+    const size_t segs = grad ? (size_t)std::max(K, 2) : 2;
+    // the float forward sweep runs on the batched solver's population kernel,
+    // one launch per checkpoint segment
+    const bool pop_fwd = f32 && population_supported(n);
     // device working set: carved from the handle's grow-only workspace
     const size_t SN = (size_t)S * N;
     const size_t sizes[] = {f32 ? 0 : 4 * N * sizeof(Real), (size_t)nck * SN * sizeof(Real),
@@ -576,7 +590,7 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
                             (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
                             (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
                             3 * S * sizeof(double), S * sizeof(gbg_sample), S * sizeof(gbg_lik_result),
-                            S * sizeof(int)};
+                            S * sizeof(int), 2 * S * sizeof(SampleRec), S * sizeof(int)};
     size_t total = 0;
     for (size_t b : sizes) total += bwork_align(b);
     if (h.adj_ws_bytes < total) {
@@ -590,10 +604,10 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
         }
         h.adj_ws_bytes = total;
     }
-    void *parts[14];
+    void *parts[16];
     {
         char *q = (char *)h.adj_ws;
-        for (int i = 0; i < 14; ++i) {
+        for (int i = 0; i < 16; ++i) {
             parts[i] = q;
             q += bwork_align(sizes[i]);
         }
@@ -613,6 +627,8 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     gbg_sample *dsm = (gbg_sample *)parts[11];
     gbg_lik_result *dlik = (gbg_lik_result *)parts[12];
     int *dns = (int *)parts[13];
+    SampleRec *drec = (SampleRec *)parts[14], *dsorted = drec + S;
+    int *drank = (int *)parts[15];
     // per-step coefficients; a < 0 marks a finished sample
     std::vector<double> ha((size_t)nmax * S), hb((size_t)nmax * S);
     for (int k = 0; k < nmax; ++k)
@@ -669,7 +685,43 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
                                cudaMemcpyDeviceToDevice, st);
     };
     ADJ_TRY(finish(ck, A[0], S));  // samples with no step keep the initial state
-    {
+    if (pop_fwd) {
+        // segment j: steps [jK, min(jK + K, nmax)) of the samples running at
+        // jK, from checkpoint j in seg slot 0, seg slot 1 the second buffer
+        Real *buf0 = seg, *buf1 = seg + SN;
+        std::vector<SampleRec> srec(S);
+        for (int j = 0; j * K < nmax; ++j) {
+            const int k0 = j * K, k1 = std::min(nmax, k0 + K), act = A[k0];
+            if (act <= 0) break;
+            ADJ_TRY(cudaMemcpyAsync(buf0, ck + (size_t)j * SN, (size_t)act * N * sizeof(Real), cudaMemcpyDeviceToDevice,
+                                    st));
+            for (int s = 0; s < act; ++s) {
+                SampleRec r = recs[s];
+                r.nsteps = std::min(ns[s], k1) - k0;
+                if (ns[s] > k1) {  // the segment ends before the sample's shortened last step
+                    r.a2 = r.a;
+                    r.b2 = r.b;
+                }
+                r.order = s;
+                srec[s] = r;
+            }
+            ADJ_TRY(cudaMemcpyAsync(drec, srec.data(), (size_t)act * sizeof(SampleRec), cudaMemcpyHostToDevice, st));
+            rc = population_steps(h, (float *)buf0, (float *)buf1, drec, dsorted, drank, act);
+            if (rc) {
+                release();
+                return rc;
+            }
+            // samples that finish in this segment: their final states
+            for (int s = A[k1]; s < act; ++s) {
+                const Real *src = (((ns[s] - k0) & 1) ? buf1 : buf0) + (size_t)s * N;
+                ADJ_TRY(cudaMemcpyAsync(fin + (size_t)s * N, src, N * sizeof(Real), cudaMemcpyDeviceToDevice, st));
+            }
+            // checkpoint j + 1: the samples still running took all K steps
+            if (grad && k1 < nmax && A[k1] > 0)
+                ADJ_TRY(cudaMemcpyAsync(ck + (size_t)(j + 1) * SN, ((K & 1) ? buf1 : buf0),
+                                        (size_t)A[k1] * N * sizeof(Real), cudaMemcpyDeviceToDevice, st));
+        }
+    } else {
         Real *cur = ck;
         for (int k = 0; k < nmax; ++k) {
             Real *nxt;

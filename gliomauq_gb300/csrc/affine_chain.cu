@@ -18,8 +18,14 @@
 // log-Jacobian of the uniform prior on theta) inside the box lo <= theta <= hi
 // with the seed voxel (rint of theta_2..4) inside the mask, -inf outside.
 //
-// Compiled with -fmad=false: the per-point terms round as the likelihood
-// kernels' do.
+// The per-point likelihood terms are evaluated in float (this GPU's FP64 rate
+// is a small fraction of its FP32 rate, and the screen only has to be one
+// fixed function: the chain returns its own log pi* at the start and end
+// points, which is what the second stage's ratio uses), summed in float per
+// thread and in double across the block. The Bernoulli terms of
+// HGG_Likelihood (:136-153) in a form without cancellation: with
+// q = (u - uc)^2 / slope, alpha = 1 - e^-q / 2 above uc and e^-q / 2 below,
+// so log alpha and log(1 - alpha) are log1p(-e^-q / 2) and log(1/2) - q.
 #include <math_constants.h>
 
 #include <cmath>
@@ -30,7 +36,7 @@
 namespace gbg {
 namespace {
 
-constexpr int kChainThreads = 256;
+constexpr int kChainThreads = 512;
 constexpr int kChainWarps = kChainThreads / 32;
 
 struct ChainArgs {
@@ -138,26 +144,44 @@ __device__ __forceinline__ double affine_phi(const float *cols, int len, int P, 
     return cols[(size_t)(P + 1) * len + i] != 0.f ? (double)x : 0.0;
 }
 
+// log Bernoulli(alpha(u)) of observation y in float, without cancellation
+__device__ __forceinline__ float log_bernoulli_f(float u, float y, float uc, float is2) {
+    const float d = u - uc;
+    const float q = d * d * is2;
+    const float lhalf_q = -0.69314718f - q;          // log(e^-q / 2)
+    const float l1m = log1pf(-0.5f * expf(-q));      // log(1 - e^-q / 2)
+    float la, lna;                                   // log alpha, log(1 - alpha)
+    if (d > 0.f) {
+        la = l1m;
+        lna = lhalf_q;
+    } else if (d < 0.f) {
+        la = lhalf_q;
+        lna = l1m;
+    } else {
+        la = lna = -0.69314718f;
+    }
+    return y == 1.f ? la : lna;
+}
+
 // log L of the model with coefficients s_c (block-wide; the total on thread 0)
 __device__ double eval_lik(const ChainArgs &a, const double *s_c, double (*s_red)[kChainWarps]) {
     float cf[16];
     for (int p = 0; p < a.P; ++p) cf[p] = (float)s_c[p];
-    double sp = 0.0, s1 = 0.0, s2 = 0.0;
+    const float scale = (float)a.pet_scale, uc1 = (float)a.t1_uc, uc2 = (float)a.t2_uc, is2 = (float)a.is2;
+    float fp = 0.f, f1 = 0.f, f2 = 0.f;
     const int items = a.n_pet > a.n_ti ? a.n_pet : a.n_ti;
     for (int i = threadIdx.x; i < items; i += kChainThreads) {
         if (i < a.n_pet) {
-            const double r = affine_phi(a.pet_cols, a.n_pet, a.P, cf, i) - a.pet_scale * a.pet_val[i];
-            sp += r * r;
+            const float r = (float)affine_phi(a.pet_cols, a.n_pet, a.P, cf, i) - scale * (float)a.pet_val[i];
+            fp += r * r;
         }
         if (i < a.n_ti) {
-            const double u = affine_phi(a.ti_cols, a.n_ti, a.P, cf, i);
-            s1 += log_bernoulli(u, a.t1_val[i], a.t1_uc, a.is2);
-            s2 += log_bernoulli(u, a.t2_val[i], a.t2_uc, a.is2);
+            const float u = (float)affine_phi(a.ti_cols, a.n_ti, a.P, cf, i);
+            f1 += log_bernoulli_f(u, (float)a.t1_val[i], uc1, is2);
+            f2 += log_bernoulli_f(u, (float)a.t2_val[i], uc2, is2);
         }
     }
-    sp = warp_sum(sp);
-    s1 = warp_sum(s1);
-    s2 = warp_sum(s2);
+    double sp = warp_sum((double)fp), s1 = warp_sum((double)f1), s2 = warp_sum((double)f2);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0) {
         s_red[0][w] = sp;

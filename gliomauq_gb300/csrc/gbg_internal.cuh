@@ -209,6 +209,15 @@ int fast_build_tables(Handle &h, double ratio);
 int launch_schedule_smooth(Handle &h, const gbg_sample *samples_device, int S, double L, double dt0,
                            SampleRec *dev_out);
 // Gaussian initial densities of S samples (float fields, the batched solver's IC)
+// Population-kernel steps on S float states starting in buf0 (buf1 the
+// second buffer, S x N each): sample s (record s, order = s) takes
+// recs[s].nsteps steps with coefficients a, b, the last one a2, b2, and ends
+// in buffer (nsteps & 1). recs: S device records; sorted / rank: device
+// scratch for S records / ints. Dense kernels only (no temporal blocking, no
+// skipping: the states may be anything).
+int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs, SampleRec *sorted, int *rank,
+                     int S);
+bool population_supported(int n);
 int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, double peak, double sigma,
                        float *phi);
 int fast_steps_single(Handle &h, double Dw, double rho, double dt, long nsteps);

@@ -1303,6 +1303,21 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
 
 }  // namespace
 
+int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs, SampleRec *sorted, int *rank,
+                     int S) {
+    if (!lanes_per_row(h.n)) {
+        set_error("fast path supports n = 32, 64 or 128");
+        return GBG_ERR_UNSUPPORTED;
+    }
+    if (int rc = fast_build_tables(h, (double)0.1f)) return rc;
+    k_sort_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(recs, S, sorted, rank);
+    h.launches++;
+    GBG_CUDA_TRY(cudaGetLastError());
+    return launch_population(h, buf0, buf1, sorted, S, false, false);
+}
+
+bool population_supported(int n) { return lanes_per_row(n) != 0; }
+
 int population_variant_count(int n) {
     PopVariant vs[32];
     return variants_for(n, vs);

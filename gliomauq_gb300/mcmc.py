@@ -336,6 +336,38 @@ def _discrepancy(lp: np.ndarray, ls: np.ndarray) -> float:
     return float(np.std(lp[ok] - ls[ok])) if ok.sum() >= 3 else np.inf
 
 
+def inner_chain(prior, spost, y: np.ndarray, ly: np.ndarray, steps: int, step: float, Lc: np.ndarray,
+                axis, axis_prob: float, rng):
+    """da's first stage on the host: `steps` Metropolis steps on the
+    surrogate posterior for every row of y (log densities ly): with `axis`
+    set, each step is with probability axis_prob a redraw of that coordinate
+    from its prior conditional (prior.redraw_axis; an independence proposal
+    whose prior factors cancel, leaving the surrogate's likelihood ratio),
+    otherwise the random walk y + step * Lc xi on the other coordinates.
+    Returns (end points, their log densities, random-walk acceptances,
+    random-walk steps)."""
+    y, ly = np.array(y, dtype=np.float64, copy=True), np.array(ly, dtype=np.float64, copy=True)
+    m, d = y.shape
+    na = nt = 0
+    for _ in range(steps):
+        prop = y + step * rng.standard_normal((m, d)) @ Lc.T
+        corr = np.zeros(m)
+        jump = np.zeros(m, dtype=bool)
+        if axis is not None:
+            prop[:, axis] = y[:, axis]
+            jump = rng.random(m) < axis_prob
+            if jump.any():
+                prop[jump] = prior.redraw_axis(y[jump], axis, rng)
+                corr[jump] = prior.logp(y[jump]) - prior.logp(prop[jump])
+        lq = spost.logpost(prop)
+        with np.errstate(invalid="ignore"):
+            a = np.isfinite(lq) & (np.log(rng.random(m)) < lq - ly + corr)
+        y[a], ly[a] = prop[a], lq[a]
+        na += int(a[~jump].sum())
+        nt += int((~jump).sum())
+    return y, ly, na, nt
+
+
 def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: int, step: float,
        rng, inner: int = 8, burn: int = 0, target: float = 0.3, chol=None, adapt: bool = False,
        rebuild_every: int = 0, axis=None, axis_prob: float = 0.5,
@@ -424,33 +456,14 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
                     Lc = _chol_cov(pts if len(pts) > 2 * d else th, axis)
                 else:
                     Lc = _chol_cov(th, axis)
-        use_gpu = gpu_chain and getattr(spost, "gpu_chain_ready", False)
-        if use_gpu:
+        if gpu_chain and getattr(spost, "gpu_chain_ready", False):
+            # random-walk acceptance fraction a1 (the step adapts to it)
             y, ls, ly, a1 = spost.chain(th, inner, step, Lc, axis, axis_prob,
                                         int(rng.integers(0, 2 ** 63)))
-            n1 = 1
         else:
-            y, ly = th.copy(), ls.copy()
-            a1 = 0.0   # random-walk acceptances (the step adapts to these)
-            n1 = 0
-        for _ in range(0 if use_gpu else inner):
-            prop = y + step * rng.standard_normal((m, d)) @ Lc.T
-            corr = np.zeros(m)
-            jump = np.zeros(m, dtype=bool)
-            if axis is not None:
-                prop[:, axis] = y[:, axis]
-                jump = rng.random(m) < axis_prob
-                if jump.any():
-                    prop[jump] = post.prior.redraw_axis(y[jump], axis, rng)
-                    # independence proposal from the prior conditional: the
-                    # prior factors cancel, leaving the likelihood ratio
-                    corr[jump] = post.prior.logp(y[jump]) - post.prior.logp(prop[jump])
-            lq = spost.logpost(prop)
-            with np.errstate(invalid="ignore"):
-                a = np.isfinite(lq) & (np.log(rng.random(m)) < lq - ly + corr)
-            y[a], ly[a] = prop[a], lq[a]
-            a1 += a[~jump].sum()
-            n1 += int((~jump).sum())
+            y, ly, na, nt = inner_chain(post.prior, spost, th, ls, inner, step, Lc, axis, axis_prob,
+                                        rng)
+            a1 = na / max(nt, 1)
         moved = np.any(y != th, axis=1)
         if moved.any():
             lpy = np.full(m, -np.inf)
@@ -463,8 +476,6 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
             th[a], lp[a], ls[a] = y[a], lpy[a], ly[a]
         else:
             a = np.zeros(m, dtype=bool)
-        if not use_gpu:
-            a1 /= max(n1, 1)
         if k < burn:
             step *= np.exp((a1 - target) / np.sqrt(k + 1.0))
         else:

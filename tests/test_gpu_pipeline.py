@@ -101,9 +101,10 @@ def _screen(h, an, prior):
 
 
 def test_gpu_screening_chain_evaluates_the_screen_density(gbg):
-    """gbg_affine_chain with 0 steps returns log pi* = the affine model's log L
-    (gbg_affine_loglik) + the prior in the sampler's coordinates, to the
-    last bits of the reduction order (1e-12 relative), -inf outside."""
+    """gbg_affine_chain with 0 steps returns its screen density log pi*: the
+    affine model's log L + the prior in the sampler's coordinates, with the
+    per-point terms in float (within 1e-6 relative + 1e-3 of the double
+    evaluation by gbg_affine_loglik), -inf outside the prior."""
     an = S.make_anatomy(N, seed=4)
     with _lib.Handle(N, "f32", max_samples=64) as h:
         h.set_anatomy(an.p_w, an.p_g)
@@ -119,52 +120,33 @@ def test_gpu_screening_chain_evaluates_the_screen_density(gbg):
     fin = np.isfinite(exp)
     assert np.array_equal(fin, np.isfinite(l0)) and np.array_equal(l0, l1)
     assert not fin[:3].any() and fin[3:].sum() > 10
-    assert np.all(np.abs(l0[fin] - exp[fin]) <= 1e-12 * np.abs(exp[fin]))
+    err = np.abs(l0[fin] - exp[fin])
+    print("float screen vs double: max abs", err.max(), "max rel", (err / np.abs(exp[fin])).max())
+    assert np.all(err <= 1e-6 * np.abs(exp[fin]) + 1e-3)
 
 
-def test_gpu_screening_chain_samples_the_screen_density(gbg):
-    """The GPU inner chain's invariant law is the screen's posterior pi*:
-    the moments of the identified coordinates after 256 chains x 400 steps
-    equal those of importance sampling pi* (evaluated by
-    gbg_affine_loglik) from a widened Laplace Gaussian, within 0.1 sd, and
-    the acceptance of its random-walk moves is in range."""
+def test_gpu_screening_chain_moves_like_the_host_chain(gbg):
+    """The GPU inner chain is the host inner chain (mcmc.inner_chain) with
+    other random numbers: from the same 1024 starting points, after 60
+    steps, the two populations agree in mean (within 5 standard errors of
+    the difference) and spread (10 %), and in random-walk acceptance."""
     an = S.make_anatomy(N, seed=4)
-    with _lib.Handle(N, "f32", max_samples=256) as h:
+    with _lib.Handle(N, "f32", max_samples=1024) as h:
         h.set_anatomy(an.p_w, an.p_g)
         _problem(h, an)
         prior = mcmc.Prior.from_anatomy(an)
         lc, sur, v_map, cov = _screen(h, an, prior)
         Lc = np.linalg.cholesky(mcmc._decoupled(cov, 0))
         rng = np.random.default_rng(5)
-        v0 = lc.prior.redraw_axis(v_map + rng.standard_normal((256, 6)) @ Lc.T, 0, rng)
+        v0 = lc.prior.redraw_axis(v_map + 1.5 * rng.standard_normal((1024, 6)) @ Lc.T, 0, rng)
         v0[~np.isfinite(lc.prior.logp(v0))] = v_map
-        y, _, _, a1 = sur.chain(v0, 100, 2.38 / np.sqrt(5), Lc, 0, 0.5, 7)  # burn-in
-        draws = []
-        for k in range(6):
-            y, _, _, a1 = sur.chain(y, 50, 2.38 / np.sqrt(5), Lc, 0, 0.5, 100 + k)
-            draws.append(y.copy())
-        draws = np.concatenate(draws)
-        # importance sampling of pi* on the identified coordinates
-        q_cov = 2.25 * cov
-        Lq = np.linalg.cholesky(q_cov)
-        x = v_map + rng.standard_normal((20000, 6)) @ Lq.T
-        x = lc.prior.redraw_axis(x, 0, rng)  # the axis from its prior conditional
-        # q density of the identified part times the prior conditional of the
-        # axis: pi*(x) / q(x) = L*(x) m(x_id) / N(x_id)
-        lq_id = -0.5 * np.sum(np.linalg.solve(np.linalg.cholesky(q_cov[1:, 1:]),
-                                              (x[:, 1:] - v_map[1:]).T) ** 2, axis=0)
-        lstar = sur.logpost(x) - lc.prior.logp(x)
-        lw = lstar + lc.prior.axis_log_marginal(x, 0) - lq_id
-        lw = np.where(np.isfinite(lw), lw, -np.inf)
-        w = np.exp(lw - lw.max())
-        w /= w.sum()
-    print("random-walk acceptance", a1, "IS ess", 1.0 / np.sum(w ** 2))
-    assert 0.1 < a1 < 0.6
-    assert 1.0 / np.sum(w ** 2) > 500
-    m_is = w @ x[:, 1:]
-    sd_is = np.sqrt(w @ (x[:, 1:] - m_is) ** 2)
-    m_ch = draws[:, 1:].mean(axis=0)
-    sd_ch = draws[:, 1:].std(axis=0)
-    print("mean diff / sd", (m_ch - m_is) / sd_is, "sd ratio", sd_ch / sd_is)
-    assert np.all(np.abs(m_ch - m_is) < 0.1 * sd_is)
-    assert np.all(np.abs(sd_ch / sd_is - 1) < 0.1)
+        step = 2.38 / np.sqrt(5)
+        yg, _, _, ag = sur.chain(v0, 60, step, Lc, 0, 0.5, 11)
+        yh, _, na, nt = mcmc.inner_chain(lc.prior, sur, v0, sur.logpost(v0), 60, step, Lc, 0, 0.5, rng)
+    ah = na / nt
+    se = np.sqrt((yg.var(axis=0) + yh.var(axis=0)) / len(v0))
+    print("acceptance gpu", ag, "host", ah, "mean diff / se", (yg.mean(axis=0) - yh.mean(axis=0)) / se,
+          "sd ratio", yg.std(axis=0) / yh.std(axis=0))
+    assert abs(ag - ah) < 0.03
+    assert np.all(np.abs(yg.mean(axis=0) - yh.mean(axis=0)) < 5 * se)
+    assert np.all(np.abs(yg.std(axis=0) / yh.std(axis=0) - 1) < 0.1)
