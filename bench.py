@@ -198,9 +198,9 @@ def cpu_baseline(an, prior, seconds=12.0, obs=None):
                           else ""))
 
 
-def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=16,
+def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=64,
                     plain_chains=4, plain_steps=1500, plain_burn=300, ref_generations=500,
-                    plain_cap_s=150.0, unet=True):
+                    plain_cap_s=150.0, unet=True, mala_steps=0, mala_burn=100):
     """Posterior effective samples per second at n^3 on one synthetic
     patient, plain single-solve MCMC against the batched + adjoint +
     surrogate pipeline, both in the scaling symmetry's coordinates
@@ -223,13 +223,20 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=1
     each. A second, longer pipeline run from fresh chains gives the
     reference posterior mean that both samplers' means are checked against
     (2 % per theta coordinate). The learned U-Net surrogate is measured as a
-    stage-1 screen in the same delayed-acceptance sampler."""
+    stage-1 screen in the same delayed-acceptance sampler. With mala_steps,
+    the adjoint MALA configuration too: 64 chains of preconditioned MALA
+    (adjoint gradients, checkpoints every 50 steps), step size adapted to
+    0.574 acceptance during mala_burn steps. The population kernel is the
+    autotuner's choice for both samplers."""
     from gliomauq_gb300 import _lib, mcmc, synthetic as Syn
     an = Syn.make_anatomy(n, seed=0)
     truth = Syn.draw_prior(an, 1, seed=10_000)[0]
     rng = np.random.default_rng(0)
     h = _lib.Handle(n, "f32", device=device, max_samples=512)
     h.set_anatomy(an.p_w, an.p_g)
+    tune_cache = os.path.join(ROOT, "gliomauq_gb300", "_build", "tune.json")
+    os.makedirs(os.path.dirname(tune_cache), exist_ok=True)
+    variant = h.autotune(probe_samples=64, cache_path=tune_cache)
     prior = mcmc.Prior.from_anatomy(an)
     # scaled time grid: the reference's step rule with the reaction's share of
     # the stability bound, per sample, with a shortened last step (smooth in
@@ -366,6 +373,20 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=1
     for k in ("identified", "symmetry_axis", "all"):
         a, b = d_pipe[f"ess_per_s_{k}"], d_plain[f"ess_per_s_{k}"]
         out[f"ess_per_s_ratio_{k}"] = a / b if b > 0 else None
+    out["population_kernel"] = h.population_variant_name(variant)
+    if mala_steps > 0:
+        post_m = mcmc.Posterior(h, an.L, dt0, prior, checkpoint_every=50)
+        lcm = mcmc.LogCoords(post_m, A=mcmc.INVARIANT_MAP)
+        v0 = start_points(64, 1.0)
+        rm = mcmc.mala(lcm, v0, mala_burn + mala_steps, 0.8, rng, burn=mala_burn,
+                       chol=np.linalg.cholesky(res.cov))
+        t_m = rm.seconds * mala_steps / (mala_burn + mala_steps)
+        d_m = diagnostics(lc.to_theta(rm.samples[mala_burn:]), t_m)
+        out["mala"] = dict(sampler="preconditioned MALA (refined Laplace covariance), 64 chains, adjoint "
+                                   "gradients with checkpoints every 50 steps, invariant coordinates",
+                           steps=mala_steps, burn=mala_burn, accept=float(rm.accept), eps=float(rm.step),
+                           ms_per_step=1e3 * rm.seconds / (mala_burn + mala_steps),
+                           mean_check=mean_check(lc.to_theta(rm.samples[mala_burn:])), **d_m)
     if unet:
         out["learned_surrogate"] = unet_screen(h, an, prior, dt0, res, rng)
     h.close()
@@ -644,9 +665,11 @@ def main():
     ap.add_argument("--only-mcmc", action="store_true",
                     help="print the ESS/s comparison alone")
     ap.add_argument("--mcmc-chains", type=int, default=64, help="pipeline chains")
-    ap.add_argument("--mcmc-inner", type=int, default=16, help="surrogate steps per solve")
+    ap.add_argument("--mcmc-inner", type=int, default=64, help="surrogate steps per solve")
     ap.add_argument("--mcmc-generations", type=int, default=300,
                     help="pipeline generations (the first 100 are burn-in)")
+    ap.add_argument("--mala-steps", type=int, default=0,
+                    help="also run the 64-chain adjoint MALA configuration for this many steps")
     ap.add_argument("--samples", type=int, default=S,
                     help="population size (profiling runs use a smaller one)")
     ap.add_argument("--variant", type=int, default=-1,
@@ -661,7 +684,8 @@ def main():
         print(json.dumps({"mcmc": mcmc_comparison(int(os.environ.get("LOCAL_RANK", "0")),
                                                   chains=args.mcmc_chains, inner=args.mcmc_inner,
                                                   generations=args.mcmc_generations,
-                                                  unet=not args.no_surrogate)}))
+                                                  unet=not args.no_surrogate,
+                                                  mala_steps=args.mala_steps)}))
         return
     set_population(args.samples)
 
@@ -801,7 +825,8 @@ def main():
         if not args.no_mcmc:
             line["mcmc"] = mcmc_comparison(local_rank, chains=args.mcmc_chains,
                                            inner=args.mcmc_inner,
-                                           generations=args.mcmc_generations)
+                                           generations=args.mcmc_generations,
+                                           mala_steps=args.mala_steps)
         if not args.no_amr:
             line["amr"] = amr_measurement(local_rank)
             line["amr"]["adaptive"] = amr_adaptive_measurement(local_rank)
