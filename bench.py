@@ -537,6 +537,85 @@ def amr_adaptive_measurement(device, level=4, seed=7, steps_per_regrid=20):
     return out
 
 
+def screen_and_statistics_measurement(device, n=128, chains=64, steps=64, reps=3, stat_samples=512):
+    """Two kernels of the sampling path at n^3 on the bench problem:
+      * the GPU screening chain (k_affine_chain, gbg_affine_chain): `chains`
+        chains x `steps` steps of the tangent screen around the truth, ms per
+        launch (host-timed call including its small copies) and observation
+        points evaluated per second;
+      * the propagation statistics (k_field_stats, gbg_field_statistics) of
+        `stat_samples` fields of n^3 floats resident in HBM, timed with CUDA
+        events on the calling stream, against measured HBM bandwidth on its
+        (2 S + 2) * 4 bytes per cell."""
+    import torch
+    import ctypes as C
+    from gliomauq_gb300 import _lib, mcmc, synthetic as Syn
+    an = Syn.make_anatomy(n, seed=0)
+    truth = Syn.draw_prior(an, 1, seed=10_000)[0]
+    h = _lib.Handle(n, "f32", device=device, max_samples=64)
+    out = {}
+    try:
+        h.set_anatomy(an.p_w, an.p_g)
+        dt0 = -1.0
+        u = h.batch_solve([truth.as_tuple()], an.L, with_loglik=False, want_phi=True, dt0=dt0)["phi"][0]
+        obs = Syn.make_observations(u.astype(np.float64), an, seed=3,
+                                    centre_xyz=(truth.x0, truth.y0, truth.z0), radius_vox=27.0 * n / 128)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2)
+        prior = mcmc.Prior.from_anatomy(an)
+        lc = mcmc.LogCoords(mcmc.Posterior(h, an.L, dt0, prior), A=mcmc.INVARIANT_MAP)
+        v_ref = lc.to_u(np.array([truth.as_tuple()]))[0]
+        d = 0.002 * lc.prior.width
+        sur = mcmc.AffineSurrogate(lc, v_ref, d, quad_axis=0)
+        rng = np.random.default_rng(0)
+        v = v_ref + 0.5 * d * rng.standard_normal((chains, 6))
+        Lc = np.diag(0.5 * d)
+        y, _, _, a1 = sur.chain(v, steps, 1.0, Lc, 0, 0.5, 1)
+        t0 = time.perf_counter()
+        for r in range(reps):
+            y, _, _, a1 = sur.chain(y, steps, 1.0, Lc, 0, 0.5, 2 + r)
+        t = (time.perf_counter() - t0) / reps
+        npts = int(h.observation_counts()[0] + h.observation_counts()[1])
+        out["screen_chain"] = {"kernel": "k_affine_chain", "chains": chains, "steps": steps,
+                               "observation_points": npts, "ms_per_launch": 1e3 * t,
+                               "us_per_step": 1e6 * t / steps,
+                               "points_per_s": chains * steps * npts / t, "random_walk_accept": a1}
+    finally:
+        h.close()
+    gbg = _lib.load()
+    dev = torch.device(f"cuda:{device}")
+    N = n ** 3
+    f = torch.rand((stat_samples, N), dtype=torch.float32, device=dev)
+    mean = torch.empty(N, dtype=torch.float32, device=dev)
+    var = torch.empty(N, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+
+    def stats():
+        rc = gbg.gbg_field_statistics(n, C.c_void_p(f.data_ptr()), stat_samples, 1, C.c_void_p(mean.data_ptr()),
+                                      C.c_void_p(var.data_ptr()), C.c_void_p(st.cuda_stream))
+        if rc:
+            raise RuntimeError(gbg.gbg_last_error())
+
+    stats()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        stats()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    peak, peak_kind = measured_peaks()
+    alg = (2 * stat_samples + 2) * 4.0 * N
+    out["field_statistics"] = {"kernel": "k_field_stats", "samples": stat_samples, "grid": n,
+                               "ms_per_launch": ms, "algorithmic_bytes": alg,
+                               "achieved_gbs": alg / (ms / 1e3) / 1e9, "peak_gbs": peak,
+                               "frac": alg / (ms / 1e3) / 1e9 / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                               "note": "inputs larger than L2 (the fields are read twice)"}
+    del f, mean, var
+    torch.cuda.empty_cache()
+    return out
+
+
 def surrogate_measurement(device, n=128, batch=32, reps=5):
     """Forward throughput of the bf16 U-Net surrogate at n^3 (its grid is
     (n/2)^3): milliseconds per sample of gbg_surrogate_loglik (features,
@@ -664,6 +743,8 @@ def main():
                     help="print the surrogate-network measurement alone (profiling runs)")
     ap.add_argument("--only-mcmc", action="store_true",
                     help="print the ESS/s comparison alone")
+    ap.add_argument("--only-kernels", action="store_true",
+                    help="print the screening-chain and propagation-statistics measurement alone")
     ap.add_argument("--mcmc-chains", type=int, default=64, help="pipeline chains")
     ap.add_argument("--mcmc-inner", type=int, default=64, help="surrogate steps per solve")
     ap.add_argument("--mcmc-generations", type=int, default=300,
@@ -679,6 +760,10 @@ def main():
         return run_reference_arm(args)
     if args.only_surrogate:
         print(json.dumps({"surrogate": surrogate_measurement(int(os.environ.get("LOCAL_RANK", "0")))}))
+        return
+    if args.only_kernels:
+        print(json.dumps({"sampling_kernels": screen_and_statistics_measurement(
+            int(os.environ.get("LOCAL_RANK", "0")))}))
         return
     if args.only_mcmc:
         print(json.dumps({"mcmc": mcmc_comparison(int(os.environ.get("LOCAL_RANK", "0")),
@@ -830,6 +915,7 @@ def main():
         if not args.no_amr:
             line["amr"] = amr_measurement(local_rank)
             line["amr"]["adaptive"] = amr_adaptive_measurement(local_rank)
+        line["sampling_kernels"] = screen_and_statistics_measurement(local_rank)
         if not args.no_surrogate:
             line["surrogate"] = surrogate_measurement(local_rank)
         print(json.dumps(line))

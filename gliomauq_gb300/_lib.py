@@ -37,7 +37,7 @@ EXPORTS = [
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
     "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_affine_set_prior_mask",
-    "gbg_affine_chain", "gbg_surrogate_set_engine",
+    "gbg_affine_chain", "gbg_observation_counts", "gbg_surrogate_set_engine",
     "gbg_set_slopes", "gbg_get_slopes", "gbg_mala_step", "gbg_run_mala",
     "gbg_population_variant_name",
 ]
@@ -193,6 +193,7 @@ def load(path: str = LIB_PATH):
         "gbg_affine_set": [vp, C.c_int, fp, fp],
         "gbg_affine_loglik": [vp, C.c_int, dp, C.POINTER(LikResult)],
         "gbg_affine_set_prior_mask": [vp, vp],
+        "gbg_observation_counts": [vp, C.POINTER(C.c_long), C.POINTER(C.c_long)],
         "gbg_affine_chain": [vp, C.POINTER(AffineChainOpts), C.c_int, C.c_int, C.c_ulonglong, dp, dp, dp, vp],
         "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
                                C.POINTER(LikParams), vp, vp],
@@ -391,6 +392,12 @@ class Handle:
         lik = (LikResult * B)()
         check(self.lib.gbg_affine_loglik(self._h, B, dptr(d), lik))
         return np.array([lik[i].total for i in range(B)])
+
+    def observation_counts(self):
+        """(PET voxels, T1/T2 points) of the observation lists."""
+        a, b = C.c_long(), C.c_long()
+        check(self.lib.gbg_observation_counts(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def affine_set_prior_mask(self, mask):
         """The prior's seed-voxel mask ([z, y, x] bool) for affine_chain."""

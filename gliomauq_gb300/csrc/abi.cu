@@ -925,6 +925,21 @@ int gbg_affine_loglik(gbg_handle *hh, int B, const double *delta, gbg_lik_result
     return GBG_OK;
 }
 
+int gbg_observation_counts(gbg_handle *hh, long *n_pet, long *n_ti) {
+    if (int rc = check_handle(hh)) return rc;
+    if (!n_pet || !n_ti) {
+        set_error("null output");
+        return GBG_ERR_ARG;
+    }
+    if (!hh->h.obs.valid) {
+        set_error("observations not set");
+        return GBG_ERR_STATE;
+    }
+    *n_pet = hh->h.obs.n_pet;
+    *n_ti = hh->h.obs.n_ti;
+    return GBG_OK;
+}
+
 int gbg_affine_set_prior_mask(gbg_handle *hh, const unsigned char *mask) {
     if (int rc = check_handle(hh)) return rc;
     Handle &h = hh->h;

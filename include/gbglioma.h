@@ -291,6 +291,9 @@ typedef struct {
     double lo[6], hi[6];
 } gbg_affine_chain_opts;
 int gbg_affine_set_prior_mask(gbg_handle *h, const unsigned char *mask);
+/* entries of the observation lists gbg_set_observations built: PET voxels and
+ * T1/T2 points */
+int gbg_observation_counts(gbg_handle *h, long *n_pet, long *n_ti);
 int gbg_affine_chain(gbg_handle *h, const gbg_affine_chain_opts *o, int B, int steps, unsigned long long seed,
                      double *v, double *lp_start, double *lp_end, int *counts);
 
