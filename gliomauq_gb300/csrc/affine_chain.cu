@@ -232,12 +232,15 @@ __global__ void __launch_bounds__(kChainThreads) k_affine_chain(ChainArgs a) {
             if (jump) {
                 redraw_axis(a, y, uniform01(a.seed, b, s, 1));
             } else {
+                // normals in float: their precision does not matter, the
+                // state they move stays double
                 double xi[6];
                 for (int k = 0; k < 3; ++k) {
-                    const double r = sqrt(-2.0 * log(uniform01(a.seed, b, s, 2 + 2 * k)));
-                    const double ang = 6.283185307179586 * uniform01(a.seed, b, s, 3 + 2 * k);
-                    xi[2 * k] = r * cos(ang);
-                    xi[2 * k + 1] = r * sin(ang);
+                    const float r = sqrtf(-2.0f * logf((float)uniform01(a.seed, b, s, 2 + 2 * k)));
+                    float sn, cs;
+                    sincospif(2.0f * (float)uniform01(a.seed, b, s, 3 + 2 * k), &sn, &cs);
+                    xi[2 * k] = (double)(r * cs);
+                    xi[2 * k + 1] = (double)(r * sn);
                 }
                 for (int i = 0; i < 6; ++i) {
                     double d = 0.0;
