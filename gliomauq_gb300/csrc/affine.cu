@@ -9,6 +9,8 @@
 // evaluation forms the B models' densities there inside the likelihood
 // reduction: per model (P + 2) floats per observation instead of a whole
 // n^3 field written and read back.
+#include <algorithm>
+
 #include "gbg_internal.cuh"
 
 namespace gbg {
@@ -27,6 +29,10 @@ __global__ void k_affine_gather(int len, const int *__restrict__ idx, size_t N, 
         for (int p = 0; p < P; ++p) cols[(size_t)(1 + p) * len + i] = J[(size_t)p * N + c];
         cols[(size_t)(P + 1) * len + i] = msk[c];
     }
+}
+
+__global__ void k_to_float(int n, const double *__restrict__ a, float *__restrict__ b) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (float)a[i];
 }
 
 }  // namespace
@@ -52,6 +58,25 @@ int affine_gather_columns(Handle &h) {
             h.launches++;
         }
         dst += (size_t)(P + 2) * lens[l];
+    }
+    // the observation values in float for the screening chain: PET, T1, T2
+    const size_t nf = (size_t)h.obs.n_pet + 2 * (size_t)h.obs.n_ti;
+    if (nf > h.aff_obs_f_cap) {
+        if (h.aff_obs_f) cudaFree(h.aff_obs_f);
+        h.aff_obs_f = nullptr;
+        h.aff_obs_f_cap = 0;
+        GBG_CUDA_TRY(cudaMalloc((void **)&h.aff_obs_f, nf * sizeof(float)));
+        h.aff_obs_f_cap = nf;
+    }
+    const double *srcs[3] = {h.obs.pet_val, h.obs.t1_val, h.obs.t2_val};
+    const int lens3[3] = {h.obs.n_pet, h.obs.n_ti, h.obs.n_ti};
+    float *fd = h.aff_obs_f;
+    for (int l = 0; l < 3; ++l) {
+        if (lens3[l] > 0) {
+            k_to_float<<<std::min((lens3[l] + 255) / 256, h.num_sms * 8), 256, 0, h.stream>>>(lens3[l], srcs[l], fd);
+            h.launches++;
+        }
+        fd += lens3[l];
     }
     GBG_CUDA_TRY(cudaGetLastError());
     h.aff_cols_stale = false;

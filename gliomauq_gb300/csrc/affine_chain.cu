@@ -47,7 +47,7 @@ struct ChainArgs {
     unsigned long long seed;
     const float *pet_cols, *ti_cols;
     int n_pet, n_ti;
-    const double *pet_val, *t1_val, *t2_val;
+    const float *pet_val, *t1_val, *t2_val;
     double pet_scale, t1_uc, t2_uc, is2, pet_sigma2;
     double *v, *lp_start, *lp_end;
     int *counts;
@@ -137,11 +137,11 @@ __device__ void coefficients(const ChainArgs &a, const double *v, double *c) {
     }
 }
 
-__device__ __forceinline__ double affine_phi(const float *cols, int len, int P, const float *cf, int i) {
+__device__ __forceinline__ float affine_phi(const float *cols, int len, int P, const float *cf, int i) {
     float x = cols[i];
     for (int p = 0; p < P; ++p) x = fmaf(cf[p], cols[(size_t)(1 + p) * len + i], x);
     x = fminf(fmaxf(x, 0.f), 1.f);
-    return cols[(size_t)(P + 1) * len + i] != 0.f ? (double)x : 0.0;
+    return cols[(size_t)(P + 1) * len + i] != 0.f ? x : 0.f;
 }
 
 // log Bernoulli(alpha(u)) of observation y in float, without cancellation
@@ -172,13 +172,13 @@ __device__ double eval_lik(const ChainArgs &a, const double *s_c, double (*s_red
     const int items = a.n_pet > a.n_ti ? a.n_pet : a.n_ti;
     for (int i = threadIdx.x; i < items; i += kChainThreads) {
         if (i < a.n_pet) {
-            const float r = (float)affine_phi(a.pet_cols, a.n_pet, a.P, cf, i) - scale * (float)a.pet_val[i];
+            const float r = affine_phi(a.pet_cols, a.n_pet, a.P, cf, i) - scale * a.pet_val[i];
             fp += r * r;
         }
         if (i < a.n_ti) {
-            const float u = (float)affine_phi(a.ti_cols, a.n_ti, a.P, cf, i);
-            f1 += log_bernoulli_f(u, (float)a.t1_val[i], uc1, is2);
-            f2 += log_bernoulli_f(u, (float)a.t2_val[i], uc2, is2);
+            const float u = affine_phi(a.ti_cols, a.n_ti, a.P, cf, i);
+            f1 += log_bernoulli_f(u, a.t1_val[i], uc1, is2);
+            f2 += log_bernoulli_f(u, a.t2_val[i], uc2, is2);
         }
     }
     double sp = warp_sum((double)fp), s1 = warp_sum((double)f1), s2 = warp_sum((double)f2);
@@ -342,9 +342,9 @@ int affine_chain(Handle &h, const gbg_affine_chain_opts &o, int B, int steps, un
     a.ti_cols = h.aff_cols + (size_t)(P + 2) * h.obs.n_pet;
     a.n_pet = h.obs.n_pet;
     a.n_ti = h.obs.n_ti;
-    a.pet_val = h.obs.pet_val;
-    a.t1_val = h.obs.t1_val;
-    a.t2_val = h.obs.t2_val;
+    a.pet_val = h.aff_obs_f;
+    a.t1_val = h.aff_obs_f + h.obs.n_pet;
+    a.t2_val = h.aff_obs_f + h.obs.n_pet + h.obs.n_ti;
     a.pet_scale = h.obs.pet_scale;
     a.t1_uc = h.obs.t1_uc;
     a.t2_uc = h.obs.t2_uc;
