@@ -275,8 +275,8 @@ int lik_evaluate_population(Handle &h, const float *buf0, const float *buf1,
 }  // namespace gbg
 
 // ---- gbg_loglik_noalloc: the same reduction with library-owned scratch ------
-// Callers that cannot allocate device memory (graph capture in progress, an
-// external allocator owning the device, a fixed real-time budget) get this
+// Callers that cannot allocate device memory (an external allocator owning
+// the device, a fixed real-time budget) get this
 // variant: its partial sums live in a fixed file-scope device array instead of
 // a handle's buffer, so the entry point allocates nothing. The array is shared
 // by every call; each call overwrites every partial it later reads, so nothing

@@ -522,9 +522,8 @@ int gbg_autotune(gbg_handle *h, int probe_samples, const char *cache_path, int *
 
 /* ---- log-likelihood without any allocation -----------------------------------
  * No counterpart in the reference: an addition for callers that cannot
- * allocate device memory -- code running while a CUDA graph is being
- * captured, a host framework whose device memory is owned by its own
- * allocator, or a real-time loop with a fixed memory budget. It evaluates the
+ * allocate device memory -- a host framework whose device memory is owned by
+ * its own allocator, or a real-time loop with a fixed memory budget. It evaluates the
  * same log-likelihood as gbg_loglik for one density field, without a handle,
  * and calls no cudaMalloc, cudaFree or other allocating routine.
  *
@@ -548,8 +547,7 @@ int gbg_autotune(gbg_handle *h, int probe_samples, const char *cache_path, int *
  * first call in a CUDA context (the primary context of a device, a context
  * the caller made current with the driver API, or the new primary context
  * after cudaDeviceReset) looks that array's address up with the context
- * current, so make the first call in each context before any stream capture
- * on it. Every call
+ * current. Every call
  * shares the array: calls whose kernels may overlap on the GPU (different
  * streams, or different host threads) race and must be serialised by the
  * caller. Lists longer than the maximum are rejected with GBG_ERR_ARG. */

@@ -1,7 +1,6 @@
 """GPU: gbg_loglik_noalloc, the log-likelihood entry point that allocates
-nothing (for callers that cannot call cudaMalloc: code running during CUDA
-graph capture, hosts whose device memory belongs to another allocator, fixed
-real-time budgets). Called through the C ABI twice in a row, each result must
+nothing (for callers that cannot call cudaMalloc: hosts whose device memory
+belongs to another allocator, fixed real-time budgets). Called through the C ABI twice in a row, each result must
 match the handle-based gbg_loglik on the same field and observations, and the
 CPU oracle (pinned to the reference's likelihood program), which shares no
 code with the two GPU entry points.
