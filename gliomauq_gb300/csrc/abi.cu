@@ -78,7 +78,7 @@ void free_handle(Handle &h) {
     void *ptrs[] = {h.pw, h.pg, h.phi[0], h.phi[1], h.b0, h.dfx, h.dfy, h.dfz, h.cx, h.cy, h.cz,
                     h.msk, h.cxs, h.sr[0], h.sr[1], h.sd[0], h.sd[1], h.mala_tt, h.bphi[0], h.bphi[1], h.bwork, h.dev_status, h.barrier,
                     h.obs.pet_idx, h.obs.pet_val, h.obs.ti_idx, h.obs.t1_val, h.obs.t2_val,
-                    h.lik_partials, h.lik_out, h.adj_ws, h.aff_phi0, h.aff_J, h.aff_cols, h.aff_delta, h.aff_mask, h.aff_chain, h.aff_obs_f,
+                    h.lik_partials, h.lik_out, h.adj_ws, h.aff_phi0, h.aff_J, h.aff_cols, h.aff_delta, h.aff_mask, h.aff_chain, h.aff_rec,
                     h.tile_live, h.live_list, h.live_count};
     for (void *p : ptrs)
         if (p) cudaFree(p);

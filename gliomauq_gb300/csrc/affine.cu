@@ -31,8 +31,19 @@ __global__ void k_affine_gather(int len, const int *__restrict__ idx, size_t N, 
     }
 }
 
-__global__ void k_to_float(int n, const double *__restrict__ a, float *__restrict__ b) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (float)a[i];
+// one 16-float record per observation point for the screening chain: phi0,
+// the P basis fields, the mask, then the observation values (PET; or T1, T2),
+// zero padding
+__global__ void k_affine_records(int len, int P, const float *__restrict__ cols, const double *__restrict__ v1,
+                                 const double *__restrict__ v2, float4 *__restrict__ rec) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+        float r[16];
+        for (int k = 0; k < 16; ++k) r[k] = 0.f;
+        for (int k = 0; k < P + 2; ++k) r[k] = cols[(size_t)k * len + i];
+        r[P + 2] = (float)v1[i];
+        if (v2) r[P + 3] = (float)v2[i];
+        for (int q = 0; q < 4; ++q) rec[(size_t)i * 4 + q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+    }
 }
 
 }  // namespace
@@ -59,24 +70,24 @@ int affine_gather_columns(Handle &h) {
         }
         dst += (size_t)(P + 2) * lens[l];
     }
-    // the observation values in float for the screening chain: PET, T1, T2
-    const size_t nf = (size_t)h.obs.n_pet + 2 * (size_t)h.obs.n_ti;
-    if (nf > h.aff_obs_f_cap) {
-        if (h.aff_obs_f) cudaFree(h.aff_obs_f);
-        h.aff_obs_f = nullptr;
-        h.aff_obs_f_cap = 0;
-        GBG_CUDA_TRY(cudaMalloc((void **)&h.aff_obs_f, nf * sizeof(float)));
-        h.aff_obs_f_cap = nf;
-    }
-    const double *srcs[3] = {h.obs.pet_val, h.obs.t1_val, h.obs.t2_val};
-    const int lens3[3] = {h.obs.n_pet, h.obs.n_ti, h.obs.n_ti};
-    float *fd = h.aff_obs_f;
-    for (int l = 0; l < 3; ++l) {
-        if (lens3[l] > 0) {
-            k_to_float<<<std::min((lens3[l] + 255) / 256, h.num_sms * 8), 256, 0, h.stream>>>(lens3[l], srcs[l], fd);
-            h.launches++;
+    // per-point records for the screening chain (P + 4 <= 16 floats)
+    const size_t npts = (size_t)h.obs.n_pet + (size_t)h.obs.n_ti;
+    if (P + 4 <= 16) {
+        if (npts > h.aff_rec_cap) {
+            if (h.aff_rec) cudaFree(h.aff_rec);
+            h.aff_rec = nullptr;
+            h.aff_rec_cap = 0;
+            GBG_CUDA_TRY(cudaMalloc((void **)&h.aff_rec, (npts ? npts : 1) * 4 * sizeof(float4)));
+            h.aff_rec_cap = npts ? npts : 1;
         }
-        fd += lens3[l];
+        if (h.obs.n_pet > 0)
+            k_affine_records<<<std::min((h.obs.n_pet + 255) / 256, h.num_sms * 8), 256, 0, h.stream>>>(
+                h.obs.n_pet, P, h.aff_cols, h.obs.pet_val, nullptr, h.aff_rec);
+        if (h.obs.n_ti > 0)
+            k_affine_records<<<std::min((h.obs.n_ti + 255) / 256, h.num_sms * 8), 256, 0, h.stream>>>(
+                h.obs.n_ti, P, h.aff_cols + (size_t)(P + 2) * h.obs.n_pet, h.obs.t1_val, h.obs.t2_val,
+                h.aff_rec + (size_t)h.obs.n_pet * 4);
+        h.launches += 2;
     }
     GBG_CUDA_TRY(cudaGetLastError());
     h.aff_cols_stale = false;

@@ -18,7 +18,9 @@
 // log-Jacobian of the uniform prior on theta) inside the box lo <= theta <= hi
 // with the seed voxel (rint of theta_2..4) inside the mask, -inf outside.
 //
-// The per-point likelihood terms are evaluated in float (this GPU's FP64 rate
+// Each observation point's model (phi0, the basis fields, the mask) and its
+// observed values are one 16-float record (affine.cu builds them), read with
+// four vector loads. The per-point likelihood terms are evaluated in float (this GPU's FP64 rate
 // is a small fraction of its FP32 rate, and the screen only has to be one
 // fixed function: the chain returns its own log pi* at the start and end
 // points, which is what the second stage's ratio uses), summed in float per
@@ -45,9 +47,8 @@ struct ChainArgs {
     double u_ref[6], chol[36], Ai[36], lo[6], hi[6], ulo[6], uhi[6];
     const unsigned char *mask;
     unsigned long long seed;
-    const float *pet_cols, *ti_cols;
+    const float4 *rec;  // per observation point, PET list then T1/T2 list: 16 floats
     int n_pet, n_ti;
-    const float *pet_val, *t1_val, *t2_val;
     double pet_scale, t1_uc, t2_uc, is2, pet_sigma2;
     double *v, *lp_start, *lp_end;
     int *counts;
@@ -137,13 +138,6 @@ __device__ void coefficients(const ChainArgs &a, const double *v, double *c) {
     }
 }
 
-__device__ __forceinline__ float affine_phi(const float *cols, int len, int P, const float *cf, int i) {
-    float x = cols[i];
-    for (int p = 0; p < P; ++p) x = fmaf(cf[p], cols[(size_t)(1 + p) * len + i], x);
-    x = fminf(fmaxf(x, 0.f), 1.f);
-    return cols[(size_t)(P + 1) * len + i] != 0.f ? x : 0.f;
-}
-
 // log Bernoulli(alpha(u)) of observation y in float, without cancellation
 __device__ __forceinline__ float log_bernoulli_f(float u, float y, float uc, float is2) {
     const float d = u - uc;
@@ -163,22 +157,39 @@ __device__ __forceinline__ float log_bernoulli_f(float u, float y, float uc, flo
     return y == 1.f ? la : lna;
 }
 
-// log L of the model with coefficients s_c (block-wide; the total on thread 0)
+// log L of the model with coefficients s_c (block-wide; the total on thread 0).
+// Point i (PET list first, then the T1/T2 list) is one 16-float record:
+// phi0, J_0 .. J_{P-1}, mask, then PET or T1, T2.
+template <int P>
 __device__ double eval_lik(const ChainArgs &a, const double *s_c, double (*s_red)[kChainWarps]) {
-    float cf[16];
-    for (int p = 0; p < a.P; ++p) cf[p] = (float)s_c[p];
+    float cf[P];
+#pragma unroll
+    for (int p = 0; p < P; ++p) cf[p] = (float)s_c[p];
     const float scale = (float)a.pet_scale, uc1 = (float)a.t1_uc, uc2 = (float)a.t2_uc, is2 = (float)a.is2;
     float fp = 0.f, f1 = 0.f, f2 = 0.f;
-    const int items = a.n_pet > a.n_ti ? a.n_pet : a.n_ti;
+    const int items = a.n_pet + a.n_ti;
+#pragma unroll 2
     for (int i = threadIdx.x; i < items; i += kChainThreads) {
-        if (i < a.n_pet) {
-            const float r = affine_phi(a.pet_cols, a.n_pet, a.P, cf, i) - scale * a.pet_val[i];
-            fp += r * r;
+        float x[16];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float4 v = __ldg(a.rec + (size_t)i * 4 + q);
+            x[4 * q] = v.x;
+            x[4 * q + 1] = v.y;
+            x[4 * q + 2] = v.z;
+            x[4 * q + 3] = v.w;
         }
-        if (i < a.n_ti) {
-            const float u = affine_phi(a.ti_cols, a.n_ti, a.P, cf, i);
-            f1 += log_bernoulli_f(u, a.t1_val[i], uc1, is2);
-            f2 += log_bernoulli_f(u, a.t2_val[i], uc2, is2);
+        float u = x[0];
+#pragma unroll
+        for (int p = 0; p < P; ++p) u = fmaf(cf[p], x[1 + p], u);
+        u = fminf(fmaxf(u, 0.f), 1.f);
+        if (x[P + 1] == 0.f) u = 0.f;
+        if (i < a.n_pet) {
+            const float r = u - scale * x[P + 2];
+            fp += r * r;
+        } else {
+            f1 += log_bernoulli_f(u, x[P + 2], uc1, is2);
+            f2 += log_bernoulli_f(u, x[P + 3], uc2, is2);
         }
     }
     double sp = warp_sum((double)fp), s1 = warp_sum((double)f1), s2 = warp_sum((double)f2);
@@ -202,6 +213,7 @@ __device__ double eval_lik(const ChainArgs &a, const double *s_c, double (*s_red
     return total;
 }
 
+template <int P>
 __global__ void __launch_bounds__(kChainThreads) k_affine_chain(ChainArgs a) {
     const int b = blockIdx.x;
     __shared__ double s_c[16];
@@ -218,7 +230,7 @@ __global__ void __launch_bounds__(kChainThreads) k_affine_chain(ChainArgs a) {
     }
     __syncthreads();
     {
-        const double L = s_eval ? eval_lik(a, s_c, s_red) : 0.0;
+        const double L = s_eval ? eval_lik<P>(a, s_c, s_red) : 0.0;
         if (threadIdx.x == 0) {
             ly = s_eval ? L + lpv : -CUDART_INF;
             a.lp_start[b] = ly;
@@ -254,7 +266,7 @@ __global__ void __launch_bounds__(kChainThreads) k_affine_chain(ChainArgs a) {
             s_eval = isfinite(lpy) ? 1 : 0;
         }
         __syncthreads();
-        const double L = s_eval ? eval_lik(a, s_c, s_red) : 0.0;
+        const double L = s_eval ? eval_lik<P>(a, s_c, s_red) : 0.0;
         if (threadIdx.x == 0) {
             const double lq = s_eval ? L + lpy : -CUDART_INF;
             // a prior-conditional redraw: its proposal density cancels the prior
@@ -338,13 +350,9 @@ int affine_chain(Handle &h, const gbg_affine_chain_opts &o, int B, int steps, un
     }
     a.mask = h.aff_mask;
     a.seed = seed;
-    a.pet_cols = h.aff_cols;
-    a.ti_cols = h.aff_cols + (size_t)(P + 2) * h.obs.n_pet;
+    a.rec = h.aff_rec;
     a.n_pet = h.obs.n_pet;
     a.n_ti = h.obs.n_ti;
-    a.pet_val = h.aff_obs_f;
-    a.t1_val = h.aff_obs_f + h.obs.n_pet;
-    a.t2_val = h.aff_obs_f + h.obs.n_pet + h.obs.n_ti;
     a.pet_scale = h.obs.pet_scale;
     a.t1_uc = h.obs.t1_uc;
     a.t2_uc = h.obs.t2_uc;
@@ -355,7 +363,10 @@ int affine_chain(Handle &h, const gbg_affine_chain_opts &o, int B, int steps, un
     a.lp_end = d_l1;
     a.counts = d_cnt;
     GBG_CUDA_TRY(cudaMemcpyAsync(d_v, v, (size_t)B * 6 * sizeof(double), cudaMemcpyHostToDevice, h.stream));
-    k_affine_chain<<<B, kChainThreads, 0, h.stream>>>(a);
+    if (P == 12)
+        k_affine_chain<12><<<B, kChainThreads, 0, h.stream>>>(a);
+    else
+        k_affine_chain<6><<<B, kChainThreads, 0, h.stream>>>(a);
     h.launches++;
     GBG_CUDA_TRY(cudaGetLastError());
     GBG_CUDA_TRY(cudaMemcpyAsync(v, d_v, (size_t)B * 6 * sizeof(double), cudaMemcpyDeviceToHost, h.stream));

@@ -159,8 +159,8 @@ struct Handle {
     double *aff_delta = nullptr;
     size_t aff_delta_cap = 0;  // doubles
     unsigned char *aff_mask = nullptr;  // the prior's seed-voxel mask (n^3, affine chain)
-    float *aff_obs_f = nullptr;         // PET, T1, T2 observation values as float (affine chain)
-    size_t aff_obs_f_cap = 0;
+    float4 *aff_rec = nullptr;          // per observation point: model + value, 16 floats (affine chain)
+    size_t aff_rec_cap = 0;             // points
     void *aff_chain = nullptr;          // affine chain scratch, grow-only
     size_t aff_chain_bytes = 0;
 };
