@@ -37,7 +37,7 @@ EXPORTS = [
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
     "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_affine_set_prior_mask",
-    "gbg_affine_chain", "gbg_observation_counts", "gbg_surrogate_set_engine",
+    "gbg_affine_chain", "gbg_observation_counts", "gbg_synthetic_observations", "gbg_surrogate_set_engine",
     "gbg_set_slopes", "gbg_get_slopes", "gbg_mala_step", "gbg_run_mala",
     "gbg_population_variant_name",
 ]
@@ -108,6 +108,11 @@ class AffineChainOpts(C.Structure):
                 ("chol", C.c_double * 36), ("u_ref", C.c_double * 6), ("quad_axis", C.c_int),
                 ("Ai", C.c_double * 36), ("log_mask", C.c_int), ("lo", C.c_double * 6),
                 ("hi", C.c_double * 6)]
+
+
+class SyntheticOpts(C.Structure):
+    _fields_ = [("uc_t1", C.c_double), ("uc_t2", C.c_double), ("alpha", C.c_double),
+                ("seed48", C.c_ulonglong)]
 
 
 class BatchOpts(C.Structure):
@@ -194,6 +199,8 @@ def load(path: str = LIB_PATH):
         "gbg_affine_loglik": [vp, C.c_int, dp, C.POINTER(LikResult)],
         "gbg_affine_set_prior_mask": [vp, vp],
         "gbg_observation_counts": [vp, C.POINTER(C.c_long), C.POINTER(C.c_long)],
+        "gbg_synthetic_observations": [C.c_int, dp, C.c_int, vp, C.POINTER(SyntheticOpts), dp, dp, dp,
+                                       C.POINTER(C.c_float)],
         "gbg_affine_chain": [vp, C.POINTER(AffineChainOpts), C.c_int, C.c_int, C.c_ulonglong, dp, dp, dp, vp],
         "gbg_loglik_noalloc": [vp, C.c_int, vp, vp, C.c_long, vp, vp, vp, C.c_long,
                                C.POINTER(LikParams), vp, vp],
@@ -598,6 +605,27 @@ class AmrHandle:
         s = AmrRunStats()
         check(self.lib.gbg_amr_last_run_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in AmrRunStats._fields_}
+
+
+def synthetic_observations(tumor, block_order=None, uc_t1=0.8, uc_t2=0.3, alpha=0.02, seed48=0):
+    """PET, T1, T2 ([z, y, x] float64) and the centre of mass (3 floats) the
+    reference's synthetic-data program makes from a tumour density
+    (gbg_synthetic_observations); block_order: (level, ix, iy, iz) rows in
+    the grid's loop order, None for x fastest."""
+    lib = load()
+    t = np.ascontiguousarray(tumor, dtype=np.float64)
+    n = t.shape[0]
+    pet, t1, t2 = (np.empty_like(t) for _ in range(3))
+    com = (C.c_float * 3)()
+    o = SyntheticOpts(uc_t1, uc_t2, alpha, seed48)
+    if block_order is None:
+        nb, bp = 0, None
+    else:
+        b = np.ascontiguousarray(block_order, dtype=np.int32).reshape(-1, 4)
+        nb, bp = b.shape[0], b.ctypes.data
+    check(lib.gbg_synthetic_observations(n, dptr(t), nb, bp, C.byref(o), dptr(pet), dptr(t1), dptr(t2),
+                                         com))
+    return pet, t1, t2, np.array(list(com), dtype=np.float32)
 
 
 def amr_ghost_tables(blocks):

@@ -18,9 +18,9 @@ LIB = os.path.join(PKG, "libgbglioma.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr"]
-NOFMA = {"rd_exact.cu", "likelihood.cu", "amr.cu", "propagation.cu", "affine_chain.cu"}
+NOFMA = {"rd_exact.cu", "likelihood.cu", "amr.cu", "propagation.cu", "affine_chain.cu", "synthetic.cu"}
 SOURCES = ["abi.cu", "rd_exact.cu", "rd_fast.cu", "likelihood.cu", "amr.cu", "amr_plan.cu", "adjoint.cu",
-           "surrogate.cu", "affine.cu", "affine_chain.cu", "propagation.cu"]
+           "surrogate.cu", "affine.cu", "affine_chain.cu", "propagation.cu", "synthetic.cu"]
 
 
 def nvcc() -> str:

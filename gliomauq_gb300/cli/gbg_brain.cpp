@@ -1,5 +1,6 @@
-// gbg_brain: the `brain -anatomy HGG_UQ` program on libgbglioma, with the
-// reference's file contract (source/Glioma/Glioma_HG_UQ.cpp):
+// gbg_brain: the `brain -anatomy HGG_UQ` program on libgbglioma (and
+// `-anatomy syntheticData`, below), with the reference's file contract
+// (source/Glioma/Glioma_HG_UQ.cpp):
 //   reads   HGG_InputParameters.txt  (Dw [cm^2/day], rho [1/day], tend [day])
 //           HGG_TumorIC.bin          (tumour centre, float32, unit coordinates)
 //           ../../Anatmoy/PatientNN/PNN_{GM,WM,CSF,T1,T2}.dat (Matrix::D3D)
@@ -39,11 +40,65 @@ int fail(const std::string &m, int code = 1) {
     return code;
 }
 
+// -anatomy syntheticData (Glioma_ProcessSyntheticData): HGG_data.dat ->
+// PET_data.dat, T1_data.dat, T2_data.dat and HGG_TumorIC.bin (the centre of
+// mass, 3 floats; the reference program writes 12 floats, of which the
+// last 9 are whatever follows its 3-float buffer). -blockorder FILE gives
+// the grid's block loop order (lines "level ix iy iz"), default x fastest;
+// -seed48 the drand48 state before the first draw (default 0, glibc's
+// unseeded state).
+int synthetic_data(Args &args) {
+    if (args.as_int("-adaptive", 0) != 0) return fail("syntheticData: only -adaptive 0 is supported");
+    const int bpd = args.as_int("-bpd", 4);
+    int level = 0;
+    while ((1 << level) < bpd) ++level;
+    if ((1 << level) != bpd) return fail("-bpd must be a power of two");
+    const int n = bpd * 16;
+    Matrix T;
+    try {
+        T = gbgcli::read_matrix("HGG_data.dat", 3);
+    } catch (const std::exception &e) {
+        return fail(e.what());
+    }
+    if (T.nx < n || T.ny < n || T.nz < n) return fail("HGG_data.dat is smaller than the grid");
+    // the grid's cells read the file's [0, n)^3 corner, as the program does
+    std::vector<double> u((size_t)n * n * n);
+    for (int z = 0; z < n; ++z)
+        for (int y = 0; y < n; ++y)
+            for (int x = 0; x < n; ++x) u[(size_t)x + (size_t)n * ((size_t)y + (size_t)n * z)] = T(x, y, z);
+    std::vector<gbg_block> order;
+    const std::string of = args.as_string("-blockorder", "");
+    if (!of.empty()) {
+        std::ifstream in(of);
+        gbg_block b;
+        while (in >> b.level >> b.ix >> b.iy >> b.iz) order.push_back(b);
+        if (order.empty()) return fail("cannot read the block order " + of);
+    }
+    gbg_synthetic_opts o = {0.8, 0.3, 0.02, (unsigned long long)std::strtoull(
+                                               args.as_string("-seed48", "0").c_str(), nullptr, 0)};
+    std::vector<double> pet(u.size()), t1(u.size()), t2(u.size());
+    float com[3];
+    if (gbg_synthetic_observations(n, u.data(), (int)order.size(), order.empty() ? nullptr : order.data(), &o,
+                                   pet.data(), t1.data(), t2.data(), com) != GBG_OK)
+        return fail(gbg_last_error(), 4);
+    gbgcli::write_d3d("PET_data.dat", n, n, n, pet);
+    gbgcli::write_d3d("T1_data.dat", n, n, n, t1);
+    gbgcli::write_d3d("T2_data.dat", n, n, n, t2);
+    FILE *f = std::fopen("HGG_TumorIC.bin", "wb");
+    if (!f) return fail("cannot write HGG_TumorIC.bin");
+    std::fwrite(com, sizeof(float), 3, f);
+    std::fclose(f);
+    if (args.as_int("-verbose", 0)) std::printf("centre of mass %f %f %f\n", com[0], com[1], com[2]);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
     Args args{argc, argv};
-    if (args.as_string("-anatomy", "") != "HGG_UQ") return fail("only -anatomy HGG_UQ is supported");
+    if (args.as_string("-anatomy", "") == "syntheticData") return synthetic_data(args);
+    if (args.as_string("-anatomy", "") != "HGG_UQ")
+        return fail("only -anatomy HGG_UQ and syntheticData are supported");
     const bool adaptive = args.as_int("-adaptive", 0) != 0;
     const int pID = args.as_int("-pID", 0);
     const int bpd = args.as_int("-bpd", 4);

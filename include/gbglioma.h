@@ -479,6 +479,33 @@ typedef struct {
 } gbg_amr_run_stats;
 int gbg_amr_last_run_stats(gbg_handle *h, gbg_amr_run_stats *stats);
 
+/* ---- synthetic observations -----------------------------------------------------
+ * PET, T1 and T2 observations from a tumour density as the reference's
+ * synthetic-data program makes them (brain -anatomy syntheticData,
+ * Glioma_ProcessSyntheticData.cpp:61-104 and 107-221, run :406-430) in its
+ * float Real: PET = u where u >= uc_t2, T1 = [u >= uc_t1], T2 = [u >= uc_t2];
+ * PET normalised by its maximum; noise alpha * N(0, 1) from drand48 pairs
+ * through Box-Muller on the cells with PET > 0, a pair drawn at every cell
+ * visited while the count of noised cells is even; normalised again; the
+ * centre of mass (unit cube, float sums in loop order) of the noised PET
+ * (what the program writes to HGG_TumorIC.bin). The loops visit the blocks
+ * of the uniform 16^3-block grid in `order` (nblocks = (n/16)^3 blocks of
+ * gbg_block; the reference's order comes from MRAG's node map, ordered by
+ * node address) or, with order null, x fastest; cells x fastest inside a
+ * block. tumor, pet, t1, t2: n^3 doubles, x fastest (HGG_data.dat and the
+ * PET/T1/T2_data.dat contents); n = 16 * 2^l. The program's values are
+ * uc_t1 = 0.8, uc_t2 = 0.3, alpha = 0.02 and the unseeded drand48 state (0
+ * with glibc). Fails with GBG_ERR_ARG when no cell reaches uc_t2 (the
+ * program divides by a zero maximum). */
+typedef struct {
+    double uc_t1, uc_t2;   /* T1 / T2 thresholds */
+    double alpha;          /* noise standard deviation (0: none) */
+    unsigned long long seed48;  /* drand48 state before the first draw */
+} gbg_synthetic_opts;
+int gbg_synthetic_observations(int n, const double *tumor, int nblocks, const gbg_block *order,
+                               const gbg_synthetic_opts *o, double *pet, double *t1, double *t2,
+                               float *centre_of_mass);
+
 /* ---- introspection ---------------------------------------------------------- */
 /* number of kernels this handle has launched since creation */
 int gbg_launch_count(gbg_handle *h, long long *count);

@@ -176,3 +176,87 @@ def propagation_stats(fields, reference_rules=True):
             a[:, 0, :] = 0
             a[:, :, 0] = 0
     return mean, var
+
+
+DRAND48_A = 0x5DEECE66D
+DRAND48_C = 0xB
+# drand48's state in a program that never seeds it: zero with glibc (POSIX
+# leaves it unspecified; other C libraries start at 0x1234ABCD330E)
+DRAND48_UNSEEDED = 0
+_M48 = (1 << 48) - 1
+
+
+def synthetic_observations(tumor, block_order, uc_t1=0.8, uc_t2=0.3, alpha=0.02, seed=DRAND48_UNSEEDED):
+    """Synthetic PET/T1/T2 observations from a tumour density as the
+    reference's Glioma_ProcessSyntheticData does them in Real = float
+    (source/Glioma/Glioma_ProcessSyntheticData.cpp): _ic (:61-104, PET = the
+    density where it is >= uc_t2 else 0, T1/T2 = density >= uc_t1 / uc_t2),
+    then run() (:406-430): _getPETstatistic (:107-153: max, and the centre of
+    mass summed in float in the grid's loop order), _normalizePETsignal
+    (:156-173), _addNoise (:176-221: drand48 pairs through Box-Muller, a new
+    pair at every cell while the count of noised cells is even, the first
+    value to a noised cell, the second kept for the next), statistics,
+    normalisation. tumor: [z, y, x] array (n = 16 * 2^l); block_order: the
+    grid's blocks (level, ix, iy, iz) in the order its loops visit them.
+    Returns (PET, T1, T2 as float64 arrays of the float values, centre of
+    mass as 3 float32)."""
+    import math
+    f32 = np.float32
+    t = np.asarray(tumor)
+    n = t.shape[0]
+    pet = t.astype(np.float32)
+    phi = np.where(pet >= f32(uc_t2), pet, f32(0)).astype(np.float32).reshape(-1)
+    t1 = (pet >= f32(uc_t1)).astype(np.float64)
+    t2 = (pet >= f32(uc_t2)).astype(np.float64)
+    # cell indices and x, y, z positions (float, as BlockInfo::pos) in loop order
+    cells, pos = [], []
+    for (lv, bx, by, bz) in np.asarray(block_order, dtype=np.int64):
+        hf = f32(2.0 ** -int(lv) / 16)
+        org = [f32(b * 2.0 ** -int(lv)) for b in (bx, by, bz)]
+        z, y, x = np.meshgrid(np.arange(16), np.arange(16), np.arange(16), indexing="ij")
+        gx, gy, gz = 16 * bx + x.ravel(), 16 * by + y.ravel(), 16 * bz + z.ravel()
+        cells.append(gx + n * (gy + n * gz))
+        pos.append(np.stack([(org[0] + hf * x.ravel().astype(np.float32)).astype(np.float32),
+                             (org[1] + hf * y.ravel().astype(np.float32)).astype(np.float32),
+                             (org[2] + hf * z.ravel().astype(np.float32)).astype(np.float32)], axis=1))
+    cells = np.concatenate(cells)
+    pos = np.concatenate(pos).astype(np.float64)
+
+    def statistic():
+        mx = f32(0)
+        mass, c = f32(0), [f32(0)] * 3
+        for k in np.flatnonzero(phi[cells] != 0):
+            p = phi[cells[k]]
+            mx = max(mx, p)
+            mass = f32(mass + p)
+            c = [f32(float(c[j]) + pos[k, j] * float(p)) for j in range(3)]
+        return mx, np.array([f32(cj / mass) for cj in c], dtype=np.float32)
+
+    def normalize(mx):
+        iscale = 1.0 / float(mx)
+        phi[:] = (phi.astype(np.float64) * iscale).astype(np.float32)
+
+    mx, com = statistic()
+    normalize(mx)
+    state, ncount, xi1, xi2 = seed, 0, 0.0, 0.0
+
+    def drand48():
+        nonlocal state
+        state = (DRAND48_A * state + DRAND48_C) & _M48
+        return state / float(1 << 48)
+
+    for c in cells:
+        if ncount % 2 == 0:
+            u1, u2 = drand48(), drand48()
+            r = math.sqrt(-2.0 * math.log(u1))
+            xi1 = r * math.cos(2.0 * math.pi * u2)
+            xi2 = r * math.sin(2.0 * math.pi * u2)
+        if phi[c] > 0:
+            v = float(phi[c]) + alpha * xi1
+            phi[c] = f32(v if 0.0 < v else 0.0)
+            xi1 = xi2
+            ncount += 1
+    mx, com = statistic()
+    normalize(mx)
+    shape = (n, n, n)
+    return phi.reshape(shape).astype(np.float64), t1, t2, com

@@ -418,6 +418,48 @@ def propagation_fixture():
         json.dump(out, f, indent=1)
 
 
+SYNTHETIC = [dict(n=64, centre=(30.3, 35.1, 28.7), radius=9.0), dict(n=32, centre=(14.6, 17.2, 15.9), radius=6.5)]
+
+
+def synthetic_tumour(n, centre, radius):
+    """A tumour-like density on n^3 made with correctly rounded operations
+    only (+, -, *, /, sqrt and integer arithmetic), so any platform makes the
+    same bits: a linear fall-off from 1.05 at the centre to 0 at twice the
+    radius, plus a +-0.02 integer-hash texture, clipped to [0, 1], as float
+    values."""
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    r = np.sqrt((x - centre[0]) ** 2 + (y - centre[1]) ** 2 + (z - centre[2]) ** 2)
+    h = ((7 * x + 13 * y + 29 * z + 3 * x * y + 5 * y * z) % 1009).astype(np.float64) / 1009.0
+    u = np.clip(1.05 - r / (2.0 * radius) * 1.05 + 0.04 * (h - 0.5), 0.0, 1.0)
+    return u.astype(np.float32).astype(np.float64)
+
+
+def synthetic_fixture():
+    """The reference's own synthetic-data program (Glioma_ProcessSyntheticData
+    built unmodified, FP32, through oracle/synthetic_main.cpp, which also
+    writes the grid's block loop order) on seeded tumours: hashes of its
+    PET/T1/T2_data.dat, its HGG_TumorIC.bin centre of mass and the block
+    order. The 32^3 case uses the program built for 2 blocks per dimension."""
+    out = []
+    for case in SYNTHETIC:
+        n = case["n"]
+        u = synthetic_tumour(n, case["centre"], case["radius"])
+        with tempfile.TemporaryDirectory() as td:
+            matrix_io.write_d3d(os.path.join(td, "HGG_data.dat"), u)
+            prog = "synthetic" if n == 64 else "synthetic_b2"
+            subprocess.run([os.path.join(refio.REF_DIR, prog), "-anatomy", "syntheticData", "-adaptive", "0",
+                            "-vtk", "0", "-verbose", "0", "-nthreads", "1"], cwd=td, check=True, capture_output=True)
+            res = {k: matrix_io.read_d3d(os.path.join(td, f"{k}_data.dat")) for k in ("PET", "T1", "T2")}
+            com = np.fromfile(os.path.join(td, "HGG_TumorIC.bin"), dtype="<f4")[:3]
+            order = np.loadtxt(os.path.join(td, "block_order.txt"), dtype=int).reshape(-1, 4)
+        out.append(dict(case, tumour_cells=int((u.astype(np.float32) >= np.float32(0.3)).sum()),
+                        block_order=order.tolist(), centre_of_mass=[float(c) for c in com],
+                        **{f"{k.lower()}_sha256": sha(v) for k, v in res.items()},
+                        pet_sum=float(res["PET"].sum())))
+    with open(os.path.join(HERE, "synthetic.json"), "w") as f:
+        json.dump(out, f)
+
+
 def cli_observations(u):
     """Observations of a model field, deterministic from a seed (numpy only)."""
     rng = np.random.default_rng(21)
@@ -439,6 +481,9 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "propagation":
         propagation_fixture()
         sys.exit(0)
+    if len(sys.argv) > 1 and sys.argv[1] == "synthetic":
+        synthetic_fixture()
+        sys.exit(0)
     if len(sys.argv) > 1 and sys.argv[1] == "adaptive":
         adaptive_fixture()
         cli_adaptive_fixture()
@@ -452,5 +497,6 @@ if __name__ == "__main__":
     cli_fixture()
     cli_adaptive_fixture()
     propagation_fixture()
+    synthetic_fixture()
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
