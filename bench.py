@@ -388,7 +388,16 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=6
                            ms_per_step=1e3 * rm.seconds / (mala_burn + mala_steps),
                            mean_check=mean_check(lc.to_theta(rm.samples[mala_burn:])), **d_m)
     if unet:
-        out["learned_surrogate"] = unet_screen(h, an, prior, dt0, res, rng)
+        out["learned_surrogate"] = ls = unet_screen(h, an, prior, dt0, res, rng)
+        # what the trained network gains: the same delayed-acceptance sampler
+        # with the network as its screen, against the tangent screen and
+        # against no screen (the plain chains)
+        out["screen_gain"] = {"identified_ess_per_s": {
+            "learned_screen": ls["da_identified_ess_per_s"],
+            "tangent_screen": d_pipe["ess_per_s_identified"],
+            "no_screen_plain": d_plain["ess_per_s_identified"]},
+            "stage2_accept": {"learned_screen": ls["da_stage2_accept"],
+                              "tangent_screen": float(res.result.history["stage2_accept"])}}
     h.close()
     return out
 
@@ -423,8 +432,14 @@ def unet_screen(h, an, prior, dt0, res, rng, train_n=256, epochs=10, gens=20, in
         t_eval = (time.perf_counter() - t0) / len(near)
         aff = mcmc.AffineSurrogate(post, res.v_map, 0.5 * np.sqrt(np.diag(res.cov)), quad_axis=0)
         aff_err = float(np.std(exact - aff.logpost(near)))
+        t0 = time.perf_counter()
         r = mcmc.da(post, sp, near, gens, 2.38 / np.sqrt(6), rng, inner=inner, burn=0, chol=Lc)
+        t_da = time.perf_counter() - t0
+        v = r.samples  # the chains' draws in the invariant coordinates
+        moved = float(np.mean(np.any(v[1:] != v[:-1], axis=2))) if len(v) > 1 else 0.0
         return {"params": sg.nparams(), "train_samples": train_n, "epochs": epochs,
+                "da_seconds": t_da, "da_fraction_of_chain_steps_that_moved": moved,
+                "da_identified_ess_per_s": float(mcmc.ess(v)[1:].min() / t_da) if moved > 0 else 0.0,
                 "train_seconds": t_train, "train_loss": loss, "heldout_density_rel_l2": dens,
                 "seconds_per_eval": t_eval,
                 "logpost_error_sd_near_mode": float(np.std(exact - approx)),
