@@ -475,11 +475,13 @@ def amr_measurement(device, level=4, steps=20, err_steps=60):
     out = {"grid": f"{len(blocks)} blocks of 16^3 at level {level} ({n}^3), periodic "
                    f"same-level ghost tables", "steps_timed": steps}
     fields = {}
-    for mode in ("f64", "f32ref", "f32"):
+    for mode in ("f64", "f32ref", "f32", "f32_separate"):
         real = 8 if mode == "f64" else 4
         d, g = (Dw, Dg) if mode == "f64" else (float(np.float32(Dw)),
                                                float(np.float32(np.float32(0.1) * np.float32(Dw))))
-        with _lib.AmrHandle(len(blocks), mode, device=device) as h:
+        with _lib.AmrHandle(len(blocks), "f32" if mode == "f32_separate" else mode, device=device) as h:
+            if mode == "f32_separate":
+                h.set_fast_variant(1)
             h.set_grid(blocks, pw, pg, amr.to_block_major(phi, level))
             h.set_ghosts(*tables)
             h.step(d, g, rho, dt, 2)
@@ -492,17 +494,24 @@ def amr_measurement(device, level=4, steps=20, err_steps=60):
             fields[mode] = amr.from_block_major(h.get_phi(), level)
         cells = len(blocks) * 4096
         # per cell-step: phi read + write and the cell's tables (exact modes:
-        # brain sum and six double face diffusivities; fast mode: six float
-        # face coefficients and the mask); per ghost (1736 per block): source
-        # value, weight (double), source block and cell (int), CSR start
-        # (long), ghost write
-        tab_bytes = 7 * 4 if mode == "f32" else real + 48
-        per_cell = 2 * real + tab_bytes + (1736 / 4096) * (real + 8 + 4 + 4 + 8 + real)
+        # brain sum and six double face diffusivities; fast mode with a
+        # separate ghost pass: six float face coefficients and the mask); per
+        # ghost (1736 per block): source value, weight (double), source block
+        # and cell (int), CSR start (long), ghost write and read. The fused
+        # fast mode: per-face floats (3 x 17/16 per cell), a mask byte, and
+        # per ghost a 32-bit start, source index, float weight and the
+        # source value, no ghost array.
+        if mode == "f32":
+            per_cell = 2 * real + 3 * 4 * 17 / 16 + 1 + (1736 / 4096) * (4 + 4 + 4 + 4)
+        else:
+            tab_bytes = 7 * 4 if mode == "f32_separate" else real + 48
+            per_cell = 2 * real + tab_bytes + (1736 / 4096) * (real + 8 + 4 + 4 + 8 + real)
         rate = cells * steps / sec
         out[mode] = {"cell_steps_per_s": rate, "seconds_per_step": sec / steps,
                      "algorithmic_bytes_per_cell_step": per_cell,
                      "algorithmic_gb_per_s": rate * per_cell / 1e9}
     b = fields["f64"]
+    out["f32_fused_equals_separate"] = bool(np.array_equal(fields["f32"], fields["f32_separate"]))
     for mode in ("f32ref", "f32"):
         out[f"{mode}_vs_f64_rel_l2"] = float(np.linalg.norm(fields[mode] - b) / np.linalg.norm(b))
     out["error_after_steps"] = err_steps

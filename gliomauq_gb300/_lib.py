@@ -37,7 +37,7 @@ EXPORTS = [
     "gbg_surrogate_nparams", "gbg_surrogate_get_params", "gbg_surrogate_set_params",
     "gbg_surrogate_train", "gbg_surrogate_loss_grad", "gbg_surrogate_features",
     "gbg_surrogate_loglik", "gbg_affine_set", "gbg_affine_loglik", "gbg_affine_set_prior_mask",
-    "gbg_affine_chain", "gbg_observation_counts", "gbg_synthetic_observations", "gbg_surrogate_set_engine",
+    "gbg_affine_chain", "gbg_observation_counts", "gbg_synthetic_observations", "gbg_amr_fast_variant", "gbg_surrogate_set_engine",
     "gbg_set_slopes", "gbg_get_slopes", "gbg_mala_step", "gbg_run_mala",
     "gbg_population_variant_name",
 ]
@@ -199,6 +199,7 @@ def load(path: str = LIB_PATH):
         "gbg_affine_loglik": [vp, C.c_int, dp, C.POINTER(LikResult)],
         "gbg_affine_set_prior_mask": [vp, vp],
         "gbg_observation_counts": [vp, C.POINTER(C.c_long), C.POINTER(C.c_long)],
+        "gbg_amr_fast_variant": [vp, C.c_int],
         "gbg_synthetic_observations": [C.c_int, dp, C.c_int, vp, C.POINTER(SyntheticOpts), dp, dp, dp,
                                        C.POINTER(C.c_float)],
         "gbg_affine_chain": [vp, C.POINTER(AffineChainOpts), C.c_int, C.c_int, C.c_ulonglong, dp, dp, dp, vp],
@@ -538,6 +539,10 @@ class AmrHandle:
     def step(self, Dw, Dg, rho, dt, nsteps=1):
         """Enqueues the steps on the handle's stream (returns before they finish)."""
         check(self.lib.gbg_amr_step(self._h, Dw, Dg, rho, dt, nsteps))
+
+    def set_fast_variant(self, variant: int):
+        """Fast FP32 step form: 0 fused ghosts (default), 1 separate ghost pass."""
+        check(self.lib.gbg_amr_fast_variant(self._h, variant))
 
     def sync(self):
         check(self.lib.gbg_sync(self._h))

@@ -731,6 +731,17 @@ int gbg_amr_step(gbg_handle *hh, double Dw, double Dg, double rho, double dt, lo
     return gbg::amr_steps(hh->h, Dw, Dg, rho, dt, nsteps);
 }
 
+int gbg_amr_fast_variant(gbg_handle *hh, int variant) {
+    if (int rc = check_amr(hh)) return rc;
+    if (variant < 0 || variant > 1) {
+        set_error("fast variant: 0 (fused) or 1 (separate ghost pass)");
+        return GBG_ERR_ARG;
+    }
+    if (hh->h.amr.fast_variant != variant) hh->h.amr.tables_valid = false;  // the layouts differ
+    hh->h.amr.fast_variant = variant;
+    return GBG_OK;
+}
+
 int gbg_amr_get_phi(gbg_handle *hh, double *phi) {
     if (int rc = check_amr(hh)) return rc;
     if (!phi || hh->h.amr.nb < 1) {

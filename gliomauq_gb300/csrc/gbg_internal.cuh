@@ -57,6 +57,11 @@ struct AmrState {
     long *gstart = nullptr;    // ghost-table offsets, nb*1736+1
     int *gsrc_block = nullptr, *gsrc_cell = nullptr;
     double *gw = nullptr;
+    // fast FP32 mode: the tables in 32-bit form for the fused step (offsets,
+    // source cell as block * 4096 + cell, float weights)
+    int *gstart32 = nullptr, *gsrc32 = nullptr;
+    float *gw32 = nullptr;
+    int fast_variant = 0;      // 0: fused ghosts, per-face tables; 1: separate ghost pass
     double *detail = nullptr;  // FWT maxima per block
     void *pw2 = nullptr, *pg2 = nullptr;  // remap targets
     int *bidx = nullptr;       // block index (ix, iy, iz) per block

@@ -374,6 +374,11 @@ int gbg_amr_set_ghosts(gbg_handle *h, const long *start, const int *src_block, c
  * BlockProcessing::pipeline_process(rhs) + process(update) do on the MRAG
  * grid (source/Glioma/Glioma_HG_UQ.cpp:266-277). */
 int gbg_amr_step(gbg_handle *h, double Dw, double Dg, double rho, double dt, long nsteps);
+/* GBG_PREC_F32 block grids: the form of the step, both with the same
+ * results bit for bit. 0 (default): ghosts evaluated while each block's lab
+ * is filled, face coefficients stored once per face; 1: a separate ghost
+ * pass and per-cell tables (kept for comparison). */
+int gbg_amr_fast_variant(gbg_handle *h, int variant);
 int gbg_amr_get_phi(gbg_handle *h, double *phi);
 /* per block: the largest interpolating-wavelet detail magnitude of phi,
  * BlockFWT::multichannel_fwt + FWTReport::getOverAll_DetailMaxMag
