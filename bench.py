@@ -769,6 +769,8 @@ def main():
                     help="print the ESS/s comparison alone")
     ap.add_argument("--only-kernels", action="store_true",
                     help="print the screening-chain and propagation-statistics measurement alone")
+    ap.add_argument("--only-amr", action="store_true",
+                    help="print the multiresolution-grid measurement alone")
     ap.add_argument("--mcmc-chains", type=int, default=64, help="pipeline chains")
     ap.add_argument("--mcmc-inner", type=int, default=64, help="surrogate steps per solve")
     ap.add_argument("--mcmc-generations", type=int, default=300,
@@ -784,6 +786,12 @@ def main():
         return run_reference_arm(args)
     if args.only_surrogate:
         print(json.dumps({"surrogate": surrogate_measurement(int(os.environ.get("LOCAL_RANK", "0")))}))
+        return
+    if args.only_amr:
+        dev = int(os.environ.get("LOCAL_RANK", "0"))
+        res = amr_measurement(dev)
+        res["adaptive"] = amr_adaptive_measurement(dev)
+        print(json.dumps({"amr": res}))
         return
     if args.only_kernels:
         print(json.dumps({"sampling_kernels": screen_and_statistics_measurement(
