@@ -351,11 +351,34 @@ __global__ void __launch_bounds__(256) k_amr_fast_step_fused(int nb, RegionTable
             const int x = c % BS, y = (c / BS) % BS, z = c / (BS * BS);
             lab[(x + 1) + LS * ((y + 1) + LS * (z + 1))] = pb[c];
         }
-        for (int g = threadIdx.x; g < NG; g += blockDim.x) {
-            const long i = (long)b * NG + g;
-            float acc = 0.0f;
-            for (int k = gstart[i]; k < gstart[i + 1]; ++k) acc = acc + phi[gsrc[k]] * gw[k];
-            lab[ghost_lab(rt, g)] = acc;
+        // the thread's ghosts (at most kGhostsPerThread) with their loads
+        // batched: all offsets, then every first term's source and weight,
+        // then those sources, then any further terms -- each ghost's sum
+        // still starts from 0 and adds its terms in table order
+        {
+            constexpr int kG = (NG + 255) / 256;
+            int st[kG], en[kG], s0[kG];
+            float w0[kG], acc[kG];
+#pragma unroll
+            for (int j = 0; j < kG; ++j) {
+                const int g = threadIdx.x + 256 * j;
+                const long i = (long)b * NG + (g < NG ? g : 0);
+                st[j] = g < NG ? gstart[i] : 0;
+                en[j] = g < NG ? gstart[i + 1] : 0;
+            }
+#pragma unroll
+            for (int j = 0; j < kG; ++j) {
+                s0[j] = st[j] < en[j] ? gsrc[st[j]] : 0;
+                w0[j] = st[j] < en[j] ? gw[st[j]] : 0.0f;
+            }
+#pragma unroll
+            for (int j = 0; j < kG; ++j) acc[j] = st[j] < en[j] ? 0.0f + phi[s0[j]] * w0[j] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < kG; ++j) {
+                for (int k = st[j] + 1; k < en[j]; ++k) acc[j] = acc[j] + phi[gsrc[k]] * gw[k];
+                const int g = threadIdx.x + 256 * j;
+                if (g < NG) lab[ghost_lab(rt, g)] = acc[j];
+            }
         }
         __syncthreads();
         const double h = 1.0 / (double)((1 << level[b]) * BS);
