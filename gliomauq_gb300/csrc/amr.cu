@@ -330,7 +330,8 @@ __global__ void k_amr_fast_faces(int nb, RegionTable rt, const float *__restrict
 
 // One CTA per block: the block's cells and its ghosts (evaluated from the
 // tables in slot order, as k_ghost_eval does) into an 18^3 lab, then 256
-// threads update 16 cells each with the per-face coefficients.
+// threads update 16 cells each with the per-face coefficients. Launched with
+// 256 threads (the loops' strides).
 __global__ void __launch_bounds__(256) k_amr_fast_step_fused(int nb, RegionTable rt, const int *__restrict__ level,
                                                              const float *__restrict__ phi,
                                                              const int *__restrict__ gstart,
@@ -347,7 +348,9 @@ __global__ void __launch_bounds__(256) k_amr_fast_step_fused(int nb, RegionTable
     for (int b = blockIdx.x; b < nb; b += gridDim.x) {
         __syncthreads();
         const float *pb = phi + (size_t)b * BC;
-        for (int c = threadIdx.x; c < BC; c += blockDim.x) {
+#pragma unroll 8
+        for (int j = 0; j < BC / 256; ++j) {
+            const int c = threadIdx.x + 256 * j;
             const int x = c % BS, y = (c / BS) % BS, z = c / (BS * BS);
             lab[(x + 1) + LS * ((y + 1) + LS * (z + 1))] = pb[c];
         }
@@ -386,7 +389,9 @@ __global__ void __launch_bounds__(256) k_amr_fast_step_fused(int nb, RegionTable
         const float bb = (float)(dt * rho);
         const float *fxb = fx + (size_t)b * NFX, *fyb = fy + (size_t)b * NFX, *fzb = fz + (size_t)b * NFX;
         const unsigned char *mb = mask + (size_t)b * BC;
-        for (int c = threadIdx.x; c < BC; c += blockDim.x) {
+#pragma unroll 4
+        for (int j = 0; j < BC / 256; ++j) {
+            const int c = threadIdx.x + 256 * j;
             const int x = c % BS, y = (c / BS) % BS, z = c / (BS * BS);
             const int l = (x + 1) + LS * ((y + 1) + LS * (z + 1));
             const float f0 = lab[l];
