@@ -485,26 +485,18 @@ __global__ void __launch_bounds__(256, MINB) k_population10(PopArgs p) {
             const int y0 = (t % p.tiles_y) * rows, z0 = (t / p.tiles_y) * p.TZ;
             const int y1 = y0 + rows - 1, z1 = z0 + p.TZ - 1;
             bool go = span_hits(ylo, yhi, k + 1, y0, y1, n) && span_hits(zlo, zhi, k + 1, z0, z1, n);
-            const bool rewrite = k == 1 && !p.tile_live[t];
-            if (go && rewrite) go = span_hits(ylo, yhi, 0, y0, y1, n) && span_hits(zlo, zhi, 0, z0, z1, n);
+            if (go && k == 1 && !p.tile_live[t])
+                go = span_hits(ylo, yhi, 0, y0, y1, n) && span_hits(zlo, zhi, 0, z0, z1, n);
             if (!go) continue;
-            // the same test for this warp's rows alone: a row outside the
-            // grown y range holds zeros in both buffers by the tile argument,
-            // row by row; a warp skips only when all its rows may (its lanes
-            // exchange values inside the march)
-            const int yr = y0 + (int)(threadIdx.x / LR);
-            if (__all_sync(0xffffffffu, !span_hits(ylo, yhi, rewrite ? 0 : k + 1, yr, yr, n))) continue;
             const size_t off = (size_t)order * p.stride;
             const bool last = k == p.rec[r].nsteps - 1;
             march_tile_s<LR, UNR>(n, p.TZ, y0, z0, in + off, out + off, p.cxs, p.cy, p.cz,
                                   last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
-            ++visited;  // rows of LR lanes: counted per lane, LR lanes per row
+            ++visited;
         }
         if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) break;
     }
-    // rows computed by this CTA: each lane counted its row's marches
-    visited = __reduce_add_sync(0xffffffffu, (unsigned)visited);
-    if ((threadIdx.x & 31) == 0 && visited) atomicAdd(p.visited, visited / LR);
+    if (threadIdx.x == 0 && visited) atomicAdd(p.visited, visited);
 }
 
 // Liveness of the tiles of rows x tz cells (full x-rows): one CTA per tile,
@@ -1216,8 +1208,7 @@ int launch_population_v(Handle &h, PopArgs &a, const PopVariant &v) {
     if (grid < 1) grid = 1;
     // barrier count and generation, and the visited-tile counter after them
     GBG_CUDA_TRY(cudaMemsetAsync(a.barrier, 0, 4 * sizeof(unsigned), h.stream));
-    // cells per counted unit: a tile, or for the skipping kernel a row march
-    h.pop_tile_cells = v.counts ? (long long)(v.skip ? 1 : v.ry) * v.tz * a.n : 0;
+    h.pop_tile_cells = v.counts ? (long long)v.ry * v.tz * a.n : 0;
     void *args[] = {&a};
     GBG_CUDA_TRY(cudaEventRecord(h.ev_pop[0], h.stream));
     GBG_CUDA_TRY(cudaLaunchCooperativeKernel(v.fn, dim3((unsigned)grid), dim3(v.threads), args, v.smem,
