@@ -345,9 +345,7 @@ struct PopArgs {
 // from the sign bit of the x-face table (one float4 load less per plane), and
 // offsets inside a sample are 32-bit, formed once per tile and advanced by a
 // plane per step. The mask is applied as the sign bit of cxs (|cxs| = cx).
-// UNR > 1 unrolls the plane loop so that the next planes' loads can be
-// issued before the current plane's arithmetic (same operations per cell).
-template <int LR, int UNR = 1>
+template <int LR>
 __device__ __forceinline__ void march_tile_s(int n, int TZ, int ty0, int tz0,
                                              const float *__restrict__ in, float *__restrict__ out,
                                              const float *__restrict__ cxs, const float *__restrict__ cy,
@@ -367,7 +365,6 @@ __device__ __forceinline__ void march_tile_s(int n, int TZ, int ty0, int tz0,
     float4 Pc = ld(in, oy + zo);
     float4 CZp = lg(cz, oy + zso);
     const unsigned last = plane * (unsigned)(n - 1);
-#pragma unroll UNR
     for (int dz = 0; dz < TZ; ++dz) {
         const unsigned zno = zo == last ? 0u : zo + plane;
         const float4 Pn = ld(in, oy + zno);
@@ -461,7 +458,7 @@ __device__ __forceinline__ bool span_hits(int lo, int hi, int grow, int a, int b
     return lo <= b && a <= hi;
 }
 
-template <int LR, int MINB, int UNR = 1>
+template <int LR, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_population10(PopArgs p) {
     const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
     int active = p.S;
@@ -490,8 +487,8 @@ __global__ void __launch_bounds__(256, MINB) k_population10(PopArgs p) {
             if (!go) continue;
             const size_t off = (size_t)order * p.stride;
             const bool last = k == p.rec[r].nsteps - 1;
-            march_tile_s<LR, UNR>(n, p.TZ, y0, z0, in + off, out + off, p.cxs, p.cy, p.cz,
-                                  last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
+            march_tile_s<LR>(n, p.TZ, y0, z0, in + off, out + off, p.cxs, p.cy, p.cz,
+                             last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
             ++visited;
         }
         if (k + 1 < maxsteps && !grid_barrier(p.barrier, p.status, gridDim.x)) break;
@@ -1096,10 +1093,10 @@ PopVariant make_signmask_variant(int tz) {
     return v;
 }
 
-template <int LR, int MINB, int UNR = 1>
+template <int LR, int MINB>
 PopVariant make_skip_variant(int tz) {
     PopVariant v;
-    v.fn = (const void *)k_population10<LR, MINB, UNR>;
+    v.fn = (const void *)k_population10<LR, MINB>;
     v.ry = 256 / LR;
     v.g = 1;
     v.threads = 256;
@@ -1107,10 +1104,7 @@ PopVariant make_skip_variant(int tz) {
     v.smem = 0;
     v.skip = true;
     v.counts = true;
-    if (UNR > 1)
-        std::snprintf(v.name, sizeof(v.name), "k_population10<%d,%d,%d> TZ %d", LR, MINB, UNR, tz);
-    else
-        std::snprintf(v.name, sizeof(v.name), "k_population10<%d,%d> TZ %d", LR, MINB, tz);
+    std::snprintf(v.name, sizeof(v.name), "k_population10<%d,%d> TZ %d", LR, MINB, tz);
     return v;
 }
 
@@ -1170,9 +1164,6 @@ int variants_for(int n, PopVariant *out) {
             out[k++] = make_pair_variant<32, 3>(32);
             out[k++] = make_tb_variant<2, true>(32);
             out[k++] = make_ws_variant<32, 8, 3, 3>(32);
-            out[k++] = make_skip_variant<32, 4, 2>(8);
-            out[k++] = make_skip_variant<32, 4, 2>(16);
-            out[k++] = make_skip_variant<32, 3, 4>(16);
             break;
         case 64:
             out[k++] = make_skip_variant<16, 4>(8);
