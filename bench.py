@@ -200,7 +200,7 @@ def cpu_baseline(an, prior, seconds=12.0, obs=None):
 
 def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=64,
                     plain_chains=4, plain_steps=1500, plain_burn=300, ref_generations=500,
-                    plain_cap_s=150.0, unet=True, mala_steps=0, mala_burn=100):
+                    plain_cap_s=150.0, unet=True, mala_steps=0, mala_burn=100, ind_prob=0.3):
     """Posterior effective samples per second at n^3 on one synthetic
     patient, plain single-solve MCMC against the batched + adjoint +
     surrogate pipeline, both in the scaling symmetry's coordinates
@@ -252,7 +252,7 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=6
     h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2)
     screen = np.array([p.as_tuple() for p in Syn.draw_prior(an, 512, seed=99)])
     res = mcmc.sample_posterior(h, an.L, prior, dt0, rng, chains=chains, generations=generations,
-                                burn=burn, inner=inner, screen_draws=screen)
+                                burn=burn, inner=inner, screen_draws=screen, ind_prob=ind_prob)
     lc = mcmc.LogCoords(mcmc.Posterior(h, an.L, dt0, prior), A=mcmc.INVARIANT_MAP)
     names = ["log c (symmetry axis)", "log rho T", "log Dw/rho", "x0", "y0", "z0"]
 
@@ -322,7 +322,7 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=6
     post_r = mcmc.LogCoords(mcmc.Posterior(h, an.L, dt0, prior), A=mcmc.INVARIANT_MAP)
     rr = mcmc.da(post_r, res.surrogate, start_points(chains, 1.0), ref_generations + burn,
                  2.38 / np.sqrt(6), np.random.default_rng(12345), inner=inner, burn=burn,
-                 chol=np.linalg.cholesky(res.cov), adapt=True, axis=0)
+                 chol=np.linalg.cholesky(res.cov), adapt=True, axis=0, ind_prob=ind_prob)
     th_ref = lc.to_theta(rr.samples[burn:]).reshape(-1, 6)
     ref_mean = th_ref.mean(axis=0)
     ref_sd = th_ref.std(axis=0)
@@ -355,7 +355,8 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=6
                       ms_per_solve=1e3 * post1.seconds / max(post1.solves, 1), **d_plain),
         "pipeline": dict(sampler=f"delayed acceptance, tangent surrogate (affine + second order "
                                  f"along the symmetry axis), {chains} chains x {inner} surrogate "
-                                 f"steps per solve, invariant coordinates",
+                                 f"steps per solve (random walk, axis redraws, independence moves "
+                                 f"with probability {ind_prob}), invariant coordinates",
                          generations=generations - burn, accept=float(res.result.accept),
                          symmetry_axis="redrawn from its prior conditional inside the surrogate chain",
                          stage1_accept=float(res.result.history["stage1_accept"]),
@@ -775,6 +776,8 @@ def main():
     ap.add_argument("--mcmc-inner", type=int, default=64, help="surrogate steps per solve")
     ap.add_argument("--mcmc-generations", type=int, default=300,
                     help="pipeline generations (the first 100 are burn-in)")
+    ap.add_argument("--mcmc-ind", type=float, default=0.3,
+                    help="probability of an independence move per screen step")
     ap.add_argument("--mala-steps", type=int, default=0,
                     help="also run the 64-chain adjoint MALA configuration for this many steps")
     ap.add_argument("--samples", type=int, default=S,
@@ -802,7 +805,7 @@ def main():
                                                   chains=args.mcmc_chains, inner=args.mcmc_inner,
                                                   generations=args.mcmc_generations,
                                                   unet=not args.no_surrogate,
-                                                  mala_steps=args.mala_steps)}))
+                                                  mala_steps=args.mala_steps, ind_prob=args.mcmc_ind)}))
         return
     set_population(args.samples)
 
@@ -943,7 +946,7 @@ def main():
             line["mcmc"] = mcmc_comparison(local_rank, chains=args.mcmc_chains,
                                            inner=args.mcmc_inner,
                                            generations=args.mcmc_generations,
-                                           mala_steps=args.mala_steps)
+                                           mala_steps=args.mala_steps, ind_prob=args.mcmc_ind)
         if not args.no_amr:
             line["amr"] = amr_measurement(local_rank)
             line["amr"]["adaptive"] = amr_adaptive_measurement(local_rank)

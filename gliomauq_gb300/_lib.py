@@ -107,7 +107,8 @@ class AffineChainOpts(C.Structure):
     _fields_ = [("axis", C.c_int), ("axis_prob", C.c_double), ("step", C.c_double),
                 ("chol", C.c_double * 36), ("u_ref", C.c_double * 6), ("quad_axis", C.c_int),
                 ("Ai", C.c_double * 36), ("log_mask", C.c_int), ("lo", C.c_double * 6),
-                ("hi", C.c_double * 6)]
+                ("hi", C.c_double * 6), ("ind_prob", C.c_double), ("ind_mean", C.c_double * 6),
+                ("ind_chol", C.c_double * 36), ("ind_inv", C.c_double * 36)]
 
 
 class SyntheticOpts(C.Structure):
@@ -416,11 +417,12 @@ class Handle:
 
     def affine_chain(self, v, steps: int, seed: int, *, step: float, chol, axis: int = -1,
                      axis_prob: float = 0.0, u_ref, quad_axis: int = -1, Ai=None, log_mask: int = 0,
-                     lo, hi):
+                     lo, hi, ind_prob: float = 0.0, ind_mean=None, ind_chol=None):
         """`steps` screening-chain steps for every row of v (B x 6) on the GPU
         (gbg_affine_chain): (v after, log pi* at the start, at the end,
-        counts B x 4: random-walk accepts and steps, redraw accepts and
-        redraws)."""
+        counts B x 6: random-walk accepts and steps, redraw accepts and
+        redraws, independence accepts and proposals). ind_chol: the
+        independence Gaussian's factor (row-major, axis decoupled)."""
         vv = np.array(np.atleast_2d(v), dtype=np.float64, order="C", copy=True)
         B = vv.shape[0]
         o = AffineChainOpts()
@@ -434,9 +436,15 @@ class Handle:
         o.log_mask = int(log_mask)
         o.lo[:] = np.asarray(lo, dtype=np.float64).reshape(6).tolist()
         o.hi[:] = np.asarray(hi, dtype=np.float64).reshape(6).tolist()
+        o.ind_prob = float(ind_prob)
+        G = np.eye(6) if ind_chol is None else np.asarray(ind_chol, dtype=np.float64).reshape(6, 6)
+        o.ind_mean[:] = np.zeros(6).tolist() if ind_mean is None else \
+            np.asarray(ind_mean, dtype=np.float64).reshape(6).tolist()
+        o.ind_chol[:] = G.reshape(36).tolist()
+        o.ind_inv[:] = np.linalg.inv(G).reshape(36).tolist()
         l0 = np.empty(B)
         l1 = np.empty(B)
-        cnt = np.zeros((B, 4), dtype=np.int32)
+        cnt = np.zeros((B, 6), dtype=np.int32)
         check(self.lib.gbg_affine_chain(self._h, C.byref(o), B, int(steps),
                                         int(seed) & 0xFFFFFFFFFFFFFFFF, dptr(vv), dptr(l0), dptr(l1),
                                         cnt.ctypes.data))

@@ -975,18 +975,21 @@ int gbg_affine_chain(gbg_handle *hh, const gbg_affine_chain_opts *o, int B, int 
         return GBG_ERR_ARG;
     }
     if (o->axis < -1 || o->axis > 5 || o->quad_axis < -1 || o->quad_axis > 5 || !(o->axis_prob >= 0) ||
-        !(o->axis_prob <= 1) || !std::isfinite(o->step) || o->log_mask < 0 || o->log_mask > 63) {
+        !(o->axis_prob <= 1) || !std::isfinite(o->step) || o->log_mask < 0 || o->log_mask > 63 ||
+        !(o->ind_prob >= 0) || !(o->ind_prob + (o->axis >= 0 ? o->axis_prob : 0.0) <= 1)) {
         set_error("affine chain options out of range");
         return GBG_ERR_ARG;
     }
     for (int i = 0; i < 36; ++i)
-        if (!std::isfinite(o->chol[i]) || !std::isfinite(o->Ai[i])) {
+        if (!std::isfinite(o->chol[i]) || !std::isfinite(o->Ai[i]) || !std::isfinite(o->ind_chol[i]) ||
+            !std::isfinite(o->ind_inv[i])) {
             set_error("non-finite affine chain matrix");
             return GBG_ERR_NONFINITE;
         }
     for (int i = 0; i < 6; ++i) {
         const bool lg = (o->log_mask >> i) & 1;
         if (!std::isfinite(o->u_ref[i]) || !std::isfinite(o->lo[i]) || !std::isfinite(o->hi[i]) ||
+            !std::isfinite(o->ind_mean[i]) ||
             !(o->hi[i] > o->lo[i]) || (lg && !(o->lo[i] > 0))) {
             set_error("bad affine chain prior box or centre");
             return GBG_ERR_ARG;

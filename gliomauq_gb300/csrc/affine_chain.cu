@@ -8,8 +8,11 @@
 // step. The moves are those of the host sampler's inner chain
 // (gliomauq_gb300/mcmc.py, da): with probability axis_prob a redraw of the
 // symmetry coordinate from its prior conditional, accepted with the ratio of
-// pi*'s likelihood factors; otherwise a random walk v + step * C xi on the
-// other coordinates. Both leave pi* invariant. Random numbers come from a
+// pi*'s likelihood factors; with probability ind_prob an independence
+// proposal m + G xi for the other coordinates (a fixed Gaussian, accepted
+// with the Metropolis-Hastings ratio of its density); otherwise a random
+// walk v + step * C xi on the other coordinates. All three leave pi*
+// invariant. Random numbers come from a
 // counter-based hash (SplitMix64 finaliser, Steele, Lea & Flood 2014) of
 // (seed, chain, step, draw), normals by the Box-Muller transform.
 //
@@ -43,8 +46,9 @@ constexpr int kChainWarps = kChainThreads / 32;
 
 struct ChainArgs {
     int steps, P, quad_axis, axis, log_mask, n;
-    double axis_prob, step;
+    double axis_prob, step, ind_prob;
     double u_ref[6], chol[36], Ai[36], lo[6], hi[6], ulo[6], uhi[6];
+    double ind_mean[6], ind_chol[36], ind_inv[36];
     const unsigned char *mask;
     unsigned long long seed;
     const float4 *rec;  // per observation point, PET list then T1/T2 list: 16 floats
@@ -220,8 +224,9 @@ __global__ void __launch_bounds__(kChainThreads) k_affine_chain(ChainArgs a) {
     __shared__ double s_red[3][kChainWarps];
     __shared__ int s_eval;
     double v[6], y[6], lpv = 0.0, lpy = 0.0, ly = 0.0;
-    int cnt[4] = {0, 0, 0, 0};
-    bool jump = false;
+    int cnt[6] = {0, 0, 0, 0, 0, 0};
+    bool jump = false, indep = false;
+    double lqd = 0.0;  // log proposal-density ratio of an independence move
     if (threadIdx.x == 0) {
         for (int i = 0; i < 6; ++i) v[i] = a.v[(size_t)b * 6 + i];
         lpv = prior_logp(a, v);
@@ -239,10 +244,38 @@ __global__ void __launch_bounds__(kChainThreads) k_affine_chain(ChainArgs a) {
     __syncthreads();  // every thread has read s_eval before thread 0 rewrites it
     for (int s = 0; s < a.steps; ++s) {
         if (threadIdx.x == 0) {
-            jump = a.axis >= 0 && uniform01(a.seed, b, s, 0) <= a.axis_prob;
+            const double um = uniform01(a.seed, b, s, 0);
+            jump = a.axis >= 0 && um <= a.axis_prob;
+            indep = !jump && um <= (a.axis >= 0 ? a.axis_prob : 0.0) + a.ind_prob;
             for (int i = 0; i < 6; ++i) y[i] = v[i];
             if (jump) {
                 redraw_axis(a, y, uniform01(a.seed, b, s, 1));
+            } else if (indep) {
+                // y = m + G xi on the coordinates other than the axis; the
+                // density ratio q(v) / q(y) with z = G^-1 (x - m)
+                double xi[6], zv[6];
+                for (int k = 0; k < 3; ++k) {
+                    const float r = sqrtf(-2.0f * logf((float)uniform01(a.seed, b, s, 2 + 2 * k)));
+                    float sn, cs;
+                    sincospif(2.0f * (float)uniform01(a.seed, b, s, 3 + 2 * k), &sn, &cs);
+                    xi[2 * k] = (double)(r * cs);
+                    xi[2 * k + 1] = (double)(r * sn);
+                }
+                if (a.axis >= 0) xi[a.axis] = 0.0;
+                double qy = 0.0, qv = 0.0;
+                for (int i = 0; i < 6; ++i) {
+                    if (i == a.axis) continue;
+                    double d = 0.0, z = 0.0;
+                    for (int j = 0; j < 6; ++j) {
+                        d += a.ind_chol[i * 6 + j] * xi[j];
+                        z += a.ind_inv[i * 6 + j] * (v[j] - a.ind_mean[j]);
+                    }
+                    y[i] = a.ind_mean[i] + d;
+                    zv[i] = z;
+                    qy += xi[i] * xi[i];
+                    qv += zv[i] * zv[i];
+                }
+                lqd = 0.5 * (qy - qv);  // log q(v) - log q(y)
             } else {
                 // normals in float: their precision does not matter, the
                 // state they move stays double
@@ -269,8 +302,9 @@ __global__ void __launch_bounds__(kChainThreads) k_affine_chain(ChainArgs a) {
         const double L = s_eval ? eval_lik<P>(a, s_c, s_red) : 0.0;
         if (threadIdx.x == 0) {
             const double lq = s_eval ? L + lpy : -CUDART_INF;
-            // a prior-conditional redraw: its proposal density cancels the prior
-            const double corr = jump ? lpv - lpy : 0.0;
+            // a prior-conditional redraw: its proposal density cancels the
+            // prior; an independence move: the proposal density ratio
+            const double corr = jump ? lpv - lpy : (indep ? lqd : 0.0);
             const double logu = log(uniform01(a.seed, b, s, 8));
             const bool acc = isfinite(lq) && (logu < lq - ly + corr);
             if (acc) {
@@ -278,15 +312,16 @@ __global__ void __launch_bounds__(kChainThreads) k_affine_chain(ChainArgs a) {
                 ly = lq;
                 lpv = lpy;
             }
-            cnt[jump ? 2 : 0] += acc ? 1 : 0;
-            cnt[jump ? 3 : 1] += 1;
+            const int kind = jump ? 2 : (indep ? 4 : 0);
+            cnt[kind] += acc ? 1 : 0;
+            cnt[kind + 1] += 1;
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
         for (int i = 0; i < 6; ++i) a.v[(size_t)b * 6 + i] = v[i];
         a.lp_end[b] = ly;
-        for (int k = 0; k < 4; ++k) a.counts[(size_t)b * 4 + k] = cnt[k];
+        for (int k = 0; k < 6; ++k) a.counts[(size_t)b * 6 + k] = cnt[k];
     }
 }
 
@@ -317,7 +352,7 @@ int affine_chain(Handle &h, const gbg_affine_chain_opts &o, int B, int steps, un
     if (h.aff_cols_stale)
         if (int rc = affine_gather_columns(h)) return rc;
     // device scratch: v (B x 6), lp_start, lp_end (B), counts (B x 4)
-    const size_t need = (size_t)B * (8 * sizeof(double) + 4 * sizeof(int));
+    const size_t need = (size_t)B * (8 * sizeof(double) + 6 * sizeof(int));
     if (need > h.aff_chain_bytes) {
         if (h.aff_chain) cudaFree(h.aff_chain);
         h.aff_chain = nullptr;
@@ -335,6 +370,12 @@ int affine_chain(Handle &h, const gbg_affine_chain_opts &o, int B, int steps, un
     a.log_mask = o.log_mask;
     a.n = h.n;
     a.axis_prob = o.axis_prob;
+    a.ind_prob = o.ind_prob;
+    for (int i = 0; i < 6; ++i) a.ind_mean[i] = o.ind_mean[i];
+    for (int i = 0; i < 36; ++i) {
+        a.ind_chol[i] = o.ind_chol[i];
+        a.ind_inv[i] = o.ind_inv[i];
+    }
     a.step = o.step;
     for (int i = 0; i < 6; ++i) {
         a.u_ref[i] = o.u_ref[i];
@@ -373,7 +414,7 @@ int affine_chain(Handle &h, const gbg_affine_chain_opts &o, int B, int steps, un
     GBG_CUDA_TRY(cudaMemcpyAsync(lp_start, d_l0, (size_t)B * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
     GBG_CUDA_TRY(cudaMemcpyAsync(lp_end, d_l1, (size_t)B * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
     if (counts)
-        GBG_CUDA_TRY(cudaMemcpyAsync(counts, d_cnt, (size_t)B * 4 * sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+        GBG_CUDA_TRY(cudaMemcpyAsync(counts, d_cnt, (size_t)B * 6 * sizeof(int), cudaMemcpyDeviceToHost, h.stream));
     GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
     return GBG_OK;
 }

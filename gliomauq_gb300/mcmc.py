@@ -337,41 +337,58 @@ def _discrepancy(lp: np.ndarray, ls: np.ndarray) -> float:
 
 
 def inner_chain(prior, spost, y: np.ndarray, ly: np.ndarray, steps: int, step: float, Lc: np.ndarray,
-                axis, axis_prob: float, rng):
+                axis, axis_prob: float, rng, ind=None):
     """da's first stage on the host: `steps` Metropolis steps on the
     surrogate posterior for every row of y (log densities ly): with `axis`
     set, each step is with probability axis_prob a redraw of that coordinate
     from its prior conditional (prior.redraw_axis; an independence proposal
-    whose prior factors cancel, leaving the surrogate's likelihood ratio),
-    otherwise the random walk y + step * Lc xi on the other coordinates.
-    Returns (end points, their log densities, random-walk acceptances,
-    random-walk steps)."""
+    whose prior factors cancel, leaving the surrogate's likelihood ratio);
+    with ind = (probability, mean, factor G, axis decoupled) an independence
+    proposal mean + G xi for the other coordinates, accepted with the ratio
+    of that Gaussian's densities; otherwise the random walk y + step * Lc xi
+    on the other coordinates. Returns (end points, their log densities,
+    random-walk acceptances, random-walk steps)."""
     y, ly = np.array(y, dtype=np.float64, copy=True), np.array(ly, dtype=np.float64, copy=True)
     m, d = y.shape
+    ip, im, ig = (0.0, None, None) if ind is None else ind
+    gi = np.linalg.inv(ig) if ip > 0 else None
+    ident = np.ones(d, dtype=bool)
+    if axis is not None:
+        ident[axis] = False
     na = nt = 0
     for _ in range(steps):
-        prop = y + step * rng.standard_normal((m, d)) @ Lc.T
+        xi = rng.standard_normal((m, d))
+        prop = y + step * xi @ Lc.T
         corr = np.zeros(m)
         jump = np.zeros(m, dtype=bool)
+        u = rng.random(m)
         if axis is not None:
             prop[:, axis] = y[:, axis]
-            jump = rng.random(m) < axis_prob
+            jump = u < axis_prob
             if jump.any():
                 prop[jump] = prior.redraw_axis(y[jump], axis, rng)
                 corr[jump] = prior.logp(y[jump]) - prior.logp(prop[jump])
+        indep = ~jump & (u < (axis_prob if axis is not None else 0.0) + ip)
+        if indep.any():
+            z = xi[indep] * ident
+            prop[indep] = np.where(ident, im + z @ ig.T, y[indep])
+            zv = ((y[indep] - im) @ gi.T) * ident
+            corr[indep] = 0.5 * (np.sum(z * z, axis=1) - np.sum(zv * zv, axis=1))
         lq = spost.logpost(prop)
         with np.errstate(invalid="ignore"):
             a = np.isfinite(lq) & (np.log(rng.random(m)) < lq - ly + corr)
         y[a], ly[a] = prop[a], lq[a]
-        na += int(a[~jump].sum())
-        nt += int((~jump).sum())
+        rwm = ~jump & ~indep
+        na += int(a[rwm].sum())
+        nt += int(rwm.sum())
     return y, ly, na, nt
 
 
 def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: int, step: float,
        rng, inner: int = 8, burn: int = 0, target: float = 0.3, chol=None, adapt: bool = False,
        rebuild_every: int = 0, axis=None, axis_prob: float = 0.5,
-       adapt_pool: bool = True, reset_stranded: bool = True, gpu_chain: bool = True) -> ChainResult:
+       adapt_pool: bool = True, reset_stranded: bool = True, gpu_chain: bool = True,
+       ind_prob: float = 0.0, ind_scale: float = 1.2) -> ChainResult:
     """Delayed-acceptance MCMC, chains in lock-step: per generation `inner`
     batched surrogate calls and one batched solver call for the chains whose
     inner chain moved. The inner random-walk proposal is y + step * C xi:
@@ -402,7 +419,11 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
     exact posterior. With gpu_chain and a surrogate that has chain() (the
     affine screen), each generation's inner chains run on the GPU in one
     launch (the same moves, device random numbers), which also returns the
-    screen's log density at the chains' current points for stage 2."""
+    screen's log density at the chains' current points for stage 2. With
+    ind_prob > 0 an inner step is, with that probability, an independence
+    proposal from a Gaussian on the coordinates other than `axis`: the
+    population's (pooled) mean and covariance inflated by ind_scale, adapted
+    with the random-walk covariance during burn-in and frozen after it."""
     w = post.prior.width
     th = np.array(theta0, dtype=np.float64)
     m, d = th.shape
@@ -411,6 +432,7 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
     Lc = _chol(post, chol)
     if axis is not None:
         Lc = np.linalg.cholesky(_decoupled(Lc @ Lc.T, axis))
+    ind_mean, ind_G = np.median(th, axis=0), ind_scale * Lc
     out = np.empty((steps, m, d))
     lp_out = np.empty((steps, m))
     acc1 = acc2 = tried = 0
@@ -453,16 +475,19 @@ def da(post: Posterior, spost: SurrogatePosterior, theta0: np.ndarray, steps: in
                     win = slice(k // 2, k)
                     keep = np.stack([~_stranded(r) for r in lp_out[win]])
                     pts = out[win][keep]
-                    Lc = _chol_cov(pts if len(pts) > 2 * d else th, axis)
+                    pts = pts if len(pts) > 2 * d else th
                 else:
-                    Lc = _chol_cov(th, axis)
+                    pts = th
+                Lc = _chol_cov(pts, axis)
+                ind_mean, ind_G = pts.mean(axis=0), ind_scale * Lc
+        ind = (ind_prob, ind_mean, ind_G) if ind_prob > 0 else None
         if gpu_chain and getattr(spost, "gpu_chain_ready", False):
             # random-walk acceptance fraction a1 (the step adapts to it)
             y, ls, ly, a1 = spost.chain(th, inner, step, Lc, axis, axis_prob,
-                                        int(rng.integers(0, 2 ** 63)))
+                                        int(rng.integers(0, 2 ** 63)), ind=ind)
         else:
             y, ly, na, nt = inner_chain(post.prior, spost, th, ls, inner, step, Lc, axis, axis_prob,
-                                        rng)
+                                        rng, ind=ind)
             a1 = na / max(nt, 1)
         moved = np.any(y != th, axis=1)
         if moved.any():
@@ -898,27 +923,31 @@ class AffineSurrogate:
             h.affine_set_prior_mask(base_prior.seed_mask)
 
     def chain(self, v: np.ndarray, steps: int, step: float, chol: np.ndarray, axis, axis_prob: float,
-              seed: int):
+              seed: int, ind=None):
         """The inner chain of da on the GPU (gbg_affine_chain): `steps` steps
-        for every row of v on this screen's posterior, the same moves as da's
-        host loop (random walk step * chol xi on the coordinates other than
-        `axis`, or with probability axis_prob a redraw of `axis` from its
-        prior conditional). Returns (end points, log pi* at the start points,
-        log pi* at the end points, random-walk acceptance fraction)."""
+        for every row of v on this screen's posterior, the same moves as
+        inner_chain (random walk step * chol xi on the coordinates other than
+        `axis`, with probability axis_prob a redraw of `axis` from its prior
+        conditional, with ind = (probability, mean, factor) independence
+        proposals). Returns (end points, log pi* at the start points, log pi*
+        at the end points, random-walk acceptance fraction); the independence
+        moves' acceptance is kept in last_ind_accept."""
         pr = self.prior
         if isinstance(pr, LogPrior):
             Ai, log_mask, lo, hi = pr.Ai, sum(1 << i for i in pr.log_idx), pr.base.lo, pr.base.hi
         else:
             Ai, log_mask, lo, hi = np.eye(6), 0, pr.lo, pr.hi
+        ip, im, ig = (0.0, None, None) if ind is None else ind
         t0 = time.perf_counter()
         y, l0, l1, cnt = self.base.handle.affine_chain(
             v, steps, seed, step=step, chol=chol, axis=-1 if axis is None else axis,
             axis_prob=axis_prob if axis is not None else 0.0, u_ref=self.u_ref,
             quad_axis=-1 if self.quad_axis is None else self.quad_axis, Ai=Ai, log_mask=log_mask,
-            lo=lo, hi=hi)
+            lo=lo, hi=hi, ind_prob=ip, ind_mean=im, ind_chol=ig)
         self.seconds += time.perf_counter() - t0
         self.calls += 1
         self.evals += int(np.atleast_2d(v).shape[0]) * (steps + 1)
+        self.last_ind_accept = float(cnt[:, 4].sum() / cnt[:, 5].sum()) if cnt[:, 5].sum() else 0.0
         rw = cnt[:, 1].sum()
         return y, l0, l1, float(cnt[:, 0].sum() / rw) if rw else 0.0
 
@@ -1012,7 +1041,7 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
                      screen: int = 512, screen_draws=None, ic_peak: float = 0.1,
                      ic_sigma: float = 1.0, adapt_pool: bool = True, adapt: bool = True,
                      rebuild_every: int = 25, reset_stranded: bool = True,
-                     polish: int = 8) -> PipelineResult:
+                     polish: int = 8, ind_prob: float = 0.0) -> PipelineResult:
     """The batched + adjoint + surrogate posterior sampler (dt0 < 0, the
     scaled time grid, makes the likelihood invariant along the scaling
     symmetry, whose coordinate is then drawn exactly from its prior
@@ -1058,7 +1087,7 @@ def sample_posterior(handle, L: float, prior: Prior, dt0: float, rng, chains: in
     run = Posterior(handle, L, dt0, prior, ic_peak=ic_peak, ic_sigma=ic_sigma)
     r = da(LogCoords(run, A=INVARIANT_MAP), sur, v0, generations, 2.38 / np.sqrt(v_map.size), rng,
            inner=inner, burn=burn, chol=Lc, adapt=adapt, rebuild_every=rebuild_every, axis=0,
-           adapt_pool=adapt_pool, reset_stranded=reset_stranded)
+           adapt_pool=adapt_pool, reset_stranded=reset_stranded, ind_prob=ind_prob)
     burn_s = r.history["burn_seconds"]
     return PipelineResult(r, post.to_theta(r.samples[burn:]), v_map, cov, setup, r.seconds - burn_s,
                           burn_s, surrogate=sur, solver_seconds=run.seconds,

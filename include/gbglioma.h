@@ -273,12 +273,16 @@ int gbg_affine_loglik(gbg_handle *h, int B, const double *delta, gbg_lik_result 
  * prior = sum of the log coordinates' u_i). c(d) = d, or with quad_axis = a
  * (d, d_a^2 / 2, d_a d_i for i != a) -- the model needs 6 or 12 fields. A step
  * is, with probability axis_prob, a redraw of coordinate `axis` from its
- * prior conditional (accepted with the likelihood ratio), otherwise
- * v + step * chol xi on the other coordinates (chol row-major 6 x 6).
+ * prior conditional (accepted with the likelihood ratio); with probability
+ * ind_prob an independence proposal ind_mean + ind_chol xi for the other
+ * coordinates (accepted with the Metropolis-Hastings ratio of that Gaussian;
+ * ind_inv = ind_chol^-1, with `axis` decoupled in both); otherwise
+ * v + step * chol xi on the other coordinates (matrices row-major 6 x 6).
  * v (B x 6) is updated in place; lp_start / lp_end get log pi* at the chains'
- * start and end points (-inf outside the prior); counts (B x 4, may be null)
- * random-walk accepts, random-walk steps, redraw accepts, redraws. seed fixes
- * the random numbers (counter-based). No reference counterpart. */
+ * start and end points (-inf outside the prior); counts (B x 6, may be null)
+ * random-walk accepts and steps, redraw accepts and redraws, independence
+ * accepts and proposals. seed fixes the random numbers (counter-based). No
+ * reference counterpart. */
 typedef struct {
     int axis;          /* coordinate redrawn from its prior conditional, -1: none */
     double axis_prob;  /* probability of a redraw per step */
@@ -289,6 +293,8 @@ typedef struct {
     double Ai[36];     /* u = Ai v */
     int log_mask;      /* bit i: theta_i = exp(u_i) */
     double lo[6], hi[6];
+    double ind_prob;       /* probability of an independence move per step */
+    double ind_mean[6], ind_chol[36], ind_inv[36];
 } gbg_affine_chain_opts;
 int gbg_affine_set_prior_mask(gbg_handle *h, const unsigned char *mask);
 /* entries of the observation lists gbg_set_observations built: PET voxels and

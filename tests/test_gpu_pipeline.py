@@ -125,11 +125,13 @@ def test_gpu_screening_chain_evaluates_the_screen_density(gbg):
     assert np.all(err <= 1e-6 * np.abs(exp[fin]) + 1e-3)
 
 
-def test_gpu_screening_chain_moves_like_the_host_chain(gbg):
+@pytest.mark.parametrize("with_ind", [False, True])
+def test_gpu_screening_chain_moves_like_the_host_chain(gbg, with_ind):
     """The GPU inner chain is the host inner chain (mcmc.inner_chain) with
     other random numbers: from the same 1024 starting points, after 60
     steps, the two populations agree in mean (within 5 standard errors of
-    the difference) and spread (10 %), and in random-walk acceptance."""
+    the difference) and spread (10 %), and in random-walk acceptance; with
+    independence moves too (from a deliberately shifted Gaussian)."""
     an = S.make_anatomy(N, seed=4)
     with _lib.Handle(N, "f32", max_samples=1024) as h:
         h.set_anatomy(an.p_w, an.p_g)
@@ -141,8 +143,11 @@ def test_gpu_screening_chain_moves_like_the_host_chain(gbg):
         v0 = lc.prior.redraw_axis(v_map + 1.5 * rng.standard_normal((1024, 6)) @ Lc.T, 0, rng)
         v0[~np.isfinite(lc.prior.logp(v0))] = v_map
         step = 2.38 / np.sqrt(5)
-        yg, _, _, ag = sur.chain(v0, 60, step, Lc, 0, 0.5, 11)
-        yh, _, na, nt = mcmc.inner_chain(lc.prior, sur, v0, sur.logpost(v0), 60, step, Lc, 0, 0.5, rng)
+        ind = (0.3, v_map + 0.5 * Lc[:, 0] + 0.3 * np.diag(Lc), 1.3 * Lc) if with_ind else None
+        ap = 0.3 if with_ind else 0.5
+        yg, _, _, ag = sur.chain(v0, 60, step, Lc, 0, ap, 11, ind=ind)
+        yh, _, na, nt = mcmc.inner_chain(lc.prior, sur, v0, sur.logpost(v0), 60, step, Lc, 0, ap, rng,
+                                         ind=ind)
     ah = na / nt
     se = np.sqrt((yg.var(axis=0) + yh.var(axis=0)) / len(v0))
     print("acceptance gpu", ag, "host", ah, "mean diff / se", (yg.mean(axis=0) - yh.mean(axis=0)) / se,

@@ -624,3 +624,53 @@ def test_tmcmc_on_the_invariant_posterior_in_log_coordinates():
     assert abs(f[:, 1].mean() - m1) < 0.15 * s1 and abs(f[:, 2].mean() - m2) < 0.15 * s2
     assert abs(f[:, 1].std() / s1 - 1) < 0.2 and abs(f[:, 2].std() / s2 - 1) < 0.2
     assert np.all(np.abs(f[:, 3:].mean(axis=0) - base.c[2:]) < 0.15 * base.s[2:])
+
+
+def test_delayed_acceptance_with_independence_moves_targets_the_posterior():
+    """The inner chain with independence proposals (a Gaussian fitted to the
+    population in burn-in, inflated) next to the random walk and the axis
+    redraws: delayed acceptance still samples the invariant stub's
+    posterior (same checks as the axis-redraw test)."""
+    rng = np.random.default_rng(12)
+    base = InvariantStub()
+    lc = mcmc.LogCoords(base, A=mcmc.INVARIANT_MAP)
+    sp = lc.surrogate(mcmc.SurrogatePosterior(InvariantSurrogate(base), base.prior))
+    v_c = np.concatenate([[np.log(0.15)], base.c])
+    v0 = v_c + np.concatenate([[0.0], base.s]) * rng.standard_normal((32, 6))
+    v0 = lc.prior.redraw_axis(v0, 0, rng)
+    chol = np.diag(np.concatenate([[0.1], base.s]))
+    r = mcmc.da(lc, sp, v0, 1500, 1.0, rng, inner=6, burn=300, chol=chol, adapt=True, axis=0,
+                axis_prob=0.3, ind_prob=0.4)
+    v = r.samples[300:]
+    flat = v.reshape(-1, 6)
+    assert np.all(np.abs(flat[:, 3:].mean(axis=0) - base.c[2:]) < 0.1 * base.s[2:])
+    assert np.all(np.abs(flat[:, 3:].std(axis=0) / base.s[2:] - 1) < 0.1)
+    m1, m2, s1, s2 = _invariant_moments(base)
+    assert abs(flat[:, 1].mean() - m1) < 0.1 * s1 and abs(flat[:, 2].mean() - m2) < 0.1 * s2
+    assert abs(flat[:, 1].std() / s1 - 1) < 0.1 and abs(flat[:, 2].std() / s2 - 1) < 0.1
+    assert np.all(mcmc.rhat(v) < 1.05)
+
+
+def test_inner_chain_independence_moves_sample_the_screen():
+    """inner_chain's independence move alone (probability 1, a deliberately
+    wrong Gaussian) samples the screen's density: long chains of a 1-D-like
+    Gaussian screen reach its mean and spread."""
+    rng = np.random.default_rng(13)
+
+    class Screen:
+        def logpost(self, v):
+            v = np.atleast_2d(v)
+            return -0.5 * np.sum(((v - 1.0) / 0.5) ** 2, axis=1)
+
+    class Flat:
+        def logp(self, v):
+            return np.zeros(np.atleast_2d(v).shape[0])
+
+    y0 = np.zeros((400, 6))
+    sc = Screen()
+    G = np.diag(np.full(6, 0.8))
+    y, ly, na, nt = mcmc.inner_chain(Flat(), sc, y0, sc.logpost(y0), 60, 0.5, np.eye(6), None, 0.0, rng,
+                                     ind=(1.0, np.full(6, 0.7), G))
+    assert nt == 0  # every step was an independence move
+    assert np.all(np.abs(y.mean(axis=0) - 1.0) < 0.1)
+    assert np.all(np.abs(y.std(axis=0) / 0.5 - 1) < 0.15)
