@@ -200,7 +200,7 @@ def cpu_baseline(an, prior, seconds=12.0, obs=None):
 
 def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=64,
                     plain_chains=4, plain_steps=1500, plain_burn=300, ref_generations=500,
-                    plain_cap_s=150.0, unet=True, mala_steps=0, mala_burn=100, ind_prob=0.3):
+                    plain_cap_s=150.0, unet=True, mala_steps=0, mala_burn=100, ind_prob=0.0):
     """Posterior effective samples per second at n^3 on one synthetic
     patient, plain single-solve MCMC against the batched + adjoint +
     surrogate pipeline, both in the scaling symmetry's coordinates
@@ -776,8 +776,9 @@ def main():
     ap.add_argument("--mcmc-inner", type=int, default=64, help="surrogate steps per solve")
     ap.add_argument("--mcmc-generations", type=int, default=300,
                     help="pipeline generations (the first 100 are burn-in)")
-    ap.add_argument("--mcmc-ind", type=float, default=0.3,
-                    help="probability of an independence move per screen step")
+    ap.add_argument("--mcmc-ind", type=float, default=0.0,
+                    help="probability of an independence move per screen step (with the axis "
+                         "redraws' 0.5, at most 0.5)")
     ap.add_argument("--mala-steps", type=int, default=0,
                     help="also run the 64-chain adjoint MALA configuration for this many steps")
     ap.add_argument("--samples", type=int, default=S,
