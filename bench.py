@@ -641,6 +641,47 @@ def screen_and_statistics_measurement(device, n=128, chains=64, steps=64, reps=3
     return out
 
 
+def adjoint_measurement(device, n=128, samples=64, reps=2):
+    """The discrete adjoint (gbg_adjoint_grad) on the bench problem at n^3:
+    forward + gradient and forward only (checkpoints every 50 steps, float
+    states, scaled time grid) for `samples` prior draws and for as many
+    draws near the truth (1 % perturbations, ~the posterior's step counts),
+    beside the batched solve of the same samples; host-timed per call."""
+    from gliomauq_gb300 import _lib, synthetic as Syn
+    an = Syn.make_anatomy(n, seed=0)
+    truth = Syn.draw_prior(an, 1, seed=10_000)[0]
+    h = _lib.Handle(n, "f32", device=device, max_samples=max(samples, 1))
+    out = {"grid": n, "samples": samples, "checkpoint_every": 50, "time_grid": "scaled (dt0 = -1)"}
+    try:
+        h.set_anatomy(an.p_w, an.p_g)
+        u = h.batch_solve([truth.as_tuple()], an.L, with_loglik=False, want_phi=True, dt0=-1.0)["phi"][0]
+        obs = Syn.make_observations(u.astype(np.float64), an, seed=3,
+                                    centre_xyz=(truth.x0, truth.y0, truth.z0), radius_vox=27.0 * n / 128)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2)
+        sets = {"prior": [p.as_tuple() for p in Syn.draw_prior(an, samples, seed=5)],
+                "near_mode": [tuple(np.array(truth.as_tuple()) *
+                                    (1 + 0.01 * np.random.default_rng(i).standard_normal(6)))
+                              for i in range(samples)]}
+        for name, smp in sets.items():
+            res = {}
+            for key, grad in (("forward_and_gradient_ms", True), ("forward_only_ms", False)):
+                h.adjoint_grad(smp, -1.0, an.L, checkpoint_every=50, want_grad=grad)
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    h.adjoint_grad(smp, -1.0, an.L, checkpoint_every=50, want_grad=grad)
+                res[key] = 1e3 * (time.perf_counter() - t0) / reps
+            h.batch_solve(smp, an.L, dt0=-1.0)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                r = h.batch_solve(smp, an.L, dt0=-1.0)
+            res["batched_solve_ms"] = 1e3 * (time.perf_counter() - t0) / reps
+            res["mean_steps"] = float(np.mean(r["nsteps"]))
+            out[name] = res
+    finally:
+        h.close()
+    return out
+
+
 def surrogate_measurement(device, n=128, batch=32, reps=5):
     """Forward throughput of the bf16 U-Net surrogate at n^3 (its grid is
     (n/2)^3): milliseconds per sample of gbg_surrogate_loglik (features,
@@ -772,6 +813,8 @@ def main():
                     help="print the screening-chain and propagation-statistics measurement alone")
     ap.add_argument("--only-amr", action="store_true",
                     help="print the multiresolution-grid measurement alone")
+    ap.add_argument("--only-adjoint", action="store_true",
+                    help="print the adjoint measurement alone")
     ap.add_argument("--mcmc-chains", type=int, default=64, help="pipeline chains")
     ap.add_argument("--mcmc-inner", type=int, default=64, help="surrogate steps per solve")
     ap.add_argument("--mcmc-generations", type=int, default=300,
@@ -790,6 +833,9 @@ def main():
         return run_reference_arm(args)
     if args.only_surrogate:
         print(json.dumps({"surrogate": surrogate_measurement(int(os.environ.get("LOCAL_RANK", "0")))}))
+        return
+    if args.only_adjoint:
+        print(json.dumps({"adjoint": adjoint_measurement(int(os.environ.get("LOCAL_RANK", "0")))}))
         return
     if args.only_amr:
         dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -952,6 +998,7 @@ def main():
             line["amr"] = amr_measurement(local_rank)
             line["amr"]["adaptive"] = amr_adaptive_measurement(local_rank)
         line["sampling_kernels"] = screen_and_statistics_measurement(local_rank)
+        line["adjoint"] = adjoint_measurement(local_rank)
         if not args.no_surrogate:
             line["surrogate"] = surrogate_measurement(local_rank)
         print(json.dumps(line))
