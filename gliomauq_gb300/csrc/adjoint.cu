@@ -267,12 +267,37 @@ __device__ __forceinline__ float4 lg4(const float *p, unsigned o) {
     return __ldg(reinterpret_cast<const float4 *>(p + o));
 }
 
+// live[t] = 1 when tile t of k_adj_back128 (rows y0 .. y0 + RY - 1, planes
+// tz0 .. tz0 + TZ - 1, every x) or its one-cell y/z halo holds a cell with
+// mask 1. On a tile without one mu is 0 on the tile and its halo, so
+// lambda_k = mu (1 + b (1 - 2 phi)) + a L(mu) and the tile's sensitivity
+// products are all zero. One block per tile.
+__global__ void k_adj_tile_live(const float *__restrict__ msk, unsigned char *__restrict__ live) {
+    using namespace fb;
+    constexpr int tiles_y = NN / RY;
+    const int t = blockIdx.x, y0 = (t % tiles_y) * RY, tz0 = (t / tiles_y) * TZ;
+    constexpr int cells = (RY + 2) * (TZ + 2) * NN;
+    int any = 0;
+    for (int c = threadIdx.x; c < cells && !any; c += blockDim.x) {
+        const int x = c % NN, r = c / NN, dy = r % (RY + 2), dz = r / (RY + 2);
+        const int y = (y0 - 1 + dy + NN) % NN, z = (tz0 - 1 + dz + NN) % NN;
+        any = msk[(size_t)NN * NN * z + (size_t)NN * y + x] != 0.0f;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) live[t] = any ? 1 : 0;
+}
+
+// live: k_adj_tile_live's flags. A sample's first two backward steps (k =
+// ns - 1, ns - 2) visit every tile, so that both lambda buffers hold the
+// zeros of the tiles without a live cell (the seed may be nonzero there);
+// later steps skip those tiles, which keeps every value but the sign of a
+// zero.
 __global__ void __launch_bounds__(320, 2)
     k_adj_back128(int S, int k, const int *__restrict__ ns, const float *__restrict__ phi, float *__restrict__ lam0,
                   float *__restrict__ lam1,
                   const float *__restrict__ cx, const float *__restrict__ cy, const float *__restrict__ cz,
                   const float *__restrict__ msk, const double *__restrict__ a, const double *__restrict__ b,
-                  double *__restrict__ gA, double *__restrict__ gB) {
+                  double *__restrict__ gA, double *__restrict__ gB, const unsigned char *__restrict__ live) {
     using namespace fb;
     constexpr unsigned plane = NN * NN, N = NN * NN * NN;
     constexpr int tiles_y = NN / RY, tiles = tiles_y * (NN / TZ);
@@ -282,6 +307,7 @@ __global__ void __launch_bounds__(320, 2)
     const int left_l = (li + LR - 1) % LR, right_l = (li + 1) % LR;
     for (int it = blockIdx.x; it < S * tiles; it += gridDim.x) {
         const int s = it % S, t = it / S;
+        if (!live[t] && k + 3 <= ns[s]) continue;
         const int y0 = (t % tiles_y) * RY, tz0 = (t / tiles_y) * TZ;
         const float *f = phi + (size_t)s * N;
         const bool odd = ((ns[s] - 1 - k) & 1) != 0;  // lambda of sample s is in lam1
@@ -308,7 +334,7 @@ __global__ void __launch_bounds__(320, 2)
         float4 CZp = lg4(cz, oy + plane * (unsigned)wz(zstart - 1));
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         float4 U2 = z4, U1 = z4, Pb = z4;  // mu at z-2, z-1; phi at z-1
-        double sa = 0.0, sb = 0.0;
+        float pa_t = 0.0f, pb_t = 0.0f;
         for (int st = 0; st < TZ + 2; ++st) {
             const int zu = zstart + st;
             const unsigned zo = plane * (unsigned)wz(zu), zno = plane * (unsigned)wz(zu + 1);
@@ -348,11 +374,13 @@ __global__ void __launch_bounds__(320, 2)
                     pa = fmaf(u[i], lap, pa);
                     pb = fmaf(u[i] * f0, 1.0f - f0, pb);
                 }
-                // a thread's four cells summed in float, the plane partials in
-                // double (the FP64 pipe is narrow on this GPU)
+                // a thread's 4 x TZ cells summed in float, widened to double
+                // once per tile: the FP64 pipe on this GPU runs at a small
+                // fraction of the FP32 rate, so a per-plane double add cost
+                // more issue slots than the plane's whole stencil
                 if (own) {
-                    sa += (double)pa;
-                    sb += (double)pb;
+                    pa_t += pa;
+                    pb_t += pb;
                 }
                 U = make_float4(u[0], u[1], u[2], u[3]);
             }
@@ -397,6 +425,7 @@ __global__ void __launch_bounds__(320, 2)
             CZp = CZ;
         }
         // per-sample sensitivities of this tile
+        double sa = (double)pa_t, sb = (double)pb_t;
         for (int o = 16; o > 0; o >>= 1) {
             sa += __shfl_down_sync(0xffffffffu, sa, o);
             sb += __shfl_down_sync(0xffffffffu, sb, o);
@@ -590,7 +619,7 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
                             (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
                             (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
                             3 * S * sizeof(double), S * sizeof(gbg_sample), S * sizeof(gbg_lik_result),
-                            S * sizeof(int), 2 * S * sizeof(SampleRec), S * sizeof(int)};
+                            S * sizeof(int), 2 * S * sizeof(SampleRec), S * sizeof(int), 1024};
     size_t total = 0;
     for (size_t b : sizes) total += bwork_align(b);
     if (h.adj_ws_bytes < total) {
@@ -604,10 +633,10 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
         }
         h.adj_ws_bytes = total;
     }
-    void *parts[16];
+    void *parts[17];
     {
         char *q = (char *)h.adj_ws;
-        for (int i = 0; i < 16; ++i) {
+        for (int i = 0; i < 17; ++i) {
             parts[i] = q;
             q += bwork_align(sizes[i]);
         }
@@ -629,6 +658,7 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     int *dns = (int *)parts[13];
     SampleRec *drec = (SampleRec *)parts[14], *dsorted = drec + S;
     int *drank = (int *)parts[15];
+    unsigned char *dlive = (unsigned char *)parts[16];
     // per-step coefficients; a < 0 marks a finished sample
     std::vector<double> ha((size_t)nmax * S), hb((size_t)nmax * S);
     for (int k = 0; k < nmax; ++k)
@@ -773,16 +803,49 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     // its lambda is in mu when that count is odd.
     const unsigned gcx = (unsigned)std::min<size_t>((N + 255) / 256, (size_t)h.num_sms * 4);
     const bool fused = f32 && n == fb::NN;
+    std::vector<SampleRec> rrec(pop_fwd ? S : 0);
+    if (fused) {
+        constexpr int tiles = (fb::NN / fb::RY) * (fb::NN / fb::TZ);
+        static_assert(tiles <= 1024, "live flags");
+        k_adj_tile_live<<<tiles, 256, 0, st>>>((const float *)t.msk, dlive);
+        h.launches++;
+    }
     for (int sgm = (nmax - 1) / K; sgm >= 0; --sgm) {
         const int k0 = sgm * K, k1 = std::min(nmax, k0 + K);
         // recompute states k0+1 .. k1-1 into seg[1..]
         ADJ_TRY(cudaMemcpyAsync(seg, ck + (size_t)sgm * S * N, (size_t)A[k0] * N * sizeof(Real),
                                 cudaMemcpyDeviceToDevice, st));
-        for (int k = k0; k < k1 - 1; ++k) {
-            k_adj_fwd<Real><<<grid_cells(h, A[k]), 256, 0, st>>>(n, A[k], seg + (size_t)(k - k0) * S * N,
-                                                                 seg + (size_t)(k - k0 + 1) * S * N, t,
-                                                                 da + (size_t)k * S, db + (size_t)k * S);
-            h.launches++;
+        if (pop_fwd) {
+            // one population launch keeping every state (slot mode): sample s
+            // takes steps k0 .. min(ns[s] - 1, k1 - 1) - 1, all full steps (a
+            // sample's shortened last step only feeds the likelihood)
+            const int act = A[k0];
+            int most = 0;
+            for (int s = 0; s < act; ++s) {
+                SampleRec r = recs[s];
+                r.nsteps = std::min(ns[s] - 1, k1 - 1) - k0;
+                r.a2 = r.a;
+                r.b2 = r.b;
+                r.order = s;
+                rrec[s] = r;
+                most = std::max(most, r.nsteps);
+            }
+            if (most > 0) {
+                ADJ_TRY(cudaMemcpyAsync(drec, rrec.data(), (size_t)act * sizeof(SampleRec), cudaMemcpyHostToDevice,
+                                        st));
+                rc = population_steps(h, (float *)seg, (float *)seg, drec, dsorted, drank, act, SN);
+                if (rc) {
+                    release();
+                    return rc;
+                }
+            }
+        } else {
+            for (int k = k0; k < k1 - 1; ++k) {
+                k_adj_fwd<Real><<<grid_cells(h, A[k]), 256, 0, st>>>(n, A[k], seg + (size_t)(k - k0) * S * N,
+                                                                     seg + (size_t)(k - k0 + 1) * S * N, t,
+                                                                     da + (size_t)k * S, db + (size_t)k * S);
+                h.launches++;
+            }
         }
         for (int k = k1 - 1; k >= k0; --k) {
             const Real *phik = seg + (size_t)(k - k0) * S * N;
@@ -793,7 +856,7 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
                 k_adj_back128<<<grid, 320, 0, st>>>(A[k], k, dns, (const float *)phik, (float *)lam, (float *)mu,
                                                     (const float *)t.cx, (const float *)t.cy, (const float *)t.cz,
                                                     (const float *)t.msk, da + (size_t)k * S, db + (size_t)k * S,
-                                                    gA + (size_t)k * S, gB + (size_t)k * S);
+                                                    gA + (size_t)k * S, gB + (size_t)k * S, dlive);
                 h.launches++;
             } else {
                 const dim3 gC(gcx, (unsigned)A[k]);

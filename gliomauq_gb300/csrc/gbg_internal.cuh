@@ -221,9 +221,10 @@ int launch_schedule_smooth(Handle &h, const gbg_sample *samples_device, int S, d
 // recs[s].nsteps steps with coefficients a, b, the last one a2, b2, and ends
 // in buffer (nsteps & 1). recs: S device records; sorted / rank: device
 // scratch for S records / ints. Dense kernels only (no temporal blocking, no
-// skipping: the states may be anything).
+// skipping: the states may be anything). slot > 0 keeps every state instead:
+// step k reads buf0 + k * slot and writes buf0 + (k + 1) * slot (buf1 unused).
 int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs, SampleRec *sorted, int *rank,
-                     int S);
+                     int S, size_t slot = 0);
 bool population_supported(int n);
 int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, double peak, double sigma,
                        float *phi);

@@ -328,6 +328,9 @@ struct PopArgs {
     int n, S, TZ, tiles_y, tiles;  // tiles per sample = tiles_y * (n / TZ)
     size_t stride;                 // cells per sample field
     float *buf0, *buf1;
+    // k_population8<..., SLOT = true> only: every state kept, step k reading
+    // buf0 + k * slot and writing buf0 + (k + 1) * slot (floats)
+    size_t slot;
     const float *cx, *cy, *cz, *msk;
     const float *cxs;              // cx, sign bit = not msk
     const SampleRec *rec;          // sorted by nsteps descending
@@ -407,7 +410,7 @@ __device__ __forceinline__ void march_tile_s(int n, int TZ, int ty0, int tz0,
     }
 }
 
-template <int LR, int MINB>
+template <int LR, int MINB, bool SLOT = false>
 __global__ void __launch_bounds__(256, MINB) k_population8(PopArgs p) {
     const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
     int active = p.S;
@@ -415,8 +418,8 @@ __global__ void __launch_bounds__(256, MINB) k_population8(PopArgs p) {
     unsigned long long visited = 0;
     for (int k = 0; k < maxsteps; ++k) {
         while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
-        const float *in = (k & 1) ? p.buf1 : p.buf0;
-        float *out = (k & 1) ? p.buf0 : p.buf1;
+        const float *in = SLOT ? p.buf0 + (size_t)k * p.slot : ((k & 1) ? p.buf1 : p.buf0);
+        float *out = SLOT ? p.buf0 + (size_t)(k + 1) * p.slot : ((k & 1) ? p.buf0 : p.buf1);
         const long items = (long)active * p.tiles;
         for (long it = blockIdx.x; it < items; it += gridDim.x) {
             const int r = (int)(it % active), t = (int)(it / active);
@@ -1079,10 +1082,10 @@ struct PopVariant {
     char name[64] = {0};  // kernel and template arguments, plus the tile depth
 };
 
-template <int LR, int MINB>
+template <int LR, int MINB, bool SLOT = false>
 PopVariant make_signmask_variant(int tz) {
     PopVariant v;
-    v.fn = (const void *)k_population8<LR, MINB>;
+    v.fn = (const void *)k_population8<LR, MINB, SLOT>;
     v.ry = 256 / LR;
     v.g = 1;
     v.threads = 256;
@@ -1178,6 +1181,18 @@ int variants_for(int n, PopVariant *out) {
     return k;
 }
 
+// the dense default's shape keeping every state (population_steps' slot mode)
+PopVariant slot_variant(int n) {
+    switch (n) {
+        case 128:
+            return make_signmask_variant<32, 4, true>(16);
+        case 64:
+            return make_signmask_variant<16, 4, true>(16);
+        default:
+            return make_signmask_variant<8, 4, true>(8);
+    }
+}
+
 // index of the first variant that is neither temporally blocked nor skipping
 int dense_default(const PopVariant *vs, int nv) {
     for (int i = 0; i < nv; ++i)
@@ -1253,7 +1268,7 @@ int ensure_live_tiles(Handle &h, int rows, int tz) {
 // boxes and the zero-filled second buffer) runs it in place of the skipping
 // kernel
 int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_sorted, int S,
-                      bool allow_tb = true, bool allow_skip = false) {
+                      bool allow_tb = true, bool allow_skip = false, size_t slot = 0) {
     const int LR = lanes_per_row(h.n);
     if (!LR) {
         set_error("fast path supports n = 32, 64 or 128");
@@ -1264,7 +1279,7 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
     int vi = h.pop_variant;
     if (vi < 0 || vi >= nv || (vs[vi].tb && !allow_tb) || (vs[vi].skip && !allow_skip))
         vi = dense_default(vs, nv);
-    const PopVariant &v = vs[vi];
+    const PopVariant v = slot ? slot_variant(h.n) : vs[vi];
     PopArgs a;
     a.n = h.n;
     a.S = S;
@@ -1274,6 +1289,7 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
     a.stride = h.N;
     a.buf0 = buf0;
     a.buf1 = buf1;
+    a.slot = slot;
     a.cx = h.cx;
     a.cy = h.cy;
     a.cz = h.cz;
@@ -1304,7 +1320,7 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
 }  // namespace
 
 int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs, SampleRec *sorted, int *rank,
-                     int S) {
+                     int S, size_t slot) {
     if (!lanes_per_row(h.n)) {
         set_error("fast path supports n = 32, 64 or 128");
         return GBG_ERR_UNSUPPORTED;
@@ -1313,7 +1329,7 @@ int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs,
     k_sort_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(recs, S, sorted, rank);
     h.launches++;
     GBG_CUDA_TRY(cudaGetLastError());
-    return launch_population(h, buf0, buf1, sorted, S, false, false);
+    return launch_population(h, buf0, buf1, sorted, S, false, false, slot);
 }
 
 bool population_supported(int n) { return lanes_per_row(n) != 0; }
