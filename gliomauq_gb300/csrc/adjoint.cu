@@ -295,8 +295,8 @@ __global__ void k_adj_tile_live(const float *__restrict__ msk, unsigned char *__
 __global__ void __launch_bounds__(320, 2)
     k_adj_back128(int S, int k, const int *__restrict__ ns, const float *__restrict__ phi, float *__restrict__ lam0,
                   float *__restrict__ lam1,
-                  const float *__restrict__ cx, const float *__restrict__ cy, const float *__restrict__ cz,
-                  const float *__restrict__ msk, const double *__restrict__ a, const double *__restrict__ b,
+                  const float *__restrict__ cxs, const float *__restrict__ cy, const float *__restrict__ cz,
+                  const double *__restrict__ a, const double *__restrict__ b,
                   double *__restrict__ gA, double *__restrict__ gB, const unsigned char *__restrict__ live) {
     using namespace fb;
     constexpr unsigned plane = NN * NN, N = NN * NN * NN;
@@ -334,6 +334,9 @@ __global__ void __launch_bounds__(320, 2)
         float4 CZp = lg4(cz, oy + plane * (unsigned)wz(zstart - 1));
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         float4 U2 = z4, U1 = z4, Pb = z4;  // mu at z-2, z-1; phi at z-1
+        // the previous plane's x/y/z face coefficients: the lambda stage's
+        // (plane z-1) are the mu stage's of one iteration before
+        float4 QX = z4, QY = z4, QZp = z4;
         float pa_t = 0.0f, pb_t = 0.0f;
         for (int st = 0; st < TZ + 2; ++st) {
             const int zu = zstart + st;
@@ -341,9 +344,10 @@ __global__ void __launch_bounds__(320, 2)
             // ---- mu at (y, zu) ----
             const float4 Pn = ld4(f, oy + zno);
             const float4 PS = ld4(f, oym + zo), PN = ld4(f, oyp + zo);
-            const float4 CX = lg4(cx, oy + zo), CY = lg4(cy, oy + zo), CYm = lg4(cy, oym + zo);
-            const float4 CZ = lg4(cz, oy + zo), M = lg4(msk, oy + zo);
+            const float4 CXS = lg4(cxs, oy + zo), CY = lg4(cy, oy + zo), CYm = lg4(cy, oym + zo);
+            const float4 CZ = lg4(cz, oy + zo);
             const float4 LI = ld4(li_, oy + zo);
+            const float4 CX = make_float4(fabsf(CXS.x), fabsf(CXS.y), fabsf(CXS.z), fabsf(CXS.w));
             float4 U;
             {
                 const float left = __shfl_sync(0xffffffffu, Pc.w, left_l);
@@ -355,7 +359,8 @@ __global__ void __launch_bounds__(320, 2)
                 const float pp[4] = {Pp.x, Pp.y, Pp.z, Pp.w}, pq[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
                 const float cy4[4] = {CY.x, CY.y, CY.z, CY.w}, cym4[4] = {CYm.x, CYm.y, CYm.z, CYm.w};
                 const float cz4[4] = {CZ.x, CZ.y, CZ.z, CZ.w}, czp4[4] = {CZp.x, CZp.y, CZp.z, CZp.w};
-                const float m4[4] = {M.x, M.y, M.z, M.w}, l4[4] = {LI.x, LI.y, LI.z, LI.w};
+                const bool on4[4] = {!signbit(CXS.x), !signbit(CXS.y), !signbit(CXS.z), !signbit(CXS.w)};
+                const float l4[4] = {LI.x, LI.y, LI.z, LI.w};
                 float u[4], pa = 0.0f, pb = 0.0f;
                 const bool own = inner && zu >= tz0 && zu < tz0 + TZ;
 #pragma unroll
@@ -369,7 +374,7 @@ __global__ void __launch_bounds__(320, 2)
                     lap = fmaf(cz4[i], pq[i] - f0, lap);
                     float v = fmaf(as, lap, f0);
                     v = fmaf(bs * f0, 1.0f - f0, v);
-                    const float g = (m4[i] != 0.0f && v >= 0.0f && v < 1.0f) ? 1.0f : 0.0f;
+                    const float g = (on4[i] && v >= 0.0f && v < 1.0f) ? 1.0f : 0.0f;
                     u[i] = g * l4[i];
                     pa = fmaf(u[i], lap, pa);
                     pb = fmaf(u[i] * f0, 1.0f - f0, pb);
@@ -388,20 +393,19 @@ __global__ void __launch_bounds__(320, 2)
             __syncthreads();
             // ---- lambda_k at (y, zu - 1) ----
             if (st >= 2 && inner) {
-                const unsigned zc = plane * (unsigned)wz(zu - 1), zb = plane * (unsigned)wz(zu - 2);
+                const unsigned zc = plane * (unsigned)wz(zu - 1);
+                const float4 QYm = lg4(cy, oym + zc);
                 const float4 S1 = *reinterpret_cast<const float4 *>(&ring[(st - 1) % 3][w - 1][x0]);
                 const float4 N1 = *reinterpret_cast<const float4 *>(&ring[(st - 1) % 3][w + 1][x0]);
-                const float4 AX = lg4(cx, oy + zc), AY = lg4(cy, oy + zc), AYm = lg4(cy, oym + zc);
-                const float4 AZ = lg4(cz, oy + zc), AZp = lg4(cz, oy + zb);
                 const float left = __shfl_sync(0xffffffffu, U1.w, left_l);
                 const float right = __shfl_sync(0xffffffffu, U1.x, right_l);
-                const float cxl = __shfl_sync(0xffffffffu, AX.w, left_l);
+                const float cxl = __shfl_sync(0xffffffffu, QX.w, left_l);
                 const float uv[6] = {left, U1.x, U1.y, U1.z, U1.w, right};
-                const float cxa[5] = {cxl, AX.x, AX.y, AX.z, AX.w};
+                const float cxa[5] = {cxl, QX.x, QX.y, QX.z, QX.w};
                 const float us[4] = {S1.x, S1.y, S1.z, S1.w}, un[4] = {N1.x, N1.y, N1.z, N1.w};
                 const float up[4] = {U2.x, U2.y, U2.z, U2.w}, uq[4] = {U.x, U.y, U.z, U.w};
-                const float cy4[4] = {AY.x, AY.y, AY.z, AY.w}, cym4[4] = {AYm.x, AYm.y, AYm.z, AYm.w};
-                const float cz4[4] = {AZ.x, AZ.y, AZ.z, AZ.w}, czp4[4] = {AZp.x, AZp.y, AZp.z, AZp.w};
+                const float cy4[4] = {QY.x, QY.y, QY.z, QY.w}, cym4[4] = {QYm.x, QYm.y, QYm.z, QYm.w};
+                const float cz4[4] = {CZp.x, CZp.y, CZp.z, CZp.w}, czp4[4] = {QZp.x, QZp.y, QZp.z, QZp.w};
                 const float p4[4] = {Pb.x, Pb.y, Pb.z, Pb.w};
                 float o[4];
 #pragma unroll
@@ -422,6 +426,9 @@ __global__ void __launch_bounds__(320, 2)
             Pb = Pc;
             Pp = Pc;
             Pc = Pn;
+            QX = CX;
+            QY = CY;
+            QZp = CZp;
             CZp = CZ;
         }
         // per-sample sensitivities of this tile
@@ -498,6 +505,8 @@ __global__ void k_adj_ic_grad(int n, const gbg_sample *__restrict__ smp, double 
     double acc[3] = {0, 0, 0};
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < (int)N; c += gridDim.x * blockDim.x) {
         const size_t i = (size_t)s * N + c;
+        // a cell outside the initial support adds exactly zero: skip its FP64 work
+        if (phi0[i] == (Real)0) continue;
         const double w = (double)lam[i] * (double)phi0[i] / (sigma * sigma);
         int x, y, z;
         decomp(c, n, x, y, z);
@@ -619,7 +628,8 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
                             (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
                             (size_t)nmax * S * sizeof(double), (size_t)nmax * S * sizeof(double),
                             3 * S * sizeof(double), S * sizeof(gbg_sample), S * sizeof(gbg_lik_result),
-                            S * sizeof(int), 2 * S * sizeof(SampleRec), S * sizeof(int), 1024};
+                            S * sizeof(int), 2 * S * sizeof(SampleRec), S * sizeof(int), 1024,
+                            4 * S * sizeof(int)};
     size_t total = 0;
     for (size_t b : sizes) total += bwork_align(b);
     if (h.adj_ws_bytes < total) {
@@ -633,10 +643,10 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
         }
         h.adj_ws_bytes = total;
     }
-    void *parts[17];
+    void *parts[18];
     {
         char *q = (char *)h.adj_ws;
-        for (int i = 0; i < 17; ++i) {
+        for (int i = 0; i < 18; ++i) {
             parts[i] = q;
             q += bwork_align(sizes[i]);
         }
@@ -659,6 +669,7 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     SampleRec *drec = (SampleRec *)parts[14], *dsorted = drec + S;
     int *drank = (int *)parts[15];
     unsigned char *dlive = (unsigned char *)parts[16];
+    int *dbox = (int *)parts[17];  // initial-support boxes (the skipping population kernel)
     // per-step coefficients; a < 0 marks a finished sample
     std::vector<double> ha((size_t)nmax * S), hb((size_t)nmax * S);
     for (int k = 0; k < nmax; ++k)
@@ -697,7 +708,8 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
     Tabs t{tab, tab + N, tab + 2 * N, tab + 3 * N};
     if (f32) {
         t = Tabs{h.cx, h.cy, h.cz, h.msk};
-        rc = launch_gaussian_ic(h, dsm, S, o.ic_peak, o.ic_sigma, (float *)ck);
+        ADJ_TRY(cudaMemsetAsync(dbox, 0, 4 * S * sizeof(int), st));
+        rc = launch_gaussian_ic(h, dsm, S, o.ic_peak, o.ic_sigma, (float *)ck, dbox);
         if (rc) {
             release();
             return rc;
@@ -736,7 +748,11 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
                 srec[s] = r;
             }
             ADJ_TRY(cudaMemcpyAsync(drec, srec.data(), (size_t)act * sizeof(SampleRec), cudaMemcpyHostToDevice, st));
-            rc = population_steps(h, (float *)buf0, (float *)buf1, drec, dsorted, drank, act);
+            // the skipping kernel may run: checkpoint j's support lies within
+            // the initial boxes grown by k0 cells, and it is zero on every
+            // cell without the mask once a step has run; second buffer zeroed
+            ADJ_TRY(cudaMemsetAsync(buf1, 0, (size_t)act * N * sizeof(Real), st));
+            rc = population_steps(h, (float *)buf0, (float *)buf1, drec, dsorted, drank, act, 0, dbox, k0);
             if (rc) {
                 release();
                 return rc;
@@ -854,8 +870,8 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
                 const long items = (long)A[k] * tiles;
                 const unsigned grid = (unsigned)std::min<long>(items, (long)h.num_sms * 8);
                 k_adj_back128<<<grid, 320, 0, st>>>(A[k], k, dns, (const float *)phik, (float *)lam, (float *)mu,
-                                                    (const float *)t.cx, (const float *)t.cy, (const float *)t.cz,
-                                                    (const float *)t.msk, da + (size_t)k * S, db + (size_t)k * S,
+                                                    h.cxs, (const float *)t.cy, (const float *)t.cz,
+                                                    da + (size_t)k * S, db + (size_t)k * S,
                                                     gA + (size_t)k * S, gB + (size_t)k * S, dlive);
                 h.launches++;
             } else {

@@ -341,6 +341,7 @@ struct PopArgs {
     const int *live_list, *live_count;
     const unsigned char *tile_live;
     const int *box;
+    int grow0;  // the first buffer's support lies within the boxes grown by grow0 cells
     unsigned long long *visited;  // tiles computed by this launch (k_population8/10)
 };
 
@@ -484,9 +485,10 @@ __global__ void __launch_bounds__(256, MINB) k_population10(PopArgs p) {
             const int ylo = n - bx.x, yhi = bx.y - 1, zlo = n - bx.z, zhi = bx.w - 1;
             const int y0 = (t % p.tiles_y) * rows, z0 = (t / p.tiles_y) * p.TZ;
             const int y1 = y0 + rows - 1, z1 = z0 + p.TZ - 1;
-            bool go = span_hits(ylo, yhi, k + 1, y0, y1, n) && span_hits(zlo, zhi, k + 1, z0, z1, n);
+            const int g = p.grow0 + k + 1;
+            bool go = span_hits(ylo, yhi, g, y0, y1, n) && span_hits(zlo, zhi, g, z0, z1, n);
             if (go && k == 1 && !p.tile_live[t])
-                go = span_hits(ylo, yhi, 0, y0, y1, n) && span_hits(zlo, zhi, 0, z0, z1, n);
+                go = span_hits(ylo, yhi, p.grow0, y0, y1, n) && span_hits(zlo, zhi, p.grow0, z0, z1, n);
             if (!go) continue;
             const size_t off = (size_t)order * p.stride;
             const bool last = k == p.rec[r].nsteps - 1;
@@ -1268,7 +1270,8 @@ int ensure_live_tiles(Handle &h, int rows, int tz) {
 // boxes and the zero-filled second buffer) runs it in place of the skipping
 // kernel
 int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_sorted, int S,
-                      bool allow_tb = true, bool allow_skip = false, size_t slot = 0) {
+                      bool allow_tb = true, bool allow_skip = false, size_t slot = 0,
+                      const int *box = nullptr, int grow0 = 0) {
     const int LR = lanes_per_row(h.n);
     if (!LR) {
         set_error("fast path supports n = 32, 64 or 128");
@@ -1302,6 +1305,7 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
     a.live_count = nullptr;
     a.tile_live = nullptr;
     a.box = nullptr;
+    a.grow0 = grow0;
     a.visited = reinterpret_cast<unsigned long long *>(h.barrier + 2);
     if (v.skip) {
         if (h.n % v.tz || h.n % v.ry) {
@@ -1312,7 +1316,7 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
         a.live_list = h.live_list;
         a.live_count = h.live_count;
         a.tile_live = h.tile_live;
-        a.box = batch_boxes(h);
+        a.box = box ? box : batch_boxes(h);
     }
     return launch_population_v(h, a, v);
 }
@@ -1320,7 +1324,7 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
 }  // namespace
 
 int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs, SampleRec *sorted, int *rank,
-                     int S, size_t slot) {
+                     int S, size_t slot, const int *box, int grow0) {
     if (!lanes_per_row(h.n)) {
         set_error("fast path supports n = 32, 64 or 128");
         return GBG_ERR_UNSUPPORTED;
@@ -1329,7 +1333,7 @@ int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs,
     k_sort_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(recs, S, sorted, rank);
     h.launches++;
     GBG_CUDA_TRY(cudaGetLastError());
-    return launch_population(h, buf0, buf1, sorted, S, false, false, slot);
+    return launch_population(h, buf0, buf1, sorted, S, false, box != nullptr && !slot, slot, box, grow0);
 }
 
 bool population_supported(int n) { return lanes_per_row(n) != 0; }
@@ -1383,8 +1387,9 @@ int launch_schedule_smooth(Handle &h, const gbg_sample *samples_device, int S, d
 }
 
 int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, double peak, double sigma,
-                       float *phi) {
-    k_gaussian_ic<<<ic_grid(h, S), 256, 0, h.stream>>>(h.n, samples_device, S, peak, sigma, h.pw, h.pg, phi);
+                       float *phi, int *box) {
+    k_gaussian_ic<<<ic_grid(h, S), 256, 0, h.stream>>>(h.n, samples_device, S, peak, sigma, h.pw, h.pg, phi,
+                                                        nullptr, nullptr, box);
     h.launches++;
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
