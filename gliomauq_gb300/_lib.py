@@ -24,7 +24,7 @@ PREC_BY_NAME = {"f64": PREC_F64, "f32ref": PREC_F32REF, "f32": PREC_F32}
 EXPORTS = [
     "gbg_create", "gbg_destroy", "gbg_last_error", "gbg_version", "gbg_set_anatomy",
     "gbg_set_phi", "gbg_get_phi", "gbg_rd_step", "gbg_run", "gbg_set_observations",
-    "gbg_loglik", "gbg_batch_solve", "gbg_batch_solve_device", "gbg_launch_count",
+    "gbg_loglik", "gbg_batch_solve", "gbg_batch_solve_device", "gbg_set_batch_graphs", "gbg_launch_count",
     "gbg_stream", "gbg_sync", "gbg_last_population_ms", "gbg_last_population_cells",
     "gbg_loglik_noalloc",
     "gbg_population_variants", "gbg_set_population_variant", "gbg_population_variant_shape",
@@ -159,6 +159,7 @@ def load(path: str = LIB_PATH):
         "gbg_last_population_cells": [vp, C.POINTER(C.c_longlong)],
         "gbg_population_variants": [vp, C.POINTER(C.c_int)],
         "gbg_set_population_variant": [vp, C.c_int],
+        "gbg_set_batch_graphs": [vp, C.c_int],
         "gbg_population_variant_name": [vp, C.c_int, C.c_char_p, C.c_int],
         "gbg_population_variant_shape": [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)],
@@ -482,6 +483,11 @@ class Handle:
 
     def set_population_variant(self, index: int):
         check(self.lib.gbg_set_population_variant(self._h, index))
+
+    def set_batch_graphs(self, enabled: bool):
+        """batch_solve as one CUDA graph launch per call (default) or as
+        separate kernel launches; the results are the same bit for bit."""
+        check(self.lib.gbg_set_batch_graphs(self._h, 1 if enabled else 0))
 
     def autotune(self, probe_samples: int = 32, cache_path: str | None = None) -> int:
         c = C.c_int()

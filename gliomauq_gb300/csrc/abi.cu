@@ -84,12 +84,14 @@ void free_handle(Handle &h) {
         if (p) cudaFree(p);
     for (cudaEvent_t e : h.ev_pop)
         if (e) cudaEventDestroy(e);
+    gbg::batch_graphs_clear(h);
     if (h.is_amr) gbg::amr_free(h);
     if (h.stream) cudaStreamDestroy(h.stream);
 }
 
 int ensure_lik_out(Handle &h, int S) {
     if (h.lik_out_cap >= S) return GBG_OK;
+    ++h.state_gen;
     if (h.lik_out) cudaFree(h.lik_out);
     h.lik_out = nullptr;
     h.lik_out_cap = 0;
@@ -218,6 +220,7 @@ int gbg_set_anatomy(gbg_handle *hh, const double *p_w, const double *p_g) {
     h.fast_valid = false;
     h.live_valid = false;
     h.mala_valid = false;
+    ++h.state_gen;
     return GBG_OK;
 }
 
@@ -508,6 +511,18 @@ int gbg_batch_solve_device(gbg_handle *hh, const gbg_sample *samples_device, int
     return gbg::batch_solve_device(h, samples_device, S, *o, loglik_device, nullptr);
 }
 
+int gbg_set_batch_graphs(gbg_handle *hh, int enabled) {
+    if (int rc = check_handle(hh)) return rc;
+    Handle &h = hh->h;
+    h.batch_graphs = enabled != 0;
+    if (!h.batch_graphs) {
+        GBG_CUDA_TRY(cudaSetDevice(h.device));
+        GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
+        gbg::batch_graphs_clear(h);
+    }
+    return GBG_OK;
+}
+
 int gbg_batch_solve(gbg_handle *hh, const gbg_sample *samples, int S, const gbg_batch_opts *o,
                     gbg_lik_result *loglik, long *nsteps_out, float *phi_out) {
     if (int rc = check_handle(hh)) return rc;
@@ -530,14 +545,24 @@ int gbg_batch_solve(gbg_handle *hh, const gbg_sample *samples, int S, const gbg_
     GBG_CUDA_TRY(cudaMemcpyAsync(d_samples, samples, sizeof(gbg_sample) * S, cudaMemcpyHostToDevice, h.stream));
     gbg_lik_result *d_lik = nullptr;
     if (o->with_loglik) {
-        if (int rc = ensure_lik_out(h, S)) return rc;
+        // sized for max_samples at once: captured graphs name this buffer
+        if (int rc = ensure_lik_out(h, std::max(S, h.max_samples))) return rc;
         d_lik = (gbg_lik_result *)h.lik_out;
     }
-    std::vector<long> steps(S);
-    int rc = gbg::batch_solve_device(h, d_samples, S, *o, d_lik, steps.data());
+    // one graph launch per call (captured on the first call with this S and
+    // these options) unless graphs are switched off for the handle
+    int rc = (h.batch_graphs && h.prec == GBG_PREC_F32)
+                 ? gbg::batch_graph_run(h, d_samples, S, *o, d_lik)
+                 : gbg::batch_solve_device(h, d_samples, S, *o, d_lik, nullptr);
     if (rc) return rc;
+    std::vector<gbg::SampleRec> recs(S);
+    GBG_CUDA_TRY(cudaMemcpyAsync(recs.data(), gbg::batch_unsorted(h), sizeof(gbg::SampleRec) * S,
+                                 cudaMemcpyDeviceToHost, h.stream));
+    GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
     rc = gbg::check_device_status(h);
     if (rc) return rc;
+    std::vector<long> steps(S);
+    for (int s = 0; s < S; ++s) steps[s] = recs[s].nsteps;
     if (nsteps_out)
         for (int s = 0; s < S; ++s) nsteps_out[s] = steps[s];
     if (loglik && d_lik)

@@ -72,6 +72,16 @@ struct AmrState {
     gbg_amr_run_stats last_run{};    // statistics of the latest gbg_amr_run
 };
 
+struct BatchGraph {
+    int S = 0, with_loglik = 0, variant = 0;
+    double L = 0, ic_peak = 0, ic_sigma = 0, dt0 = 0;
+    const void *samples = nullptr, *lik = nullptr;  // device pointers the graph reads / writes
+    unsigned long long gen = 0, last_use = 0;
+    long long launches = 0;  // kernels per replay
+    long long tile_cells = 0;  // the captured population kernel's cells per tile
+    cudaGraphExec_t exec = nullptr;
+};
+
 struct Handle {
     int n = 0;
     size_t N = 0;
@@ -123,6 +133,16 @@ struct Handle {
 
     // population-kernel shape (index into the candidates for this n; 0 = default)
     int pop_variant = 0;
+
+    // CUDA graphs of the batched solve (gbg_batch_solve): one per sample
+    // count, options and population-kernel shape, captured from the handle's
+    // stream. state_gen counts the changes that invalidate a captured graph
+    // (a buffer it names reallocated, a table or tile list it reads rebuilt,
+    // new observations); a graph captured at another generation is captured
+    // anew.
+    unsigned long long state_gen = 0;
+    bool batch_graphs = true;
+    std::vector<BatchGraph> graphs;
 
     // tiles of the skipping population kernel (k_population10): a tile (RY
     // rows of full x-rows by TZ planes) is live when one of its cells has a
@@ -231,6 +251,17 @@ int launch_schedule_smooth(Handle &h, const gbg_sample *samples_device, int S, d
 int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs, SampleRec *sorted, int *rank,
                      int S, size_t slot = 0, const int *box = nullptr, int grow0 = 0);
 bool population_supported(int n);
+// Builds and allocates what batch_solve_device would build or allocate on
+// first use (fast tables, the skipping kernel's tile list, likelihood
+// partials for S samples), so that a stream capture of it records launches
+// and copies only.
+int batch_prepare(Handle &h, int S, const gbg_batch_opts &o);
+int lik_reserve(Handle &h, int S);
+// batch_solve_device through a CUDA graph of it (captured on first use for
+// this S and options, replayed after); no step counts.
+int batch_graph_run(Handle &h, const gbg_sample *samples_device, int S, const gbg_batch_opts &o,
+                    gbg_lik_result *loglik_device);
+void batch_graphs_clear(Handle &h);
 int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, double peak, double sigma,
                        float *phi, int *box = nullptr);
 int fast_steps_single(Handle &h, double Dw, double rho, double dt, long nsteps);

@@ -21,6 +21,7 @@
 #include "lik_terms.cuh"
 
 namespace gbg {
+
 namespace {
 
 constexpr int kLikThreads = 256;
@@ -160,16 +161,9 @@ int run_lik(Handle &h, const Src &src, int S, gbg_lik_result *out_device) {
         set_error("observations not set");
         return GBG_ERR_STATE;
     }
+    if (int rc = lik_reserve(h, S)) return rc;
     const int items = h.obs.n_pet > h.obs.n_ti ? h.obs.n_pet : h.obs.n_ti;
     const int chunks = items > 0 ? (items + kLikChunk - 1) / kLikChunk : 1;
-    const size_t need = (size_t)S * chunks * 3;
-    if (need > h.lik_partials_cap) {
-        if (h.lik_partials) cudaFree(h.lik_partials);
-        h.lik_partials = nullptr;
-        h.lik_partials_cap = 0;
-        GBG_CUDA_TRY(cudaMalloc((void **)&h.lik_partials, need * sizeof(double)));
-        h.lik_partials_cap = need;
-    }
     LikArgs a;
     a.n_pet = h.obs.n_pet;
     a.n_ti = h.obs.n_ti;
@@ -195,6 +189,23 @@ int run_lik(Handle &h, const Src &src, int S, gbg_lik_result *out_device) {
 
 }  // namespace
 
+// Partial-sum storage of the likelihood reduction for S samples.
+int lik_reserve(Handle &h, int S) {
+    const int items = h.obs.n_pet > h.obs.n_ti ? h.obs.n_pet : h.obs.n_ti;
+    const int chunks = items > 0 ? (items + kLikChunk - 1) / kLikChunk : 1;
+    const size_t need = (size_t)S * chunks * 3;
+    if (need > h.lik_partials_cap) {
+        ++h.state_gen;
+        if (h.lik_partials) cudaFree(h.lik_partials);
+        h.lik_partials = nullptr;
+        h.lik_partials_cap = 0;
+        GBG_CUDA_TRY(cudaMalloc((void **)&h.lik_partials, need * sizeof(double)));
+        h.lik_partials_cap = need;
+    }
+    return GBG_OK;
+}
+
+
 int lik_set_observations(Handle &h, const double *pet, const double *t1, const double *t2,
                          const double *points, long npoints, const gbg_lik_params &p) {
     const int n = h.n;
@@ -202,6 +213,7 @@ int lik_set_observations(Handle &h, const double *pet, const double *t1, const d
         set_error("likelihood parameters out of range");
         return GBG_ERR_ARG;
     }
+    ++h.state_gen;  // captured batched solves name the observation lists
     std::vector<int> pet_idx, ti_idx;
     std::vector<double> pet_val, v1, v2;
     for (int iz = 0; iz < n; iz++)

@@ -1218,10 +1218,15 @@ int launch_population_v(Handle &h, PopArgs &a, const PopVariant &v) {
     GBG_CUDA_TRY(cudaMemsetAsync(a.barrier, 0, 4 * sizeof(unsigned), h.stream));
     h.pop_tile_cells = v.counts ? (long long)v.ry * v.tz * a.n : 0;
     void *args[] = {&a};
-    GBG_CUDA_TRY(cudaEventRecord(h.ev_pop[0], h.stream));
+    // inside a stream capture the events become record nodes of the graph
+    // (recorded at each replay), so gbg_last_population_ms times replays too
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    GBG_CUDA_TRY(cudaStreamIsCapturing(h.stream, &cap));
+    const unsigned evf = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    GBG_CUDA_TRY(cudaEventRecordWithFlags(h.ev_pop[0], h.stream, evf));
     GBG_CUDA_TRY(cudaLaunchCooperativeKernel(v.fn, dim3((unsigned)grid), dim3(v.threads), args, v.smem,
                                              h.stream));
-    GBG_CUDA_TRY(cudaEventRecord(h.ev_pop[1], h.stream));
+    GBG_CUDA_TRY(cudaEventRecordWithFlags(h.ev_pop[1], h.stream, evf));
     h.ev_pop_recorded = true;
     h.launches++;
     return GBG_OK;
@@ -1246,6 +1251,7 @@ bool variant_is_skip(const Handle &h) {
 // changes or another tile shape is asked for.
 int ensure_live_tiles(Handle &h, int rows, int tz) {
     if (h.live_valid && h.live_ry == rows && h.live_tz == tz) return GBG_OK;
+    ++h.state_gen;
     const int tiles = (h.n / rows) * (h.n / tz);
     if (!h.tile_live) {
         // sized for the smallest tiles any variant uses (rows >= 8, tz >= 8)
@@ -1397,6 +1403,7 @@ int launch_gaussian_ic(Handle &h, const gbg_sample *samples_device, int S, doubl
 
 int fast_build_tables(Handle &h, double ratio) {
     if (h.fast_valid && h.fast_ratio == ratio) return GBG_OK;
+    ++h.state_gen;
     k_fast_tables<<<grid_for(h, h.N), 256, 0, h.stream>>>(h.n, h.pw, h.pg, ratio, h.cx, h.cy,
                                                            h.cz, h.msk, h.cxs);
     h.launches++;
@@ -1482,6 +1489,102 @@ int batch_solve_device(Handle &h, const gbg_sample *samples_device, int S,
         GBG_CUDA_TRY(cudaStreamSynchronize(h.stream));
         for (int s = 0; s < S; ++s) nsteps_host[s] = tmp[s].nsteps;
     }
+    return GBG_OK;
+}
+
+int batch_prepare(Handle &h, int S, const gbg_batch_opts &o) {
+    if (h.prec != GBG_PREC_F32) return GBG_OK;  // the eager path reports the error
+    if (int rc = fast_build_tables(h, (double)0.1f)) return rc;
+    if (variant_is_skip(h)) {
+        PopVariant vs[32];
+        variants_for(h.n, vs);
+        const PopVariant &v = vs[h.pop_variant];
+        if (h.n % v.tz == 0 && h.n % v.ry == 0)
+            if (int rc = ensure_live_tiles(h, v.ry, v.tz)) return rc;
+    }
+    if (o.with_loglik)
+        if (int rc = lik_reserve(h, S)) return rc;
+    return GBG_OK;
+}
+
+void batch_graphs_clear(Handle &h) {
+    for (BatchGraph &g : h.graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    h.graphs.clear();
+}
+
+// Graphs kept per handle; the least recently used is dropped beyond this.
+constexpr size_t kMaxBatchGraphs = 8;
+
+int batch_graph_run(Handle &h, const gbg_sample *samples_device, int S, const gbg_batch_opts &o,
+                    gbg_lik_result *loglik_device) {
+    static unsigned long long use_clock = 0;
+    const int wl = (o.with_loglik && loglik_device) ? 1 : 0;
+    auto same = [&](const BatchGraph &g) {
+        return g.S == S && g.with_loglik == wl && g.variant == h.pop_variant && g.L == o.L && g.ic_peak == o.ic_peak &&
+               g.ic_sigma == o.ic_sigma && g.dt0 == o.dt0 && g.samples == samples_device &&
+               g.lik == (const void *)loglik_device;
+    };
+    BatchGraph *hit = nullptr;
+    for (BatchGraph &g : h.graphs)
+        if (same(g)) hit = &g;
+    if (hit && hit->gen != h.state_gen) {  // stale: drop it
+        cudaGraphExecDestroy(hit->exec);
+        h.graphs.erase(h.graphs.begin() + (hit - h.graphs.data()));
+        hit = nullptr;
+    }
+    if (!hit) {
+        if (int rc = batch_prepare(h, S, o)) return rc;
+        const long long l0 = h.launches;
+        GBG_CUDA_TRY(cudaStreamBeginCapture(h.stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = batch_solve_device(h, samples_device, S, o, loglik_device, nullptr);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(h.stream, &graph);
+        const long long per = h.launches - l0;
+        h.launches = l0;
+        if (rc || ec != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            if (!rc) set_error(std::string("batched solve capture: ") + cudaGetErrorString(ec));
+            return rc ? rc : GBG_ERR_CUDA;
+        }
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            cudaGetLastError();
+            set_error(std::string("batched solve graph: ") + cudaGetErrorString(ei));
+            return GBG_ERR_CUDA;
+        }
+        if (h.graphs.size() >= kMaxBatchGraphs) {
+            size_t old = 0;
+            for (size_t i = 1; i < h.graphs.size(); ++i)
+                if (h.graphs[i].last_use < h.graphs[old].last_use) old = i;
+            cudaGraphExecDestroy(h.graphs[old].exec);
+            h.graphs.erase(h.graphs.begin() + old);
+        }
+        BatchGraph g;
+        g.S = S;
+        g.with_loglik = wl;
+        g.variant = h.pop_variant;
+        g.L = o.L;
+        g.ic_peak = o.ic_peak;
+        g.ic_sigma = o.ic_sigma;
+        g.dt0 = o.dt0;
+        g.samples = samples_device;
+        g.lik = loglik_device;
+        g.gen = h.state_gen;
+        g.launches = per;
+        g.tile_cells = h.pop_tile_cells;
+        g.exec = exec;
+        h.graphs.push_back(g);
+        hit = &h.graphs.back();
+    }
+    hit->last_use = ++use_clock;
+    GBG_CUDA_TRY(cudaGraphLaunch(hit->exec, h.stream));
+    h.launches += hit->launches;
+    h.pop_tile_cells = hit->tile_cells;
+    h.ev_pop_recorded = true;
     return GBG_OK;
 }
 

@@ -180,6 +180,16 @@ typedef struct {
  * modes only (GBG_PREC_F32 or GBG_PREC_F32REF). */
 int gbg_batch_solve(gbg_handle *h, const gbg_sample *samples, int S, const gbg_batch_opts *o,
                     gbg_lik_result *loglik, long *nsteps_out, float *phi_out);
+/* gbg_batch_solve runs as one CUDA graph launch per call: the first call
+ * with a given S and options captures the device-side sequence (schedule,
+ * sort, initial densities, the persistent cooperative population kernel,
+ * the likelihood reduction) from the handle's stream, later calls copy the
+ * samples in, replay the graph and copy the results out. Graphs are kept per
+ * population-kernel shape (gbg_set_population_variant, gbg_autotune), at most
+ * 8 per handle, and captured anew after the anatomy or the observations
+ * change. enabled = 0 launches the kernels one by one
+ * instead (the same results, bit for bit). Default: enabled. */
+int gbg_set_batch_graphs(gbg_handle *h, int enabled);
 /* Device-resident entry: samples_device (S gbg_sample) and loglik_device (S
  * gbg_lik_result, or null) are device pointers; runs on the handle's stream
  * and returns without synchronising. */

@@ -188,3 +188,52 @@ def test_skipping_kernel_equals_dense_on_edge_cases(gbg, n):
                 for j in range(len(smp)):
                     assert np.array_equal(got["phi"][j], ref["phi"][j]), (names[i], sigma, j)
         assert list(ref["nsteps"][2:5]) == [1, 2, 0]
+
+
+def test_graph_replay_equals_separate_launches(gbg):
+    """gbg_batch_solve as one CUDA graph launch per call: the first call with
+    a sample count and options captures the graph, later calls replay it with
+    new samples; densities, step counts and log L equal the separately
+    launched kernels bit for bit, and a graph is captured anew after the
+    observations, the anatomy or the population kernel change."""
+    an, samples = _setup()
+    n = an.n
+    rng = np.random.default_rng(7)
+    sets = [[s.as_tuple() for s in samples]]
+    for _ in range(2):
+        sets.append([(s.Dw * (1 + 0.2 * rng.random()), s.rho * (1 + 0.2 * rng.random()),
+                      s.x0 + rng.random(), s.y0 - rng.random(), s.z0, s.T * (0.8 + 0.4 * rng.random()))
+                     for s in samples])
+    truth = np.clip(S.gaussian_ic(an, 15.0, 16.0, 15.0, peak=0.9, sigma=2.0), 0, 1)
+    obs = [S.make_observations(truth, an, seed=sd, centre_xyz=(15, 16, 15), radius_vox=9.0)
+           for sd in (3, 5)]
+
+    def solve(h, smp, dt0):
+        r = h.batch_solve(smp, an.L, want_phi=True, dt0=dt0)
+        return r["phi"], r["nsteps"], np.array([d["total"] for d in r["loglik"]])
+
+    def run(graphs):
+        out = []
+        with _lib.Handle(n, "f32", max_samples=len(samples)) as h:
+            h.set_batch_graphs(graphs)
+            h.set_anatomy(an.p_w, an.p_g)
+            for o in obs:
+                h.set_observations(o.pet, o.t1, o.t2, o.points, LIK, step_pet=1, step_ti=1)
+                for smp in sets:
+                    for dt0 in (0.0, -1.0):
+                        l0 = h.launch_count()
+                        out.append(solve(h, smp, dt0) + (h.launch_count() - l0,))
+            h.set_population_variant(len(h.population_variants()) - 1)  # the last candidate
+            out.append(solve(h, sets[1], 0.0) + (None,))
+            h.set_anatomy(an.p_w * 0.5 + an.p_g * 0.5, an.p_g * 0.5 + an.p_w * 0.5)
+            out.append(solve(h, sets[2], -1.0) + (None,))
+        return out
+
+    eager, graph = run(False), run(True)
+    assert len(eager) == len(graph)
+    for i, (e, g) in enumerate(zip(eager, graph)):
+        assert np.array_equal(e[0], g[0]), i
+        assert np.array_equal(e[1], g[1]), i
+        assert np.array_equal(e[2], g[2]), i
+        if e[3] is not None:
+            assert e[3] == g[3], (i, e[3], g[3])
