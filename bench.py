@@ -562,6 +562,40 @@ def amr_adaptive_measurement(device, level=4, seed=7, steps_per_regrid=20):
     return out
 
 
+def graph_measurement(device, n=128, reps=20):
+    """gbg_batch_solve per call (host-timed, host buffers in and out) with the
+    call as one CUDA graph launch (the default) and as separate kernel
+    launches, for a single sample (the plain chain's solve) and for 64 (a
+    pipeline generation), prior draws near the truth on the scaled grid."""
+    from gliomauq_gb300 import _lib, synthetic as Syn
+    an = Syn.make_anatomy(n, seed=0)
+    truth = Syn.draw_prior(an, 1, seed=10_000)[0]
+    h = _lib.Handle(n, "f32", device=device, max_samples=64)
+    out = {}
+    try:
+        h.set_anatomy(an.p_w, an.p_g)
+        u = h.batch_solve([truth.as_tuple()], an.L, with_loglik=False, want_phi=True, dt0=-1.0)["phi"][0]
+        obs = Syn.make_observations(u.astype(np.float64), an, seed=3,
+                                    centre_xyz=(truth.x0, truth.y0, truth.z0), radius_vox=27.0 * n / 128)
+        h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2)
+        rng = np.random.default_rng(1)
+        for S in (1, 64):
+            smp = [tuple(np.array(truth.as_tuple()) * (1 + 0.01 * rng.standard_normal(6))) for _ in range(S)]
+            res = {}
+            for key, graphs in (("graph_ms", True), ("separate_launches_ms", False)):
+                h.set_batch_graphs(graphs)
+                for _ in range(3):
+                    h.batch_solve(smp, an.L, dt0=-1.0)
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    h.batch_solve(smp, an.L, dt0=-1.0)
+                res[key] = 1e3 * (time.perf_counter() - t0) / reps
+            out[f"samples_{S}"] = res
+    finally:
+        h.close()
+    return out
+
+
 def screen_and_statistics_measurement(device, n=128, chains=64, steps=64, reps=3, stat_samples=512):
     """Two kernels of the sampling path at n^3 on the bench problem:
       * the GPU screening chain (k_affine_chain, gbg_affine_chain): `chains`
@@ -676,6 +710,7 @@ def adjoint_measurement(device, n=128, samples=64, reps=2):
                 r = h.batch_solve(smp, an.L, dt0=-1.0)
             res["batched_solve_ms"] = 1e3 * (time.perf_counter() - t0) / reps
             res["mean_steps"] = float(np.mean(r["nsteps"]))
+            res["max_steps"] = int(np.max(r["nsteps"]))
             out[name] = res
     finally:
         h.close()
@@ -813,6 +848,8 @@ def main():
                     help="print the screening-chain and propagation-statistics measurement alone")
     ap.add_argument("--only-amr", action="store_true",
                     help="print the multiresolution-grid measurement alone")
+    ap.add_argument("--adjoint-samples", type=int, default=64,
+                    help="samples per set in the adjoint measurement")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="print the adjoint measurement alone")
     ap.add_argument("--mcmc-chains", type=int, default=64, help="pipeline chains")
@@ -835,7 +872,8 @@ def main():
         print(json.dumps({"surrogate": surrogate_measurement(int(os.environ.get("LOCAL_RANK", "0")))}))
         return
     if args.only_adjoint:
-        print(json.dumps({"adjoint": adjoint_measurement(int(os.environ.get("LOCAL_RANK", "0")))}))
+        print(json.dumps({"adjoint": adjoint_measurement(int(os.environ.get("LOCAL_RANK", "0")),
+                                                         samples=args.adjoint_samples)}))
         return
     if args.only_amr:
         dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -844,8 +882,9 @@ def main():
         print(json.dumps({"amr": res}))
         return
     if args.only_kernels:
-        print(json.dumps({"sampling_kernels": screen_and_statistics_measurement(
-            int(os.environ.get("LOCAL_RANK", "0")))}))
+        dev = int(os.environ.get("LOCAL_RANK", "0"))
+        print(json.dumps({"sampling_kernels": screen_and_statistics_measurement(dev),
+                          "batch_call": graph_measurement(dev)}))
         return
     if args.only_mcmc:
         print(json.dumps({"mcmc": mcmc_comparison(int(os.environ.get("LOCAL_RANK", "0")),
@@ -998,6 +1037,7 @@ def main():
             line["amr"] = amr_measurement(local_rank)
             line["amr"]["adaptive"] = amr_adaptive_measurement(local_rank)
         line["sampling_kernels"] = screen_and_statistics_measurement(local_rank)
+        line["batch_call"] = graph_measurement(local_rank)
         line["adjoint"] = adjoint_measurement(local_rank)
         if not args.no_surrogate:
             line["surrogate"] = surrogate_measurement(local_rank)
