@@ -834,7 +834,10 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
         if (pop_fwd) {
             // one population launch keeping every state (slot mode): sample s
             // takes steps k0 .. min(ns[s] - 1, k1 - 1) - 1, all full steps (a
-            // sample's shortened last step only feeds the likelihood)
+            // sample's shortened last step only feeds the likelihood); the
+            // skipping kernel computes the tiles its rule keeps (the
+            // checkpoint's support lies within the initial boxes grown by k0)
+            // and writes zeros over the rest
             const int act = A[k0];
             int most = 0;
             for (int s = 0; s < act; ++s) {
@@ -849,7 +852,7 @@ int run_adjoint(Handle &h, const gbg_sample *samples, int S, const gbg_adjoint_o
             if (most > 0) {
                 ADJ_TRY(cudaMemcpyAsync(drec, rrec.data(), (size_t)act * sizeof(SampleRec), cudaMemcpyHostToDevice,
                                         st));
-                rc = population_steps(h, (float *)seg, (float *)seg, drec, dsorted, drank, act, SN);
+                rc = population_steps(h, (float *)seg, (float *)seg, drec, dsorted, drank, act, SN, dbox, k0);
                 if (rc) {
                     release();
                     return rc;

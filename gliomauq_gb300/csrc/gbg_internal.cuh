@@ -243,11 +243,11 @@ int launch_schedule_smooth(Handle &h, const gbg_sample *samples_device, int S, d
 // scratch for S records / ints. Dense kernels only (no temporal blocking, no
 // skipping: the states may be anything). slot > 0 keeps every state instead:
 // step k reads buf0 + k * slot and writes buf0 + (k + 1) * slot (buf1 unused).
-// box non-null (slot 0): the skipping kernel may run, given per-sample
-// support boxes as launch_gaussian_ic records them (indexed by record order)
-// of an initial state whose support lies within them grown by grow0 cells,
-// that state zero on every cell without the mask unless grow0 = 0, and a
-// zero-filled buf1.
+// box non-null: the skipping kernel may run, given per-sample support boxes
+// as launch_gaussian_ic records them (indexed by record order) of an initial
+// state whose support lies within them grown by grow0 cells; with slot 0 it
+// also needs that state zero on every cell without the mask unless
+// grow0 = 0, and a zero-filled buf1 (in slot mode it writes every tile).
 int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs, SampleRec *sorted, int *rank,
                      int S, size_t slot = 0, const int *box = nullptr, int grow0 = 0);
 bool population_supported(int n);

@@ -462,35 +462,58 @@ __device__ __forceinline__ bool span_hits(int lo, int hi, int grow, int a, int b
     return lo <= b && a <= hi;
 }
 
-template <int LR, int MINB>
+// Zeros over a tile of rows x TZ planes (march_tile_s's thread mapping).
+template <int LR>
+__device__ __forceinline__ void zero_tile(int n, int TZ, int ty0, int tz0, float *__restrict__ out) {
+    const int x0 = 4 * ((threadIdx.x & 31) % LR);
+    const int y = ty0 + (int)(threadIdx.x / LR);
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int z = tz0; z < tz0 + TZ; ++z)
+        *reinterpret_cast<float4 *>(out + x0 + (size_t)n * ((size_t)y + (size_t)n * z)) = z4;
+}
+
+// SLOT = true keeps every state (step k reads buf0 + k * slot, writes
+// buf0 + (k + 1) * slot): every round visits every tile of its active
+// samples, computing those the rule above keeps and writing zeros over the
+// others (a slot's previous contents are arbitrary), so each state is
+// complete.
+template <int LR, int MINB, bool SLOT = false>
 __global__ void __launch_bounds__(256, MINB) k_population10(PopArgs p) {
     const int maxsteps = p.S > 0 ? p.rec[0].nsteps : 0;
     int active = p.S;
     const int rows = 256 / LR;
     const int n = p.n;
-    const int nlive = *p.live_count;
+    const int nlive = SLOT ? p.tiles : *p.live_count;
     unsigned long long visited = 0;
     for (int k = 0; k < maxsteps; ++k) {
         while (active > 0 && p.rec[active - 1].nsteps <= k) --active;
-        const float *in = (k & 1) ? p.buf1 : p.buf0;
-        float *out = (k & 1) ? p.buf0 : p.buf1;
-        const int ntiles = k == 1 ? p.tiles : nlive;
+        const float *in = SLOT ? p.buf0 + (size_t)k * p.slot : ((k & 1) ? p.buf1 : p.buf0);
+        float *out = SLOT ? p.buf0 + (size_t)(k + 1) * p.slot : ((k & 1) ? p.buf0 : p.buf1);
+        const int ntiles = (SLOT || k == 1) ? p.tiles : nlive;
         const long items = (long)active * ntiles;
         for (long it = blockIdx.x; it < items; it += gridDim.x) {
             const int r = (int)(it % active), ti = (int)(it / active);
-            const int t = k == 1 ? ti : p.live_list[ti];
+            const int t = (SLOT || k == 1) ? ti : p.live_list[ti];
             const int order = p.rec[r].order;
+            const size_t off = (size_t)order * p.stride;
             const int4 bx = reinterpret_cast<const int4 *>(p.box)[order];
-            if (bx.y == 0) continue;  // no nonzero initial cell: the sample stays 0
-            const int ylo = n - bx.x, yhi = bx.y - 1, zlo = n - bx.z, zhi = bx.w - 1;
             const int y0 = (t % p.tiles_y) * rows, z0 = (t / p.tiles_y) * p.TZ;
+            if (bx.y == 0) {  // no nonzero initial cell: the sample stays 0
+                if (SLOT) zero_tile<LR>(n, p.TZ, y0, z0, out + off);
+                continue;
+            }
+            const int ylo = n - bx.x, yhi = bx.y - 1, zlo = n - bx.z, zhi = bx.w - 1;
             const int y1 = y0 + rows - 1, z1 = z0 + p.TZ - 1;
             const int g = p.grow0 + k + 1;
             bool go = span_hits(ylo, yhi, g, y0, y1, n) && span_hits(zlo, zhi, g, z0, z1, n);
-            if (go && k == 1 && !p.tile_live[t])
+            if (SLOT)
+                go = go && p.tile_live[t];
+            else if (go && k == 1 && !p.tile_live[t])
                 go = span_hits(ylo, yhi, p.grow0, y0, y1, n) && span_hits(zlo, zhi, p.grow0, z0, z1, n);
-            if (!go) continue;
-            const size_t off = (size_t)order * p.stride;
+            if (!go) {
+                if (SLOT) zero_tile<LR>(n, p.TZ, y0, z0, out + off);
+                continue;
+            }
             const bool last = k == p.rec[r].nsteps - 1;
             march_tile_s<LR>(n, p.TZ, y0, z0, in + off, out + off, p.cxs, p.cy, p.cz,
                              last ? p.rec[r].a2 : p.rec[r].a, last ? p.rec[r].b2 : p.rec[r].b);
@@ -1098,10 +1121,10 @@ PopVariant make_signmask_variant(int tz) {
     return v;
 }
 
-template <int LR, int MINB>
+template <int LR, int MINB, bool SLOT = false>
 PopVariant make_skip_variant(int tz) {
     PopVariant v;
-    v.fn = (const void *)k_population10<LR, MINB>;
+    v.fn = (const void *)k_population10<LR, MINB, SLOT>;
     v.ry = 256 / LR;
     v.g = 1;
     v.threads = 256;
@@ -1183,8 +1206,17 @@ int variants_for(int n, PopVariant *out) {
     return k;
 }
 
-// the dense default's shape keeping every state (population_steps' slot mode)
-PopVariant slot_variant(int n) {
+// the kernels keeping every state (population_steps' slot mode): the dense
+// default's shape, or the skipping kernel with tile depth tz
+PopVariant slot_variant(int n, bool skip, int tz) {
+    if (skip) switch (n) {
+            case 128:
+                return make_skip_variant<32, 4, true>(tz);
+            case 64:
+                return make_skip_variant<16, 4, true>(tz);
+            default:
+                return make_skip_variant<8, 4, true>(tz);
+        }
     switch (n) {
         case 128:
             return make_signmask_variant<32, 4, true>(16);
@@ -1288,7 +1320,11 @@ int launch_population(Handle &h, float *buf0, float *buf1, const SampleRec *rec_
     int vi = h.pop_variant;
     if (vi < 0 || vi >= nv || (vs[vi].tb && !allow_tb) || (vs[vi].skip && !allow_skip))
         vi = dense_default(vs, nv);
-    const PopVariant v = slot ? slot_variant(h.n) : vs[vi];
+    // slot mode: the skipping kernel when boxes are given, at the chosen
+    // skipping shape's tile depth (the default one's otherwise)
+    const int slot_tz = (h.pop_variant >= 0 && h.pop_variant < nv && vs[h.pop_variant].skip) ? vs[h.pop_variant].tz
+                                                                                            : vs[0].tz;
+    const PopVariant v = slot ? slot_variant(h.n, box != nullptr, slot_tz) : vs[vi];
     PopArgs a;
     a.n = h.n;
     a.S = S;
@@ -1339,7 +1375,7 @@ int population_steps(Handle &h, float *buf0, float *buf1, const SampleRec *recs,
     k_sort_schedule<<<(S + 127) / 128, 128, 0, h.stream>>>(recs, S, sorted, rank);
     h.launches++;
     GBG_CUDA_TRY(cudaGetLastError());
-    return launch_population(h, buf0, buf1, sorted, S, false, box != nullptr && !slot, slot, box, grow0);
+    return launch_population(h, buf0, buf1, sorted, S, false, box != nullptr, slot, box, grow0);
 }
 
 bool population_supported(int n) { return lanes_per_row(n) != 0; }
