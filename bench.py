@@ -200,7 +200,8 @@ def cpu_baseline(an, prior, seconds=12.0, obs=None):
 
 def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=64,
                     plain_chains=4, plain_steps=1500, plain_burn=300, ref_generations=500,
-                    plain_cap_s=150.0, unet=True, mala_steps=0, mala_burn=100, ind_prob=0.0):
+                    plain_cap_s=150.0, unet=True, mala_steps=0, mala_burn=100, ind_prob=0.0,
+                    unet_train=20000, unet_epochs=3):
     """Posterior effective samples per second at n^3 on one synthetic
     patient, plain single-solve MCMC against the batched + adjoint +
     surrogate pipeline, both in the scaling symmetry's coordinates
@@ -389,7 +390,8 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=6
                            ms_per_step=1e3 * rm.seconds / (mala_burn + mala_steps),
                            mean_check=mean_check(lc.to_theta(rm.samples[mala_burn:])), **d_m)
     if unet:
-        out["learned_surrogate"] = ls = unet_screen(h, an, prior, dt0, res, rng)
+        out["learned_surrogate"] = ls = unet_screen(h, an, prior, dt0, res, rng, train_n=unet_train,
+                                                    epochs=unet_epochs)
         # what the trained network gains: the same delayed-acceptance sampler
         # with the network as its screen, against the tangent screen and
         # against no screen (the plain chains)
@@ -403,7 +405,7 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=6
     return out
 
 
-def unet_screen(h, an, prior, dt0, res, rng, train_n=256, epochs=10, gens=20, inner=8):
+def unet_screen(h, an, prior, dt0, res, rng, train_n=20000, epochs=3, gens=20, inner=8):
     """The bf16 U-Net as the stage-1 screen: trained by the library's
     kernels on `train_n` prior draws (batched solver targets), then its
     held-out density error, its log-posterior error near the mode, and the
@@ -853,6 +855,9 @@ def main():
     ap.add_argument("--only-adjoint", action="store_true",
                     help="print the adjoint measurement alone")
     ap.add_argument("--mcmc-chains", type=int, default=64, help="pipeline chains")
+    ap.add_argument("--unet-train", type=int, default=20000,
+                    help="prior draws (batched-solver targets) the U-Net screen is trained on")
+    ap.add_argument("--unet-epochs", type=int, default=3, help="training passes over them")
     ap.add_argument("--mcmc-inner", type=int, default=64, help="surrogate steps per solve")
     ap.add_argument("--mcmc-generations", type=int, default=300,
                     help="pipeline generations (the first 100 are burn-in)")
@@ -891,7 +896,9 @@ def main():
                                                   chains=args.mcmc_chains, inner=args.mcmc_inner,
                                                   generations=args.mcmc_generations,
                                                   unet=not args.no_surrogate,
-                                                  mala_steps=args.mala_steps, ind_prob=args.mcmc_ind)}))
+                                                  mala_steps=args.mala_steps, ind_prob=args.mcmc_ind,
+                                                  unet_train=args.unet_train,
+                                                  unet_epochs=args.unet_epochs)}))
         return
     set_population(args.samples)
 
@@ -1032,7 +1039,8 @@ def main():
             line["mcmc"] = mcmc_comparison(local_rank, chains=args.mcmc_chains,
                                            inner=args.mcmc_inner,
                                            generations=args.mcmc_generations,
-                                           mala_steps=args.mala_steps, ind_prob=args.mcmc_ind)
+                                           mala_steps=args.mala_steps, ind_prob=args.mcmc_ind,
+                                           unet_train=args.unet_train, unet_epochs=args.unet_epochs)
         if not args.no_amr:
             line["amr"] = amr_measurement(local_rank)
             line["amr"]["adaptive"] = amr_adaptive_measurement(local_rank)
