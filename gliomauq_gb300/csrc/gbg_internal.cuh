@@ -141,6 +141,7 @@ struct Handle {
     // new observations); a graph captured at another generation is captured
     // anew.
     unsigned long long state_gen = 0;
+    unsigned long long graph_clock = 0;  // replay counter (least recently used graph)
     bool batch_graphs = true;
     std::vector<BatchGraph> graphs;
 

@@ -1554,7 +1554,6 @@ constexpr size_t kMaxBatchGraphs = 8;
 
 int batch_graph_run(Handle &h, const gbg_sample *samples_device, int S, const gbg_batch_opts &o,
                     gbg_lik_result *loglik_device) {
-    static unsigned long long use_clock = 0;
     const int wl = (o.with_loglik && loglik_device) ? 1 : 0;
     auto same = [&](const BatchGraph &g) {
         return g.S == S && g.with_loglik == wl && g.variant == h.pop_variant && g.L == o.L && g.ic_peak == o.ic_peak &&
@@ -1616,7 +1615,7 @@ int batch_graph_run(Handle &h, const gbg_sample *samples_device, int S, const gb
         h.graphs.push_back(g);
         hit = &h.graphs.back();
     }
-    hit->last_use = ++use_clock;
+    hit->last_use = ++h.graph_clock;
     GBG_CUDA_TRY(cudaGraphLaunch(hit->exec, h.stream));
     h.launches += hit->launches;
     h.pop_tile_cells = hit->tile_cells;
