@@ -564,6 +564,88 @@ def amr_adaptive_measurement(device, level=4, seed=7, steps_per_regrid=20):
     return out
 
 
+def c1_measurement(device, n=64, reps=5, lik_reps=50):
+    """The plain forward solve of the CPU-runnable configuration (uniform
+    64^3, 1 mm voxels, Dw = 0.13 mm^2/day, Dg = Dw/10, rho = 0.025/day,
+    Gaussian seed of peak 0.1 and sigma 1 voxel, T = 300 days, the
+    reference's dt rule and loop) as one solve per call: the GPU's FP64
+    (bit-identical to the reference) and fast FP32 paths, and 512 such solves
+    at once on the batched solver; beside them, on the host cores, the
+    oracle's FP64 restatement of the reference step and its block-lab port
+    (the reference's FP32 default), one whole solve each. Then likelihood
+    evaluations per second (HGG_Likelihood: stepPet 3, stepTi 2, selective
+    points): gbg_loglik on the GPU-resident field against the oracle's
+    restatement on the host."""
+    from gliomauq_gb300 import _lib, synthetic as Syn
+    from oracle import oracle
+    an = Syn.make_anatomy(n, seed=0)
+    Dw, rho, T = 0.0013, 0.025, 300.0
+    c = (n / 2 + 0.3, n / 2 - 0.6, n / 2 + 0.2)
+    phi0 = Syn.gaussian_ic(an, *c, peak=0.1, sigma=1.0)
+    dt, dw, dg = Syn.reference_dt(n, Dw, an.L)
+    steps = Syn.num_steps(dt, T)
+    cells = float(n ** 3 * steps)
+    out = {"grid": n, "steps": steps, "cell_steps_per_solve": cells}
+    cores = os.cpu_count() or 1
+    for prec in ("f64", "f32"):
+        h = _lib.Handle(n, prec, device=device)
+        try:
+            h.set_anatomy(an.p_w, an.p_g)
+            t_, d, g = Syn.reference_dt(n, Dw, an.L, f32=(prec == "f32"))
+            k_ = Syn.num_steps(t_, T)
+            h.set_phi(phi0)
+            h.rd_step(d, g, rho, t_, k_)  # warm-up
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                h.set_phi(phi0)
+                h.rd_step(d, g, rho, t_, k_)
+                u = h.get_phi()
+            sec = (time.perf_counter() - t0) / reps
+            out[f"gpu_{prec}"] = {"solves_per_s": 1.0 / sec, "cell_steps_per_s": n ** 3 * k_ / sec,
+                                  "note": "one solve per call: upload, steps, download"}
+            if prec == "f64":
+                obs = Syn.make_observations(u, an, seed=3, centre_xyz=c, radius_vox=27.0 * n / 128)
+                h.set_observations(obs.pet, obs.t1, obs.t2, obs.points, LIK, step_pet=3, step_ti=2)
+                h.loglik()
+                t0 = time.perf_counter()
+                for _ in range(lik_reps):
+                    h.loglik()
+                gl = lik_reps / (time.perf_counter() - t0)
+                t0 = time.perf_counter()
+                for _ in range(5):
+                    oracle.loglik(u, obs.pet, obs.t1, obs.t2, obs.points, LIK, 3, 2, True)
+                cl = 5 / (time.perf_counter() - t0)
+                out["likelihood_evals_per_s"] = {"gpu": gl, "cpu_port_1_thread": cl,
+                                                 "note": "gbg_loglik on the resident field, result "
+                                                         "copied to the host per call"}
+        finally:
+            h.close()
+    hb = _lib.Handle(n, "f32", device=device, max_samples=512)
+    try:
+        hb.set_anatomy(an.p_w, an.p_g)
+        smp = [(Dw, rho) + c + (T,)] * 512
+        hb.batch_solve(smp, an.L, with_loglik=False)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            hb.batch_solve(smp, an.L, with_loglik=False)
+        sec = (time.perf_counter() - t0) / reps
+        out["gpu_batched_512_f32"] = {"solves_per_s": 512 / sec, "dense_equivalent_cell_steps_per_s": 512 * cells / sec,
+                                      "note": "the skipping kernel computes only tiles that can be nonzero"}
+    finally:
+        hb.close()
+    t0 = time.perf_counter()
+    oracle.rd_solve(an.p_w, an.p_g, phi0, dw, dg, rho, dt, steps, "f64", cores)
+    sec = time.perf_counter() - t0
+    out["cpu_oracle_f64"] = {"solves_per_s": 1.0 / sec, "cell_steps_per_s": cells / sec, "threads": cores}
+    d32 = Syn.reference_dt(n, Dw, an.L, f32=True)
+    g = oracle.BlockGrid(an.p_w, an.p_g, phi0)
+    t0 = time.perf_counter()
+    g.steps(d32[1], d32[2], rho, d32[0], steps, cores)
+    sec = time.perf_counter() - t0
+    out["cpu_blocklab_port_f32"] = {"solves_per_s": 1.0 / sec, "cell_steps_per_s": cells / sec, "threads": cores}
+    return out
+
+
 def graph_measurement(device, n=128, reps=20):
     """gbg_batch_solve per call (host-timed, host buffers in and out) with the
     call as one CUDA graph launch (the default) and as separate kernel
@@ -889,7 +971,8 @@ def main():
     if args.only_kernels:
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         print(json.dumps({"sampling_kernels": screen_and_statistics_measurement(dev),
-                          "batch_call": graph_measurement(dev)}))
+                          "batch_call": graph_measurement(dev),
+                          "c1_plain_solve": c1_measurement(dev)}))
         return
     if args.only_mcmc:
         print(json.dumps({"mcmc": mcmc_comparison(int(os.environ.get("LOCAL_RANK", "0")),
@@ -1046,6 +1129,7 @@ def main():
             line["amr"]["adaptive"] = amr_adaptive_measurement(local_rank)
         line["sampling_kernels"] = screen_and_statistics_measurement(local_rank)
         line["batch_call"] = graph_measurement(local_rank)
+        line["c1_plain_solve"] = c1_measurement(local_rank)
         line["adjoint"] = adjoint_measurement(local_rank)
         if not args.no_surrogate:
             line["surrogate"] = surrogate_measurement(local_rank)
