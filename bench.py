@@ -201,7 +201,7 @@ def cpu_baseline(an, prior, seconds=12.0, obs=None):
 def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=64,
                     plain_chains=4, plain_steps=1500, plain_burn=300, ref_generations=500,
                     plain_cap_s=150.0, unet=True, mala_steps=0, mala_burn=100, ind_prob=0.0,
-                    unet_train=20000, unet_epochs=3):
+                    unet_train=20000, unet_epochs=3, seed=0):
     """Posterior effective samples per second at n^3 on one synthetic
     patient, plain single-solve MCMC against the batched + adjoint +
     surrogate pipeline, both in the scaling symmetry's coordinates
@@ -232,7 +232,7 @@ def mcmc_comparison(device, n=128, chains=64, generations=300, burn=100, inner=6
     from gliomauq_gb300 import _lib, mcmc, synthetic as Syn
     an = Syn.make_anatomy(n, seed=0)
     truth = Syn.draw_prior(an, 1, seed=10_000)[0]
-    rng = np.random.default_rng(0)
+    rng = np.random.default_rng(seed)
     h = _lib.Handle(n, "f32", device=device, max_samples=512)
     h.set_anatomy(an.p_w, an.p_g)
     tune_cache = os.path.join(ROOT, "gliomauq_gb300", "_build", "tune.json")
@@ -940,6 +940,7 @@ def main():
     ap.add_argument("--unet-train", type=int, default=20000,
                     help="prior draws (batched-solver targets) the U-Net screen is trained on")
     ap.add_argument("--unet-epochs", type=int, default=3, help="training passes over them")
+    ap.add_argument("--mcmc-seed", type=int, default=0, help="random stream of both samplers")
     ap.add_argument("--mcmc-inner", type=int, default=64, help="surrogate steps per solve")
     ap.add_argument("--mcmc-generations", type=int, default=300,
                     help="pipeline generations (the first 100 are burn-in)")
@@ -981,7 +982,7 @@ def main():
                                                   unet=not args.no_surrogate,
                                                   mala_steps=args.mala_steps, ind_prob=args.mcmc_ind,
                                                   unet_train=args.unet_train,
-                                                  unet_epochs=args.unet_epochs)}))
+                                                  unet_epochs=args.unet_epochs, seed=args.mcmc_seed)}))
         return
     set_population(args.samples)
 
