@@ -11,7 +11,8 @@ log-likelihood accumulated in FP64.
   value  : solves/s with the sample parameters already resident on the GPU
            (gbg_batch_solve_device), CUDA events on the library's stream
   e2e    : solves/s through the host C-ABI entry gbg_batch_solve (parameters
-           copied in, log-likelihoods and step counts copied out each step)
+           copied in, one CUDA graph launch, log-likelihoods and step counts
+           copied out each step)
   roofline: the population kernel's algorithmic bytes (8 B per cell-step it
            computes, plus 8/S B of shared anatomy) over its event-timed
            duration, against the measured HBM copy bandwidth; the skipping
